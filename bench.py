@@ -1,0 +1,497 @@
+#!/usr/bin/env python3
+"""Benchmark of the level-set hot path: reinitialization + mean curvature on a
+256^3 grid (WENO5 / TVD-RK3), the workload LSMLIB's reinitialization drivers
+run, in the GB300 FP32 form, with the FP64 form beside it.
+
+Workload (one "step"): phi = (|x| - 0.5) * (0.1 + (x-0.3)^2 + (y-0.3)^2 +
+(z+0.2)^2) on cell centres of [-1,1]^3, N = 256, dx = 2/N, 3 ghost cells;
+20 pseudo-time TVD-RK3 iterations of the reinitialization equation with HJ
+WENO5 plus/minus derivatives, dtau = 0.5 dx, smoothed sign from phi0
+(epsilon = dx), signed linear extrapolation in the ghost cells after every
+stage (the reference drivers' boundary condition); then second-order mean
+curvature.  Unit of work: one interior cell advanced one full TVD-RK3
+iteration (a cell-update).  Inputs are synthetic (seedless analytic field).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line (rank 0).  --impl reference times the reference's own
+CPU kernels (LSMLIB's Fortran translated to C under oracle/_ref, else the C
+oracle) on the host cores for a bounded sample of the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "WENO5+TVD-RK3 reinitialization cell-updates/s (256^3, 20 iterations + mean curvature)"
+UNIT = "Gcell-updates/s"
+N_DEFAULT = 256
+ITERS = 20
+GHOST = 3
+# algorithmic bytes of the fused FP32 stage kernel per cell (phi0 sign form):
+# stage 1 reads phi^n and phi0 and writes phi1 (12 B), stages 2 and 3 also
+# read phi^n (16 B): 44 B per cell-update = 11 * 4 B
+ALG_BYTES_PER_CELL_UPDATE = {"f32": 44.0, "f64": 88.0}
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def boxes(n):
+    fb = (0, n - 1, 0, n - 1, 0, n - 1)
+    gb = (-GHOST, n - 1 + GHOST) * 3
+    gb = (gb[0], gb[1], gb[0], gb[1], gb[0], gb[1])
+    return gb, fb
+
+
+def initial_phi(n):
+    """Config-2 level set on cell centres x_i = -1 + (i + 1/2) dx, ghosts included."""
+    dx = 2.0 / n
+    c = -1.0 + (np.arange(-GHOST, n + GHOST) + 0.5) * dx
+    X, Y, Z = np.meshgrid(c, c, c, indexing="ij")
+    r = np.sqrt(X * X + Y * Y + Z * Z)
+    phi = (r - 0.5) * (0.1 + (X - 0.3) ** 2 + (Y - 0.3) ** 2 + (Z + 0.2) ** 2)
+    return np.asfortranarray(phi), dx
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.lines = []
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU reference sample (reference arm and cpu_baseline)
+# ---------------------------------------------------------------------------
+def cpu_library():
+    """(ctypes handle, kind): the reference's own kernels translated to C when
+    built (oracle/_ref), else the C oracle restatement."""
+    ref = os.path.join(ROOT, "oracle", "_ref", "liblsmref.so")
+    if not os.path.exists(ref):
+        try:
+            from oracle import build as ob
+            ob.build()
+        except Exception:
+            pass
+    if os.path.exists(ref):
+        return ctypes.CDLL(ref, mode=ctypes.RTLD_LOCAL), "reference"
+    orc = os.path.join(ROOT, "oracle", "liblsmoracle.so")
+    if not os.path.exists(orc):
+        from oracle import build as ob
+        ob.build_oracle()
+    return ctypes.CDLL(orc, mode=ctypes.RTLD_LOCAL), "port"
+
+
+def _ip(v):
+    return ctypes.byref(ctypes.c_int(int(v)))
+
+
+def _dp(v):
+    return ctypes.byref(ctypes.c_double(float(v)))
+
+
+def _arr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class CpuReinit:
+    """LSMLIB's reinitialization call sequence on the host, split into k-slabs
+    over threads (ctypes releases the GIL): per stage each thread runs
+    lsm3dhjweno5 -> lsm3dcomputereinitializationeqnrhs -> lsm3dtvdrk3stageN on
+    its slab, then the six signed-linear-extrapolation face calls fill the
+    ghost cells."""
+
+    def __init__(self, lib, phi, gb, fb, dx, threads):
+        self.lib, self.gb, self.fb, self.dx = lib, gb, fb, dx
+        self.phi = phi.copy(order="F")
+        self.phi0 = phi.copy(order="F")
+        shape = phi.shape
+        z = lambda: np.zeros(shape, order="F")
+        self.u1, self.u2, self.un = z(), z(), z()
+        self.pp = [z(), z(), z()]
+        self.pm = [z(), z(), z()]
+        self.rhs = z()
+        nk = fb[5] - fb[4] + 1
+        t = max(1, min(threads, nk))
+        edges = np.linspace(fb[4], fb[5] + 1, t + 1).astype(int)
+        self.slabs = [(edges[s], edges[s + 1] - 1) for s in range(t) if edges[s + 1] > edges[s]]
+        nx, ny = fb[1] - fb[0] + 7, fb[3] - fb[2] + 7
+        self.d1 = [np.zeros((nx, ny, (k1 - k0 + 7)), order="F") for k0, k1 in self.slabs]
+
+    def _slab_stage(self, s, src, out, stage, dt):
+        lib, gb, fb = self.lib, self.gb, self.fb
+        k0, k1 = self.slabs[s]
+        sfb = (fb[0], fb[1], fb[2], fb[3], k0, k1)
+        dgb = (fb[0] - 3, fb[1] + 3, fb[2] - 3, fb[3] + 3, k0 - 3, k1 + 3)
+        G = [_ip(v) for v in gb]
+        F = [_ip(v) for v in sfb]
+        D = [_ip(v) for v in dgb]
+        dx = _dp(self.dx)
+        lib.lsm3dhjweno5_(_arr(self.pp[0]), _arr(self.pp[1]), _arr(self.pp[2]), *G,
+                          _arr(self.pm[0]), _arr(self.pm[1]), _arr(self.pm[2]), *G,
+                          _arr(src), *G, _arr(self.d1[s]), *D, *F, dx, dx, dx)
+        lib.lsm3dcomputereinitializationeqnrhs_(
+            _arr(self.rhs), *G, _arr(src), *G, _arr(self.phi0), *G,
+            _arr(self.pp[0]), _arr(self.pp[1]), _arr(self.pp[2]), *G,
+            _arr(self.pm[0]), _arr(self.pm[1]), _arr(self.pm[2]), *G, *F, dx, dx, dx, _ip(1))
+        if stage == 1:
+            lib.lsm3dtvdrk3stage1_(_arr(out), *G, _arr(self.phi), *G, _arr(self.rhs), *G, *F, _dp(dt))
+        elif stage == 2:
+            lib.lsm3dtvdrk3stage2_(_arr(out), *G, _arr(src), *G, _arr(self.phi), *G, _arr(self.rhs), *G,
+                                   *F, _dp(dt))
+        else:
+            lib.lsm3dtvdrk3stage3_(_arr(out), *G, _arr(src), *G, _arr(self.phi), *G, _arr(self.rhs), *G,
+                                   *F, _dp(dt))
+
+    def _bc(self, a):
+        G = [_ip(v) for v in self.gb]
+        F = [_ip(v) for v in self.fb]
+        for face in range(6):
+            self.lib.lsm3dsignedlinearextrapolation_(_arr(a), *G, *F, _ip(face))
+
+    def _stage(self, src, out, stage, dt):
+        ths = [threading.Thread(target=self._slab_stage, args=(s, src, out, stage, dt))
+               for s in range(len(self.slabs))]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        self._bc(out)
+
+    def iterate(self, n, dt):
+        for _ in range(n):
+            self._stage(self.phi, self.u1, 1, dt)
+            self._stage(self.u1, self.u2, 2, dt)
+            self._stage(self.u2, self.un, 3, dt)
+            self.phi, self.un = self.un, self.phi
+
+
+def cpu_sample(n, iters, threads, warmup=0):
+    """Time `iters` reinitialization iterations of the full n^3 workload on the
+    host; returns (cell-updates/s, seconds, kind)."""
+    lib, kind = cpu_library()
+    phi, dx = initial_phi(n)
+    gb, fb = boxes(n)
+    r = CpuReinit(lib, phi, gb, fb, dx, threads)
+    if warmup:
+        r.iterate(warmup, 0.5 * dx)
+    t0 = time.perf_counter()
+    r.iterate(iters, 0.5 * dx)
+    sec = time.perf_counter() - t0
+    return n ** 3 * iters / sec, sec, kind
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers
+# ---------------------------------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, world, device):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+def reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n = args.n
+    lib, kind = cpu_library()
+    phi, dx = initial_phi(n)
+    gb, fb = boxes(n)
+    r = CpuReinit(lib, phi, gb, fb, dx, threads)
+    per_step = 1  # iterations of the 20 per step: a bounded sample of the workload
+    for _ in range(args.warmup):
+        r.iterate(per_step, 0.5 * dx)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r.iterate(per_step, 0.5 * dx)
+    sec = time.perf_counter() - t0
+    value = n ** 3 * per_step * args.steps / sec / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (analytic level set)",
+        "config": {"workload": "reinit-weno5-tvdrk3-256", "n": n, "iterations_per_step": per_step,
+                   "bc": "signed linear extrapolation"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": "%d reinitialization iteration(s) of the %d^3 workload per step, "
+                                   "k-slabs over %d host threads" % (per_step, n, threads)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def gpu_arm(args, world, rank, local):
+    import torch
+    import lsmlib_gb300 as L
+    from lsmlib_gb300 import build as B
+    B.build()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    h = L.lib()
+    stream = torch.cuda.current_stream(dev)
+    L.set_stream(stream.cuda_stream)
+
+    n = args.n
+    gb, fb = boxes(n)
+    phi64, dx = initial_phi(n)
+    dtau = 0.5 * dx
+    bc = L.BC_SIGNED_LINEAR
+
+    def dev_tensor(a, dtype):
+        return torch.from_numpy(np.ascontiguousarray(a.T)).to(dev, dtype)
+
+    pristine = dev_tensor(phi64, torch.float32)
+    phi = torch.empty_like(pristine)
+    kappa = torch.zeros_like(pristine)
+    cells = n ** 3
+
+    def step():
+        phi.copy_(pristine)
+        L.reinit_weno5_tvdrk3(phi, gb, fb, dx, dtau, ITERS, use_phi0_for_sgn=1, bc=bc, precision="f32")
+        L.mean_curvature_o2(kappa, gb, phi, gb, fb, dx, precision="f32")
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    launches0 = L.launch_count()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(world)
+    launches = L.launch_count() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = max_over_ranks(ms, world, dev)
+    value = world * cells * ITERS / (ms / 1e3) / 1e9
+
+    # roofline of the dominant kernel (the fused reinitialization stage):
+    # stage-only time from the difference of two runs, periodic boundaries
+    # (no ghost-fill launches), so the difference is 3*(n_b - n_a) stage
+    # launches exactly
+    def stage_time(iters, reps=3):
+        best = None
+        for _ in range(reps):
+            phi.copy_(pristine)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            L.reinit_weno5_tvdrk3(phi, gb, fb, dx, dtau, iters, use_phi0_for_sgn=1, bc=L.BC_PERIODIC,
+                                  precision="f32")
+            b.record(stream)
+            torch.cuda.synchronize()
+            t = a.elapsed_time(b)
+            best = t if best is None else min(best, t)
+        return best
+
+    t1, t11 = stage_time(1), stage_time(11)
+    stage_ms = (t11 - t1) / 30.0
+    bytes_per_launch = ALG_BYTES_PER_CELL_UPDATE["f32"] / 3.0 * cells
+    achieved = bytes_per_launch / (stage_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": MEASURED_STAGE_TRAFFIC,
+                "kernel": "k_stage<float, REINIT> (fused WENO5 + reinit RHS + TVD-RK3 stage)",
+                "stage_ms": stage_ms, "peak_source": peak_kind}
+
+    # end to end through the C ABI with host (pinned) buffers
+    host_phi = torch.from_numpy(np.ascontiguousarray(phi64.T).astype(np.float32)).pin_memory()
+    host_work = torch.empty_like(host_phi).pin_memory()
+    host_kappa = torch.zeros_like(host_phi).pin_memory()
+    e2e_steps = max(1, min(args.steps, 3))
+
+    def e2e_step():
+        host_work.copy_(host_phi)
+        wk = host_work.numpy()
+        L.reinit_weno5_tvdrk3(wk.ctypes.data, gb, fb, dx, dtau, ITERS, use_phi0_for_sgn=1, bc=bc,
+                              precision="f32")
+        L.mean_curvature_o2(host_kappa.numpy().ctypes.data, gb, wk.ctypes.data, gb, fb, dx,
+                            precision="f32")
+
+    e2e_step()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_sec = (time.perf_counter() - t0) / e2e_steps
+    e2e_sec = max_over_ranks(e2e_sec, world, dev)
+    arr_bytes = host_phi.numel() * 4
+    e2e = {"value": world * cells * ITERS / e2e_sec / 1e9, "unit": UNIT,
+           # reinit: phi in and out; curvature: phi in, kappa in and out
+           "h2d_bytes_per_step": 3 * arr_bytes, "d2h_bytes_per_step": 2 * arr_bytes}
+
+    # FP64 parity form on the same workload, and the FP32 error against it
+    phi_d64 = dev_tensor(phi64, torch.float64)
+    kap64 = torch.zeros_like(phi_d64)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    L.reinit_weno5_tvdrk3(phi_d64, gb, fb, dx, dtau, ITERS, use_phi0_for_sgn=1, bc=bc, precision="f64")
+    L.mean_curvature_o2(kap64, gb, phi_d64, gb, fb, dx, precision="f64")
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms64 = a.elapsed_time(b)
+    step()
+    torch.cuda.synchronize()
+    inner = (slice(GHOST, -GHOST),) * 3
+    p32 = phi.double().cpu().numpy()[inner]
+    p64 = phi_d64.cpu().numpy()[inner]
+    k32 = kappa.double().cpu().numpy()[inner]
+    k64 = kap64.cpu().numpy()[inner]
+    band = np.abs(p64) < 3 * dx
+    err = {"phi_linf": float(np.max(np.abs(p32 - p64))), "phi_l1": float(np.mean(np.abs(p32 - p64))),
+           "kappa_band_linf": float(np.max(np.abs(k32 - k64)[band])),
+           "kappa_band_l1": float(np.mean(np.abs(k32 - k64)[band]))}
+    fp64 = {"value": cells * ITERS / (ms64 / 1e3) / 1e9, "unit": UNIT, "ms_per_step": ms64,
+            "fp32_speedup": ms64 / ms}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (analytic level set of the reinitialization workload)",
+        "config": {"workload": "reinit-weno5-tvdrk3-256 + mean curvature", "n": n,
+                   "iterations": ITERS, "dtau": "0.5 dx", "sign": "phi0 form, eps = dx",
+                   "bc": "signed linear extrapolation", "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "l2": "inputs larger than L2 (4 x 79 MB padded FP32 fields per stage)"},
+        "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+        "fp64": fp64, "fp32_error_vs_fp64": err,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, sec, kind = cpu_sample(n, 1, threads)
+        line["cpu_baseline"] = {"value": v / 1e9, "unit": UNIT, "cores": threads, "kind": kind,
+                                "sample": "1 reinitialization iteration of the %d^3 workload "
+                                          "(%.1f s), k-slabs over %d host threads" % (n, sec, threads)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# DRAM bytes per fused FP32 reinitialization stage launch at 256^3 from ncu
+# (profiles/ summary); None until captured
+MEASURED_STAGE_TRAFFIC = None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+    else:
+        gpu_arm(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,121 @@
+/*
+ * lsmgpu — GB300-native implementation of LSMLIB's data-parallel level-set
+ * kernels.
+ *
+ * This header holds the library's own entry points (runtime control, status,
+ * and the fused time-stepping calls).  The drop-in entry points that replace
+ * LSMLIB's Fortran toolbox routines, with LSMLIB's symbol names and argument
+ * lists, are declared in lsmgpu_toolbox3d.h.
+ *
+ * Pointer rules for every entry point
+ *  - A pointer to device or managed memory is used in place; the call is
+ *    asynchronous on the library stream (lsmgpu_set_stream), except that a
+ *    scalar result written to host memory (a dt, a norm) waits for the stream.
+ *  - A pointer to host memory (pageable or pinned) is staged: copied to the
+ *    device, computed, and copied back before the call returns, which is the
+ *    synchronous behaviour LSMLIB's serial routines have.
+ *  - Scratch arrays of the LSMLIB interface (D1, D2, D3 of the dense
+ *    derivative routines) are accepted and not written.
+ *
+ * Errors: LSMLIB's routines return nothing and do not check their input.  Here
+ * each call validates its index boxes (the fill box plus the stencil's reach
+ * must lie inside every ghost box it reads) and records a status that
+ * lsmgpu_get_last_error() returns; an invalid call computes nothing.
+ */
+#ifndef LSMGPU_H
+#define LSMGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define LSMGPU_OK 0
+#define LSMGPU_ERR_BOUNDS 1      /* an index box does not cover a stencil  */
+#define LSMGPU_ERR_CUDA 2        /* a CUDA runtime call failed             */
+#define LSMGPU_ERR_ARGUMENT 3    /* null pointer or unsupported option     */
+#define LSMGPU_ERR_CAPACITY 4    /* a size exceeds a documented maximum    */
+#define LSMGPU_ERR_TIMEOUT 5     /* a bounded device wait gave up          */
+
+/* Returns the status of the last lsmgpu call made on this host thread and,
+ * when msg is not NULL, copies a description into msg (at most len bytes,
+ * NUL-terminated). */
+int lsmgpu_get_last_error(char *msg, int len);
+
+/* Sets the CUDA stream (a cudaStream_t passed as void*) the library launches
+ * on; NULL selects the legacy default stream. */
+void lsmgpu_set_stream(void *stream);
+void *lsmgpu_get_stream(void);
+
+/* Waits for all work the library queued on its stream. */
+int lsmgpu_synchronize(void);
+
+/* Number of kernels the library has launched since the process started (or
+ * since lsmgpu_reset_launch_count). */
+long long lsmgpu_launch_count(void);
+void lsmgpu_reset_launch_count(void);
+
+/* ---------------------------------------------------------------------------
+ * Fused WENO5 / TVD-RK3 time steppers.
+ *
+ * Each call advances phi (column-major over the ghost box gb[6] = {ilo, ihi,
+ * jlo, jhi, klo, khi}) by whole TVD-RK3 steps over the fill box fb[6].  Every
+ * stage is one kernel that computes the HJ WENO5 derivatives, the right-hand
+ * side and the stage update in one pass; after each stage the 3 ghost layers
+ * are refreshed with the boundary condition `bc`.  The result equals the
+ * LSMLIB call sequence per stage
+ *   HJ derivatives -> RHS -> TVDRK3StageN -> ghost fill
+ * and, for the _f64 forms, matches it bit for bit.  The fill box needs at
+ * least 6 cells per axis and 3 ghost cells on every side; ghost cells beyond
+ * the third layer are left untouched.  The _f32 forms store and compute in
+ * single precision.  Returns an LSMGPU_* status.
+ * ------------------------------------------------------------------------- */
+#define LSMGPU_BC_PERIODIC 0      /* periodic wrap of the fill box           */
+#define LSMGPU_BC_LINEAR 1        /* lsm3dLinearExtrapolation on the six faces,
+                                     x then y then z                         */
+#define LSMGPU_BC_SIGNED_LINEAR 2 /* lsm3dSignedLinearExtrapolation, same order */
+#define LSMGPU_BC_COPY 3          /* lsm3dCopyExtrapolation (homogeneous
+                                     Neumann), same order                    */
+
+/* Reinitialization: n_iter pseudo-time steps of d(phi)/dt = sgn(1 - |grad phi|)
+ * (lsm3dComputeReinitializationEqnRHS with HJ WENO5 plus/minus derivatives),
+ * step dtau.  use_phi0_for_sgn = 1 takes the smoothed sign from the initial
+ * phi, 0 from the current stage's phi. */
+int lsmgpu_reinit_weno5_tvdrk3_f64(double *phi, const int *gb, const int *fb, double dx, double dy,
+                                   double dz, double dtau, int n_iter, int use_phi0_for_sgn, int bc);
+int lsmgpu_reinit_weno5_tvdrk3_f32(float *phi, const int *gb, const int *fb, float dx, float dy,
+                                   float dz, float dtau, int n_iter, int use_phi0_for_sgn, int bc);
+
+/* Advection: n_steps steps of d(phi)/dt = -u . grad(phi) with upwind HJ WENO5
+ * (lsm3dUpwindHJWENO5 + lsm3dAddAdvectionTermToLSERHS), step dt.  The velocity
+ * is either three fields over the ghost box vel_gb (vel_x/y/z non-NULL) or,
+ * when vel_x is NULL, the constant vel_const[3]. */
+int lsmgpu_advect_weno5_tvdrk3_f64(double *phi, const int *gb, const int *fb, const double *vel_x,
+                                   const double *vel_y, const double *vel_z, const int *vel_gb,
+                                   const double *vel_const, double dx, double dy, double dz,
+                                   double dt, int n_steps, int bc);
+int lsmgpu_advect_weno5_tvdrk3_f32(float *phi, const int *gb, const int *fb, const float *vel_x,
+                                   const float *vel_y, const float *vel_z, const int *vel_gb,
+                                   const float *vel_const, float dx, float dy, float dz, float dt,
+                                   int n_steps, int bc);
+
+/* Second-order mean curvature of phi over the fill box fb in one pass: the
+ * sequence lsm3dCentralGradOrder2 -> lsm3dGradientMagnitude ->
+ * lsm3dComputeMeanCurvatureOrder2.  kappa (and grad_phi_mag when not NULL)
+ * are column-major over kappa_gb; phi over phi_gb, which must hold one ghost
+ * cell around fb. */
+int lsmgpu_mean_curvature_o2_f64(double *kappa, const int *kappa_gb, const double *phi,
+                                 const int *phi_gb, double *grad_phi_mag, const int *fb, double dx,
+                                 double dy, double dz);
+int lsmgpu_mean_curvature_o2_f32(float *kappa, const int *kappa_gb, const float *phi,
+                                 const int *phi_gb, float *grad_phi_mag, const int *fb, float dx,
+                                 float dy, float dz);
+
+/* Library version string. */
+const char *lsmgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LSMGPU_H */

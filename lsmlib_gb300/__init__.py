@@ -1,0 +1,181 @@
+"""lsmlib_gb300 — GB300-native level-set kernels with LSMLIB's C interface.
+
+The product is the shared library ``liblsmgpu.so`` (CUDA, sm_103a) in this
+directory.  It exports LSMLIB's 3D toolbox routines under LSMLIB's own symbol
+names and argument lists (include/lsmgpu_toolbox3d.h) plus fused
+time-stepping entry points (include/lsmgpu.h).  This module is a thin ctypes
+binding used by the tests and the benchmark:
+
+* :func:`lib` loads the library (and fails loudly when it is missing — there
+  is no CPU fallback);
+* :data:`ABI` lists every drop-in entry point with its argument list
+  (name, kind, is-array, written), mirroring the reference's Fortran
+  signature;
+* :func:`invoke` calls an entry point by symbol name with arguments given by
+  their LSMLIB names.
+"""
+import ctypes
+import json
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liblsmgpu.so")
+
+with open(os.path.join(_HERE, "abi.json")) as _f:
+    ABI = json.load(_f)
+
+_lib = None
+
+
+def lib(path=None):
+    """Load liblsmgpu.so once and return the ctypes handle."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(
+            "liblsmgpu.so is not built (%s); run `python -m lsmlib_gb300.build` "
+            "— the level-set kernels have no CPU fallback" % p)
+    handle = ctypes.CDLL(p, mode=ctypes.RTLD_LOCAL)
+    handle.lsmgpu_get_last_error.restype = ctypes.c_int
+    handle.lsmgpu_get_last_error.argtypes = [ctypes.c_char_p, ctypes.c_int]
+    handle.lsmgpu_set_stream.argtypes = [ctypes.c_void_p]
+    handle.lsmgpu_get_stream.restype = ctypes.c_void_p
+    handle.lsmgpu_launch_count.restype = ctypes.c_longlong
+    handle.lsmgpu_version.restype = ctypes.c_char_p
+    if path is None:
+        _lib = handle
+    return handle
+
+
+def last_error(handle=None):
+    """(code, message) of the last call on this thread."""
+    h = handle or lib()
+    buf = ctypes.create_string_buffer(512)
+    code = h.lsmgpu_get_last_error(buf, 512)
+    return code, buf.value.decode()
+
+
+def check(handle=None):
+    code, msg = last_error(handle)
+    if code != 0:
+        raise RuntimeError("lsmgpu error %d: %s" % (code, msg))
+
+
+def set_stream(stream_ptr, handle=None):
+    (handle or lib()).lsmgpu_set_stream(ctypes.c_void_p(stream_ptr or 0))
+
+
+def launch_count(handle=None):
+    return int((handle or lib()).lsmgpu_launch_count())
+
+
+_SCALAR_CT = {"real": ctypes.c_double, "double": ctypes.c_double, "int": ctypes.c_int,
+              "logical": ctypes.c_int, "int1": ctypes.c_ubyte}
+
+
+def _ptr(v):
+    """Address of an array argument: numpy array, torch tensor or int."""
+    if v is None:
+        return None
+    if isinstance(v, int):
+        return ctypes.c_void_p(v)
+    if hasattr(v, "data_ptr"):
+        return ctypes.c_void_p(v.data_ptr())
+    if hasattr(v, "ctypes"):
+        return ctypes.c_void_p(v.ctypes.data)
+    raise TypeError("unsupported array argument %r" % type(v))
+
+
+def invoke(handle, sym, values, abi=None):
+    """Call `sym` on `handle` (any library exporting LSMLIB's signatures).
+
+    `values` maps each LSMLIB argument name to an array (numpy / torch /
+    device address) or a scalar.  Scalars are passed by reference, as
+    Fortran does; the returned dict holds every scalar argument's value
+    after the call (so outputs such as dt can be read back).
+    """
+    spec = (abi or ABI)[sym]
+    args, refs = [], {}
+    for name, kind, is_arr, _written in spec["args"]:
+        if name not in values:
+            raise KeyError("%s: missing argument %s" % (sym, name))
+        v = values[name]
+        if is_arr:
+            args.append(_ptr(v))
+        else:
+            r = _SCALAR_CT[kind](v)
+            refs[name] = r
+            args.append(ctypes.byref(r))
+    fn = getattr(handle, sym)
+    fn.restype = None
+    fn(*args)
+    return {k: r.value for k, r in refs.items()}
+
+
+# ---------------------------------------------------------------------------
+# fused time steppers (include/lsmgpu.h)
+# ---------------------------------------------------------------------------
+BC_PERIODIC, BC_LINEAR, BC_SIGNED_LINEAR, BC_COPY = 0, 1, 2, 3
+
+
+def _box(b):
+    return (ctypes.c_int * 6)(*[int(v) for v in b])
+
+
+def _fused(name, real):
+    h = lib()
+    fn = getattr(h, name)
+    fn.restype = ctypes.c_int
+    return fn, real
+
+
+def reinit_weno5_tvdrk3(phi, gb, fb, dx, dtau, n_iter, use_phi0_for_sgn=0, bc=BC_PERIODIC,
+                        precision="f64", dy=None, dz=None):
+    """Reinitialise `phi` in place (numpy array in Fortran order over `gb`, or
+    a torch/device address) with n_iter WENO5 / TVD-RK3 pseudo-time steps."""
+    real = ctypes.c_double if precision == "f64" else ctypes.c_float
+    fn, _ = _fused("lsmgpu_reinit_weno5_tvdrk3_" + precision, real)
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, real, real, real, real,
+                   ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    rc = fn(_ptr(phi), _box(gb), _box(fb), dx, dy or dx, dz or dx, dtau, int(n_iter),
+            int(use_phi0_for_sgn), int(bc))
+    if rc != 0:
+        raise RuntimeError("lsmgpu reinit failed: %s" % (last_error()[1],))
+
+
+def advect_weno5_tvdrk3(phi, gb, fb, dx, dt, n_steps, vel=None, vel_gb=None, vel_const=None,
+                        bc=BC_PERIODIC, precision="f64", dy=None, dz=None):
+    """Advect `phi` in place by n_steps WENO5 / TVD-RK3 steps with velocity
+    fields `vel` (3 arrays over vel_gb) or the constant `vel_const`."""
+    real = ctypes.c_double if precision == "f64" else ctypes.c_float
+    fn, _ = _fused("lsmgpu_advect_weno5_tvdrk3_" + precision, real)
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                   real, real, real, real, ctypes.c_int, ctypes.c_int]
+    if vel is not None:
+        vx, vy, vz = (_ptr(v) for v in vel)
+        vgb = _box(vel_gb)
+        vc = None
+    else:
+        vx = vy = vz = None
+        vgb = None
+        vc = (real * 3)(*vel_const)
+    rc = fn(_ptr(phi), _box(gb), _box(fb), vx, vy, vz, vgb, vc, dx, dy or dx, dz or dx, dt,
+            int(n_steps), int(bc))
+    if rc != 0:
+        raise RuntimeError("lsmgpu advect failed: %s" % (last_error()[1],))
+
+
+def mean_curvature_o2(kappa, kappa_gb, phi, phi_gb, fb, dx, grad_phi_mag=None, precision="f64",
+                      dy=None, dz=None):
+    """Second-order mean curvature of phi into kappa (and |grad phi|)."""
+    real = ctypes.c_double if precision == "f64" else ctypes.c_float
+    fn, _ = _fused("lsmgpu_mean_curvature_o2_" + precision, real)
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                   ctypes.c_void_p, ctypes.c_void_p, real, real, real]
+    rc = fn(_ptr(kappa), _box(kappa_gb), _ptr(phi), _box(phi_gb), _ptr(grad_phi_mag), _box(fb),
+            dx, dy or dx, dz or dx)
+    if rc != 0:
+        raise RuntimeError("lsmgpu mean curvature failed: %s" % (last_error()[1],))

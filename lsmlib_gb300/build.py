@@ -1,0 +1,83 @@
+"""Build liblsmgpu.so (the GB300 kernels behind the C interface) in-tree.
+
+Each .cu file under csrc/ compiles to its own object with nvcc for sm_103a,
+in parallel; the objects link into lsmlib_gb300/liblsmgpu.so.  Translation
+units that hold FP64 parity kernels are compiled with -fmad=false so their
+products and sums round exactly like LSMLIB's Fortran (no fused multiply-add);
+the FP32 fast-path units keep FMA contraction.
+
+Usage:  python -m lsmlib_gb300.build   (or lsmlib_gb300.build.build())
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "liblsmgpu.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+          "--expt-relaxed-constexpr", "-I", os.path.join(HERE, "..", "include")]
+
+# FP64 parity units: no contraction of a*b+c into FMA
+NO_FMA = {"dense.cu", "local.cu", "fused_f64.cu", "narrowband.cu", "batched_f64.cu"}
+
+
+def nvcc():
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the lsmgpu CUDA library cannot be built")
+
+
+def _compile(src, extra):
+    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+    if os.path.exists(obj) and os.path.getmtime(obj) >= _newest_input(src):
+        return obj, ""
+    flags = list(COMMON)
+    if os.path.basename(src) in NO_FMA:
+        flags += ["-fmad=false"]
+    cmd = [nvcc()] + ARCH + flags + extra + ["-c", src, "-o", obj]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), p.stdout + p.stderr))
+    return obj, p.stdout + p.stderr
+
+
+def _newest_input(src):
+    t = os.path.getmtime(src)
+    for d in (CSRC, os.path.join(HERE, "..", "include")):
+        for f in os.listdir(d):
+            if f.endswith((".cuh", ".h")):
+                t = max(t, os.path.getmtime(os.path.join(d, f)))
+    return t
+
+
+def build(verbose=False, extra=None):
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    extra = list(extra or [])
+    with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
+        results = list(ex.map(lambda s: _compile(s, extra), srcs))
+    objs = [o for o, _ in results]
+    if verbose:
+        for _, log in results:
+            if log.strip():
+                print(log)
+    newest = max(os.path.getmtime(o) for o in objs)
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
+        tmp = LIB + ".tmp"
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
+        p = subprocess.run(cmd, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), p.stdout + p.stderr))
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

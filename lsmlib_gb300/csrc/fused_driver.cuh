@@ -1,0 +1,231 @@
+// Host drivers of the fused WENO5 / TVD-RK3 time steppers (advection and
+// reinitialization), shared by the FP64 parity unit and the FP32 unit.
+//
+// A call repacks the caller's array (LSMLIB ghost-box layout) into the padded
+// work layout once, runs every stage kernel on the library stream, and
+// unpacks the result.  Three work buffers rotate through the stages:
+//   stage 1: A -> B,  stage 2: B (+ A at the cell) -> C,
+//   stage 3: C (+ A at the cell) -> A   (in place: each cell reads only its
+//   own A value, the stencil comes from C).
+#pragma once
+
+#include "fused_stage.cuh"
+#include "lsmgpu_common.cuh"
+#include "../../include/lsmgpu.h"
+
+namespace lsmgpu {
+namespace fused {
+
+// copy between the caller's ghost-box array and the padded layout over the
+// region the layout holds (interior plus GX/3 ghost cells), clipped to the
+// caller's box; cells of the layout outside the caller's box are zeroed
+template <class R>
+__global__ void k_pack(R *dst, Layout L, View<const R> src, Box gb, int ilo, int jlo, int klo) {
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x) - GX;
+  const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y) - GY;
+  const int k = (int)(blockIdx.z * blockDim.z + threadIdx.z) - GZ;
+  if (i > L.nx + 2 || j > L.ny + 2 || k > L.nz + 2) return;
+  const int gi = i + ilo, gj = j + jlo, gk = k + klo;
+  R v = R(0);
+  if (gi >= gb.lo[0] && gi <= gb.hi[0] && gj >= gb.lo[1] && gj <= gb.hi[1] && gk >= gb.lo[2] &&
+      gk <= gb.hi[2])
+    v = src(gi, gj, gk);
+  dst[L.idx(i, j, k)] = v;
+}
+
+template <class R>
+__global__ void k_unpack(View<R> dst, Box gb, const R *src, Layout L, int ilo, int jlo, int klo) {
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x) - 3;
+  const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y) - 3;
+  const int k = (int)(blockIdx.z * blockDim.z + threadIdx.z) - 3;
+  if (i > L.nx + 2 || j > L.ny + 2 || k > L.nz + 2) return;
+  const int gi = i + ilo, gj = j + jlo, gk = k + klo;
+  if (gi >= gb.lo[0] && gi <= gb.hi[0] && gj >= gb.lo[1] && gj <= gb.hi[1] && gk >= gb.lo[2] &&
+      gk <= gb.hi[2])
+    dst(gi, gj, gk) = src[L.idx(i, j, k)];
+}
+
+// Extrapolation into the 3 ghost layers along one axis: linear
+// (boundary_conditions3d.f:46-169, phi(ghost) = phi(edge) + slope*dist with
+// slope = phi(edge) - phi(next inside)), signed linear (:193-337) or copy
+// (:352-462, the homogeneous Neumann fill).  Axes run x, y, z in turn over
+// the full extent of the other two axes (ghosts included), as the
+// reference's six face calls in that order do.
+template <class R>
+__global__ void k_linear_bc(R *phi, Layout L, int axis, int kind) {
+  const int a = (int)(blockIdx.x * blockDim.x + threadIdx.x) - 3;
+  const int b = (int)(blockIdx.y * blockDim.y + threadIdx.y) - 3;
+  const int n[3] = {L.nx, L.ny, L.nz};
+  const int o1 = axis == 0 ? 1 : 0, o2 = axis == 2 ? 1 : 2;
+  if (a > n[o1] + 2 || b > n[o2] + 2) return;
+  int c[3];
+  c[o1] = a;
+  c[o2] = b;
+  const int nn = n[axis];
+  // lower face
+  c[axis] = 0;
+  const R e0 = phi[L.idx(c[0], c[1], c[2])];
+  c[axis] = 1;
+  const R n0 = phi[L.idx(c[0], c[1], c[2])];
+  // upper face
+  c[axis] = nn - 1;
+  const R e1 = phi[L.idx(c[0], c[1], c[2])];
+  c[axis] = nn - 2;
+  const R n1 = phi[L.idx(c[0], c[1], c[2])];
+  R s0 = e0 - n0, s1 = e1 - n1;
+  if (kind == LSMGPU_BC_SIGNED_LINEAR) {
+    // boundary_conditions3d.f:203-206: slope = sign(1, phi_edge)*|diff|
+    s0 = copysign(R(1.0), e0) * fabs(e0 - n0);
+    s1 = copysign(R(1.0), e1) * fabs(e1 - n1);
+  }
+#pragma unroll
+  for (int g = 1; g <= 3; g++) {
+    c[axis] = -g;
+    phi[L.idx(c[0], c[1], c[2])] = (kind == LSMGPU_BC_COPY) ? e0 : e0 + s0 * R(g);
+    c[axis] = nn - 1 + g;
+    phi[L.idx(c[0], c[1], c[2])] = (kind == LSMGPU_BC_COPY) ? e1 : e1 + s1 * R(g);
+  }
+}
+
+template <class R>
+void launch_bc(R *buf, const Layout &L, int bc) {
+  if (bc == LSMGPU_BC_PERIODIC) return;  // written by the stage kernel
+  const int n[3] = {L.nx, L.ny, L.nz};
+  for (int axis = 0; axis < 3; axis++) {
+    const int o1 = axis == 0 ? 1 : 0, o2 = axis == 2 ? 1 : 2;
+    dim3 blk(32, 8);
+    dim3 grd((unsigned)((n[o1] + 6 + 31) / 32), (unsigned)((n[o2] + 6 + 7) / 8));
+    LSMGPU_LAUNCH(k_linear_bc<R>, grd, blk, 0, buf, L, axis, bc);
+  }
+}
+
+template <class R, int MODE, bool EXACT>
+void launch_stage(const CUtensorMap &tm, const StageArgs<R> &a) {
+  const Layout &L = a.L;
+  dim3 blk(TX, TY);
+  dim3 grd((unsigned)((L.nx + TX - 1) / TX), (unsigned)((L.ny + TY - 1) / TY), (unsigned)((L.nz + TZ - 1) / TZ));
+  const size_t smem = (size_t)SX * SY * SZ * sizeof(R);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_stage<R, MODE, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr_set = true;
+  }
+  k_stage<R, MODE, EXACT><<<grd, blk, smem, stream()>>>(tm, a);
+  note_launch();
+}
+
+struct RunSpec {
+  int mode;          // ADV_CONST / ADV_FIELD / REINIT
+  int n_steps;
+  int bc;            // LSMGPU_BC_*
+  int use0;
+  double dt, dx, dy, dz;
+  double vconst[3];
+};
+
+// Runs n_steps full TVD-RK3 steps on the caller's phi (device or host).
+template <class R, bool EXACT>
+int run(const char *name, R *phi_user, const Box &gb, const Box &fb, const R *vx, const R *vy, const R *vz,
+        const Box &vb, const RunSpec &rs) {
+  Call call(name);
+  if (!gb.contains(fb, 3, 3, 3)) call.fail("ghost box must hold 3 ghost cells around the fill box");
+  const int nx = (int)fb.n(0), ny = (int)fb.n(1), nz = (int)fb.n(2);
+  if (fb.empty() || nx < 6 || ny < 6 || nz < 6) call.fail("fill box must be at least 6 cells per axis");
+  if (rs.mode == ADV_FIELD && !vb.contains(fb, 0, 0, 0)) call.fail("velocity ghost box does not cover the fill box");
+  if (rs.bc < LSMGPU_BC_PERIODIC || rs.bc > LSMGPU_BC_COPY) {
+    set_error(LSMGPU_ERR_ARGUMENT, "%s: unknown boundary condition %d", name, rs.bc);
+    return LSMGPU_ERR_ARGUMENT;
+  }
+  if (!call.ok()) return LSMGPU_ERR_BOUNDS;
+  if (rs.n_steps <= 0) return LSMGPU_OK;
+
+  R *phi_d = call.inout(phi_user, gb.size());
+  const R *vel_d[3] = {nullptr, nullptr, nullptr};
+  if (rs.mode == ADV_FIELD) {
+    vel_d[0] = call.in(vx, vb.size());
+    vel_d[1] = call.in(vy, vb.size());
+    vel_d[2] = call.in(vz, vb.size());
+  }
+  Layout L = make_layout(nx, ny, nz);
+  const long long ne = L.elems();
+  R *A = call.temp<R>(ne), *B = call.temp<R>(ne), *C = call.temp<R>(ne);
+  R *P0 = (rs.mode == REINIT && rs.use0) ? call.temp<R>(ne) : nullptr;
+  R *V[3] = {nullptr, nullptr, nullptr};
+  if (rs.mode == ADV_FIELD)
+    for (int d = 0; d < 3; d++) V[d] = call.temp<R>(ne);
+  int *err = call.temp<int>(1);
+  if (!call.ok()) return lsmgpu_get_last_error(nullptr, 0);
+
+  cudaStream_t s = stream();
+  cudaMemsetAsync(err, 0, sizeof(int), s);
+  cudaMemsetAsync(B, 0, (size_t)ne * sizeof(R), s);
+  cudaMemsetAsync(C, 0, (size_t)ne * sizeof(R), s);
+  {
+    dim3 blk(32, 4, 2);
+    dim3 grd((unsigned)((nx + 7 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));
+    LSMGPU_LAUNCH(k_pack<R>, grd, blk, 0, A, L, view((const R *)phi_d, gb), gb, fb.lo[0], fb.lo[1], fb.lo[2]);
+    if (rs.mode == ADV_FIELD)
+      for (int d = 0; d < 3; d++)
+        LSMGPU_LAUNCH(k_pack<R>, grd, blk, 0, V[d], L, view(vel_d[d], vb), vb, fb.lo[0], fb.lo[1], fb.lo[2]);
+  }
+  if (P0) cudaMemcpyAsync(P0, A, (size_t)ne * sizeof(R), cudaMemcpyDeviceToDevice, s);
+
+  CUtensorMap tA, tB, tC;
+  const long long ex = (long long)nx + GX + 3, ey = (long long)ny + 2 * GY, ez = (long long)nz + 2 * GZ;
+  if (!encode_tmap_3d(&tA, A, sizeof(R), ex, ey, ez, L.py, L.pz, SX, SY, SZ) ||
+      !encode_tmap_3d(&tB, B, sizeof(R), ex, ey, ez, L.py, L.pz, SX, SY, SZ) ||
+      !encode_tmap_3d(&tC, C, sizeof(R), ex, ey, ez, L.py, L.pz, SX, SY, SZ)) {
+    call.fail("tensor map encoding failed");
+    return LSMGPU_ERR_CUDA;
+  }
+
+  StageArgs<R> a{};
+  a.L = L;
+  a.phi0 = P0;
+  for (int d = 0; d < 3; d++) a.vel[d] = V[d];
+  a.vconst[0] = (R)rs.vconst[0]; a.vconst[1] = (R)rs.vconst[1]; a.vconst[2] = (R)rs.vconst[2];
+  a.inv[0] = R(1.0) / (R)rs.dx; a.inv[1] = R(1.0) / (R)rs.dy; a.inv[2] = R(1.0) / (R)rs.dz;
+  a.dt = (R)rs.dt;
+  {
+    R m = rmax(rmax((R)rs.dx, (R)rs.dy), (R)rs.dz);
+    a.dx_sq = m * m;
+  }
+  a.use0 = rs.use0;
+  a.periodic = rs.bc == LSMGPU_BC_PERIODIC;
+  a.err = err;
+
+  for (int step = 0; step < rs.n_steps; step++) {
+    a.stage = 1; a.phi_n = A; a.out = B;
+    if (rs.mode == REINIT) launch_stage<R, REINIT, EXACT>(tA, a);
+    else if (rs.mode == ADV_CONST) launch_stage<R, ADV_CONST, EXACT>(tA, a);
+    else launch_stage<R, ADV_FIELD, EXACT>(tA, a);
+    launch_bc(B, L, rs.bc);
+    a.stage = 2; a.out = C;
+    if (rs.mode == REINIT) launch_stage<R, REINIT, EXACT>(tB, a);
+    else if (rs.mode == ADV_CONST) launch_stage<R, ADV_CONST, EXACT>(tB, a);
+    else launch_stage<R, ADV_FIELD, EXACT>(tB, a);
+    launch_bc(C, L, rs.bc);
+    a.stage = 3; a.out = A;
+    if (rs.mode == REINIT) launch_stage<R, REINIT, EXACT>(tC, a);
+    else if (rs.mode == ADV_CONST) launch_stage<R, ADV_CONST, EXACT>(tC, a);
+    else launch_stage<R, ADV_FIELD, EXACT>(tC, a);
+    launch_bc(A, L, rs.bc);
+  }
+  {
+    dim3 blk(32, 4, 2);
+    dim3 grd((unsigned)((nx + 6 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));
+    LSMGPU_LAUNCH(k_unpack<R>, grd, blk, 0, view(phi_d, gb), gb, A, L, fb.lo[0], fb.lo[1], fb.lo[2]);
+  }
+  int herr = 0;
+  cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s);
+  call.finish();
+  cudaStreamSynchronize(s);
+  if (herr != 0) {
+    set_error(herr, "%s: a bounded device wait gave up (TMA tile load)", name);
+    return herr;
+  }
+  return lsmgpu_get_last_error(nullptr, 0);
+}
+
+}  // namespace fused
+}  // namespace lsmgpu

@@ -1,0 +1,238 @@
+// Fused TVD Runge-Kutta stage kernels: one kernel per stage computes the
+// HJ WENO5 derivatives, the level-set right-hand side (advection, or the
+// reinitialization Hamiltonian) and the stage update in a single pass, with
+// the periodic ghost images of the result written in the same pass.
+//
+// Work layout in HBM (one buffer per stage field): interior cells (0..nx-1,
+// 0..ny-1, 0..nz-1) with GX = 4 ghost cells below x and 3 above, 3 ghost
+// layers in y and z; rows padded to a multiple of 32 elements so each row
+// starts on a 128-byte boundary.  A CTA of 32 x 8 threads owns a 32 x 8 x 8
+// tile and stages the tile plus its 3-cell halo (40 x 14 x 14 elements) into
+// shared memory with one 3D TMA load; the x origin of the box is the tile's
+// 32-aligned row offset, which satisfies TMA's 16-byte rule for both element
+// sizes.  Each thread then walks the 8 cells of its z column.
+//
+// EXACT selects the FP64 parity arithmetic (LSMLIB's operation order; the
+// including unit is compiled with -fmad=false).  Otherwise the FP32 form runs
+// with FMA contraction and an epsilon-scaled WENO weight formula that cannot
+// under- or overflow in single precision (see weno5_fast).
+#pragma once
+
+#include "lsmgpu_common.cuh"
+#include "stencil_math.cuh"
+#include "tma.cuh"
+
+namespace lsmgpu {
+namespace fused {
+
+constexpr int GX = 4, GY = 3, GZ = 3;
+constexpr int TX = 32, TY = 8, TZ = 8;
+constexpr int SX = TX + 8, SY = TY + 6, SZ = TZ + 6;
+constexpr uint32_t kMaxPolls = 1u << 22;
+
+struct Layout {
+  int nx, ny, nz;
+  long long py, pz;  // element pitches of y and z
+  __host__ __device__ long long idx(int i, int j, int k) const {
+    return (long long)(i + GX) + py * (long long)(j + GY) + pz * (long long)(k + GZ);
+  }
+  __host__ long long elems() const { return pz * (long long)(nz + 2 * GZ); }
+};
+
+inline Layout make_layout(int nx, int ny, int nz) {
+  Layout L;
+  L.nx = nx; L.ny = ny; L.nz = nz;
+  L.py = ((long long)nx + GX + 3 + 31) / 32 * 32;
+  L.pz = L.py * (long long)(ny + 2 * GY);
+  return L;
+}
+
+enum Mode { ADV_CONST = 0, ADV_FIELD = 1, REINIT = 2 };
+
+template <class R>
+struct StageArgs {
+  Layout L;
+  const R *phi_n;    // u^n at the cell (stages 2 and 3)
+  const R *phi0;     // sign source of the phi0 reinitialization form
+  const R *vel[3];   // velocity fields (ADV_FIELD)
+  R *out;
+  R vconst[3];       // constant velocity (ADV_CONST)
+  R inv[3];          // 1/dx, 1/dy, 1/dz
+  R dt, dx_sq;
+  int stage;         // 1, 2 or 3
+  int use0;          // reinitialization sign from phi0
+  int periodic;      // write periodic ghost images of the result
+  int *err;
+};
+
+// ---------------------------------------------------------------------------
+// FP32 arithmetic
+// ---------------------------------------------------------------------------
+// WENO5-JS with the nonlinear weights rewritten as
+//   w_k = d_k prod_{j != k} q_j / sum_i d_i prod_{j != i} q_j,
+//   q_k = (S_k / eps + 1)^2,
+// which equals d_k/(S_k+eps)^2 normalised.  S_k <= 64 max v^2 and
+// eps >= 1e-6 max v^2, so 1 <= q_k <= 4.2e15 and every product stays below
+// 2e31: no underflow to 0/0 on near-flat data (where the direct form's
+// (S+eps)^2 underflows in FP32) and no overflow, with two reciprocals
+// instead of four divisions.
+__device__ __forceinline__ float weno5_fast(float v1, float v2, float v3, float v4, float v5) {
+  const float c13 = 1.f / 3.f, c76 = 7.f / 6.f, c116 = 11.f / 6.f, c16 = 1.f / 6.f, c56 = 5.f / 6.f;
+  const float c1312 = 13.f / 12.f;
+  const float m = fmaxf(fmaxf(fmaxf(v1 * v1, v2 * v2), fmaxf(v3 * v3, v4 * v4)), v5 * v5);
+  const float eps = fmaf(1e-6f, m, 1e-36f);
+  const float p1 = fmaf(c13, v1, fmaf(-c76, v2, c116 * v3));
+  const float p2 = fmaf(-c16, v2, fmaf(c56, v3, c13 * v4));
+  const float p3 = fmaf(c13, v3, fmaf(c56, v4, -c16 * v5));
+  float t = v1 - 2.f * v2 + v3, u = v1 - 4.f * v2 + 3.f * v3;
+  const float S1 = fmaf(c1312 * t, t, 0.25f * u * u);
+  t = v2 - 2.f * v3 + v4; u = v2 - v4;
+  const float S2 = fmaf(c1312 * t, t, 0.25f * u * u);
+  t = v3 - 2.f * v4 + v5; u = 3.f * v3 - 4.f * v4 + v5;
+  const float S3 = fmaf(c1312 * t, t, 0.25f * u * u);
+  const float r = __fdividef(1.f, eps);
+  float q1 = fmaf(S1, r, 1.f), q2 = fmaf(S2, r, 1.f), q3 = fmaf(S3, r, 1.f);
+  q1 *= q1; q2 *= q2; q3 *= q3;
+  const float n1 = 0.1f * (q2 * q3), n2 = 0.6f * (q1 * q3), n3 = 0.3f * (q1 * q2);
+  return __fdividef(fmaf(n1, p1, fmaf(n2, p2, n3 * p3)), n1 + n2 + n3);
+}
+
+template <class R, bool EXACT>
+__device__ __forceinline__ R weno(R v1, R v2, R v3, R v4, R v5) {
+  if constexpr (EXACT) return weno5_exact<R>(v1, v2, v3, v4, v5);
+  else return (R)weno5_fast((float)v1, (float)v2, (float)v3, (float)v4, (float)v5);
+}
+
+// reinitialization RHS; the FP32 form keeps the FP64 zero tolerance so it
+// approximates the FP64 computation, and uses reciprocal square roots
+template <class R, bool EXACT>
+__device__ __forceinline__ R reinit_term(R pc, const R gp[3], const R gm[3], R dx_sq, bool use0) {
+  if constexpr (EXACT) {
+    return reinit_rhs<R>(pc, gp, gm, dx_sq, use0);
+  } else {
+    float st[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const float u = (pc > 0.f) ? fmaxf(-gp[d], 0.f) : fmaxf(gp[d], 0.f);
+      const float w = (pc > 0.f) ? fmaxf(gm[d], 0.f) : fmaxf(-gm[d], 0.f);
+      st[d] = fmaxf(u, w);
+    }
+    if (!(fabsf(pc) >= 1e-11f)) return 0.f;
+    const float n2 = fmaf(st[0], st[0], fmaf(st[1], st[1], st[2] * st[2]));
+    const float den = use0 ? fmaf(pc, pc, (float)dx_sq) : fmaf(pc, pc, n2 * (float)dx_sq);
+    const float sgn = pc * rsqrtf(den);
+    return sgn * (1.f - sqrtf(n2));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// the stage kernel
+// ---------------------------------------------------------------------------
+template <class R, int MODE, bool EXACT>
+__global__ void __launch_bounds__(TX * TY) k_stage(const __grid_constant__ CUtensorMap tm, StageArgs<R> a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  R *tile = reinterpret_cast<R *>(smem_raw);
+  __shared__ __align__(8) uint64_t bar;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int tid = tx + TX * ty;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+
+  if (tid == 0) {
+    prefetch_tmap(&tm);
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    mbar_arrive_expect_tx(&bar, (uint32_t)(SX * SY * SZ * sizeof(R)));
+    // padded coordinates of interior cell (x0 - 4, y0 - 3, z0 - 3)
+    tma_load_3d(tile, &tm, x0 + GX - 4, y0 + GY - 3, z0 + GZ - 3, &bar);
+  }
+  if (!mbar_wait(&bar, 0, kMaxPolls)) {
+    if (tid == 0) atomicExch(a.err, LSMGPU_ERR_TIMEOUT);
+    mbar_wait(&bar, 0, kMaxPolls);  // let an in-flight copy land before exit
+    return;
+  }
+
+  const Layout &L = a.L;
+  const int i = x0 + tx, j = y0 + ty;
+  if (i >= L.nx || j >= L.ny) return;
+  const int sx = tx + 4, sy = ty + 3;
+  const int kmax = min(TZ, L.nz - z0);
+
+  for (int tz = 0; tz < kmax; tz++) {
+    const int k = z0 + tz;
+    const int sz = tz + 3;
+    const R *c = tile + (sz * SY + sy) * SX + sx;
+    const int st[3] = {1, SX, SX * SY};
+    R rhs;
+    if (MODE == REINIT) {
+      R gp[3], gm[3];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        R v[6];  // scaled D1(c-2 .. c+3)
+#pragma unroll
+        for (int f = -2; f <= 3; f++) v[f + 2] = (c[f * st[d]] - c[(f - 1) * st[d]]) * a.inv[d];
+        gp[d] = weno<R, EXACT>(v[5], v[4], v[3], v[2], v[1]);
+        gm[d] = weno<R, EXACT>(v[0], v[1], v[2], v[3], v[4]);
+      }
+      const long long cell = L.idx(i, j, k);
+      const R pc = a.use0 ? a.phi0[cell] : c[0];
+      rhs = reinit_term<R, EXACT>(pc, gp, gm, a.dx_sq, a.use0 != 0);
+    } else {
+      R g[3], vel[3];
+      const long long cell = L.idx(i, j, k);
+#pragma unroll
+      for (int d = 0; d < 3; d++) vel[d] = (MODE == ADV_CONST) ? a.vconst[d] : a.vel[d][cell];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        // spatial_derivatives3d.f.in:2756-2812
+        if (fabs(vel[d]) < Consts<double>::zero_tol) {
+          g[d] = R(0);
+        } else if (vel[d] > R(0)) {
+          R v[5];
+#pragma unroll
+          for (int f = -2; f <= 2; f++) v[f + 2] = (c[f * st[d]] - c[(f - 1) * st[d]]) * a.inv[d];
+          g[d] = weno<R, EXACT>(v[0], v[1], v[2], v[3], v[4]);
+        } else {
+          R v[5];
+#pragma unroll
+          for (int f = -1; f <= 3; f++) v[f + 1] = (c[f * st[d]] - c[(f - 1) * st[d]]) * a.inv[d];
+          g[d] = weno<R, EXACT>(v[4], v[3], v[2], v[1], v[0]);
+        }
+      }
+      // lsm3dZeroOutLevelSetEqnRHS then lsm3dAddAdvectionTermToLSERHS
+      // (level_set_evolution3d.f.in:38, :113-116)
+      rhs = R(0) - (vel[0] * g[0] + vel[1] * g[1] + vel[2] * g[2]);
+    }
+
+    const long long cell = L.idx(i, j, k);
+    R u;
+    if (a.stage == 1) {
+      u = c[0] + a.dt * rhs;  // tvd_runge_kutta3d.f:78
+    } else if (a.stage == 2) {
+      u = R(0.75) * a.phi_n[cell] + R(0.25) * (c[0] + a.dt * rhs);  // :403-404
+    } else {
+      u = R(1.0 / 3.0) * a.phi_n[cell] + R(2.0 / 3.0) * (c[0] + a.dt * rhs);  // :490-492
+    }
+    a.out[cell] = u;
+
+    if (a.periodic) {
+      // periodic images in the ghost layers (3 cells per side)
+      int oi[2] = {0, 0}, oj[2] = {0, 0}, ok_[2] = {0, 0};
+      int ni = 1, nj = 1, nk = 1;
+      if (i < 3) oi[ni++] = L.nx; else if (i >= L.nx - 3) oi[ni++] = -L.nx;
+      if (j < 3) oj[nj++] = L.ny; else if (j >= L.ny - 3) oj[nj++] = -L.ny;
+      if (k < 3) ok_[nk++] = L.nz; else if (k >= L.nz - 3) ok_[nk++] = -L.nz;
+      if (ni + nj + nk > 3) {
+        for (int p = 0; p < ni; p++)
+          for (int q = 0; q < nj; q++)
+            for (int r = 0; r < nk; r++)
+              if (p | q | r) a.out[L.idx(i + oi[p], j + oj[q], k + ok_[r])] = u;
+      }
+    }
+  }
+}
+
+}  // namespace fused
+}  // namespace lsmgpu

@@ -1,0 +1,143 @@
+// lsmgpu — GB300-native level-set kernels behind LSMLIB's C interface.
+//
+// Common device/host helpers: column-major views with arbitrary lower bounds
+// (LSMLIB's a(ilo:ihi, jlo:jhi, klo:khi) layout), launch geometry, and the
+// per-call staging context that lets every C entry point accept either device
+// pointers (used in place, asynchronous on the library stream) or host
+// pointers (copied to device, computed, copied back, synchronous — the
+// semantics LSMLIB's serial Fortran routines have).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "../../include/lsmgpu.h"
+
+namespace lsmgpu {
+
+// ---------------------------------------------------------------------------
+// index spaces
+// ---------------------------------------------------------------------------
+struct Box {
+  int lo[3], hi[3];
+  __host__ __device__ long long n(int d) const { return (long long)hi[d] - lo[d] + 1; }
+  __host__ __device__ long long size() const {
+    long long a = n(0), b = n(1), c = n(2);
+    return (a > 0 && b > 0 && c > 0) ? a * b * c : 0;
+  }
+  __host__ __device__ bool empty() const { return hi[0] < lo[0] || hi[1] < lo[1] || hi[2] < lo[2]; }
+  // true when `o` (grown by `g` cells per side along each axis) fits in this box
+  __host__ bool contains(const Box &o, int gx, int gy, int gz) const {
+    if (o.empty()) return true;
+    return o.lo[0] - gx >= lo[0] && o.hi[0] + gx <= hi[0] && o.lo[1] - gy >= lo[1] &&
+           o.hi[1] + gy <= hi[1] && o.lo[2] - gz >= lo[2] && o.hi[2] + gz <= hi[2];
+  }
+};
+
+inline Box mkbox(const int *ilo, const int *ihi, const int *jlo, const int *jhi,
+                 const int *klo, const int *khi) {
+  Box b;
+  b.lo[0] = *ilo; b.hi[0] = *ihi;
+  b.lo[1] = *jlo; b.hi[1] = *jhi;
+  b.lo[2] = *klo; b.hi[2] = *khi;
+  return b;
+}
+
+// A device view of one column-major array.
+template <class T>
+struct View {
+  T *p;
+  int lo0, lo1, lo2;
+  long long s1, s2;
+  __device__ __forceinline__ long long off(int i, int j, int k) const {
+    return (long long)(i - lo0) + s1 * (long long)(j - lo1) + s2 * (long long)(k - lo2);
+  }
+  __device__ __forceinline__ T &operator()(int i, int j, int k) const { return p[off(i, j, k)]; }
+  __device__ __forceinline__ long long stride(int d) const { return d == 0 ? 1 : (d == 1 ? s1 : s2); }
+};
+
+template <class T>
+inline View<T> view(T *p, const Box &b) {
+  View<T> v;
+  v.p = p;
+  v.lo0 = b.lo[0]; v.lo1 = b.lo[1]; v.lo2 = b.lo[2];
+  v.s1 = b.n(0);
+  v.s2 = b.n(0) * b.n(1);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// launch geometry over a fill box: x fastest, one thread per cell
+// ---------------------------------------------------------------------------
+struct Grid3 {
+  dim3 grid, block;
+};
+inline Grid3 cover(const Box &fb, int bx = 32, int by = 4, int bz = 2) {
+  Grid3 g;
+  g.block = dim3(bx, by, bz);
+  g.grid = dim3((unsigned)((fb.n(0) + bx - 1) / bx), (unsigned)((fb.n(1) + by - 1) / by),
+                (unsigned)((fb.n(2) + bz - 1) / bz));
+  return g;
+}
+
+#define LSMGPU_CELL_INDEX(fb, i, j, k)                 \
+  const int i = (fb).lo[0] + blockIdx.x * blockDim.x + threadIdx.x; \
+  const int j = (fb).lo[1] + blockIdx.y * blockDim.y + threadIdx.y; \
+  const int k = (fb).lo[2] + blockIdx.z * blockDim.z + threadIdx.z; \
+  if (i > (fb).hi[0] || j > (fb).hi[1] || k > (fb).hi[2]) return;
+
+// ---------------------------------------------------------------------------
+// runtime (runtime.cu)
+// ---------------------------------------------------------------------------
+cudaStream_t stream();                      // library stream (lsmgpu_set_stream)
+void note_launch();                         // counts kernels for lsmgpu_launch_count()
+void set_error(int code, const char *fmt, ...);
+void clear_error();
+bool cuda_ok(cudaError_t e, const char *what);  // records and returns false on error
+
+// Per-call staging context.
+class Call {
+ public:
+  explicit Call(const char *name);
+  ~Call();
+  // Array arguments.  `n` is the element count of the array's ghost box.
+  // in():    read by the kernel
+  // inout(): read and written (output arrays keep cells the kernel does not
+  //          touch, so a host-resident output is copied both ways)
+  // out():   written in full by the kernel (no copy in)
+  template <class T> T *in(const T *p, long long n) { return (T *)stage(p, n * (long long)sizeof(T), true, false); }
+  template <class T> T *inout(T *p, long long n) { return (T *)stage(p, n * (long long)sizeof(T), true, true); }
+  template <class T> T *out(T *p, long long n) { return (T *)stage(p, n * (long long)sizeof(T), false, true); }
+  // Device-only temporary memory for this call.
+  template <class T> T *temp(long long n) { return (T *)arena_alloc(n * (long long)sizeof(T)); }
+  // Scalar output written by a kernel into device memory and copied to *dst
+  // (host or device) by finish().
+  template <class T> T *scalar_out(T *dst) { return (T *)scalar(dst, sizeof(T)); }
+  bool ok() const { return ok_; }
+  bool host_staged() const { return host_staged_; }
+  // Launch check + copies back + synchronisation when anything was staged.
+  void finish();
+  void fail(const char *msg);
+
+ private:
+  void *stage(const void *p, long long bytes, bool copy_in, bool copy_out);
+  void *scalar(void *dst, size_t bytes);
+  void *arena_alloc(long long bytes);
+  const char *name_;
+  bool ok_ = true, host_staged_ = false, finished_ = false, need_sync_ = false;
+  struct Back { void *host; void *dev; long long bytes; };
+  Back backs_[64];
+  int nback_ = 0;
+  long long arena_mark_ = 0;
+  bool locked_ = false;
+};
+
+// Launch `kern` on the library stream and count it.
+#define LSMGPU_LAUNCH(kern, grid, block, smem, ...)                       \
+  do {                                                                    \
+    kern<<<(grid), (block), (smem), ::lsmgpu::stream()>>>(__VA_ARGS__);   \
+    ::lsmgpu::note_launch();                                              \
+  } while (0)
+
+}  // namespace lsmgpu

@@ -1,0 +1,238 @@
+// Runtime services for the C entry points: status side channel, library
+// stream, launch counting, a grow-only device arena for staged host arrays and
+// temporaries, and the per-call staging context.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <atomic>
+#include <mutex>
+#include <vector>
+
+#include "lsmgpu_common.cuh"
+
+namespace lsmgpu {
+
+namespace {
+
+thread_local int g_err = LSMGPU_OK;
+thread_local char g_msg[512] = "";
+std::atomic<cudaStream_t> g_stream{nullptr};
+std::atomic<long long> g_launches{0};
+
+// Device arena: a list of chunks per device, bump-allocated, reset at the
+// start of each call.  All users run in the library stream's order, so memory
+// handed out by one call may be reused by the next.
+struct Chunk { char *p; long long cap; };
+struct Arena {
+  std::vector<Chunk> chunks;
+  int cur = 0;
+  long long used = 0;
+};
+std::mutex g_lock;
+Arena g_arena[64];
+
+}  // namespace
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+cudaStream_t stream() { return g_stream.load(); }
+
+void set_error(int code, const char *fmt, ...) {
+  g_err = code;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_msg, sizeof(g_msg), fmt, ap);
+  va_end(ap);
+}
+
+void clear_error() {
+  g_err = LSMGPU_OK;
+  g_msg[0] = 0;
+}
+
+bool cuda_ok(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return true;
+  set_error(LSMGPU_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return false;
+}
+
+Call::Call(const char *name) : name_(name) {
+  clear_error();
+  g_lock.lock();
+  locked_ = true;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  Arena &a = g_arena[dev & 63];
+  a.cur = 0;
+  a.used = 0;
+}
+
+Call::~Call() {
+  if (!finished_) finish();
+  if (locked_) g_lock.unlock();
+}
+
+void Call::fail(const char *msg) {
+  if (ok_) set_error(LSMGPU_ERR_BOUNDS, "%s: %s", name_, msg);
+  ok_ = false;
+}
+
+void *Call::arena_alloc(long long bytes) {
+  if (!ok_) return nullptr;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  Arena &a = g_arena[dev & 63];
+  long long need = (bytes + 255) & ~255LL;
+  if (need == 0) need = 256;
+  while (a.cur < (int)a.chunks.size()) {
+    Chunk &c = a.chunks[a.cur];
+    if (a.used + need <= c.cap) {
+      void *p = c.p + a.used;
+      a.used += need;
+      return p;
+    }
+    a.cur++;
+    a.used = 0;
+  }
+  long long cap = need < (64LL << 20) ? (64LL << 20) : need;
+  void *p = nullptr;
+  if (!cuda_ok(cudaMalloc(&p, (size_t)cap), "cudaMalloc(arena)")) {
+    ok_ = false;
+    return nullptr;
+  }
+  a.chunks.push_back({(char *)p, cap});
+  a.cur = (int)a.chunks.size() - 1;
+  a.used = need;
+  return p;
+}
+
+void *Call::stage(const void *p, long long bytes, bool copy_in, bool copy_out) {
+  if (!ok_) return nullptr;
+  if (p == nullptr) {
+    set_error(LSMGPU_ERR_ARGUMENT, "%s: null array pointer", name_);
+    ok_ = false;
+    return nullptr;
+  }
+  cudaPointerAttributes attr;
+  cudaError_t e = cudaPointerGetAttributes(&attr, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    attr.type = cudaMemoryTypeUnregistered;
+  }
+  if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) return (void *)p;
+  // host memory: stage through the arena
+  host_staged_ = true;
+  need_sync_ = true;
+  void *d = arena_alloc(bytes);
+  if (!d) return nullptr;
+  if (copy_in && bytes > 0) {
+    if (!cuda_ok(cudaMemcpyAsync(d, p, (size_t)bytes, cudaMemcpyHostToDevice, stream()),
+                 "cudaMemcpyAsync(H2D)")) {
+      ok_ = false;
+      return nullptr;
+    }
+  }
+  if (copy_out) {
+    if (nback_ >= 64) {
+      set_error(LSMGPU_ERR_ARGUMENT, "%s: too many staged outputs", name_);
+      ok_ = false;
+      return nullptr;
+    }
+    backs_[nback_++] = {(void *)p, d, bytes};
+  }
+  return d;
+}
+
+void *Call::scalar(void *dst, size_t bytes) {
+  if (!ok_) return nullptr;
+  if (dst == nullptr) {
+    set_error(LSMGPU_ERR_ARGUMENT, "%s: null scalar output", name_);
+    ok_ = false;
+    return nullptr;
+  }
+  void *d = arena_alloc((long long)bytes);
+  if (!d) return nullptr;
+  cudaPointerAttributes attr;
+  cudaError_t e = cudaPointerGetAttributes(&attr, dst);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    attr.type = cudaMemoryTypeUnregistered;
+  }
+  if (!(attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged)) need_sync_ = true;
+  backs_[nback_++] = {dst, d, (long long)bytes};
+  return d;
+}
+
+void Call::finish() {
+  if (finished_) return;
+  finished_ = true;
+  if (ok_) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_error(LSMGPU_ERR_CUDA, "%s: kernel launch: %s", name_, cudaGetErrorString(e));
+      ok_ = false;
+    }
+  }
+  if (ok_) {
+    for (int b = 0; b < nback_; b++) {
+      if (backs_[b].bytes <= 0) continue;
+      if (!cuda_ok(cudaMemcpyAsync(backs_[b].host, backs_[b].dev, (size_t)backs_[b].bytes,
+                                   cudaMemcpyDefault, stream()),
+                   "cudaMemcpyAsync(D2H)")) {
+        ok_ = false;
+        break;
+      }
+    }
+  }
+  if (need_sync_) {
+    cudaError_t e = cudaStreamSynchronize(stream());
+    if (ok_ && e != cudaSuccess) {
+      set_error(LSMGPU_ERR_CUDA, "%s: %s", name_, cudaGetErrorString(e));
+      ok_ = false;
+    }
+  }
+  if (locked_) {
+    locked_ = false;
+    g_lock.unlock();
+  }
+}
+
+}  // namespace lsmgpu
+
+using namespace lsmgpu;
+
+extern "C" {
+
+int lsmgpu_get_last_error(char *msg, int len) {
+  if (msg && len > 0) {
+    strncpy(msg, g_msg, (size_t)len - 1);
+    msg[len - 1] = 0;
+  }
+  return g_err;
+}
+
+void lsmgpu_set_stream(void *s) {
+  cudaStream_t old = g_stream.load();
+  if (old != (cudaStream_t)s) {
+    // the arena is reused in stream order: drain the old stream first
+    std::lock_guard<std::mutex> guard(g_lock);
+    cudaStreamSynchronize(old);
+    g_stream.store((cudaStream_t)s);
+  }
+}
+
+void *lsmgpu_get_stream(void) { return (void *)g_stream.load(); }
+
+int lsmgpu_synchronize(void) {
+  clear_error();
+  if (!cuda_ok(cudaStreamSynchronize(g_stream.load()), "cudaStreamSynchronize")) return g_err;
+  return LSMGPU_OK;
+}
+
+long long lsmgpu_launch_count(void) { return g_launches.load(); }
+void lsmgpu_reset_launch_count(void) { g_launches.store(0); }
+
+const char *lsmgpu_version(void) { return "lsmgpu 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,211 @@
+// Per-cell stencil arithmetic shared by the drop-in kernels and the fused
+// stage kernels.
+//
+// Every routine here evaluates one LSMLIB formula on values already in
+// registers, with the operations in the order LSMLIB's Fortran performs them:
+// translation units that include this header for the FP64 parity form are
+// compiled with -fmad=false, so each product and sum rounds exactly as the
+// reference's does and the results are bit-identical to it.
+//
+// Index convention (LSMLIB spatial_derivatives3d.f.in:19-45): the first
+// undivided difference D1(i) = phi(i) - phi(i-1) sits on the face between
+// cells i-1 and i.  For a cell c, `a[m]` holds phi(c + m - 3), m = 0..6, so
+// D1(c+f) = a[f+3] - a[f+2].
+#pragma once
+
+namespace lsmgpu {
+
+template <class R>
+__host__ __device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : b; }
+template <class R>
+__host__ __device__ __forceinline__ R rmin(R a, R b) { return a < b ? a : b; }
+
+// LSMLIB template constants for the FP64 build (src/CMakeLists.txt:10-20).
+template <class R> struct Consts;
+template <> struct Consts<double> {
+  static constexpr double zero_tol = 1.e-11;
+  static constexpr double tiny = 1.e-36;
+};
+template <> struct Consts<float> {
+  static constexpr float zero_tol = 1.e-5f;
+  static constexpr float tiny = 1.e-36f;
+};
+
+// Undivided differences around one cell along one axis.
+template <class R>
+struct Diffs {
+  R d1[6];  // D1(c+f), f = -2..3
+  R d2[5];  // D2(c+f), f = -2..2
+  R d3[4];  // D3(c+f), f = -1..2
+  __device__ __forceinline__ R D1(int f) const { return d1[f + 2]; }
+  __device__ __forceinline__ R D2(int f) const { return d2[f + 2]; }
+  __device__ __forceinline__ R D3(int f) const { return d3[f + 1]; }
+};
+
+// order: 1 (D1 only), 2 (D1, D2), 3 (D1, D2, D3).  lsm3dComputeDn
+// (spatial_derivatives3d.f.in:49-176): odd n subtracts the left neighbour,
+// even n negates (Dn-1(i) - Dn-1(i+1)), which equals Dn-1(i+1) - Dn-1(i)
+// exactly.
+template <class R, int ORDER>
+__device__ __forceinline__ void make_diffs(Diffs<R> &d, const R a[7]) {
+#pragma unroll
+  for (int f = -2; f <= 3; f++) d.d1[f + 2] = a[f + 3] - a[f + 2];
+  if (ORDER >= 2) {
+#pragma unroll
+    for (int f = -2; f <= 2; f++) d.d2[f + 2] = d.d1[f + 3] - d.d1[f + 2];
+  }
+  if (ORDER >= 3) {
+#pragma unroll
+    for (int f = -1; f <= 2; f++) d.d3[f + 1] = d.d2[f + 2] - d.d2[f + 1];
+  }
+}
+
+// ENO1 (spatial_derivatives3d.f.in:299-300)
+template <class R> __device__ __forceinline__ R eno1_plus(const Diffs<R> &d, R inv) { return d.D1(1) * inv; }
+template <class R> __device__ __forceinline__ R eno1_minus(const Diffs<R> &d, R inv) { return d.D1(0) * inv; }
+
+// ENO2 (spatial_derivatives3d.f.in:520-535)
+template <class R>
+__device__ __forceinline__ R eno2_plus(const Diffs<R> &d, R inv) {
+  const R h = R(0.5);
+  R c = (fabs(d.D2(0)) < fabs(d.D2(1))) ? d.D2(0) : d.D2(1);
+  return (d.D1(1) - h * c) * inv;
+}
+template <class R>
+__device__ __forceinline__ R eno2_minus(const Diffs<R> &d, R inv) {
+  const R h = R(0.5);
+  R c = (fabs(d.D2(-1)) < fabs(d.D2(0))) ? d.D2(-1) : d.D2(0);
+  return (d.D1(0) + h * c) * inv;
+}
+
+// ENO3 (spatial_derivatives3d.f.in:842-896)
+template <class R>
+__device__ __forceinline__ R eno3_plus(const Diffs<R> &d, R inv) {
+  const R third = R(1.0 / 3.0), sixth = R(1.0 / 6.0), h = R(0.5);
+  R x = d.D1(1);
+  if (fabs(d.D2(0)) < fabs(d.D2(1))) {
+    x = x - h * d.D2(0);
+    R c = (fabs(d.D3(0)) < fabs(d.D3(1))) ? d.D3(0) : d.D3(1);
+    x = x - sixth * c;
+  } else {
+    x = x - h * d.D2(1);
+    R c = (fabs(d.D3(1)) < fabs(d.D3(2))) ? d.D3(1) : d.D3(2);
+    x = x + third * c;
+  }
+  return x * inv;
+}
+template <class R>
+__device__ __forceinline__ R eno3_minus(const Diffs<R> &d, R inv) {
+  const R third = R(1.0 / 3.0), sixth = R(1.0 / 6.0), h = R(0.5);
+  R x = d.D1(0);
+  if (fabs(d.D2(-1)) < fabs(d.D2(0))) {
+    x = x + h * d.D2(-1);
+    R c = (fabs(d.D3(-1)) < fabs(d.D3(0))) ? d.D3(-1) : d.D3(0);
+    x = x + third * c;
+  } else {
+    x = x + h * d.D2(0);
+    R c = (fabs(d.D3(0)) < fabs(d.D3(1))) ? d.D3(0) : d.D3(1);
+    x = x - sixth * c;
+  }
+  return x * inv;
+}
+
+// WENO5-JS on five scaled first differences, in the exact form of
+// spatial_derivatives3d.f.in:1296-1323 (parity form).
+template <class R>
+__device__ __forceinline__ R weno5_exact(R v1, R v2, R v3, R v4, R v5) {
+  const R c13 = R(1.0 / 3.0), c76 = R(7.0 / 6.0), c116 = R(11.0 / 6.0);
+  const R c16 = R(1.0 / 6.0), c56 = R(5.0 / 6.0), c1312 = R(13.0 / 12.0);
+  const R c14 = R(0.25);
+  R m = v1 * v1;
+  m = rmax(m, v2 * v2);
+  m = rmax(m, v3 * v3);
+  m = rmax(m, v4 * v4);
+  m = rmax(m, v5 * v5);
+  const R eps = R(1e-6) * m + Consts<R>::tiny;
+  const R p1 = c13 * v1 - c76 * v2 + c116 * v3;
+  const R p2 = -(c16 * v2) + c56 * v3 + c13 * v4;
+  const R p3 = c13 * v3 + c56 * v4 - c16 * v5;
+  R t = v1 - R(2.0) * v2 + v3;
+  R u = v1 - R(4.0) * v2 + R(3.0) * v3;
+  const R S1 = c1312 * (t * t) + c14 * (u * u);
+  t = v2 - R(2.0) * v3 + v4;
+  u = v2 - v4;
+  const R S2 = c1312 * (t * t) + c14 * (u * u);
+  t = v3 - R(2.0) * v4 + v5;
+  u = R(3.0) * v3 - R(4.0) * v4 + v5;
+  const R S3 = c1312 * (t * t) + c14 * (u * u);
+  R a1 = R(0.1) / ((S1 + eps) * (S1 + eps));
+  R a2 = R(0.6) / ((S2 + eps) * (S2 + eps));
+  R a3 = R(0.3) / ((S3 + eps) * (S3 + eps));
+  const R inv_sum = R(1.0) / (a1 + a2 + a3);
+  a1 = a1 * inv_sum;
+  a2 = a2 * inv_sum;
+  a3 = a3 * inv_sum;
+  return a1 * p1 + a2 * p2 + a3 * p3;
+}
+
+// plus side: v = D1(c+3..c-1); minus side: v = D1(c-2..c+2)
+// (spatial_derivatives3d.f.in:1286-1367)
+template <class R>
+__device__ __forceinline__ R weno5_plus(const Diffs<R> &d, R inv) {
+  return weno5_exact<R>(d.D1(3) * inv, d.D1(2) * inv, d.D1(1) * inv, d.D1(0) * inv, d.D1(-1) * inv);
+}
+template <class R>
+__device__ __forceinline__ R weno5_minus(const Diffs<R> &d, R inv) {
+  return weno5_exact<R>(d.D1(-2) * inv, d.D1(-1) * inv, d.D1(0) * inv, d.D1(1) * inv, d.D1(2) * inv);
+}
+
+// Godunov |grad phi|^2 of level_set_evolution3d.f.in:210-223 for normal
+// speed sign `pos` (vn > 0).
+template <class R>
+__device__ __forceinline__ R godunov_normal_sq(bool pos, const R p[3], const R m[3]) {
+  R s = R(0);
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    R a, b;
+    if (pos) {
+      a = rmax(m[d], R(0));
+      b = rmin(p[d], R(0));
+    } else {
+      a = rmin(m[d], R(0));
+      b = rmax(p[d], R(0));
+    }
+    const R t = rmax(a * a, b * b);
+    s = (d == 0) ? t : s + t;
+  }
+  return s;
+}
+
+// Reinitialization right-hand side of reinitialization3d.f.in:159-199 (Peng
+// form, use0 = false) and :217-256 (phi0 form, use0 = true).  `pc` is phi
+// (or phi0) at the cell.
+template <class R>
+__device__ __forceinline__ R reinit_rhs(R pc, const R gp[3], const R gm[3], R dx_sq, bool use0) {
+  R st[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    R u, w;
+    if (pc > R(0)) {
+      u = rmax(-gp[d], R(0));
+      w = rmax(gm[d], R(0));
+    } else {
+      u = rmax(gp[d], R(0));
+      w = rmax(-gm[d], R(0));
+    }
+    st[d] = rmax(u, w);
+  }
+  if (!(fabs(pc) >= Consts<R>::zero_tol)) return R(0);
+  const R n2 = st[0] * st[0] + st[1] * st[1] + st[2] * st[2];
+  const R sgn = use0 ? pc / sqrt(pc * pc + dx_sq) : pc / sqrt(pc * pc + n2 * dx_sq);
+  return sgn * (R(1.0) - sqrt(n2));
+}
+
+// Curvature numerator in the term order of curvature3d.f.in:109-117.
+template <class R>
+__device__ __forceinline__ R curv_numerator(R xx, R yy, R zz, R xy, R xz, R yz, R x, R y, R z) {
+  return xx * y * y + yy * x * x - R(2) * xy * x * y + xx * z * z + zz * x * x - R(2) * xz * x * z +
+         yy * z * z + zz * y * y - R(2) * yz * y * z;
+}
+
+}  // namespace lsmgpu

@@ -1,0 +1,109 @@
+"""Multi-step runs composed from the oracle's LSMLIB-signature routines, the
+way LSMLIB's drivers compose them (per stage: derivatives -> RHS -> TVD-RK3
+stage -> ghost fill).  These are the references the fused GPU steppers are
+checked against."""
+import numpy as np
+
+import lsmlib_gb300 as L
+from tests import harness as H
+
+BC_FNS = {L.BC_LINEAR: "lsm3dlinearextrapolation_",
+          L.BC_SIGNED_LINEAR: "lsm3dsignedlinearextrapolation_",
+          L.BC_COPY: "lsm3dcopyextrapolation_"}
+
+_BC_ABI = {
+    name: {"args": [["phi", "real", True, True]] +
+           [[n, "int", False, False] for n in
+            ("ilo_gb", "ihi_gb", "jlo_gb", "jhi_gb", "klo_gb", "khi_gb",
+             "ilo_fb", "ihi_fb", "jlo_fb", "jhi_fb", "klo_fb", "khi_fb", "bdry_location_idx")]}
+    for name in BC_FNS.values()}
+
+
+def periodic_fill(phi, gb, fb):
+    """Periodic images in the 3 ghost layers around fb (all faces, edges and
+    corners), in place."""
+    n = [fb[1] - fb[0] + 1, fb[3] - fb[2] + 1, fb[5] - fb[4] + 1]
+    idx = []
+    for a in range(3):
+        lo, hi = fb[2 * a] - 3, fb[2 * a + 1] + 3
+        full = np.arange(lo, hi + 1)
+        src = (full - fb[2 * a]) % n[a] + fb[2 * a]
+        idx.append((full - gb[2 * a], src - gb[2 * a]))
+    (dx_, sx_), (dy_, sy_), (dz_, sz_) = idx
+    phi[np.ix_(dx_, dy_, dz_)] = phi[np.ix_(sx_, sy_, sz_)].copy()
+
+
+def apply_bc(lib, phi, gb, fb, bc):
+    if bc == L.BC_PERIODIC:
+        periodic_fill(phi, gb, fb)
+        return
+    name = BC_FNS[bc]
+    for face in range(6):
+        vals = {"phi": phi, "bdry_location_idx": face}
+        for n_, v in zip(("ilo_gb", "ihi_gb", "jlo_gb", "jhi_gb", "klo_gb", "khi_gb"), gb):
+            vals[n_] = v
+        for n_, v in zip(("ilo_fb", "ihi_fb", "jlo_fb", "jhi_fb", "klo_fb", "khi_fb"), fb):
+            vals[n_] = v
+        L.invoke(lib, name, vals, abi=_BC_ABI)
+
+
+def _rhs(lib, mode, phi, gb, fb, dx, vel, phi0, use0):
+    shape = H.shape_of(gb)
+    z = lambda: np.zeros(shape, order="F")
+    if mode == "reinit":
+        pp = [z(), z(), z()]
+        pm = [z(), z(), z()]
+        vals, _ = H.make_call("lsm3dhjweno5_", gb, fb, arrays={
+            "phi": phi, "phi_x_plus": pp[0], "phi_y_plus": pp[1], "phi_z_plus": pp[2],
+            "phi_x_minus": pm[0], "phi_y_minus": pm[1], "phi_z_minus": pm[2]},
+            scalars={"dx": dx, "dy": dx, "dz": dx})
+        L.invoke(lib, "lsm3dhjweno5_", vals)
+        rhs = z()
+        vals, _ = H.make_call("lsm3dcomputereinitializationeqnrhs_", gb, fb, arrays={
+            "reinit_rhs": rhs, "phi": phi, "phi0": phi0, "phi_x_plus": pp[0],
+            "phi_y_plus": pp[1], "phi_z_plus": pp[2], "phi_x_minus": pm[0],
+            "phi_y_minus": pm[1], "phi_z_minus": pm[2]},
+            scalars={"dx": dx, "dy": dx, "dz": dx, "use_phi0_for_sgn": use0})
+        L.invoke(lib, "lsm3dcomputereinitializationeqnrhs_", vals)
+        return rhs
+    g = [z(), z(), z()]
+    vals, _ = H.make_call("lsm3dupwindhjweno5_", gb, fb, arrays={
+        "phi": phi, "phi_x": g[0], "phi_y": g[1], "phi_z": g[2],
+        "vel_x": vel[0], "vel_y": vel[1], "vel_z": vel[2]}, scalars={"dx": dx, "dy": dx, "dz": dx})
+    L.invoke(lib, "lsm3dupwindhjweno5_", vals)
+    rhs = np.asfortranarray(np.random.default_rng(0).standard_normal(shape))
+    vals, _ = H.make_call("lsm3dzerooutlevelseteqnrhs_", gb, fb, arrays={"lse_rhs": rhs})
+    L.invoke(lib, "lsm3dzerooutlevelseteqnrhs_", vals)
+    vals, _ = H.make_call("lsm3daddadvectiontermtolserhs_", gb, fb, arrays={
+        "lse_rhs": rhs, "phi_x": g[0], "phi_y": g[1], "phi_z": g[2],
+        "vel_x": vel[0], "vel_y": vel[1], "vel_z": vel[2]})
+    L.invoke(lib, "lsm3daddadvectiontermtolserhs_", vals)
+    return rhs
+
+
+def tvdrk3_run(lib, mode, phi, gb, fb, dx, dt, n_steps, bc, vel=None, use0=0):
+    """n_steps TVD-RK3 steps of advection ('advect', velocity fields `vel`)
+    or reinitialization ('reinit'); returns the new phi (input untouched)."""
+    phi = phi.copy(order="F")
+    phi0 = phi.copy(order="F")
+    for _ in range(n_steps):
+        u1 = np.zeros_like(phi, order="F")
+        rhs = _rhs(lib, mode, phi, gb, fb, dx, vel, phi0, use0)
+        vals, _ = H.make_call("lsm3dtvdrk3stage1_", gb, fb, arrays={
+            "u_stage1": u1, "u_cur": phi, "rhs": rhs}, scalars={"dt": dt})
+        L.invoke(lib, "lsm3dtvdrk3stage1_", vals)
+        apply_bc(lib, u1, gb, fb, bc)
+        u2 = np.zeros_like(phi, order="F")
+        rhs = _rhs(lib, mode, u1, gb, fb, dx, vel, phi0, use0)
+        vals, _ = H.make_call("lsm3dtvdrk3stage2_", gb, fb, arrays={
+            "u_stage2": u2, "u_stage1": u1, "u_cur": phi, "rhs": rhs}, scalars={"dt": dt})
+        L.invoke(lib, "lsm3dtvdrk3stage2_", vals)
+        apply_bc(lib, u2, gb, fb, bc)
+        un = np.zeros_like(phi, order="F")
+        rhs = _rhs(lib, mode, u2, gb, fb, dx, vel, phi0, use0)
+        vals, _ = H.make_call("lsm3dtvdrk3stage3_", gb, fb, arrays={
+            "u_next": un, "u_stage2": u2, "u_cur": phi, "rhs": rhs}, scalars={"dt": dt})
+        L.invoke(lib, "lsm3dtvdrk3stage3_", vals)
+        apply_bc(lib, un, gb, fb, bc)
+        phi = un
+    return phi
