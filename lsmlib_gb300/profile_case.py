@@ -1,0 +1,52 @@
+"""Run one fused call of the level-set hot path on cuda:0, for profilers.
+
+  python -m lsmlib_gb300.profile_case --mode reinit --n 256 --iters 1 --precision f32
+
+Builds the same analytic field as bench.py, moves it to the device, and runs
+`iters` WENO5 / TVD-RK3 iterations (3 stage kernels each) of reinitialization
+or constant-velocity advection, then the mean curvature.  The stage kernels
+are k_stage<float|double, mode>; ncu can select them with -k regex:k_stage.
+"""
+import argparse
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--mode", choices=["reinit", "advect"], default="reinit")
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--iters", type=int, default=1)
+    ap.add_argument("--precision", choices=["f32", "f64"], default="f32")
+    ap.add_argument("--bc", type=int, default=2)
+    a = ap.parse_args()
+    import torch
+    import lsmlib_gb300 as L
+    from lsmlib_gb300 import build as B
+    import bench
+    B.build()
+    L.set_stream(torch.cuda.current_stream().cuda_stream)
+    gb, fb = bench.boxes(a.n)
+    phi64, dx = bench.initial_phi(a.n)
+    dt = torch.float32 if a.precision == "f32" else torch.float64
+    phi = torch.from_numpy(np.ascontiguousarray(phi64.T)).cuda().to(dt)
+    kappa = torch.zeros_like(phi)
+    if a.mode == "reinit":
+        L.reinit_weno5_tvdrk3(phi, gb, fb, dx, 0.5 * dx, a.iters, use_phi0_for_sgn=1, bc=a.bc,
+                              precision=a.precision)
+    else:
+        L.advect_weno5_tvdrk3(phi, gb, fb, dx, dx / 3.5, a.iters, vel_const=(1.0, 0.5, 0.25),
+                              bc=a.bc, precision=a.precision)
+    L.mean_curvature_o2(kappa, gb, phi, gb, fb, dx, precision=a.precision)
+    torch.cuda.synchronize()
+    L.check()
+    print("ok", a.mode, a.n, a.iters, a.precision, "launches", L.launch_count())
+
+
+if __name__ == "__main__":
+    main()
