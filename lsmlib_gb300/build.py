@@ -21,7 +21,7 @@ LIB = os.path.join(HERE, "liblsmgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-          "--expt-relaxed-constexpr", "-I", os.path.join(HERE, "..", "include")]
+          "--expt-relaxed-constexpr", "--extended-lambda", "-I", os.path.join(HERE, "..", "include")]
 
 # FP64 parity units: no contraction of a*b+c into FMA
 NO_FMA = {"dense.cu", "local.cu", "fused_f64.cu", "narrowband.cu", "batched_f64.cu"}
