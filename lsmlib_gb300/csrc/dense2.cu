@@ -1,0 +1,245 @@
+// Further drop-in dense entry points: central Hessian, averaged and upwinded
+// gradients, the two LSE terms whose loops mix the fill box and the ghost box,
+// and the ghost-cell boundary conditions.  FP64 parity form (compiled with
+// -fmad=false).
+#include "lsmgpu_common.cuh"
+#include "stencil_math.cuh"
+#include "../../include/lsmgpu_toolbox3d.h"
+
+namespace lsmgpu {
+namespace {
+
+typedef double R;
+
+#define BOXARG(b) const int *b##_ilo, const int *b##_ihi, const int *b##_jlo, const int *b##_jhi, const int *b##_klo, const int *b##_khi
+#define BOXOF(b) mkbox(b##_ilo, b##_ihi, b##_jlo, b##_jhi, b##_klo, b##_khi)
+
+template <class F>
+__global__ void k_box(F f, Box b) {
+  LSMGPU_CELL_INDEX(b, i, j, k);
+  f(i, j, k);
+}
+template <class F>
+void for_box(const Box &b, F f) {
+  if (b.empty()) return;
+  Grid3 g = cover(b);
+  LSMGPU_LAUNCH(k_box<F>, g.grid, g.block, 0, f, b);
+}
+
+View<const R> vin(Call &c, const R *p, const Box &b) { return view((const R *)c.in(p, b.size()), b); }
+View<R> vio(Call &c, R *p, const Box &b) { return view(c.inout(p, b.size()), b); }
+
+// one axis of the combined Godunov selection (level_set_evolution3d.f.in:630-649)
+__device__ __forceinline__ R ext_pick(R v, R vn, R p, R m) {
+  const R hp = v + vn * p, hm = v + vn * m;
+  if (hp > R(0)) return (hm > R(0)) ? m : -v / vn;
+  if (hm < R(0)) return p;
+  return (fabs(hp) > fabs(hm)) ? p : m;
+}
+
+// boundary conditions (boundary_conditions3d.f:46-639)
+enum { BC_LINEAR, BC_SIGNED, BC_COPY };
+
+void face_extrapolate(const char *name, R *phi, const Box &gb, const Box &fb, int face, int kind) {
+  Call call(name);
+  if (face < 0 || face > 5) return;  // the reference does nothing for other values
+  const int axis = face / 2, upper = face % 2;
+  const int edge = upper ? fb.hi[axis] : fb.lo[axis];
+  const int inner = upper ? edge - 1 : edge + 1;
+  if (edge < gb.lo[axis] || edge > gb.hi[axis] || (kind != BC_COPY && (inner < gb.lo[axis] || inner > gb.hi[axis])))
+    call.fail("fill-box edge outside the ghost box");
+  if (!call.ok()) return;
+  View<R> P = vio(call, phi, gb);
+  if (!call.ok()) return;
+  Box plane = gb;  // one thread per line through the face
+  plane.lo[axis] = plane.hi[axis] = 0;
+  const int first = upper ? edge + 1 : gb.lo[axis];
+  const int last = upper ? gb.hi[axis] : edge - 1;
+  if (last < first) return;
+  for_box(plane, [=] __device__(int i, int j, int k) {
+    int c[3] = {i, j, k};
+    c[axis] = edge;
+    const R e = P(c[0], c[1], c[2]);
+    R slope = R(0);
+    if (kind != BC_COPY) {
+      c[axis] = inner;
+      const R nx = P(c[0], c[1], c[2]);
+      slope = (kind == BC_LINEAR) ? e - nx : copysign(R(1.0), e) * fabs(e - nx);
+    }
+    for (int m = first; m <= last; m++) {
+      c[axis] = m;
+      if (kind == BC_COPY)
+        P(c[0], c[1], c[2]) = e;
+      else
+        P(c[0], c[1], c[2]) = e + slope * (R)(upper ? m - edge : edge - m);
+    }
+  });
+  call.finish();
+}
+
+}  // namespace
+}  // namespace lsmgpu
+
+using namespace lsmgpu;
+
+extern "C" {
+
+void lsm3dcentralhessian_(R *phi_xx, R *phi_xy, R *phi_xz, R *phi_yy, R *phi_yz, R *phi_zz, BOXARG(h),
+                          const R *phi, BOXARG(g), BOXARG(fb), const R *dx, const R *dy, const R *dz) {
+  Call call("lsm3dcentralhessian_");
+  Box hb = BOXOF(h), gb = BOXOF(g), fb = BOXOF(fb);
+  if (!gb.contains(fb, 1, 1, 1) || !hb.contains(fb, 0, 0, 0)) call.fail("ghost box does not cover the stencil");
+  if (!call.ok() || fb.empty()) return;
+  View<R> XX = vio(call, phi_xx, hb), XY = vio(call, phi_xy, hb), XZ = vio(call, phi_xz, hb),
+          YY = vio(call, phi_yy, hb), YZ = vio(call, phi_yz, hb), ZZ = vio(call, phi_zz, hb);
+  View<const R> F = vin(call, phi, gb);
+  if (!call.ok()) return;
+  const R ddx = *dx, ddy = *dy, ddz = *dz;
+  for_box(fb, [=] __device__(int i, int j, int k) {
+    const R *c = F.p + F.off(i, j, k);
+    const long long sx = 1, sy = F.s1, sz = F.s2;
+    XX(i, j, k) = (c[sx] - 2 * c[0] + c[-sx]) / (ddx * ddx);
+    XY(i, j, k) = R(0.25) * (c[sx + sy] - c[-sx + sy] - c[sx - sy] + c[-sx - sy]) / (ddx * ddy);
+    XZ(i, j, k) = R(0.25) * (c[sx + sz] - c[-sx + sz] - c[sx - sz] + c[-sx - sz]) / (ddx * ddz);
+    YY(i, j, k) = (c[sy] - 2 * c[0] + c[-sy]) / (ddy * ddy);
+    YZ(i, j, k) = R(0.25) * (c[sy + sz] - c[-sy + sz] - c[sy - sz] + c[-sy - sz]) / (ddy * ddz);
+    ZZ(i, j, k) = (c[sz] - 2 * c[0] + c[-sz]) / (ddz * ddz);
+  });
+  call.finish();
+}
+
+void lsm3daveragegradphi_(R *phi_x, R *phi_y, R *phi_z, BOXARG(g), const R *phi_x_plus, const R *phi_y_plus,
+                          const R *phi_z_plus, BOXARG(p), const R *phi_x_minus, const R *phi_y_minus,
+                          const R *phi_z_minus, BOXARG(m), BOXARG(fb)) {
+  Call call("lsm3daveragegradphi_");
+  Box gb = BOXOF(g), pb = BOXOF(p), mb = BOXOF(m), fb = BOXOF(fb);
+  if (!gb.contains(fb, 0, 0, 0) || !pb.contains(fb, 0, 0, 0) || !mb.contains(fb, 0, 0, 0))
+    call.fail("ghost box does not cover the fill box");
+  if (!call.ok() || fb.empty()) return;
+  View<R> X = vio(call, phi_x, gb), Y = vio(call, phi_y, gb), Z = vio(call, phi_z, gb);
+  View<const R> XP = vin(call, phi_x_plus, pb), YP = vin(call, phi_y_plus, pb), ZP = vin(call, phi_z_plus, pb);
+  View<const R> XM = vin(call, phi_x_minus, mb), YM = vin(call, phi_y_minus, mb), ZM = vin(call, phi_z_minus, mb);
+  if (!call.ok()) return;
+  for_box(fb, [=] __device__(int i, int j, int k) {
+    X(i, j, k) = R(0.5) * (XP(i, j, k) + XM(i, j, k));
+    Y(i, j, k) = R(0.5) * (YP(i, j, k) + YM(i, j, k));
+    Z(i, j, k) = R(0.5) * (ZP(i, j, k) + ZM(i, j, k));
+  });
+  call.finish();
+}
+
+void lsm3dphiupwindgradf_(R *F_x, R *F_y, R *F_z, BOXARG(g), const R *F_x_plus, const R *F_y_plus,
+                          const R *F_z_plus, BOXARG(p), const R *F_x_minus, const R *F_y_minus,
+                          const R *F_z_minus, BOXARG(m), const R *phi, BOXARG(f), BOXARG(fb)) {
+  Call call("lsm3dphiupwindgradf_");
+  Box gb = BOXOF(g), pb = BOXOF(p), mb = BOXOF(m), phb = BOXOF(f), fb = BOXOF(fb);
+  if (!gb.contains(fb, 0, 0, 0) || !pb.contains(fb, 0, 0, 0) || !mb.contains(fb, 0, 0, 0) ||
+      !phb.contains(fb, 1, 1, 1))
+    call.fail("ghost box does not cover the stencil");
+  if (!call.ok() || fb.empty()) return;
+  View<R> O[3] = {vio(call, F_x, gb), vio(call, F_y, gb), vio(call, F_z, gb)};
+  View<const R> PL[3] = {vin(call, F_x_plus, pb), vin(call, F_y_plus, pb), vin(call, F_z_plus, pb)};
+  View<const R> MI[3] = {vin(call, F_x_minus, mb), vin(call, F_y_minus, mb), vin(call, F_z_minus, mb)};
+  View<const R> PH = vin(call, phi, phb);
+  if (!call.ok()) return;
+  View<R> O0 = O[0], O1 = O[1], O2 = O[2];
+  View<const R> P0 = PL[0], P1 = PL[1], P2 = PL[2], M0 = MI[0], M1 = MI[1], M2 = MI[2];
+  // spatial_derivatives3d.f.in:3355-3459
+  for_box(fb, [=] __device__(int i, int j, int k) {
+    const R *c = PH.p + PH.off(i, j, k);
+    const R pc = c[0];
+    const long long s[3] = {1, PH.s1, PH.s2};
+    for (int d = 0; d < 3; d++) {
+      const View<R> &o = d == 0 ? O0 : (d == 1 ? O1 : O2);
+      const View<const R> &pl = d == 0 ? P0 : (d == 1 ? P1 : P2);
+      const View<const R> &mi = d == 0 ? M0 : (d == 1 ? M1 : M2);
+      const R nm = c[-s[d]], np = c[s[d]];
+      if (pc > R(0)) {
+        if (nm <= pc) o(i, j, k) = (np < nm) ? pl(i, j, k) : mi(i, j, k);
+        else if (np <= pc) o(i, j, k) = pl(i, j, k);
+        else o(i, j, k) = R(0);
+      } else if (pc < R(0)) {
+        if (nm >= pc) o(i, j, k) = (np > nm) ? pl(i, j, k) : mi(i, j, k);
+        else if (np >= pc) o(i, j, k) = pl(i, j, k);
+        else o(i, j, k) = R(0);
+      }
+    }
+  });
+  call.finish();
+}
+
+// level_set_evolution3d.f.in:514-521: k from klo_fb to khi_gb, j from jlo_fb to
+// jhi_gb, i over the whole ghost box of the rhs
+void lsm3daddconstprecomputedcurvtermtolserhs_(R *lse_rhs, BOXARG(r), const R *kappa, BOXARG(k),
+                                               const R *grad_phi_mag, BOXARG(g), const R *b, BOXARG(fb)) {
+  Call call("lsm3daddconstprecomputedcurvtermtolserhs_");
+  Box rb = BOXOF(r), kb = BOXOF(k), gb = BOXOF(g), fb = BOXOF(fb);
+  Box loop = rb;
+  loop.lo[1] = fb.lo[1];
+  loop.lo[2] = fb.lo[2];
+  if (!kb.contains(loop, 0, 0, 0) || !gb.contains(loop, 0, 0, 0)) call.fail("kappa / grad_phi_mag ghost box does not cover the loop range");
+  if (!call.ok() || loop.empty()) return;
+  View<R> O = vio(call, lse_rhs, rb);
+  View<const R> K = vin(call, kappa, kb), G = vin(call, grad_phi_mag, gb);
+  if (!call.ok()) return;
+  const R bb = *b;
+  for_box(loop, [=] __device__(int i, int j, int k) { O(i, j, k) = O(i, j, k) + bb * K(i, j, k) * G(i, j, k); });
+  call.finish();
+}
+
+void lsm3daddexternalandnormalveltermtolserhs_(R *lse_rhs, BOXARG(r), const R *phi_x_plus, const R *phi_y_plus,
+                                               const R *phi_z_plus, BOXARG(p), const R *phi_x_minus,
+                                               const R *phi_y_minus, const R *phi_z_minus, BOXARG(m),
+                                               const R *vel_n, const R *vel_x, const R *vel_y, const R *vel_z,
+                                               BOXARG(v), BOXARG(fb)) {
+  Call call("lsm3daddexternalandnormalveltermtolserhs_");
+  Box rb = BOXOF(r), pb = BOXOF(p), mb = BOXOF(m), vb = BOXOF(v), fb = BOXOF(fb);
+  Box loop = rb;
+  loop.lo[1] = fb.lo[1];
+  loop.lo[2] = fb.lo[2];
+  if (!pb.contains(loop, 0, 0, 0) || !mb.contains(loop, 0, 0, 0) || !vb.contains(loop, 0, 0, 0))
+    call.fail("ghost box does not cover the loop range");
+  if (!call.ok() || loop.empty()) return;
+  View<R> O = vio(call, lse_rhs, rb);
+  View<const R> XP = vin(call, phi_x_plus, pb), YP = vin(call, phi_y_plus, pb), ZP = vin(call, phi_z_plus, pb);
+  View<const R> XM = vin(call, phi_x_minus, mb), YM = vin(call, phi_y_minus, mb), ZM = vin(call, phi_z_minus, mb);
+  View<const R> VN = vin(call, vel_n, vb), VX = vin(call, vel_x, vb), VY = vin(call, vel_y, vb), VZ = vin(call, vel_z, vb);
+  if (!call.ok()) return;
+  for_box(loop, [=] __device__(int i, int j, int k) {
+    const R w = VN(i, j, k), ux = VX(i, j, k), uy = VY(i, j, k), uz = VZ(i, j, k);
+    const R gx = ext_pick(ux, w, XP(i, j, k), XM(i, j, k));
+    const R gy = ext_pick(uy, w, YP(i, j, k), YM(i, j, k));
+    const R gz = ext_pick(uz, w, ZP(i, j, k), ZM(i, j, k));
+    const R n2 = gx * gx + gy * gy + gz * gz;
+    if (fabs(w) >= Consts<R>::zero_tol && n2 >= Consts<R>::zero_tol)
+      O(i, j, k) = O(i, j, k) - ux * gx - uy * gy - uz * gz - w * sqrt(n2);
+    else
+      O(i, j, k) = O(i, j, k) - ux * gx - uy * gy - uz * gz;
+  });
+  call.finish();
+}
+
+#define BCARGS R *phi, BOXARG(g), BOXARG(fb), const int *bdry_location_idx
+void lsm3dlinearextrapolation_(BCARGS) {
+  face_extrapolate("lsm3dlinearextrapolation_", phi, BOXOF(g), BOXOF(fb), *bdry_location_idx, BC_LINEAR);
+}
+void lsm3dsignedlinearextrapolation_(BCARGS) {
+  face_extrapolate("lsm3dsignedlinearextrapolation_", phi, BOXOF(g), BOXOF(fb), *bdry_location_idx, BC_SIGNED);
+}
+void lsm3dcopyextrapolation_(BCARGS) {
+  face_extrapolate("lsm3dcopyextrapolation_", phi, BOXOF(g), BOXOF(fb), *bdry_location_idx, BC_COPY);
+}
+void lsm3dhomogeneousneumanneno1_(BCARGS) {
+  face_extrapolate("lsm3dhomogeneousneumanneno1_", phi, BOXOF(g), BOXOF(fb), *bdry_location_idx, BC_COPY);
+}
+void lsm3dhomogeneousneumanneno2_(BCARGS) {
+  face_extrapolate("lsm3dhomogeneousneumanneno2_", phi, BOXOF(g), BOXOF(fb), *bdry_location_idx, BC_COPY);
+}
+void lsm3dhomogeneousneumanneno3_(BCARGS) {
+  face_extrapolate("lsm3dhomogeneousneumanneno3_", phi, BOXOF(g), BOXOF(fb), *bdry_location_idx, BC_COPY);
+}
+void lsm3dhomogeneousneumannweno5_(BCARGS) {
+  face_extrapolate("lsm3dhomogeneousneumannweno5_", phi, BOXOF(g), BOXOF(fb), *bdry_location_idx, BC_COPY);
+}
+
+}  // extern "C"

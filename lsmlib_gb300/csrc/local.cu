@@ -29,13 +29,29 @@ struct List {
   int decl;  // declared lower bound of the arrays
 };
 
+// cells outside the narrow_band array, or whose stencil would leave an array's
+// ghost box, are skipped (LSMLIB reads outside the arrays there)
 struct Gate {
   View<const U8> nb;
+  Box nbb;   // narrow_band's ghost box
+  Box safe;  // cells whose stencil stays inside every array this routine touches
   signed char mark;
-  __device__ __forceinline__ bool operator()(int i, int j, int k) const {
-    return (signed char)nb(i, j, k) <= mark;
+  __device__ __forceinline__ bool ok(int i, int j, int k) const { return inbox(safe, i, j, k) && inbox(nbb, i, j, k); }
+  __device__ __forceinline__ bool pass(int i, int j, int k) const { return (signed char)nb(i, j, k) <= mark; }
+  __device__ __forceinline__ bool operator()(int i, int j, int k) const { return ok(i, j, k) && pass(i, j, k); }
+  Gate with(const Box &s, unsigned char m) const {
+    Gate g = *this;
+    g.safe = s;
+    g.mark = (signed char)m;
+    return g;
   }
 };
+
+inline Box everything() {
+  Box b;
+  for (int d = 0; d < 3; d++) { b.lo[d] = -2147483647; b.hi[d] = 2147483647; }
+  return b;
+}
 
 // one thread per list entry l in [lo, hi]
 template <class F>
@@ -75,6 +91,8 @@ struct LocalCall {
   Gate gate(const unsigned char *nb, const Box &b, unsigned char mark) {
     Gate g;
     g.nb = view((const U8 *)c.in(nb, b.size()), b);
+    g.nbb = b;
+    g.safe = everything();
     g.mark = (signed char)mark;
     return g;
   }
@@ -83,7 +101,10 @@ struct LocalCall {
 };
 
 // undivided differences over a list (spatial_derivatives3d_local.f.in:43-138)
-void dn_local(View<R> dn, View<const R> dm, int n, int dir, const List &L, int lo, int hi, Gate g) {
+void dn_local(View<R> dn, const Box &db, View<const R> dm, const Box &mb, int n, int dir, const List &L, int lo,
+              int hi, Gate g) {
+  // Dn(i) reads Dm(i) and Dm(i - 1) (odd n) or Dm(i + 1) (even n) along dir
+  g.safe = isect(g.safe, isect(db, inner_axis(mb, dir, n % 2 == 1 ? 1 : 0, n % 2 == 1 ? 0 : 1)));
   int o0 = 0, o1 = 0, o2 = 0;
   const int off = (n % 2 == 1) ? 1 : -1;
   const R sgn = (n % 2 == 1) ? R(1.0) : R(-1.0);
@@ -91,7 +112,8 @@ void dn_local(View<R> dn, View<const R> dm, int n, int dir, const List &L, int l
   if (dir == 1) o1 = off;
   if (dir == 2) o2 = off;
   for_list(L, lo, hi, [=] __device__(int i, int j, int k) {
-    if (g(i, j, k))
+    if (!g.ok(i, j, k)) return;
+    if (g.pass(i, j, k))
       dn(i, j, k) = sgn * (dm(i, j, k) - dm(i - o0, j - o1, k - o2));
     else
       dn(i, j, k) = R(1.0e10);
@@ -167,7 +189,7 @@ void lsm3dcomputednlocal_(R *dn, BOXARG(d), const R *dm, BOXARG(m), const int *n
   View<R> D = lc.inout(dn, db);
   View<const R> M = lc.in(dm, mb);
   if (!lc.c.ok()) return;
-  dn_local(D, M, *n, *dir - 1, L, *nlo, *nhi, g);
+  dn_local(D, db, M, mb, *n, *dir - 1, L, *nlo, *nhi, g);
   lc.c.finish();
 }
 
@@ -187,11 +209,13 @@ void lsm3dhjeno1local_(PMARGS, R *d1, BOXARG(d1), DXP, IDX3, const int *nlo0, co
   View<R> D1 = lc.inout(d1, BOXOF(d1));
   if (!lc.c.ok()) return;
   const R inv[3] = {R(1.0) / *dx, R(1.0) / *dy, R(1.0) / *dz};
+  const Box d1b = BOXOF(d1), fbx = BOXOF(f), outb = isect(pb, mb);
   for (int d = 0; d < 3; d++) {
-    dn_local(D1, F, 1, d, L, *nlo0, *nhi1, gd1);
+    dn_local(D1, d1b, F, fbx, 1, d, L, *nlo0, *nhi1, gd1);
     const R w = inv[d];
+    const Gate gd = gfb.with(isect(outb, inner_axis(d1b, d, 0, 1)), *mark_fb);
     for_list(L, *nlo0, *nhi0, [=] __device__(int i, int j, int k) {
-      if (!gfb(i, j, k)) return;
+      if (!gd(i, j, k)) return;
       const long long c = D1.off(i, j, k), s = dstride(D1, d);
       P[d](i, j, k) = D1.p[c + s] * w;
       M[d](i, j, k) = D1.p[c] * w;
@@ -217,13 +241,15 @@ void lsm3dhjeno2local_(PMARGS, R *d1, BOXARG(d1), R *d2, BOXARG(d2), DXP, IDX3, 
   View<R> D1 = lc.inout(d1, BOXOF(d1)), D2 = lc.inout(d2, BOXOF(d2));
   if (!lc.c.ok()) return;
   const R inv[3] = {R(1.0) / *dx, R(1.0) / *dy, R(1.0) / *dz};
+  const Box d1b = BOXOF(d1), d2b = BOXOF(d2), fbx = BOXOF(f), outb = isect(pb, mb);
   for (int d = 0; d < 3; d++) {
-    dn_local(D1, F, 1, d, L, *nlo0, *nhi2, g1);
+    dn_local(D1, d1b, F, fbx, 1, d, L, *nlo0, *nhi2, g1);
     View<const R> D1c{D1.p, D1.lo0, D1.lo1, D1.lo2, D1.s1, D1.s2};
-    dn_local(D2, D1c, 2, d, L, *nlo0, *nhi1, g2);
+    dn_local(D2, d2b, D1c, d1b, 2, d, L, *nlo0, *nhi1, g2);
     const R w = inv[d];
+    const Gate gd = gfb.with(isect(outb, isect(inner_axis(d1b, d, 0, 1), inner_axis(d2b, d, 1, 1))), *mark_fb);
     for_list(L, *nlo0, *nhi0, [=] __device__(int i, int j, int k) {
-      if (!gfb(i, j, k)) return;
+      if (!gd(i, j, k)) return;
       const long long a = D1.off(i, j, k), b = D2.off(i, j, k);
       const long long s1 = dstride(D1, d), s2 = dstride(D2, d);
       const R *q = D2.p;
@@ -255,13 +281,17 @@ void lsm3dhjeno3local_(PMARGS, R *d1, BOXARG(d1), R *d2, BOXARG(d2), R *d3, BOXA
   View<R> D1 = lc.inout(d1, BOXOF(d1)), D2 = lc.inout(d2, BOXOF(d2)), D3 = lc.inout(d3, BOXOF(d3));
   if (!lc.c.ok()) return;
   const R inv[3] = {R(1.0) / *dx, R(1.0) / *dy, R(1.0) / *dz};
+  const Box d1b = BOXOF(d1), d2b = BOXOF(d2), d3b = BOXOF(d3), fbx = BOXOF(f), outb = isect(pb, mb);
   for (int d = 0; d < 3; d++) {
-    dn_local(D1, F, 1, d, L, *nlo0, *nhi3, g1);
-    dn_local(D2, View<const R>{D1.p, D1.lo0, D1.lo1, D1.lo2, D1.s1, D1.s2}, 2, d, L, *nlo0, *nhi2, g2);
-    dn_local(D3, View<const R>{D2.p, D2.lo0, D2.lo1, D2.lo2, D2.s1, D2.s2}, 3, d, L, *nlo0, *nhi1, g3);
+    dn_local(D1, d1b, F, fbx, 1, d, L, *nlo0, *nhi3, g1);
+    dn_local(D2, d2b, View<const R>{D1.p, D1.lo0, D1.lo1, D1.lo2, D1.s1, D1.s2}, d1b, 2, d, L, *nlo0, *nhi2, g2);
+    dn_local(D3, d3b, View<const R>{D2.p, D2.lo0, D2.lo1, D2.lo2, D2.s1, D2.s2}, d2b, 3, d, L, *nlo0, *nhi1, g3);
     const R w = inv[d];
+    const Gate gd = gfb.with(isect(outb, isect(inner_axis(d1b, d, 0, 1), isect(inner_axis(d2b, d, 1, 1),
+                                                                               inner_axis(d3b, d, 1, 2)))),
+                             *mark_fb);
     for_list(L, *nlo0, *nhi0, [=] __device__(int i, int j, int k) {
-      if (!gfb(i, j, k)) return;
+      if (!gd(i, j, k)) return;
       const R third = R(1.0 / 3.0), sixth = R(1.0 / 6.0), h = R(0.5);
       const long long a = D1.off(i, j, k), b = D2.off(i, j, k), c3 = D3.off(i, j, k);
       const long long s1 = dstride(D1, d), s2 = dstride(D2, d), s3 = dstride(D3, d);
@@ -305,11 +335,13 @@ void lsm3dhjweno5local_(PMARGS, R *d1, BOXARG(d1), DXP, IDX3, const int *nlo0, c
   View<R> D1 = lc.inout(d1, BOXOF(d1));
   if (!lc.c.ok()) return;
   const R inv[3] = {R(1.0) / *dx, R(1.0) / *dy, R(1.0) / *dz};
+  const Box d1b = BOXOF(d1), fbx = BOXOF(f), outb = isect(pb, mb);
   for (int d = 0; d < 3; d++) {
-    dn_local(D1, F, 1, d, L, *nlo0, *nhi3, g1);
+    dn_local(D1, d1b, F, fbx, 1, d, L, *nlo0, *nhi3, g1);
     const R w = inv[d];
+    const Gate gd = gfb.with(isect(outb, inner_axis(d1b, d, 2, 3)), *mark_fb);
     for_list(L, *nlo0, *nhi0, [=] __device__(int i, int j, int k) {
-      if (!gfb(i, j, k)) return;
+      if (!gd(i, j, k)) return;
       const long long c = D1.off(i, j, k), s = dstride(D1, d);
       const R *q = D1.p;
       P[d](i, j, k) = weno5_local(q[c + 3 * s] * w, q[c + 2 * s] * w, q[c + s] * w, q[c] * w, q[c - s] * w);
@@ -331,6 +363,7 @@ void lsm3dcentralgradorder2local_(R *phi_x, R *phi_y, R *phi_z, BOXARG(g), const
   Box gb = BOXOF(g);
   View<R> X = lc.inout(phi_x, gb), Y = lc.inout(phi_y, gb), Z = lc.inout(phi_z, gb);
   View<const R> F = lc.in(phi, BOXOF(f));
+  g.safe = isect(gb, inner(BOXOF(f), 1, 1, 1, 1, 1, 1));
   if (!lc.c.ok()) return;
   const R fx = R(0.5) / *dx, fy = R(0.5) / *dy, fz = R(0.5) / *dz;
   for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) {
@@ -349,6 +382,7 @@ void lsm3dcentralgradorder4local_(R *phi_x, R *phi_y, R *phi_z, BOXARG(g), const
   Box gb = BOXOF(g);
   View<R> X = lc.inout(phi_x, gb), Y = lc.inout(phi_y, gb), Z = lc.inout(phi_z, gb);
   View<const R> F = lc.in(phi, BOXOF(f));
+  g.safe = isect(gb, inner(BOXOF(f), 2, 2, 2, 2, 2, 2));
   if (!lc.c.ok()) return;
   const R c12 = R(0.0833333333333333333333);
   const R fx = c12 / *dx, fy = c12 / *dy, fz = c12 / *dz;
@@ -369,6 +403,7 @@ void lsm3dlaplacianorder2local_(R *lap, BOXARG(g), const R *phi, BOXARG(f), DXP,
   LSETUP("lsm3dlaplacianorder2local_")
   View<R> O = lc.inout(lap, BOXOF(g));
   View<const R> F = lc.in(phi, BOXOF(f));
+  g.safe = isect(BOXOF(g), inner(BOXOF(f), 1, 1, 1, 1, 1, 1));
   if (!lc.c.ok()) return;
   const R a = R(1.0) / *dx / *dx, b = R(1.0) / *dy / *dy, e = R(1.0) / *dz / *dz;
   for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) {
@@ -442,6 +477,7 @@ __global__ void k_avegrad_final(const R *psum, const int *pcnt, int nb, R *out) 
 void lsm3dcomputeavegradphilocal_(R *grad_phi_ave, const R *phi, BOXARG(f), DXP, LTAIL) {
   LSETUP("lsm3dcomputeavegradphilocal_")
   View<const R> F = lc.in(phi, BOXOF(f));
+  g.safe = inner(BOXOF(f), 1, 1, 1, 1, 1, 1);
   R *out = lc.c.scalar_out(grad_phi_ave);
   const long long n = (long long)*nhi - *nlo + 1;
   const int nb = n > 0 ? (int)((n + 255) / 256) : 1;
@@ -461,6 +497,7 @@ void lsm3dgradientmagnitudelocal_(const R *phi_x, const R *phi_y, const R *phi_z
   Box gb = BOXOF(g);
   View<const R> X = lc.in(phi_x, gb), Y = lc.in(phi_y, gb), Z = lc.in(phi_z, gb);
   View<R> O = lc.inout(grad_phi_mag, gb);
+  g.safe = gb;
   if (!lc.c.ok()) return;
   for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) {
     if (!g(i, j, k)) return;
@@ -483,6 +520,7 @@ static void rk_local(const char *name, int kind, R *out, const Box &ob, const R 
   View<R> O = lc.inout(out, ob);
   View<const R> A = kind ? lc.in(a, ab) : View<const R>{};
   View<const R> U = lc.in(u, ub), Lr = lc.in(rhs, rb);
+  g.safe = isect(isect(ob, ub), kind ? isect(rb, ab) : rb);
   if (!lc.c.ok()) return;
   for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) {
     if (!g(i, j, k)) return;
@@ -524,7 +562,10 @@ void lsm3dzerooutlevelseteqnrhslocal_(R *lse_rhs, BOXARG(r), IDX3, const int *nl
   List L = lc.list(index_x, index_y, index_z, *nlo, *nhi);
   View<R> O = lc.inout(lse_rhs, BOXOF(r));
   if (!lc.c.ok()) return;
-  for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) { O(i, j, k) = R(0); });
+  const Box rb = BOXOF(r);
+  for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) {
+    if (inbox(rb, i, j, k)) O(i, j, k) = R(0);
+  });
   lc.c.finish();
 }
 
@@ -536,6 +577,7 @@ void lsm3daddadvectiontermtolserhslocal_(R *lse_rhs, BOXARG(r), const R *phi_x, 
   View<R> O = lc.inout(lse_rhs, BOXOF(r));
   View<const R> X = lc.in(phi_x, gb), Y = lc.in(phi_y, gb), Z = lc.in(phi_z, gb);
   View<const R> VX = lc.in(vel_x, vb), VY = lc.in(vel_y, vb), VZ = lc.in(vel_z, vb);
+  g.safe = isect(BOXOF(r), isect(gb, vb));
   if (!lc.c.ok()) return;
   for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) {
     if (!g(i, j, k)) return;
@@ -553,6 +595,7 @@ static void normal_local(const char *name, R *rhs, const Box &rb, const R *pxp, 
   View<const R> XP = lc.in(pxp, pb), YP = lc.in(pyp, pb), ZP = lc.in(pzp, pb);
   View<const R> XM = lc.in(pxm, mb), YM = lc.in(pym, mb), ZM = lc.in(pzm, mb);
   View<const R> V = cst ? View<const R>{} : lc.in(vn, vb);
+  g.safe = isect(rb, isect(pb, cst ? mb : isect(mb, vb)));
   if (!lc.c.ok()) return;
   for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) {
     if (!g(i, j, k)) return;
@@ -591,6 +634,7 @@ void lsm3daddconstcurvtermtolserhslocal_(R *lse_rhs, BOXARG(r), const R *phi_x, 
   View<const R> X = lc.in(phi_x, gb), Y = lc.in(phi_y, gb), Z = lc.in(phi_z, gb);
   View<const R> XX = lc.in(phi_xx, hb), XY = lc.in(phi_xy, hb), XZ = lc.in(phi_xz, hb),
                 YY = lc.in(phi_yy, hb), YZ = lc.in(phi_yz, hb), ZZ = lc.in(phi_zz, hb);
+  g.safe = isect(BOXOF(r), isect(gb, hb));
   if (!lc.c.ok()) return;
   const R bb = *b;
   for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) {
@@ -619,6 +663,7 @@ void lsm3dcomputereinitializationeqnrhslocal_(R *reinit_rhs, BOXARG(r), const R 
   View<const R> P0 = use0 ? lc.in(phi0, BOXOF(z)) : View<const R>{};
   View<const R> XP = lc.in(phi_x_plus, pb), YP = lc.in(phi_y_plus, pb), ZP = lc.in(phi_z_plus, pb);
   View<const R> XM = lc.in(phi_x_minus, mb), YM = lc.in(phi_y_minus, mb), ZM = lc.in(phi_z_minus, mb);
+  g.safe = isect(isect(BOXOF(r), use0 ? BOXOF(z) : BOXOF(f)), isect(pb, mb));
   if (!lc.c.ok()) return;
   R dx_sq = rmax(rmax(*dx, *dy), *dz);
   dx_sq = dx_sq * dx_sq;
@@ -639,6 +684,7 @@ void lsm3dcomputemeancurvatureorder2local_(R *kappa, BOXARG(k), const R *phi, BO
   View<R> K = lc.inout(kappa, BOXOF(k));
   View<const R> F = lc.in(phi, BOXOF(f));
   View<const R> X = lc.in(phi_x, gb), Y = lc.in(phi_y, gb), Z = lc.in(phi_z, gb), G = lc.in(grad_phi_mag, gb);
+  g.safe = isect(isect(BOXOF(k), gb), inner(BOXOF(f), 1, 1, 1, 1, 1, 1));
   if (!lc.c.ok()) return;
   const R dxv = *dx, dyv = *dy, dzv = *dz;
   const R fxx = R(1.0) / dxv / dxv, fyy = R(1.0) / dyv / dyv, fzz = R(1.0) / dzv / dzv;
@@ -720,6 +766,7 @@ void lsm3dmaxnormdifflocal_(R *max_norm_diff, const R *field1, BOXARG(a), const 
   LRed A{};
   A.a = lc.in(field1, BOXOF(a));
   A.b = lc.in(field2, BOXOF(b));
+  g.safe = isect(BOXOF(a), BOXOF(b));
   list_max<3>(lc, A, g, L, *nlo, *nhi, max_norm_diff, R(0.0), 1, R(0));  // starts at 0 (:72)
 }
 
@@ -729,6 +776,7 @@ void lsm3dcomputestableadvectiondtlocal_(R *dt, const R *vel_x, const R *vel_y, 
   Box vb = BOXOF(v);
   LRed A{};
   A.a = lc.in(vel_x, vb); A.b = lc.in(vel_y, vb); A.c = lc.in(vel_z, vb);
+  g.safe = vb;
   A.ix = R(1.0) / *dx; A.iy = R(1.0) / *dy; A.iz = R(1.0) / *dz;
   list_max<0>(lc, A, g, L, *nlo, *nhi, dt, R(-1.0), 0, *cfl_number);
 }
@@ -745,6 +793,7 @@ static void normal_dt_local(const char *name, int mode, R *dt, const R *vn, cons
   A.xp = lc.in(pxp, pb); A.yp = lc.in(pyp, pb); A.zp = lc.in(pzp, pb);
   A.xm = lc.in(pxm, mb); A.ym = lc.in(pym, mb); A.zm = lc.in(pzm, mb);
   if (mode == 1) A.vn = lc.in(vn, vb);
+  g.safe = isect(isect(pb, mb), mode == 1 ? vb : pb);
   A.vc = vc;
   A.ix = R(1.0) / dx; A.iy = R(1.0) / dy; A.iz = R(1.0) / dz;
   R mx = max3 ? rmax(rmax(dx, dy), dz) : rmax(rmax(dx, dy), dz);
@@ -784,6 +833,7 @@ void lsm3dmultiplycutofflserhslocal_(const R *phi, R *lse_rhs, BOXARG(g), LTAIL,
   Box gb = BOXOF(g);
   View<const R> F = lc.in(phi, gb);
   View<R> O = lc.inout(lse_rhs, gb);
+  g.safe = gb;
   if (!lc.c.ok()) return;
   const R bt = *beta, gm = *gamma;
   const R c1 = gm - 3 * bt;
@@ -813,7 +863,10 @@ void lsm3dimposemasklocal_(R *dest, BOXARG(d), const R *src, BOXARG(s), const R 
   View<R> D = lc.inout(dest, BOXOF(d));
   View<const R> S = lc.in(src, BOXOF(s)), M = lc.in(mask, BOXOF(m));
   if (!lc.c.ok()) return;
-  for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) { D(i, j, k) = rmax(M(i, j, k), S(i, j, k)); });
+  const Box sb = isect(BOXOF(d), isect(BOXOF(s), BOXOF(m)));
+  for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) {
+    if (inbox(sb, i, j, k)) D(i, j, k) = rmax(M(i, j, k), S(i, j, k));
+  });
   lc.c.finish();
 }
 
@@ -823,7 +876,10 @@ void lsm3dcopydatalocal_(R *dest, BOXARG(d), const R *src, BOXARG(s), IDX3, cons
   View<R> D = lc.inout(dest, BOXOF(d));
   View<const R> S = lc.in(src, BOXOF(s));
   if (!lc.c.ok()) return;
-  for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) { D(i, j, k) = S(i, j, k); });
+  const Box sb = isect(BOXOF(d), BOXOF(s));
+  for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) {
+    if (inbox(sb, i, j, k)) D(i, j, k) = S(i, j, k);
+  });
   lc.c.finish();
 }
 

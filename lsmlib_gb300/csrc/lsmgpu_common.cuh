@@ -35,6 +35,32 @@ struct Box {
   }
 };
 
+__host__ __device__ inline bool inbox(const Box &b, int i, int j, int k) {
+  return i >= b.lo[0] && i <= b.hi[0] && j >= b.lo[1] && j <= b.hi[1] && k >= b.lo[2] && k <= b.hi[2];
+}
+inline Box isect(const Box &a, const Box &b) {
+  Box r;
+  for (int d = 0; d < 3; d++) {
+    r.lo[d] = a.lo[d] > b.lo[d] ? a.lo[d] : b.lo[d];
+    r.hi[d] = a.hi[d] < b.hi[d] ? a.hi[d] : b.hi[d];
+  }
+  return r;
+}
+// the cells c of b for which c - lo_reach .. c + hi_reach (per axis) stay in b
+inline Box inner(const Box &b, int rx0, int rx1, int ry0, int ry1, int rz0, int rz1) {
+  Box r = b;
+  r.lo[0] += rx0; r.hi[0] -= rx1;
+  r.lo[1] += ry0; r.hi[1] -= ry1;
+  r.lo[2] += rz0; r.hi[2] -= rz1;
+  return r;
+}
+inline Box inner_axis(const Box &b, int axis, int lo_reach, int hi_reach) {
+  Box r = b;
+  r.lo[axis] += lo_reach;
+  r.hi[axis] -= hi_reach;
+  return r;
+}
+
 inline Box mkbox(const int *ilo, const int *ihi, const int *jlo, const int *jhi,
                  const int *klo, const int *khi) {
   Box b;

@@ -28,6 +28,27 @@ typedef signed char mark_t;
 #define B3(n) mk_box(n##_ilo, n##_ihi, n##_jlo, n##_jhi, n##_klo, n##_khi)
 #define DX_ARGS const real_t *dx, const real_t *dy, const real_t *dz
 
+/* Cells outside an array's ghost box, or whose stencil would leave it, are
+ * skipped: LSMLIB reads outside its arrays there (undefined behaviour), and
+ * the GPU library skips the same cells. */
+static int inb(const gbox *b, int i, int j, int k) {
+  return i >= b->lo[0] && i <= b->hi[0] && j >= b->lo[1] && j <= b->hi[1] && k >= b->lo[2] &&
+         k <= b->hi[2];
+}
+/* cell c with c-lo..c+hi along `axis` inside b */
+static int inb_axis(const gbox *b, int axis, int lo, int hi, int i, int j, int k) {
+  int c[3] = {i, j, k};
+  for (int a = 0; a < 3; a++) {
+    int l = (a == axis) ? lo : 0, h = (a == axis) ? hi : 0;
+    if (c[a] - l < b->lo[a] || c[a] + h > b->hi[a]) return 0;
+  }
+  return 1;
+}
+/* cell with a reach of r on every axis inside b */
+static int inb_r(const gbox *b, int r, int i, int j, int k) {
+  return inb_axis(b, 0, r, r, i, j, k) && inb_axis(b, 1, r, r, i, j, k) && inb_axis(b, 2, r, r, i, j, k);
+}
+
 /* iterate list entries l = lo..hi of lists declared from `decl` */
 #define FOR_LIST(decl, lo, hi)                                       \
   for (int l = (lo); l <= (hi); l++)                                   \
@@ -48,6 +69,9 @@ static void dn_local(real_t *dn, const gbox *db, const real_t *dm, const gbox *m
     sgn = -1.0;
   }
   FOR_LIST(decl, lo, hi) {
+    if (!inb(db, i, j, k) || !inb_axis(mb, dir, n % 2 == 1 ? 1 : 0, n % 2 == 1 ? 0 : 1, i, j, k) ||
+        !inb(nbb, i, j, k))
+      continue;
     if (nb[at(nbb, i, j, k)] <= mark)
       dn[at(db, i, j, k)] =
           sgn * (dm[at(mb, i, j, k)] - dm[at(mb, i - off[0], j - off[1], k - off[2])]);
@@ -82,6 +106,9 @@ void lsm3dhjeno1local_(PM_ARGS, real_t *d1, A3(d1), DX_ARGS, LIST_ARGS, const in
   for (int d = 0; d < 3; d++) {
     dn_local(d1, &D1, phi, &F, 1, d, ix, iy, iz, *nlo0, *nlo0, *nhi1, nb, &NB, *mark_d1);
     FOR_LIST(*nlo0, *nlo0, *nhi0) {
+      if (!inb(&P, i, j, k) || !inb(&M, i, j, k) || !inb(&NB, i, j, k) ||
+          !inb_axis(&D1, d, 0, 1, i, j, k))
+        continue;
       if (nb[at(&NB, i, j, k)] <= *mark_fb) {
         long c = at(&D1, i, j, k);
         pp[d][at(&P, i, j, k)] = d1[c + sh(&D1, d, 1)] * inv[d];
@@ -102,6 +129,9 @@ void lsm3dhjeno2local_(PM_ARGS, real_t *d1, A3(d1), real_t *d2, A3(d2), DX_ARGS,
     dn_local(d1, &D1, phi, &F, 1, d, ix, iy, iz, *nlo0, *nlo0, *nhi2, nb, &NB, *mark_d1);
     dn_local(d2, &D2, d1, &D1, 2, d, ix, iy, iz, *nlo0, *nlo0, *nhi1, nb, &NB, *mark_d2);
     FOR_LIST(*nlo0, *nlo0, *nhi0) {
+      if (!inb(&P, i, j, k) || !inb(&M, i, j, k) || !inb(&NB, i, j, k) ||
+          !inb_axis(&D1, d, 0, 1, i, j, k) || !inb_axis(&D2, d, 1, 1, i, j, k))
+        continue;
       if (nb[at(&NB, i, j, k)] <= *mark_fb) {
         long a = at(&D1, i, j, k), b = at(&D2, i, j, k);
         long s1 = sh(&D1, d, 1), s2 = sh(&D2, d, 1);
@@ -131,6 +161,10 @@ void lsm3dhjeno3local_(PM_ARGS, real_t *d1, A3(d1), real_t *d2, A3(d2), real_t *
     dn_local(d2, &D2, d1, &D1, 2, d, ix, iy, iz, *nlo0, *nlo0, *nhi2, nb, &NB, *mark_d2);
     dn_local(d3, &D3, d2, &D2, 3, d, ix, iy, iz, *nlo0, *nlo0, *nhi1, nb, &NB, *mark_d3);
     FOR_LIST(*nlo0, *nlo0, *nhi0) {
+      if (!inb(&P, i, j, k) || !inb(&M, i, j, k) || !inb(&NB, i, j, k) ||
+          !inb_axis(&D1, d, 0, 1, i, j, k) || !inb_axis(&D2, d, 1, 1, i, j, k) ||
+          !inb_axis(&D3, d, 1, 2, i, j, k))
+        continue;
       if (nb[at(&NB, i, j, k)] > *mark_fb) continue;
       long a = at(&D1, i, j, k), b = at(&D2, i, j, k), c3 = at(&D3, i, j, k);
       long s1 = sh(&D1, d, 1), s2 = sh(&D2, d, 1), s3 = sh(&D3, d, 1);
@@ -203,6 +237,9 @@ void lsm3dhjweno5local_(PM_ARGS, real_t *d1, A3(d1), DX_ARGS, LIST_ARGS, const i
     dn_local(d1, &D1, phi, &F, 1, d, ix, iy, iz, *nlo0, *nlo0, *nhi3, nb, &NB, *mark_d1);
     const long s = sh(&D1, d, 1);
     FOR_LIST(*nlo0, *nlo0, *nhi0) {
+      if (!inb(&P, i, j, k) || !inb(&M, i, j, k) || !inb(&NB, i, j, k) ||
+          !inb_axis(&D1, d, 2, 3, i, j, k))
+        continue;
       if (nb[at(&NB, i, j, k)] > *mark_fb) continue;
       long c = at(&D1, i, j, k);
       real_t w = inv[d];
@@ -215,7 +252,7 @@ void lsm3dhjweno5local_(PM_ARGS, real_t *d1, A3(d1), DX_ARGS, LIST_ARGS, const i
 }
 
 #define LOCAL_TAIL LIST_ARGS, const int *nlo, const int *nhi, NB_ARGS, const mark_t *mark_fb
-#define GATE (nb[at(&NB, i, j, k)] <= *mark_fb)
+#define GATE (inb(&NB, i, j, k) && nb[at(&NB, i, j, k)] <= *mark_fb)
 
 /* lsm3dCentralGradOrder2LOCAL (spatial_derivatives3d_local.f.in:763-848) */
 void lsm3dcentralgradorder2local_(real_t *px, real_t *py, real_t *pz, A3(g), const real_t *phi,
@@ -224,7 +261,7 @@ void lsm3dcentralgradorder2local_(real_t *px, real_t *py, real_t *pz, A3(g), con
   real_t fac[3] = {0.5 / *dx, 0.5 / *dy, 0.5 / *dz};
   real_t *o[3] = {px, py, pz};
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&G, i, j, k) && inb_r(&F, 1, i, j, k))) continue;
     const real_t *c = phi + at(&F, i, j, k);
     for (int d = 0; d < 3; d++) o[d][at(&G, i, j, k)] = (c[F.s[d]] - c[-F.s[d]]) * fac[d];
   }
@@ -238,7 +275,7 @@ void lsm3dcentralgradorder4local_(real_t *px, real_t *py, real_t *pz, A3(g), con
   real_t fac[3] = {c12 / *dx, c12 / *dy, c12 / *dz};
   real_t *o[3] = {px, py, pz};
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&G, i, j, k) && inb_r(&F, 2, i, j, k))) continue;
     const real_t *c = phi + at(&F, i, j, k);
     for (int d = 0; d < 3; d++) {
       long s = F.s[d];
@@ -253,7 +290,7 @@ void lsm3dlaplacianorder2local_(real_t *lap, A3(g), const real_t *phi, A3(f), DX
   gbox G = B3(g), F = B3(f), NB = NBBOX;
   real_t a = 1.0 / *dx / *dx, b = 1.0 / *dy / *dy, e = 1.0 / *dz / *dz;
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&G, i, j, k) && inb_r(&F, 1, i, j, k))) continue;
     const real_t *c = phi + at(&F, i, j, k);
     long sx = F.s[0], sy = F.s[1], sz = F.s[2];
     lap[at(&G, i, j, k)] = a * (c[sx] - 2.0 * c[0] + c[-sx]) + b * (c[sy] - 2.0 * c[0] + c[-sy]) +
@@ -268,7 +305,7 @@ void lsm3dcomputeavegradphilocal_(real_t *ave, const real_t *phi, A3(f), DX_ARGS
   real_t s = 0.0;
   int count = 0;
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb_r(&F, 1, i, j, k))) continue;
     const real_t *c = phi + at(&F, i, j, k);
     real_t g[3];
     for (int d = 0; d < 3; d++) g[d] = (c[F.s[d]] - c[-F.s[d]]) * fac[d];
@@ -285,7 +322,7 @@ void lsm3dgradientmagnitudelocal_(const real_t *px, const real_t *py, const real
                                   real_t *mag, A3(g), LOCAL_TAIL) {
   gbox G = B3(g), NB = NBBOX;
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&G, i, j, k))) continue;
     long c = at(&G, i, j, k);
     real_t x2 = px[c] * px[c], y2 = py[c] * py[c], z2 = pz[c] * pz[c];
     if (x2 < ORACLE_ZERO_TOL) x2 = 0.0;
@@ -301,7 +338,8 @@ void lsm3drk1steplocal_(real_t *un, A3(a), const real_t *u, A3(b), const real_t 
                         const real_t *dt, LOCAL_TAIL) {
   gbox A = B3(a), B = B3(b), C = B3(c), NB = NBBOX;
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (GATE) un[at(&A, i, j, k)] = u[at(&B, i, j, k)] + *dt * rhs[at(&C, i, j, k)];
+    if (GATE && inb(&A, i, j, k) && inb(&B, i, j, k) && inb(&C, i, j, k))
+      un[at(&A, i, j, k)] = u[at(&B, i, j, k)] + *dt * rhs[at(&C, i, j, k)];
   }
 }
 void lsm3dtvdrk2stage1local_(real_t *un, A3(a), const real_t *u, A3(b), const real_t *rhs, A3(c),
@@ -318,7 +356,7 @@ void lsm3dtvdrk2stage2local_(real_t *un, A3(a), const real_t *u1, A3(b), const r
                              const real_t *rhs, A3(d), const real_t *dt, LOCAL_TAIL) {
   gbox A = B3(a), B = B3(b), C = B3(c), D = B3(d), NB = NBBOX;
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (GATE)
+    if (GATE && inb(&A, i, j, k) && inb(&B, i, j, k) && inb(&C, i, j, k) && inb(&D, i, j, k))
       un[at(&A, i, j, k)] =
           0.5 * (u[at(&C, i, j, k)] + u1[at(&B, i, j, k)] + *dt * rhs[at(&D, i, j, k)]);
   }
@@ -327,7 +365,7 @@ void lsm3dtvdrk3stage2local_(real_t *u2, A3(a), const real_t *u1, A3(b), const r
                              const real_t *rhs, A3(d), const real_t *dt, LOCAL_TAIL) {
   gbox A = B3(a), B = B3(b), C = B3(c), D = B3(d), NB = NBBOX;
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (GATE)
+    if (GATE && inb(&A, i, j, k) && inb(&B, i, j, k) && inb(&C, i, j, k) && inb(&D, i, j, k))
       u2[at(&A, i, j, k)] = 0.75 * u[at(&C, i, j, k)] +
                             0.25 * (u1[at(&B, i, j, k)] + *dt * rhs[at(&D, i, j, k)]);
   }
@@ -337,7 +375,7 @@ void lsm3dtvdrk3stage3local_(real_t *un, A3(a), const real_t *u2, A3(b), const r
   gbox A = B3(a), B = B3(b), C = B3(c), D = B3(d), NB = NBBOX;
   const real_t c13 = 1.0 / 3.0, c23 = 2.0 / 3.0;
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (GATE)
+    if (GATE && inb(&A, i, j, k) && inb(&B, i, j, k) && inb(&C, i, j, k) && inb(&D, i, j, k))
       un[at(&A, i, j, k)] = c13 * u[at(&C, i, j, k)] +
                             c23 * (u2[at(&B, i, j, k)] + *dt * rhs[at(&D, i, j, k)]);
   }
@@ -347,7 +385,9 @@ void lsm3dtvdrk3stage3local_(real_t *un, A3(a), const real_t *u2, A3(b), const r
 void lsm3dzerooutlevelseteqnrhslocal_(real_t *rhs, A3(r), LIST_ARGS, const int *nlo,
                                       const int *nhi) {
   gbox R = B3(r);
-  FOR_LIST(*nlo, *nlo, *nhi) rhs[at(&R, i, j, k)] = 0.0; /* no mark test (:44-50) */
+  FOR_LIST(*nlo, *nlo, *nhi) {
+    if (inb(&R, i, j, k)) rhs[at(&R, i, j, k)] = 0.0; /* no mark test (:44-50) */
+  }
 }
 
 void lsm3daddadvectiontermtolserhslocal_(real_t *rhs, A3(r), const real_t *px, const real_t *py,
@@ -355,7 +395,7 @@ void lsm3daddadvectiontermtolserhslocal_(real_t *rhs, A3(r), const real_t *px, c
                                          const real_t *vy, const real_t *vz, A3(v), LOCAL_TAIL) {
   gbox R = B3(r), G = B3(g), V = B3(v), NB = NBBOX;
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&R, i, j, k) && inb(&G, i, j, k) && inb(&V, i, j, k))) continue;
     long r = at(&R, i, j, k), g = at(&G, i, j, k), v = at(&V, i, j, k);
     rhs[r] = rhs[r] - (vx[v] * px[g] + vy[v] * py[g] + vz[v] * pz[g]);
   }
@@ -380,7 +420,7 @@ void lsm3daddnormalveltermtolserhslocal_(real_t *rhs, A3(r), const real_t *pxp, 
                                          const real_t *vn, A3(v), LOCAL_TAIL) {
   gbox R = B3(r), P = B3(p), M = B3(m), V = B3(v), NB = NBBOX;
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&R, i, j, k) && inb(&P, i, j, k) && inb(&M, i, j, k) && inb(&V, i, j, k))) continue;
     real_t w = vn[at(&V, i, j, k)];
     long a = at(&P, i, j, k), b = at(&M, i, j, k), r = at(&R, i, j, k);
     real_t s = godunov_sq(w, pxp[a], pyp[a], pzp[a], pxm[b], pym[b], pzm[b]);
@@ -396,7 +436,7 @@ void lsm3daddconstnormalveltermtolserhslocal_(real_t *rhs, A3(r), const real_t *
   gbox R = B3(r), P = B3(p), M = B3(m), NB = NBBOX;
   real_t w = *vel_n;
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&R, i, j, k) && inb(&P, i, j, k) && inb(&M, i, j, k))) continue;
     long a = at(&P, i, j, k), b = at(&M, i, j, k), r = at(&R, i, j, k);
     real_t s = godunov_sq(w, pxp[a], pyp[a], pzp[a], pxm[b], pym[b], pzm[b]);
     if (fabs(w) >= ORACLE_ZERO_TOL) rhs[r] = rhs[r] - w * sqrt(s);
@@ -416,7 +456,7 @@ void lsm3daddconstcurvtermtolserhslocal_(real_t *rhs, A3(r), const real_t *px, c
                                          const real_t *b, LOCAL_TAIL) {
   gbox R = B3(r), G = B3(g), H = B3(h), NB = NBBOX;
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&R, i, j, k) && inb(&G, i, j, k) && inb(&H, i, j, k))) continue;
     long g = at(&G, i, j, k), h = at(&H, i, j, k), r = at(&R, i, j, k);
     real_t m2 = px[g] * px[g] + py[g] * py[g] + pz[g] * pz[g];
     real_t curv = 0.0;
@@ -436,7 +476,7 @@ void lsm3dcomputereinitializationeqnrhslocal_(
   dx_sq = dx_sq * dx_sq;
   const int use0 = (*use_phi0_for_sgn == 1);
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&R, i, j, k) && inb(use0 ? &Z : &F, i, j, k) && inb(&P, i, j, k) && inb(&M, i, j, k))) continue;
     real_t pc = use0 ? phi0[at(&Z, i, j, k)] : phi[at(&F, i, j, k)];
     long a = at(&P, i, j, k), b = at(&M, i, j, k);
     real_t gp[3] = {pxp[a], pyp[a], pzp[a]}, gm[3] = {pxm[b], pym[b], pzm[b]}, st[3];
@@ -464,7 +504,7 @@ void lsm3dcomputemeancurvatureorder2local_(real_t *kappa, A3(k), const real_t *p
   real_t fxy = 0.25 / *dx / *dy, fxz = 0.25 / *dx / *dz, fyz = 0.25 / *dy / *dz;
   long sx = F.s[0], sy = F.s[1], sz = F.s[2];
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&K, i, j, k) && inb(&G, i, j, k) && inb_r(&F, 1, i, j, k))) continue;
     const real_t *c = phi + at(&F, i, j, k);
     real_t xx = (c[sx] - 2.0 * c[0] + c[-sx]) * fxx;
     real_t yy = (c[sy] - 2.0 * c[0] + c[-sy]) * fyy;
@@ -485,7 +525,7 @@ void lsm3dmaxnormdifflocal_(real_t *out, const real_t *f1, A3(a), const real_t *
   gbox A = B3(a), B = B3(b), NB = NBBOX;
   real_t m = 0.0; /* :72 */
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&A, i, j, k) && inb(&B, i, j, k))) continue;
     real_t d = fabs(f1[at(&A, i, j, k)] - f2[at(&B, i, j, k)]);
     if (d > m) m = d;
   }
@@ -498,7 +538,7 @@ void lsm3dcomputestableadvectiondtlocal_(real_t *dt, const real_t *vx, const rea
   gbox V = B3(v), NB = NBBOX;
   real_t ix_ = 1.0 / *dx, iy_ = 1.0 / *dy, iz_ = 1.0 / *dz, m = -1.0;
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&V, i, j, k))) continue;
     long c = at(&V, i, j, k);
     real_t u = fabs(vx[c]) * ix_ + fabs(vy[c]) * iy_ + fabs(vz[c]) * iz_;
     if (u > m) m = u;
@@ -515,7 +555,7 @@ void lsm3dcomputestablenormalveldtlocal_(real_t *dt, const real_t *vn, A3(v), co
   real_t max_dx_sq = mx * mx;
   real_t inv[3] = {1.0 / *dx, 1.0 / *dy, 1.0 / *dz}, best = -1.0;
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&V, i, j, k) && inb(&P, i, j, k) && inb(&M, i, j, k))) continue;
     long a = at(&P, i, j, k), b = at(&M, i, j, k);
     real_t cx = fmax2(fabs(pxp[a]), fabs(pxm[b]));
     real_t cy = fmax2(fabs(pyp[a]), fabs(pym[b]));
@@ -544,7 +584,7 @@ void lsm3dcomputestableconstnormalveldtlocal_(real_t *dt, const real_t *vel_n, c
   real_t max_dx_sq = mx * mx;
   real_t inv[3] = {1.0 / *dx, 1.0 / *dy, 1.0 / *dz}, best = -1.0, avn = fabs(*vel_n);
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&P, i, j, k) && inb(&M, i, j, k))) continue;
     long a = at(&P, i, j, k), b = at(&M, i, j, k);
     real_t cx = fmax2(fabs(pxp[a]), fabs(pxm[b]));
     real_t cy = fmax2(fabs(pyp[a]), fabs(pym[b]));
@@ -694,7 +734,7 @@ void lsm3dmultiplycutofflserhslocal_(const real_t *phi, real_t *rhs, A3(g), LOCA
   real_t c2 = (*gamma - *beta);
   c2 = c2 * c2 * c2;
   FOR_LIST(*nlo, *nlo, *nhi) {
-    if (!GATE) continue;
+    if (!GATE || !(inb(&G, i, j, k))) continue;
     long c = at(&G, i, j, k);
     real_t a = fabs(phi[c]), co;
     if (a <= *beta) {
@@ -749,12 +789,17 @@ void lsm3dcheckouternarrowbandlayer_(int *change_sign, const real_t *phi, A3(g),
 void lsm3dimposemasklocal_(real_t *dest, A3(d), const real_t *src, A3(s), const real_t *mask,
                            A3(m), LIST_ARGS, const int *nlo, const int *nhi) {
   gbox D = B3(d), S = B3(s), M = B3(m);
-  FOR_LIST(*nlo, *nlo, *nhi) dest[at(&D, i, j, k)] = fmax2(mask[at(&M, i, j, k)], src[at(&S, i, j, k)]);
+  FOR_LIST(*nlo, *nlo, *nhi) {
+    if (inb(&D, i, j, k) && inb(&S, i, j, k) && inb(&M, i, j, k))
+      dest[at(&D, i, j, k)] = fmax2(mask[at(&M, i, j, k)], src[at(&S, i, j, k)]);
+  }
 }
 
 /* lsm3dCopyDataLocal (:725-774) */
 void lsm3dcopydatalocal_(real_t *dest, A3(d), const real_t *src, A3(s), LIST_ARGS, const int *nlo,
                          const int *nhi) {
   gbox D = B3(d), S = B3(s);
-  FOR_LIST(*nlo, *nlo, *nhi) dest[at(&D, i, j, k)] = src[at(&S, i, j, k)];
+  FOR_LIST(*nlo, *nlo, *nhi) {
+    if (inb(&D, i, j, k) && inb(&S, i, j, k)) dest[at(&D, i, j, k)] = src[at(&S, i, j, k)];
+  }
 }

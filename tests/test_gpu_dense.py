@@ -10,7 +10,7 @@ import pytest
 import lsmlib_gb300 as L
 from tests import harness as H
 
-DENSE = list(L.ABI)
+from tests.test_oracle_pin import DENSE
 
 
 @pytest.mark.gpu
