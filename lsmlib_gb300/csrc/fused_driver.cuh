@@ -106,11 +106,20 @@ void launch_stage(const CUtensorMap &tm, const StageArgs<R> &a) {
   dim3 grd((unsigned)((L.nx + TX - 1) / TX), (unsigned)((L.ny + TY - 1) / TY), (unsigned)((L.nz + TZ - 1) / TZ));
   const size_t smem = (size_t)SX * SY * SZ * sizeof(R);
   static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_stage<R, MODE, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr_set = true;
+  if constexpr (!EXACT && sizeof(R) == 4) {
+    // FP32 form: the packed cell-pair kernel
+    if (!attr_set) {
+      cudaFuncSetAttribute(k_stage_f32<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      attr_set = true;
+    }
+    k_stage_f32<MODE><<<grd, blk, smem, stream()>>>(tm, a);
+  } else {
+    if (!attr_set) {
+      cudaFuncSetAttribute(k_stage<R, MODE, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      attr_set = true;
+    }
+    k_stage<R, MODE, EXACT><<<grd, blk, smem, stream()>>>(tm, a);
   }
-  k_stage<R, MODE, EXACT><<<grd, blk, smem, stream()>>>(tm, a);
   note_launch();
 }
 

@@ -236,3 +236,171 @@ __global__ void __launch_bounds__(TX * TY) k_stage(const __grid_constant__ CUten
 
 }  // namespace fused
 }  // namespace lsmgpu
+
+// ---------------------------------------------------------------------------
+// FP32 stage kernel on cell pairs: each thread advances cells (z, z+1) of its
+// column together, one cell per lane of Blackwell's packed FP32x2
+// instructions (FADD2 / FMUL2 / FFMA2), which halves the issued instructions
+// of the WENO5 arithmetic.  Comparisons, selections and the reciprocals stay
+// per lane.
+// ---------------------------------------------------------------------------
+namespace lsmgpu {
+namespace fused {
+
+__device__ __forceinline__ float2 sp(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// WENO5-JS on two cells at once, the epsilon-scaled weight form of
+// weno5_fast with the common factors folded: smoothness and epsilon are both
+// scaled by 12 (only S/eps enters the weights) and the candidate stencils by
+// 6 (divided out with the normalisation).
+__device__ __forceinline__ float2 weno5_x2(float2 v1, float2 v2, float2 v3, float2 v4, float2 v5) {
+  const float2 q1s = mul2(v1, v1), q2s = mul2(v2, v2), q3s = mul2(v3, v3), q4s = mul2(v4, v4), q5s = mul2(v5, v5);
+  float2 m;
+  m.x = fmaxf(fmaxf(fmaxf(q1s.x, q2s.x), fmaxf(q3s.x, q4s.x)), q5s.x);
+  m.y = fmaxf(fmaxf(fmaxf(q1s.y, q2s.y), fmaxf(q3s.y, q4s.y)), q5s.y);
+  const float2 eps = fma2(sp(12e-6f), m, sp(12e-36f));
+  // 6 * candidate stencils
+  const float2 P1 = fma2(sp(2.f), v1, fma2(sp(-7.f), v2, mul2(sp(11.f), v3)));
+  const float2 P2 = fma2(sp(-1.f), v2, fma2(sp(5.f), v3, mul2(sp(2.f), v4)));
+  const float2 P3 = fma2(sp(2.f), v3, fma2(sp(5.f), v4, mul2(sp(-1.f), v5)));
+  // 12 * smoothness indicators: 13 t^2 + 3 u^2
+  float2 t = fma2(sp(-2.f), v2, add2(v1, v3));
+  float2 u = fma2(sp(-4.f), v2, fma2(sp(3.f), v3, v1));
+  const float2 S1 = fma2(mul2(sp(13.f), t), t, mul2(mul2(sp(3.f), u), u));
+  t = fma2(sp(-2.f), v3, add2(v2, v4));
+  u = fma2(sp(-1.f), v4, v2);
+  const float2 S2 = fma2(mul2(sp(13.f), t), t, mul2(mul2(sp(3.f), u), u));
+  t = fma2(sp(-2.f), v4, add2(v3, v5));
+  u = fma2(sp(-4.f), v4, fma2(sp(3.f), v3, v5));
+  const float2 S3 = fma2(mul2(sp(13.f), t), t, mul2(mul2(sp(3.f), u), u));
+  const float2 r = make_float2(__fdividef(1.f, eps.x), __fdividef(1.f, eps.y));
+  float2 w1 = fma2(S1, r, sp(1.f)), w2 = fma2(S2, r, sp(1.f)), w3 = fma2(S3, r, sp(1.f));
+  w1 = mul2(w1, w1);
+  w2 = mul2(w2, w2);
+  w3 = mul2(w3, w3);
+  const float2 n1 = mul2(sp(0.1f), mul2(w2, w3));
+  const float2 n2 = mul2(sp(0.6f), mul2(w1, w3));
+  const float2 n3 = mul2(sp(0.3f), mul2(w1, w2));
+  const float2 num = fma2(n1, P1, fma2(n2, P2, mul2(n3, P3)));
+  const float2 den = mul2(sp(6.f), add2(add2(n1, n2), n3));
+  return make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(TX * TY) k_stage_f32(const __grid_constant__ CUtensorMap tm, StageArgs<float> a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float *tile = reinterpret_cast<float *>(smem_raw);
+  __shared__ __align__(8) uint64_t bar;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int tid = tx + TX * ty;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+  if (tid == 0) {
+    prefetch_tmap(&tm);
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    mbar_arrive_expect_tx(&bar, (uint32_t)(SX * SY * SZ * sizeof(float)));
+    tma_load_3d(tile, &tm, x0 + GX - 4, y0 + GY - 3, z0 + GZ - 3, &bar);
+  }
+  if (!mbar_wait(&bar, 0, kMaxPolls)) {
+    if (tid == 0) atomicExch(a.err, LSMGPU_ERR_TIMEOUT);
+    mbar_wait(&bar, 0, kMaxPolls);
+    return;
+  }
+  const Layout &L = a.L;
+  const int i = x0 + tx, j = y0 + ty;
+  if (i >= L.nx || j >= L.ny) return;
+  const int sx = tx + 4, sy = ty + 3;
+  const int kmax = min(TZ, L.nz - z0);
+  const int st[3] = {1, SX, SX * SY};
+  const float2 inv[3] = {sp(a.inv[0]), sp(a.inv[1]), sp(a.inv[2])};
+
+  for (int tz = 0; tz < kmax; tz += 2) {
+    const bool two = tz + 1 < kmax;  // the second lane is a real cell
+    const float *c0 = tile + ((tz + 3) * SY + sy) * SX + sx;
+    const float *c1 = two ? c0 + SX * SY : c0;
+    const int k0 = z0 + tz, k1 = two ? k0 + 1 : k0;
+    const long long cell0 = L.idx(i, j, k0), cell1 = L.idx(i, j, k1);
+    float2 rhs;
+    if (MODE == REINIT) {
+      float gp0[3], gp1[3], gm0[3], gm1[3];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        float2 v[6];  // scaled D1(c-2 .. c+3) for both cells
+#pragma unroll
+        for (int f = -2; f <= 3; f++)
+          v[f + 2] = mul2(make_float2(c0[f * st[d]] - c0[(f - 1) * st[d]], c1[f * st[d]] - c1[(f - 1) * st[d]]), inv[d]);
+        const float2 p = weno5_x2(v[5], v[4], v[3], v[2], v[1]);
+        const float2 m = weno5_x2(v[0], v[1], v[2], v[3], v[4]);
+        gp0[d] = p.x; gp1[d] = p.y;
+        gm0[d] = m.x; gm1[d] = m.y;
+      }
+      const float pc0 = a.use0 ? a.phi0[cell0] : c0[0];
+      const float pc1 = a.use0 ? a.phi0[cell1] : c1[0];
+      rhs.x = reinit_term<float, false>(pc0, gp0, gm0, a.dx_sq, a.use0 != 0);
+      rhs.y = reinit_term<float, false>(pc1, gp1, gm1, a.dx_sq, a.use0 != 0);
+    } else {
+      float vel0[3], vel1[3];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        vel0[d] = (MODE == ADV_CONST) ? a.vconst[d] : a.vel[d][cell0];
+        vel1[d] = (MODE == ADV_CONST) ? a.vconst[d] : a.vel[d][cell1];
+      }
+      float2 dot = sp(0.f);
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        // per lane: the backward stencil D1(c-2..c+2) for v > 0, the forward
+        // stencil D1(c+3..c-1) otherwise (spatial_derivatives3d.f.in:2756-2812)
+        float2 v[5];
+        const int s = st[d];
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+          const int f0 = (vel0[d] > 0.f) ? q - 2 : 3 - q;
+          const int f1 = (vel1[d] > 0.f) ? q - 2 : 3 - q;
+          v[q] = mul2(make_float2(c0[f0 * s] - c0[(f0 - 1) * s], c1[f1 * s] - c1[(f1 - 1) * s]), inv[d]);
+        }
+        float2 g = weno5_x2(v[0], v[1], v[2], v[3], v[4]);
+        if (fabsf(vel0[d]) < 1e-11f) g.x = 0.f;
+        if (fabsf(vel1[d]) < 1e-11f) g.y = 0.f;
+        dot = fma2(make_float2(vel0[d], vel1[d]), g, dot);
+      }
+      rhs = make_float2(-dot.x, -dot.y);
+    }
+    const float2 u0 = make_float2(c0[0], c1[0]);
+    float2 u;
+    if (a.stage == 1) {
+      u = fma2(sp(a.dt), rhs, u0);
+    } else {
+      const float2 un = make_float2(a.phi_n[cell0], a.phi_n[cell1]);
+      if (a.stage == 2)
+        u = fma2(sp(0.75f), un, mul2(sp(0.25f), fma2(sp(a.dt), rhs, u0)));
+      else
+        u = fma2(sp(1.f / 3.f), un, mul2(sp(2.f / 3.f), fma2(sp(a.dt), rhs, u0)));
+    }
+    for (int lane = 0; lane < (two ? 2 : 1); lane++) {
+      const int k = lane ? k1 : k0;
+      const float val = lane ? u.y : u.x;
+      a.out[L.idx(i, j, k)] = val;
+      if (a.periodic) {
+        int oi[2] = {0, 0}, oj[2] = {0, 0}, ok_[2] = {0, 0};
+        int ni = 1, nj = 1, nk = 1;
+        if (i < 3) oi[ni++] = L.nx; else if (i >= L.nx - 3) oi[ni++] = -L.nx;
+        if (j < 3) oj[nj++] = L.ny; else if (j >= L.ny - 3) oj[nj++] = -L.ny;
+        if (k < 3) ok_[nk++] = L.nz; else if (k >= L.nz - 3) ok_[nk++] = -L.nz;
+        if (ni + nj + nk > 3)
+          for (int p = 0; p < ni; p++)
+            for (int q = 0; q < nj; q++)
+              for (int r = 0; r < nk; r++)
+                if (p | q | r) a.out[L.idx(i + oi[p], j + oj[q], k + ok_[r])] = val;
+      }
+    }
+  }
+}
+
+}  // namespace fused
+}  // namespace lsmgpu
