@@ -111,6 +111,30 @@ int lsmgpu_mean_curvature_o2_f32(float *kappa, const int *kappa_gb, const float 
                                  const int *phi_gb, float *grad_phi_mag, const int *fb, float dx,
                                  float dy, float dz);
 
+/* Allocation-free CFL-stable advection dt.  No counterpart in LSMLIB: it is
+ * lsm3dcomputestableadvectiondt_ (same arguments, same result) for callers
+ * that cannot let a library allocate device memory — a solver running inside
+ * another framework's memory pool that owns all device memory, or a
+ * time-step loop that must not stall on the device synchronisation cudaMalloc
+ * and cudaFree can cause.  It calls no allocator: its reduction scratch is a
+ * fixed 512 KiB __device__ array in the library, so
+ *  - the velocity arrays must already be in device (or managed) memory;
+ *  - the index box may hold at most 536,870,912 cells (65536 blocks of 8192
+ *    cells); larger boxes return LSMGPU_ERR_CAPACITY and compute nothing;
+ *  - dt may point to host or device memory (a host dt waits for the stream);
+ *  - the first call on each device looks up the scratch address
+ *    (cudaGetSymbolAddress); make that first call before any stream capture;
+ *  - every call on a device shares the scratch and overwrites it, so calls
+ *    that may overlap on the GPU (other streams or host threads) race and
+ *    must be serialised by the caller.
+ * Returns an LSMGPU_* status. */
+int lsmgpu_compute_stable_advection_dt_noalloc(
+    double *dt, const double *vel_x, const double *vel_y, const double *vel_z, const int *ilo_vel_gb,
+    const int *ihi_vel_gb, const int *jlo_vel_gb, const int *jhi_vel_gb, const int *klo_vel_gb,
+    const int *khi_vel_gb, const int *ilo_ib, const int *ihi_ib, const int *jlo_ib, const int *jhi_ib,
+    const int *klo_ib, const int *khi_ib, const double *dx, const double *dy, const double *dz,
+    const double *cfl_number);
+
 /* Library version string. */
 const char *lsmgpu_version(void);
 

@@ -24,7 +24,8 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr", "--extended-lambda", "-I", os.path.join(HERE, "..", "include")]
 
 # FP64 parity units: no contraction of a*b+c into FMA
-NO_FMA = {"dense.cu", "dense2.cu", "local.cu", "band.cu", "fused_f64.cu", "batched_f64.cu", "adjoint_f64.cu"}
+NO_FMA = {"dense.cu", "dense2.cu", "local.cu", "band.cu", "fused_f64.cu", "batched_f64.cu", "adjoint_f64.cu",
+          "noalloc.cu"}
 
 
 def nvcc():
