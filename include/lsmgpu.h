@@ -111,6 +111,26 @@ int lsmgpu_mean_curvature_o2_f32(float *kappa, const int *kappa_gb, const float 
                                  const int *phi_gb, float *grad_phi_mag, const int *fb, float dx,
                                  float dy, float dz);
 
+/* Batched advection of many independent grids (FP32): n_grids grids packed in
+ * one array, grid g occupying (nx+6)(ny+6)(nz+6) values (3 ghost cells per
+ * side, column-major) from phi + offsets[g]; dims holds (nx, ny, nz) per grid,
+ * vel the constant velocity (u, v, w) per grid, spacing (dx, dy, dz) per grid
+ * and dt one step per grid.  Each TVD-RK3 stage of all grids is one
+ * persistent kernel launch pulling 32 x 8 x TZ tiles from a work counter; the
+ * n_steps x 3 launches are captured in a CUDA graph.  TZ and the CTAs per SM
+ * are picked by an autotuner on the first call for a batch shape.  Periodic
+ * boundaries only (bc = LSMGPU_BC_PERIODIC).  flags: LSMGPU_BATCH_LOOP runs
+ * one single-grid launch per grid per stage instead (for comparison),
+ * LSMGPU_BATCH_NO_GRAPH launches without a graph, LSMGPU_BATCH_TZ(n) forces
+ * tile depth n (4, 8 or 16) and skips the autotuner.  The result is the same
+ * in every mode. */
+#define LSMGPU_BATCH_LOOP 1
+#define LSMGPU_BATCH_NO_GRAPH 2
+#define LSMGPU_BATCH_TZ(n) ((n) << 8)
+int lsmgpu_advect_batch_weno5_tvdrk3_f32(float *phi, const long long *offsets, const int *dims,
+                                         int n_grids, const float *vel, const float *spacing,
+                                         const float *dt, int n_steps, int bc, int flags);
+
 /* Allocation-free CFL-stable advection dt.  No counterpart in LSMLIB: it is
  * lsm3dcomputestableadvectiondt_ (same arguments, same result) for callers
  * that cannot let a library allocate device memory — a solver running inside

@@ -179,3 +179,32 @@ def mean_curvature_o2(kappa, kappa_gb, phi, phi_gb, fb, dx, grad_phi_mag=None, p
             dx, dy or dx, dz or dx)
     if rc != 0:
         raise RuntimeError("lsmgpu mean curvature failed: %s" % (last_error()[1],))
+
+
+BATCH_LOOP, BATCH_NO_GRAPH = 1, 2
+
+
+def batch_tz(n):
+    return n << 8
+
+
+def advect_batch_weno5_tvdrk3(phi, offsets, dims, vel, spacing, dt, n_steps, flags=0):
+    """Advect a packed batch of grids in place (FP32).  `phi` is one float32
+    buffer (numpy, torch or device address); grid g holds (nx+6)(ny+6)(nz+6)
+    values from offsets[g]; dims/vel/spacing are (n, 3) arrays, dt has n
+    entries."""
+    import numpy as np
+    h = lib()
+    fn = h.lsmgpu_advect_batch_weno5_tvdrk3_f32
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    dm = np.ascontiguousarray(dims, dtype=np.int32)
+    v = np.ascontiguousarray(vel, dtype=np.float32)
+    sp = np.ascontiguousarray(spacing, dtype=np.float32)
+    d = np.ascontiguousarray(dt, dtype=np.float32)
+    rc = fn(_ptr(phi), off.ctypes.data, dm.ctypes.data, len(off), v.ctypes.data, sp.ctypes.data,
+            d.ctypes.data, int(n_steps), BC_PERIODIC, int(flags))
+    if rc != 0:
+        raise RuntimeError("lsmgpu batch advect failed: %s" % (last_error()[1],))

@@ -289,34 +289,17 @@ __device__ __forceinline__ float2 weno5_x2(float2 v1, float2 v2, float2 v3, floa
   return make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(TX * TY) k_stage_f32(const __grid_constant__ CUtensorMap tm, StageArgs<float> a) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  float *tile = reinterpret_cast<float *>(smem_raw);
-  __shared__ __align__(8) uint64_t bar;
+// Computes one 32 x 8 x TZ_ tile whose haloed input (40 x 14 x (TZ_ + 6)) is
+// in `tile`; shared by the single-grid kernel and the batched persistent
+// kernel (which picks TZ_ with its autotuner).
+template <int MODE, int TZ_ = TZ>
+__device__ __forceinline__ void f32_tile(const float *tile, const StageArgs<float> &a, int x0, int y0, int z0) {
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int tid = tx + TX * ty;
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
-  if (tid == 0) {
-    prefetch_tmap(&tm);
-    mbar_init(&bar, 1);
-    fence_barrier_init();
-  }
-  __syncthreads();
-  if (tid == 0) {
-    mbar_arrive_expect_tx(&bar, (uint32_t)(SX * SY * SZ * sizeof(float)));
-    tma_load_3d(tile, &tm, x0 + GX - 4, y0 + GY - 3, z0 + GZ - 3, &bar);
-  }
-  if (!mbar_wait(&bar, 0, kMaxPolls)) {
-    if (tid == 0) atomicExch(a.err, LSMGPU_ERR_TIMEOUT);
-    mbar_wait(&bar, 0, kMaxPolls);
-    return;
-  }
   const Layout &L = a.L;
   const int i = x0 + tx, j = y0 + ty;
   if (i >= L.nx || j >= L.ny) return;
   const int sx = tx + 4, sy = ty + 3;
-  const int kmax = min(TZ, L.nz - z0);
+  const int kmax = min(TZ_, L.nz - z0);
   const int st[3] = {1, SX, SX * SY};
   const float2 inv[3] = {sp(a.inv[0]), sp(a.inv[1]), sp(a.inv[2])};
 
@@ -400,6 +383,32 @@ __global__ void __launch_bounds__(TX * TY) k_stage_f32(const __grid_constant__ C
       }
     }
   }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(TX * TY) k_stage_f32(const __grid_constant__ CUtensorMap tm, StageArgs<float> a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float *tile = reinterpret_cast<float *>(smem_raw);
+  __shared__ __align__(8) uint64_t bar;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int tid = tx + TX * ty;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+  if (tid == 0) {
+    prefetch_tmap(&tm);
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    mbar_arrive_expect_tx(&bar, (uint32_t)(SX * SY * SZ * sizeof(float)));
+    tma_load_3d(tile, &tm, x0 + GX - 4, y0 + GY - 3, z0 + GZ - 3, &bar);
+  }
+  if (!mbar_wait(&bar, 0, kMaxPolls)) {
+    if (tid == 0) atomicExch(a.err, LSMGPU_ERR_TIMEOUT);
+    mbar_wait(&bar, 0, kMaxPolls);
+    return;
+  }
+  f32_tile<MODE, TZ>(tile, a, x0, y0, z0);
 }
 
 }  // namespace fused

@@ -48,6 +48,7 @@ def apply_bc(lib, phi, gb, fb, bc):
 
 
 def _rhs(lib, mode, phi, gb, fb, dx, vel, phi0, use0):
+    dx, dy, dz = dx if isinstance(dx, (tuple, list)) else (dx, dx, dx)
     shape = H.shape_of(gb)
     z = lambda: np.zeros(shape, order="F")
     if mode == "reinit":
@@ -56,20 +57,20 @@ def _rhs(lib, mode, phi, gb, fb, dx, vel, phi0, use0):
         vals, _ = H.make_call("lsm3dhjweno5_", gb, fb, arrays={
             "phi": phi, "phi_x_plus": pp[0], "phi_y_plus": pp[1], "phi_z_plus": pp[2],
             "phi_x_minus": pm[0], "phi_y_minus": pm[1], "phi_z_minus": pm[2]},
-            scalars={"dx": dx, "dy": dx, "dz": dx})
+            scalars={"dx": dx, "dy": dy, "dz": dz})
         L.invoke(lib, "lsm3dhjweno5_", vals)
         rhs = z()
         vals, _ = H.make_call("lsm3dcomputereinitializationeqnrhs_", gb, fb, arrays={
             "reinit_rhs": rhs, "phi": phi, "phi0": phi0, "phi_x_plus": pp[0],
             "phi_y_plus": pp[1], "phi_z_plus": pp[2], "phi_x_minus": pm[0],
             "phi_y_minus": pm[1], "phi_z_minus": pm[2]},
-            scalars={"dx": dx, "dy": dx, "dz": dx, "use_phi0_for_sgn": use0})
+            scalars={"dx": dx, "dy": dy, "dz": dz, "use_phi0_for_sgn": use0})
         L.invoke(lib, "lsm3dcomputereinitializationeqnrhs_", vals)
         return rhs
     g = [z(), z(), z()]
     vals, _ = H.make_call("lsm3dupwindhjweno5_", gb, fb, arrays={
         "phi": phi, "phi_x": g[0], "phi_y": g[1], "phi_z": g[2],
-        "vel_x": vel[0], "vel_y": vel[1], "vel_z": vel[2]}, scalars={"dx": dx, "dy": dx, "dz": dx})
+        "vel_x": vel[0], "vel_y": vel[1], "vel_z": vel[2]}, scalars={"dx": dx, "dy": dy, "dz": dz})
     L.invoke(lib, "lsm3dupwindhjweno5_", vals)
     rhs = np.asfortranarray(np.random.default_rng(0).standard_normal(shape))
     vals, _ = H.make_call("lsm3dzerooutlevelseteqnrhs_", gb, fb, arrays={"lse_rhs": rhs})
