@@ -111,6 +111,27 @@ int lsmgpu_mean_curvature_o2_f32(float *kappa, const int *kappa_gb, const float 
                                  const int *phi_gb, float *grad_phi_mag, const int *fb, float dx,
                                  float dy, float dz);
 
+/* Narrow-band curvature flow: n_steps TVD-RK3 steps of
+ * phi_t + Vn |grad phi| = 0, Vn = a_n - b_n * kappa, on a narrow band of
+ * half-width gamma (inner width beta, 3 neighbour levels) rebuilt from phi
+ * every rebuild_every steps (lsm3dDetermineNarrowBand).  Per stage, on
+ * level-0 cells: mean curvature (central differences), HJ WENO5 plus/minus on
+ * the band, the Godunov normal-velocity RHS, the cubic cut-off between beta
+ * and gamma, the TVD-RK3 stage update — the LSMLIB *_LOCAL sequence, one
+ * gather kernel per stage.  dt is the CFL-stable normal-velocity dt of stage 1
+ * of each step (lsm3dComputeStableNormalVelDtLOCAL, CFL number cfl).  phi is
+ * column-major over gb (every band cell must lie 3 cells inside gb); dx is
+ * the spacing of all three axes.  dt_log (n_steps doubles) and band_log (one
+ * level-0 cell count per rebuild) are optional host outputs.  The _f64 form
+ * matches the LSMLIB sequence bit for bit; the _f32 form stores phi in single
+ * precision and keeps the band's distance test in double. */
+int lsmgpu_band_flow_weno5_tvdrk3_f64(double *phi, const int *gb, const int *fb, double dx, double a_n,
+                                      double b_n, double cfl, double gamma, double beta, int n_steps,
+                                      int rebuild_every, double *dt_log, long long *band_log);
+int lsmgpu_band_flow_weno5_tvdrk3_f32(float *phi, const int *gb, const int *fb, float dx, float a_n,
+                                      float b_n, float cfl, float gamma, float beta, int n_steps,
+                                      int rebuild_every, double *dt_log, long long *band_log);
+
 /* Batched advection of many independent grids (FP32): n_grids grids packed in
  * one array, grid g occupying (nx+6)(ny+6)(nz+6) values (3 ghost cells per
  * side, column-major) from phi + offsets[g]; dims holds (nx, ny, nz) per grid,

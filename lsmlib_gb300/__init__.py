@@ -208,3 +208,23 @@ def advect_batch_weno5_tvdrk3(phi, offsets, dims, vel, spacing, dt, n_steps, fla
             d.ctypes.data, int(n_steps), BC_PERIODIC, int(flags))
     if rc != 0:
         raise RuntimeError("lsmgpu batch advect failed: %s" % (last_error()[1],))
+
+
+def band_flow_weno5_tvdrk3(phi, gb, fb, dx, n_steps, rebuild_every, gamma, beta, a_n=1.0, b_n=0.1,
+                           cfl=0.5, precision="f64"):
+    """Narrow-band curvature flow in place; returns (dt per step, level-0
+    cells per rebuild)."""
+    import numpy as np
+    real = ctypes.c_double if precision == "f64" else ctypes.c_float
+    h = lib()
+    fn = getattr(h, "lsmgpu_band_flow_weno5_tvdrk3_" + precision)
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, real, real, real, real, real, real,
+                   ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    dts = np.zeros(max(n_steps, 1), np.float64)
+    bands = np.zeros(max((n_steps + rebuild_every - 1) // rebuild_every, 1), np.int64)
+    rc = fn(_ptr(phi), _box(gb), _box(fb), dx, a_n, b_n, cfl, gamma, beta, int(n_steps), int(rebuild_every),
+            dts.ctypes.data, bands.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("lsmgpu band flow failed: %s" % (last_error()[1],))
+    return dts[:n_steps], bands

@@ -1,0 +1,277 @@
+// Fused narrow-band curvature flow: phi_t + Vn |grad phi| = 0 with
+// Vn = a_n - b_n * kappa, HJ WENO5 on a narrow band, TVD-RK3, the band rebuilt
+// every `rebuild_every` steps.  It replaces the LSMLIB local call sequence
+// per stage (on level-0 cells):
+//   lsm3dCentralGradOrder2LOCAL -> lsm3dGradientMagnitudeLocal ->
+//   lsm3dComputeMeanCurvatureOrder2Local -> Vn = a_n - b_n*kappa ->
+//   HJ WENO5 LOCAL -> lsm3dZeroOut/AddNormalVelTermToLSERHSLOCAL ->
+//   (stage 1: lsm3dComputeStableNormalVelDtLOCAL) ->
+//   lsm3dMultiplyCutOffLSERHSLOCAL -> lsm3dTVDRK3StageNLOCAL
+// with one gather kernel per stage (stage 1 is split at the dt reduction),
+// and the band build of band.cuh.  Band levels 1..3 of the stage fields hold
+// phi^n: they are refreshed at every rebuild and never written by a stage.
+//
+// LSMGPU_BANDFLOW_EXACT selects the FP64 parity arithmetic (this unit is
+// compiled with -fmad=false); the FP32 form uses the fast WENO weights.
+#pragma once
+#include <vector>
+
+#include "band.cuh"
+#include "fused_stage.cuh"
+#include "stencil_math.cuh"
+#include "../../include/lsmgpu.h"
+
+namespace lsmgpu {
+namespace bandflow {
+
+template <class R>
+struct BandArgs {
+  View<const R> src;      // stage source (phi^n, u1, u2)
+  View<const R> phin;     // phi^n (stages 2, 3)
+  View<R> out;            // stage output
+  const int *ix, *iy, *iz;
+  int n0;                 // level-0 entries (list elements 0..n0-1)
+  R dx, a_n, b_n, beta, gamma, cfl;
+  R *rhs;                 // per level-0 entry (stage 1)
+  const R *dt;            // device scalar
+  unsigned long long *key;
+  int stage;
+};
+
+__device__ __forceinline__ unsigned long long okey(double v) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  return (u & 0x8000000000000000ULL) ? ~u : (u | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ double okey_inv(unsigned long long k) {
+  unsigned long long u = (k & 0x8000000000000000ULL) ? (k & 0x7fffffffffffffffULL) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
+// WENO5 with the local routines' epsilon floor (spatial_derivatives2d_local.f.in:892)
+template <class R, bool EXACT>
+__device__ __forceinline__ R weno_local(R v1, R v2, R v3, R v4, R v5) {
+  if constexpr (EXACT) {
+    const R c13 = 1.0 / 3.0, c76 = 7.0 / 6.0, c116 = 11.0 / 6.0, c16 = 1.0 / 6.0, c56 = 5.0 / 6.0;
+    const R c1312 = 13.0 / 12.0, c14 = 0.25;
+    R m = v1 * v1;
+    m = rmax(m, v2 * v2);
+    m = rmax(m, v3 * v3);
+    m = rmax(m, v4 * v4);
+    m = rmax(m, v5 * v5);
+    const R eps = R(1e-6) * m + R(1.e-35);
+    const R p1 = c13 * v1 - c76 * v2 + c116 * v3;
+    const R p2 = -(c16 * v2) + c56 * v3 + c13 * v4;
+    const R p3 = c13 * v3 + c56 * v4 - c16 * v5;
+    R t = v1 - R(2.0) * v2 + v3, u = v1 - R(4.0) * v2 + R(3.0) * v3;
+    const R S1 = c1312 * (t * t) + c14 * (u * u);
+    t = v2 - R(2.0) * v3 + v4; u = v2 - v4;
+    const R S2 = c1312 * (t * t) + c14 * (u * u);
+    t = v3 - R(2.0) * v4 + v5; u = R(3.0) * v3 - R(4.0) * v4 + v5;
+    const R S3 = c1312 * (t * t) + c14 * (u * u);
+    R a1 = R(0.1) / ((S1 + eps) * (S1 + eps));
+    R a2 = R(0.6) / ((S2 + eps) * (S2 + eps));
+    R a3 = R(0.3) / ((S3 + eps) * (S3 + eps));
+    const R is = R(1.0) / (a1 + a2 + a3);
+    a1 = a1 * is; a2 = a2 * is; a3 = a3 * is;
+    return a1 * p1 + a2 * p2 + a3 * p3;
+  } else {
+    return (R)fused::weno5_fast((float)v1, (float)v2, (float)v3, (float)v4, (float)v5);
+  }
+}
+
+// the RHS of one level-0 cell, before the cut-off; also the cell's H/dx for dt
+template <class R, bool EXACT>
+__device__ __forceinline__ R cell_rhs(const BandArgs<R> &a, int i, int j, int k, R &h_over_dx) {
+  const R *c = a.src.p + a.src.off(i, j, k);
+  const long long s[3] = {1, a.src.s1, a.src.s2};
+  const R dx = a.dx;
+  // central gradient, |grad phi| with zero_tol clamps, mean curvature
+  // (spatial_derivatives3d_local.f.in:825-839, :1251-1272; curvature3d_local.f.in)
+  const R f = R(0.5) / dx;
+  const R g0 = (c[s[0]] - c[-s[0]]) * f, g1 = (c[s[1]] - c[-s[1]]) * f, g2 = (c[s[2]] - c[-s[2]]) * f;
+  const R tol = Consts<double>::zero_tol;
+  R x2 = g0 * g0, y2 = g1 * g1, z2 = g2 * g2;
+  if (x2 < tol) x2 = R(0);
+  if (y2 < tol) y2 = R(0);
+  if (z2 < tol) z2 = R(0);
+  const R t = sqrt(x2 + y2 + z2);
+  const R mag = (t < tol) ? R(0) : t;
+  const R fxx = R(1.0) / dx / dx, fxy = R(0.25) / dx / dx;
+  const R xx = (c[s[0]] - R(2.0) * c[0] + c[-s[0]]) * fxx;
+  const R yy = (c[s[1]] - R(2.0) * c[0] + c[-s[1]]) * fxx;
+  const R zz = (c[s[2]] - R(2.0) * c[0] + c[-s[2]]) * fxx;
+  const R xy = (c[s[0] + s[1]] - c[s[0] - s[1]] - c[-s[0] + s[1]] + c[-s[0] - s[1]]) * fxy;
+  const R xz = (c[s[0] + s[2]] - c[s[0] - s[2]] - c[-s[0] + s[2]] + c[-s[0] - s[2]]) * fxy;
+  const R yz = (c[s[1] + s[2]] - c[s[1] - s[2]] - c[-s[1] + s[2]] + c[-s[1] - s[2]]) * fxy;
+  const R den = mag * mag * mag;
+  const R kappa = (den < tol) ? R(0) : curv_numerator(xx, yy, zz, xy, xz, yz, g0, g1, g2) / den;
+  const R vn = a.a_n - a.b_n * kappa;
+  // HJ WENO5 plus/minus from the band values of src
+  const R inv = R(1.0) / dx;
+  R gp[3], gm[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    R v[6];
+#pragma unroll
+    for (int q = -2; q <= 3; q++) v[q + 2] = (c[q * s[d]] - c[(q - 1) * s[d]]) * inv;
+    gp[d] = weno_local<R, EXACT>(v[5], v[4], v[3], v[2], v[1]);
+    gm[d] = weno_local<R, EXACT>(v[0], v[1], v[2], v[3], v[4]);
+  }
+  // Godunov normal-velocity term (level_set_evolution3d_local.f.in:236-273)
+  const R sq = godunov_normal_sq<R>(vn > R(0), gp, gm);
+  R rhs = R(0);
+  if (fabs(vn) >= tol) rhs = rhs - vn * sqrt(sq);
+  // H/dx of math_utils3d_local.f.in:396-414
+  const R mx2 = dx * dx;
+  const R cx = rmax(fabs(gp[0]), fabs(gm[0])), cy = rmax(fabs(gp[1]), fabs(gm[1])), cz = rmax(fabs(gp[2]), fabs(gm[2]));
+  const R ng = sqrt(cx * cx + cy * cy + cz * cz + mx2);
+  h_over_dx = (ng > tol) ? fabs(vn) / ng * (cx * inv + cy * inv + cz * inv) : R(-1.0);
+  return rhs;
+}
+
+// cubic cut-off between beta and gamma (localization3d.f:527-553)
+template <class R>
+__device__ __forceinline__ R cutoff(R rhs, R phi, R beta, R gamma) {
+  const R av = fabs(phi);
+  R co;
+  if (av <= beta) {
+    co = R(1);
+  } else if (av <= gamma) {
+    const R c1 = gamma - 3 * beta;
+    R c2 = (gamma - beta);
+    c2 = c2 * c2 * c2;
+    const R tt = av - gamma;
+    co = (tt * tt * (2 * av + c1)) / c2;
+  } else {
+    co = R(0);
+  }
+  return co * rhs;
+}
+
+template <class R>
+__device__ __forceinline__ R rk_update(int stage, R un, R us, R dt, R rhs) {
+  if (stage == 1) return un + dt * rhs;
+  if (stage == 2) return R(0.75) * un + R(0.25) * (us + dt * rhs);
+  return R(1.0 / 3.0) * un + R(2.0 / 3.0) * (us + dt * rhs);
+}
+
+// stage 1, pass 1: RHS (cut off) per entry and the dt maximum
+template <class R, bool EXACT>
+__global__ void k_band_rhs(BandArgs<R> a) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  double h = -1.0e308;
+  if (l < a.n0) {
+    const int i = a.ix[l], j = a.iy[l], k = a.iz[l];
+    R hd;
+    const R r = cell_rhs<R, EXACT>(a, i, j, k, hd);
+    h = (double)hd;
+    a.rhs[l] = cutoff<R>(r, a.src(i, j, k), a.beta, a.gamma);
+  }
+  for (int o = 16; o > 0; o >>= 1) h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(a.key, okey(h));
+}
+
+template <class R>
+__global__ void k_band_dt(const unsigned long long *key, R *dt, R cfl, double *dt_log) {
+  double m = okey_inv(*key);
+  if (m < -1.0) m = -1.0;  // the reference's running maximum starts at -1
+  const R d = cfl / ((R)m + (R)Consts<double>::tiny);
+  *dt = d;
+  if (dt_log) *dt_log = (double)d;
+}
+
+// stage 1, pass 2: the update
+template <class R>
+__global__ void k_band_update1(BandArgs<R> a) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= a.n0) return;
+  const int i = a.ix[l], j = a.iy[l], k = a.iz[l];
+  a.out(i, j, k) = rk_update<R>(1, a.src(i, j, k), a.src(i, j, k), *a.dt, a.rhs[l]);
+}
+
+// stages 2 and 3: RHS, cut-off and update in one pass
+template <class R, bool EXACT>
+__global__ void k_band_stage(BandArgs<R> a) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= a.n0) return;
+  const int i = a.ix[l], j = a.iy[l], k = a.iz[l];
+  R hd;
+  const R us = a.src(i, j, k);
+  const R r = cutoff<R>(cell_rhs<R, EXACT>(a, i, j, k, hd), us, a.beta, a.gamma);
+  a.out(i, j, k) = rk_update<R>(a.stage, a.phin(i, j, k), us, *a.dt, r);
+}
+
+template <class R, bool EXACT>
+int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n, R b_n, R cfl, R gamma, R beta,
+        int n_steps, int rebuild_every, double *dt_log, long long *band_log) {
+  Call call(name);
+  if (!gb.contains(fb, 0, 0, 0)) call.fail("fill box outside the ghost box");
+  if (rebuild_every <= 0) call.fail("rebuild_every must be positive");
+  if (!call.ok()) return LSMGPU_ERR_BOUNDS;
+  if (n_steps <= 0) return LSMGPU_OK;
+  const long long n = gb.size();
+  R *phi = call.inout(phi_user, n);
+  R *u1 = call.temp<R>(n), *u2 = call.temp<R>(n);
+  U8 *nb = call.temp<U8>(n);
+  int *ix = call.temp<int>(n), *iy = call.temp<int>(n), *iz = call.temp<int>(n), *outer = call.temp<int>(n);
+  R *rhs = call.temp<R>(n);
+  R *dt = call.temp<R>(1);
+  unsigned long long *key = call.temp<unsigned long long>(1);
+  double *dtl = dt_log ? call.temp<double>(n_steps) : nullptr;
+  if (!call.ok()) return lsmgpu_get_last_error(nullptr, 0);
+  cudaStream_t s = stream();
+  const int level = 3;
+  std::vector<int> lo, hi;
+  int ob[4];
+  int n0 = 0, nrebuild = 0;
+  for (int step = 0; step < n_steps; step++) {
+    if (step % rebuild_every == 0) {
+      long long c0 = 0;
+      if (!band_build<R>(call, phi, gb, nb, gb, ix, iy, iz, 0, (int)(n - 1), outer, 0, (int)(n - 1), (double)gamma,
+                         (double)beta, level, lo, hi, ob, &c0))
+        return lsmgpu_get_last_error(nullptr, 0);
+      n0 = (int)c0;
+      if (band_log) band_log[nrebuild] = c0;
+      nrebuild++;
+      // stage fields hold phi^n off the updated cells
+      cudaMemcpyAsync(u1, phi, n * sizeof(R), cudaMemcpyDeviceToDevice, s);
+      cudaMemcpyAsync(u2, phi, n * sizeof(R), cudaMemcpyDeviceToDevice, s);
+    }
+    if (n0 == 0) continue;
+    BandArgs<R> a{};
+    a.ix = ix; a.iy = iy; a.iz = iz;
+    a.n0 = n0;
+    a.dx = dx; a.a_n = a_n; a.b_n = b_n; a.beta = beta; a.gamma = gamma; a.cfl = cfl;
+    a.rhs = rhs;
+    a.dt = dt;
+    a.key = key;
+    const unsigned blocks = (unsigned)((n0 + 127) / 128);
+    // stage 1
+    a.src = view((const R *)phi, gb);
+    a.phin = a.src;
+    a.out = view(u1, gb);
+    a.stage = 1;
+    cudaMemsetAsync(key, 0, sizeof(unsigned long long), s);
+    LSMGPU_LAUNCH((k_band_rhs<R, EXACT>), blocks, 128, 0, a);
+    LSMGPU_LAUNCH(k_band_dt<R>, 1, 1, 0, key, dt, cfl, dtl ? dtl + step : nullptr);
+    LSMGPU_LAUNCH(k_band_update1<R>, blocks, 128, 0, a);
+    // stage 2
+    a.src = view((const R *)u1, gb);
+    a.out = view(u2, gb);
+    a.phin = view((const R *)phi, gb);
+    a.stage = 2;
+    LSMGPU_LAUNCH((k_band_stage<R, EXACT>), blocks, 128, 0, a);
+    // stage 3 (in place on phi: each cell reads only its own phi^n)
+    a.src = view((const R *)u2, gb);
+    a.out = view(phi, gb);
+    a.stage = 3;
+    LSMGPU_LAUNCH((k_band_stage<R, EXACT>), blocks, 128, 0, a);
+  }
+  if (dt_log) cudaMemcpyAsync(dt_log, dtl, sizeof(double) * n_steps, cudaMemcpyDeviceToHost, s);
+  call.finish();
+  cudaStreamSynchronize(s);
+  return lsmgpu_get_last_error(nullptr, 0);
+}
+
+}  // namespace bandflow
+}  // namespace lsmgpu

@@ -108,3 +108,101 @@ def tvdrk3_run(lib, mode, phi, gb, fb, dx, dt, n_steps, bc, vel=None, use0=0):
         apply_bc(lib, un, gb, fb, bc)
         phi = un
     return phi
+
+
+# ---------------------------------------------------------------------------
+# narrow-band curvature flow: the LSMLIB *_local call sequence
+# ---------------------------------------------------------------------------
+def band_run(lib, phi, gb, fb, dx, n_steps, rebuild_every, gamma, beta, a_n, b_n, cfl, level=3):
+    """n_steps TVD-RK3 steps of phi_t + Vn |grad phi| = 0 with Vn = a_n - b_n*kappa
+    on a narrow band rebuilt every `rebuild_every` steps (width gamma, inner
+    width beta, `level` neighbour levels).  Per stage, on level-0 cells:
+    central gradient -> |grad phi| -> mean curvature (kappa) -> Vn;
+    HJ WENO5 plus/minus on the band; Godunov normal-velocity RHS; cubic
+    cut-off between beta and gamma; TVD-RK3 stage.  dt = CFL-stable normal
+    velocity dt from stage 1 of each step.  Band levels 1..level of the stage
+    fields hold phi^n (refreshed at each rebuild).  Returns (phi, dts, bands)."""
+    shape = H.shape_of(gb)
+    cap = int(np.prod(shape))
+    phi = phi.copy(order="F")
+    z = lambda: np.zeros(shape, order="F")
+    nb = np.zeros(shape, np.uint8, order="F")
+    ix, iy, iz = (np.zeros(cap, np.int32) for _ in range(3))
+    outer = np.zeros(cap, np.int32)
+    n_lo = np.zeros(level + 1, np.int32)
+    n_hi = np.zeros(level + 1, np.int32)
+    box6 = lambda prefix: {"%s%s%s" % (w, "_" + prefix if prefix else "", "_gb"): v
+                           for w, v in zip(("ilo", "ihi", "jlo", "jhi", "klo", "khi"), gb)}
+    u1, u2 = z(), z()
+    dts, bands = [], []
+    pp, pm = [z(), z(), z()], [z(), z(), z()]
+    g3, mag, kap, vn, rhs, d1 = [z(), z(), z()], z(), z(), z(), z(), z()
+
+    def lists(level0_only=True):
+        return {"index_x": ix, "index_y": iy, "index_z": iz, "narrow_band": nb,
+                "nlo_index": int(n_lo[0]), "nhi_index": int(n_hi[0])}
+
+    def call(sym, arrays, scalars):
+        vals, _ = H.make_call(sym, gb, fb, arrays=arrays, scalars=scalars)
+        return L.invoke(lib, sym, vals)
+
+    def rhs_of(src, want_dt):
+        common = dict(lists())
+        sc = {"dx": dx, "dy": dx, "dz": dx, "mark_fb": 1,
+              "nlo_index": int(n_lo[0]), "nhi_index": int(n_hi[0])}
+        call("lsm3dcentralgradorder2local_", dict(common, phi=src, phi_x=g3[0], phi_y=g3[1], phi_z=g3[2]), sc)
+        call("lsm3dgradientmagnitudelocal_", dict(common, phi_x=g3[0], phi_y=g3[1], phi_z=g3[2],
+                                                 grad_phi_mag=mag), sc)
+        call("lsm3dcomputemeancurvatureorder2local_", dict(common, kappa=kap, phi=src, phi_x=g3[0],
+                                                           phi_y=g3[1], phi_z=g3[2], grad_phi_mag=mag), sc)
+        vn[...] = a_n - b_n * kap
+        sw = dict(sc)
+        for l in range(4):
+            sw["nlo_index%d" % l] = int(n_lo[min(l, level)])
+            sw["nhi_index%d" % l] = int(n_hi[min(l, level)])
+        sw.update({"mark_d1": level + 1})
+        call("lsm3dhjweno5local_", dict(common, phi=src, d1=d1, phi_x_plus=pp[0], phi_y_plus=pp[1],
+                                        phi_z_plus=pp[2], phi_x_minus=pm[0], phi_y_minus=pm[1],
+                                        phi_z_minus=pm[2]), sw)
+        call("lsm3dzerooutlevelseteqnrhslocal_", dict(common, lse_rhs=rhs), sc)
+        call("lsm3daddnormalveltermtolserhslocal_", dict(common, lse_rhs=rhs, phi_x_plus=pp[0],
+                                                         phi_y_plus=pp[1], phi_z_plus=pp[2],
+                                                         phi_x_minus=pm[0], phi_y_minus=pm[1],
+                                                         phi_z_minus=pm[2], vel_n=vn), sc)
+        dt = None
+        if want_dt:
+            out = call("lsm3dcomputestablenormalveldtlocal_", dict(common, vel_n=vn, phi_x_plus=pp[0],
+                                                                   phi_y_plus=pp[1], phi_z_plus=pp[2],
+                                                                   phi_x_minus=pm[0], phi_y_minus=pm[1],
+                                                                   phi_z_minus=pm[2]),
+                       dict(sc, cfl_number=cfl, dt=0.0))
+            dt = out["dt"]
+        call("lsm3dmultiplycutofflserhslocal_", dict(common, phi=src, lse_rhs=rhs),
+             dict(sc, beta=beta, gamma=gamma))
+        return dt
+
+    for step in range(n_steps):
+        if step % rebuild_every == 0:
+            vals = {"phi": phi, "narrow_band": nb, "index_x": ix, "index_y": iy, "index_z": iz,
+                    "nlo_index": 0, "nhi_index": cap - 1, "n_lo": n_lo, "n_hi": n_hi,
+                    "index_outer": outer, "nlo_index_outer": 0, "nhi_index_outer": cap - 1,
+                    "nlo_outer_plus": 0, "nhi_outer_plus": 0, "nlo_outer_minus": 0,
+                    "nhi_outer_minus": 0, "width": gamma, "width_inner": beta, "level": level}
+            for w, v in zip(("ilo_gb", "ihi_gb", "jlo_gb", "jhi_gb", "klo_gb", "khi_gb"), gb):
+                vals[w] = v
+                vals[w.replace("_gb", "_nb_gb")] = v
+            L.invoke(lib, "lsm3ddeterminenarrowband_", vals)
+            bands.append((nb.copy(), ix[:n_hi[level] + 1].copy(), iy[:n_hi[level] + 1].copy(),
+                          iz[:n_hi[level] + 1].copy(), n_lo.copy(), n_hi.copy()))
+            u1[...] = phi
+            u2[...] = phi
+        dt = rhs_of(phi, True)
+        dts.append(dt)
+        common = dict(lists())
+        sc = {"dt": dt, "mark_fb": 1, "nlo_index": int(n_lo[0]), "nhi_index": int(n_hi[0])}
+        call("lsm3dtvdrk3stage1local_", dict(common, u_stage1=u1, u_cur=phi, rhs=rhs), sc)
+        rhs_of(u1, False)
+        call("lsm3dtvdrk3stage2local_", dict(common, u_stage2=u2, u_stage1=u1, u_cur=phi, rhs=rhs), sc)
+        rhs_of(u2, False)
+        call("lsm3dtvdrk3stage3local_", dict(common, u_next=phi, u_stage2=u2, u_cur=phi, rhs=rhs), sc)
+    return phi, dts, bands
