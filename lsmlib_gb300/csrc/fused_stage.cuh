@@ -338,14 +338,20 @@ __device__ __forceinline__ void f32_tile(const float *tile, const StageArgs<floa
 #pragma unroll
       for (int d = 0; d < 3; d++) {
         // per lane: the backward stencil D1(c-2..c+2) for v > 0, the forward
-        // stencil D1(c+3..c-1) otherwise (spatial_derivatives3d.f.in:2756-2812)
+        // stencil D1(c+3..c-1) otherwise (spatial_derivatives3d.f.in:2756-2812);
+        // the six differences are loaded at fixed offsets and the lane's
+        // stencil is selected in registers
+        float2 D[6];
+#pragma unroll
+        for (int f = -2; f <= 3; f++)
+          D[f + 2] = mul2(make_float2(c0[f * st[d]] - c0[(f - 1) * st[d]], c1[f * st[d]] - c1[(f - 1) * st[d]]),
+                          inv[d]);
+        const bool b0 = vel0[d] > 0.f, b1 = vel1[d] > 0.f;
         float2 v[5];
-        const int s = st[d];
 #pragma unroll
         for (int q = 0; q < 5; q++) {
-          const int f0 = (vel0[d] > 0.f) ? q - 2 : 3 - q;
-          const int f1 = (vel1[d] > 0.f) ? q - 2 : 3 - q;
-          v[q] = mul2(make_float2(c0[f0 * s] - c0[(f0 - 1) * s], c1[f1 * s] - c1[(f1 - 1) * s]), inv[d]);
+          v[q].x = b0 ? D[q].x : D[5 - q].x;
+          v[q].y = b1 ? D[q].y : D[5 - q].y;
         }
         float2 g = weno5_x2(v[0], v[1], v[2], v[3], v[4]);
         if (fabsf(vel0[d]) < 1e-11f) g.x = 0.f;
