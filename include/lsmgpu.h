@@ -152,6 +152,40 @@ int lsmgpu_advect_batch_weno5_tvdrk3_f32(float *phi, const long long *offsets, c
                                          int n_grids, const float *vel, const float *spacing,
                                          const float *dt, int n_steps, int bc, int flags);
 
+/* Reverse-mode gradient of a periodic advection objective.  No counterpart in
+ * LSMLIB (LSMLIB has no adjoint); the forward map is LSMLIB's advection step
+ * on a periodic grid (lsm3dUpwindHJWENO5, spatial_derivatives3d.f.in:2628;
+ * lsm3dAddAdvectionTermToLSERHS, level_set_evolution3d.f.in:113; TVD RK3,
+ * tvd_runge_kutta3d.f:78/403/490), the same arithmetic as
+ * lsmgpu_advect_weno5_tvdrk3_* with LSMGPU_BC_PERIODIC:
+ *   phi_T = n_steps steps of phi_t + vel . grad phi = 0 from phi (the
+ *           periodic extension of its fill-box values; its ghost entries are
+ *           ignored), time step dt (held fixed, not differentiated);
+ *   J     = sum over fill-box cells of (H(phi_T) - H(phi_target))^2 dx dy dz,
+ *           H = LSMLIB's smoothed Heaviside (lsm_calculus_toolbox.h:41) of
+ *           width heaviside_eps, accumulated in FP64.
+ * Outputs (any may be NULL; velocity gradients all three or none, and only
+ * with grad_phi): *J; grad_phi = dJ/dphi over gb; grad_vel_* = dJ/dvel_*
+ * over vel_gb.  Ghost entries of the gradients are set to zero.  Forward
+ * states are kept every checkpoint_every steps and the steps between are
+ * recomputed in the reverse sweep (device memory: about
+ * 3 * checkpoint_every + n_steps / checkpoint_every + 16 padded fields).
+ * Arrays may be host or device memory (host arrays are staged).
+ * Returns an LSMGPU_* status. */
+int lsmgpu_advect_adjoint_weno5_tvdrk3_f64(const double *phi, const int *gb, const int *fb,
+                                           const double *vel_x, const double *vel_y, const double *vel_z,
+                                           const int *vel_gb, const double *phi_target, double dx, double dy,
+                                           double dz, double dt, int n_steps, int checkpoint_every,
+                                           double heaviside_eps, double *J, double *grad_phi,
+                                           double *grad_vel_x, double *grad_vel_y, double *grad_vel_z);
+/* FP32 state and adjoint fields; FP64 objective. */
+int lsmgpu_advect_adjoint_weno5_tvdrk3_f32(const float *phi, const int *gb, const int *fb,
+                                           const float *vel_x, const float *vel_y, const float *vel_z,
+                                           const int *vel_gb, const float *phi_target, float dx, float dy,
+                                           float dz, float dt, int n_steps, int checkpoint_every,
+                                           double heaviside_eps, double *J, float *grad_phi,
+                                           float *grad_vel_x, float *grad_vel_y, float *grad_vel_z);
+
 /* Allocation-free CFL-stable advection dt.  No counterpart in LSMLIB: it is
  * lsm3dcomputestableadvectiondt_ (same arguments, same result) for callers
  * that cannot let a library allocate device memory — a solver running inside

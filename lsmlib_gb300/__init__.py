@@ -228,3 +228,36 @@ def band_flow_weno5_tvdrk3(phi, gb, fb, dx, n_steps, rebuild_every, gamma, beta,
     if rc != 0:
         raise RuntimeError("lsmgpu band flow failed: %s" % (last_error()[1],))
     return dts[:n_steps], bands
+
+
+def _zeros_like(a):
+    """A zero array of the same kind, dtype, shape and device as `a`."""
+    if hasattr(a, "data_ptr"):
+        import torch
+        return torch.zeros_like(a)
+    import numpy as np
+    return np.zeros_like(a, order="F")
+
+
+def advect_adjoint_weno5_tvdrk3(phi, gb, fb, vel, vel_gb, phi_target, dx, dt, n_steps, heaviside_eps,
+                                checkpoint_every=8, precision="f64", dy=None, dz=None, grads=True,
+                                grad_vel=True):
+    """Objective J of n_steps periodic advection steps and (when `grads`) its
+    gradients.  Returns (J, grad_phi, [grad_vel_x, grad_vel_y, grad_vel_z]);
+    the gradients are new arrays of the kind of `phi` / `vel` (None when not
+    requested)."""
+    real = ctypes.c_double if precision == "f64" else ctypes.c_float
+    h = lib()
+    fn = getattr(h, "lsmgpu_advect_adjoint_weno5_tvdrk3_" + precision)
+    fn.restype = ctypes.c_int
+    fn.argtypes = ([ctypes.c_void_p] * 8 + [real] * 4 + [ctypes.c_int, ctypes.c_int, ctypes.c_double] +
+                   [ctypes.c_void_p] * 5)
+    J = ctypes.c_double(0.0)
+    gphi = _zeros_like(phi) if grads else None
+    gv = [_zeros_like(v) for v in vel] if (grads and grad_vel) else [None, None, None]
+    rc = fn(_ptr(phi), _box(gb), _box(fb), _ptr(vel[0]), _ptr(vel[1]), _ptr(vel[2]), _box(vel_gb),
+            _ptr(phi_target), dx, dy or dx, dz or dx, dt, int(n_steps), int(checkpoint_every),
+            float(heaviside_eps), ctypes.byref(J), _ptr(gphi), _ptr(gv[0]), _ptr(gv[1]), _ptr(gv[2]))
+    if rc != 0:
+        raise RuntimeError("lsmgpu advect adjoint failed: %s" % (last_error()[1],))
+    return J.value, gphi, gv

@@ -1,0 +1,252 @@
+// Host driver of the advection adjoint: forward sweep with checkpoints,
+// objective, then per checkpoint segment a forward recomputation that keeps
+// every stage state and the reverse sweep over it.
+//
+// Memory (padded layout, E elements per field): 3 forward fields, one
+// checkpoint per `ckpt` steps, 3*ckpt - 1 segment stage states, 3 adjoint
+// fields, 3 velocity fields, 3 velocity accumulators and the target.
+#pragma once
+
+#include <vector>
+
+#include "adjoint.cuh"
+#include "fused_driver.cuh"
+
+namespace lsmgpu {
+namespace adj {
+
+struct AdjSpec {
+  int n_steps, ckpt;
+  double dt, dx, dy, dz, eps;
+};
+
+template <class R, bool EXACT>
+void set_adj_smem() {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_adj_stage<R, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(R) * (size_t)kSmemElems));
+    attr = true;
+  }
+}
+
+template <class R, bool EXACT>
+void launch_adj_stage(const AdjStageArgs<R> &a) {
+  const Layout &L = a.L;
+  const size_t smem = sizeof(R) * (size_t)kSmemElems;
+  set_adj_smem<R, EXACT>();
+  dim3 blk(AX, AY);
+  dim3 grd((unsigned)((L.nx + AX - 1) / AX), (unsigned)((L.ny + AY - 1) / AY),
+           (unsigned)((L.nz + a.zchunk - 1) / a.zchunk));
+  k_adj_stage<R, EXACT><<<grd, blk, smem, stream()>>>(a);
+  note_launch();
+}
+
+// z planes per CTA: the chunk count c minimising waves(c) * (planes(c) + 6),
+// the time of the slowest SM (each CTA marches its planes plus 6 warm-up
+// planes; waves = ceil(CTAs / resident CTA slots))
+template <class R, bool EXACT>
+int pick_zchunk(const Layout &L) {
+  int sms = 152, dev = 0, per_sm = 1;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  set_adj_smem<R, EXACT>();
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adj_stage<R, EXACT>, AX * AY,
+                                                sizeof(R) * (size_t)kSmemElems);
+  if (per_sm < 1) per_sm = 1;
+  const long long slots = (long long)sms * per_sm;
+  const long long xy = (long long)((L.nx + AX - 1) / AX) * ((L.ny + AY - 1) / AY);
+  int best = L.nz;
+  long long best_cost = -1;
+  for (int c = 1; c <= (L.nz + 7) / 8; c++) {
+    const int z = (L.nz + c - 1) / c;
+    const long long waves = (xy * c + slots - 1) / slots;
+    const long long cost = waves * (z + 6);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = z;
+    }
+  }
+  return best;
+}
+
+template <class R, bool EXACT>
+int run(const char *name, const R *phi_user, const Box &gb, const Box &fb, const R *const vel_user[3],
+        const Box &vb, const R *tgt_user, const AdjSpec &sp, double *J_user, R *gphi_user,
+        R *const gvel_user[3]) {
+  using fused::StageArgs;
+  Call call(name);
+  if (!gb.contains(fb, 3, 3, 3)) call.fail("ghost box must hold 3 ghost cells around the fill box");
+  if (!vb.contains(fb, 0, 0, 0)) call.fail("velocity ghost box does not cover the fill box");
+  const int nx = (int)fb.n(0), ny = (int)fb.n(1), nz = (int)fb.n(2);
+  if (fb.empty() || nx < 6 || ny < 6 || nz < 6) call.fail("fill box must be at least 6 cells per axis");
+  if (!call.ok()) return LSMGPU_ERR_BOUNDS;
+  const int ngv = (gvel_user[0] != nullptr) + (gvel_user[1] != nullptr) + (gvel_user[2] != nullptr);
+  if (sp.n_steps < 0 || sp.ckpt < 1 || !(sp.eps > 0.0) || (ngv != 0 && ngv != 3) ||
+      (ngv == 3 && !gphi_user)) {
+    set_error(LSMGPU_ERR_ARGUMENT,
+              "%s: need n_steps >= 0, checkpoint_every >= 1, heaviside_eps > 0, and velocity gradients "
+              "either all three (with grad_phi) or none",
+              name);
+    return LSMGPU_ERR_ARGUMENT;
+  }
+  const bool want_grad = gphi_user != nullptr, want_gvel = ngv == 3;
+
+  const R *phi_d = call.in(phi_user, gb.size());
+  const R *tgt_d = call.in(tgt_user, gb.size());
+  const R *vel_d[3];
+  for (int d = 0; d < 3; d++) vel_d[d] = call.in(vel_user[d], vb.size());
+  R *gphi_d = want_grad ? call.out(gphi_user, gb.size()) : nullptr;
+  R *gvel_d[3] = {nullptr, nullptr, nullptr};
+  if (want_gvel)
+    for (int d = 0; d < 3; d++) gvel_d[d] = call.out(gvel_user[d], vb.size());
+  double *J_d = J_user ? call.scalar_out(J_user) : nullptr;
+
+  const Layout L = fused::make_layout(nx, ny, nz);
+  const long long ne = L.elems();
+  const int K = sp.ckpt;
+  const int nck = sp.n_steps > 0 ? (sp.n_steps + K - 1) / K : 1;
+  R *X = call.temp<R>(ne), *T1 = call.temp<R>(ne), *T2 = call.temp<R>(ne), *TG = call.temp<R>(ne);
+  R *V[3];
+  for (int d = 0; d < 3; d++) V[d] = call.temp<R>(ne);
+  std::vector<R *> ck(nck);
+  for (int c = 0; c < nck; c++) ck[c] = call.temp<R>(ne);
+  const long long ncell = (long long)nx * ny * nz;
+  const int nblk = (int)((ncell + kObjThreads - 1) / kObjThreads);
+  double *partial = call.temp<double>(nblk);
+  double *Jdev = call.temp<double>(1);
+  int *err = call.temp<int>(1);
+  R *LA = nullptr, *LB = nullptr, *LC = nullptr, *GV[3] = {nullptr, nullptr, nullptr};
+  std::vector<R *> U;
+  if (want_grad) {
+    LA = call.temp<R>(ne);
+    LB = call.temp<R>(ne);
+    LC = call.temp<R>(ne);
+    if (want_gvel)
+      for (int d = 0; d < 3; d++) GV[d] = call.temp<R>(ne);
+    U.assign(3 * K, nullptr);
+    for (int m = 1; m < 3 * K; m++) U[m] = call.temp<R>(ne);
+  }
+  if (!call.ok()) return lsmgpu_get_last_error(nullptr, 0);
+
+  cudaStream_t s = stream();
+  cudaMemsetAsync(err, 0, sizeof(int), s);
+  {
+    dim3 blk(32, 4, 2);
+    dim3 grd((unsigned)((nx + 7 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));
+    LSMGPU_LAUNCH(fused::k_pack<R>, grd, blk, 0, ck[0], L, view(phi_d, gb), gb, fb.lo[0], fb.lo[1], fb.lo[2]);
+    LSMGPU_LAUNCH(fused::k_pack<R>, grd, blk, 0, TG, L, view(tgt_d, gb), gb, fb.lo[0], fb.lo[1], fb.lo[2]);
+    for (int d = 0; d < 3; d++)
+      LSMGPU_LAUNCH(fused::k_pack<R>, grd, blk, 0, V[d], L, view(vel_d[d], vb), vb, fb.lo[0], fb.lo[1], fb.lo[2]);
+    dim3 gf((unsigned)((nx + 6 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));
+    // the initial state is the periodic extension of the fill-box values
+    LSMGPU_LAUNCH(k_fill_periodic<R>, gf, blk, 0, ck[0], L);
+  }
+  cudaMemcpyAsync(X, ck[0], (size_t)ne * sizeof(R), cudaMemcpyDeviceToDevice, s);
+
+  const long long ex = (long long)nx + fused::GX + 3, ey = (long long)ny + 2 * fused::GY,
+                  ez = (long long)nz + 2 * fused::GZ;
+  auto tmap = [&](const R *p, CUtensorMap *m) {
+    return encode_tmap_3d(m, p, sizeof(R), ex, ey, ez, L.py, L.pz, fused::SX, fused::SY, fused::SZ);
+  };
+  CUtensorMap tX, tT1, tT2;
+  if (!tmap(X, &tX) || !tmap(T1, &tT1) || !tmap(T2, &tT2)) {
+    call.fail("tensor map encoding failed");
+    return LSMGPU_ERR_CUDA;
+  }
+
+  StageArgs<R> fa{};
+  fa.L = L;
+  for (int d = 0; d < 3; d++) fa.vel[d] = V[d];
+  fa.inv[0] = R(1.0) / (R)sp.dx;
+  fa.inv[1] = R(1.0) / (R)sp.dy;
+  fa.inv[2] = R(1.0) / (R)sp.dz;
+  fa.dt = (R)sp.dt;
+  fa.periodic = 1;
+  fa.err = err;
+  // one forward TVD-RK3 step: src -> o1 -> o2 -> dst (dst may be src)
+  auto fwd_step = [&](const CUtensorMap &t_src, R *src, const CUtensorMap &t_o1, R *o1,
+                      const CUtensorMap &t_o2, R *o2, R *dst) {
+    fa.phi_n = src;
+    fa.stage = 1; fa.out = o1;
+    fused::launch_stage<R, fused::ADV_FIELD, EXACT>(t_src, fa);
+    fa.stage = 2; fa.out = o2;
+    fused::launch_stage<R, fused::ADV_FIELD, EXACT>(t_o1, fa);
+    if (dst) {
+      fa.stage = 3; fa.out = dst;
+      fused::launch_stage<R, fused::ADV_FIELD, EXACT>(t_o2, fa);
+    }
+  };
+
+  // ---- forward sweep with checkpoints ----------------------------------------
+  for (int n = 0; n < sp.n_steps; n++) {
+    fwd_step(tX, X, tT1, T1, tT2, T2, X);
+    if ((n + 1) % K == 0 && (n + 1) < sp.n_steps)
+      cudaMemcpyAsync(ck[(n + 1) / K], X, (size_t)ne * sizeof(R), cudaMemcpyDeviceToDevice, s);
+  }
+  const double vol = sp.dx * sp.dy * sp.dz;
+  LSMGPU_LAUNCH(k_objective<R>, dim3((unsigned)nblk), dim3(kObjThreads), 0, X, TG, L, sp.eps, vol, LA, partial);
+  LSMGPU_LAUNCH(k_objective_fold, dim3(1), dim3(1024), 0, partial, nblk, vol, J_d ? J_d : Jdev);
+
+  // ---- reverse sweep ------------------------------------------------------------
+  if (want_grad) {
+    if (want_gvel)
+      for (int d = 0; d < 3; d++) cudaMemsetAsync(GV[d], 0, (size_t)ne * sizeof(R), s);
+    std::vector<CUtensorMap> tU(3 * K);
+    for (int m = 1; m < 3 * K; m++)
+      if (!tmap(U[m], &tU[m])) {
+        call.fail("tensor map encoding failed");
+        return LSMGPU_ERR_CUDA;
+      }
+    AdjStageArgs<R> aa{};
+    aa.L = L;
+    for (int d = 0; d < 3; d++) {
+      aa.vel[d] = V[d];
+      aa.gvel[d] = GV[d];
+    }
+    aa.dt = (R)sp.dt;
+    aa.inv[0] = fa.inv[0]; aa.inv[1] = fa.inv[1]; aa.inv[2] = fa.inv[2];
+    aa.zchunk = pick_zchunk<R, EXACT>(L);
+    for (int seg = nck - 1; seg >= 0 && sp.n_steps > 0; seg--) {
+      const int s0 = seg * K, s1 = (s0 + K < sp.n_steps) ? s0 + K : sp.n_steps, ns = s1 - s0;
+      U[0] = ck[seg];
+      if (!tmap(U[0], &tU[0])) {
+        call.fail("tensor map encoding failed");
+        return LSMGPU_ERR_CUDA;
+      }
+      for (int m = 0; m < ns; m++)
+        fwd_step(tU[3 * m], U[3 * m], tU[3 * m + 1], U[3 * m + 1], tU[3 * m + 2], U[3 * m + 2],
+                 m + 1 < ns ? U[3 * m + 3] : nullptr);
+      for (int m = ns - 1; m >= 0; m--) {
+        aa.s = U[3 * m + 2]; aa.M = LA; aa.mscale = R(2.0 / 3.0);
+        aa.P = nullptr; aa.Q = nullptr; aa.out = LB;
+        launch_adj_stage<R, EXACT>(aa);
+        aa.s = U[3 * m + 1]; aa.M = LB; aa.mscale = R(0.25); aa.out = LC;
+        launch_adj_stage<R, EXACT>(aa);
+        aa.s = U[3 * m]; aa.M = LC; aa.mscale = R(1.0);
+        aa.P = LA; aa.pscale = R(1.0 / 3.0); aa.Q = LB; aa.qscale = R(0.75); aa.out = LA;
+        launch_adj_stage<R, EXACT>(aa);
+      }
+    }
+    Grid3 gg = cover(gb);
+    LSMGPU_LAUNCH(k_unpack_interior<R>, gg.grid, gg.block, 0, view(gphi_d, gb), gb, LA, L, fb.lo[0], fb.lo[1],
+                  fb.lo[2]);
+    if (want_gvel) {
+      Grid3 gv = cover(vb);
+      for (int d = 0; d < 3; d++)
+        LSMGPU_LAUNCH(k_unpack_interior<R>, gv.grid, gv.block, 0, view(gvel_d[d], vb), vb, GV[d], L, fb.lo[0],
+                      fb.lo[1], fb.lo[2]);
+    }
+  }
+  int herr = 0;
+  cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s);
+  call.finish();
+  cudaStreamSynchronize(s);
+  if (herr != 0) {
+    set_error(herr, "%s: a bounded device wait gave up (TMA tile load)", name);
+    return herr;
+  }
+  return lsmgpu_get_last_error(nullptr, 0);
+}
+
+}  // namespace adj
+}  // namespace lsmgpu
