@@ -64,6 +64,27 @@ def initial_phi(n):
     return np.asfortranarray(phi), dx
 
 
+def adjoint_case(n, seed=3, noise=0.05, shift=0.1, r=0.4):
+    """The gradient workload (192^3 in its published form): periodic
+    [-1, 1]^3 with n cells per axis, phi0 = sphere of radius r, target = the
+    sphere shifted by `shift` in x, velocity (sin(pi y) cos(pi z),
+    sin(pi z) cos(pi x), sin(pi x) cos(pi y)) plus N(0, noise) per cell
+    (numpy seed `seed`), dt at CFL 0.5.  Returns interior arrays (Fortran
+    order), the spacing and dt; the objective width is 1.5 dx."""
+    h = 2.0 / n
+    c = -1.0 + (np.arange(n) + 0.5) * h
+    X, Y, Z = np.meshgrid(c, c, c, indexing="ij")
+    phi = np.sqrt(X ** 2 + Y ** 2 + Z ** 2) - r
+    tgt = np.sqrt((X - shift) ** 2 + Y ** 2 + Z ** 2) - r
+    rng = np.random.default_rng(seed)
+    base = (np.sin(np.pi * Y) * np.cos(np.pi * Z), np.sin(np.pi * Z) * np.cos(np.pi * X),
+            np.sin(np.pi * X) * np.cos(np.pi * Y))
+    vel = [b + rng.normal(0.0, noise, X.shape) for b in base]
+    dt = 0.5 / float(np.max((np.abs(vel[0]) + np.abs(vel[1]) + np.abs(vel[2])) / h))
+    f = np.asfortranarray
+    return f(phi), [f(v) for v in vel], f(tgt), h, dt
+
+
 # ---------------------------------------------------------------------------
 # clocks sampled during the timed region
 # ---------------------------------------------------------------------------

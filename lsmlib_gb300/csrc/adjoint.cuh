@@ -21,15 +21,18 @@
 // is Vbar(j) - Vbar(j+1).  So each output cell needs the slots of the cells
 // within 3 of it along each axis.
 //
-// Kernel (one per adjoint stage): a CTA of 32 x 16 threads owns a 32 x 16
-// column of cells and marches along z through a chunk of planes.
-//   z: each thread keeps a 7-value window of s down its own column and a ring
-//      of six face sums, computing the slots of the cell 3 planes ahead;
-//   x, y: per plane the CTA stages the plane's s (a cross of 44 x 16 and
-//      32 x 28 cells) in shared memory, computes the slots of the 38 x 16
-//      x-extended and 32 x 22 y-extended cells into shared memory, then each
-//      thread gathers its two faces per axis.
-// Redundant slot work: x 38/32, y 22/16, z (chunk + 6)/chunk.
+// Kernels (two per adjoint stage, neither uses shared memory or block
+// barriers):
+//   k_adj_xz: a warp owns a row segment of 32 cells along x, the middle 26 of
+//     which it writes, and marches along z through a chunk of planes.  Each
+//     lane keeps a 7-value window of s down its column and a ring of six
+//     z-face sums (z slots of the cell 3 planes ahead); per output plane it
+//     computes the x slots of its cell and the warp sums x faces with
+//     shuffles.  It writes out = mu + dt (A_x + A_z) (+ P, Q terms).
+//   k_adj_y: a thread owns an (x, z) column and marches along y through a
+//     chunk with the same window / face-ring scheme; it adds dt A_y to out.
+// Redundant slot work: x and z 32/26, y (chunk + 6)/chunk, z also
+// (chunk + 6)/chunk.
 //
 // All indices wrap periodically, so the adjoint fields need no ghost cells;
 // the forward states use the fused steppers' padded layout (their periodic
@@ -45,11 +48,8 @@ namespace adj {
 
 using fused::Layout;
 
-constexpr int AX = 32, AY = 16;              // threads / cells per plane
-constexpr int HX = AX + 12, HY = AY + 12;    // staged s plane: 44 x 28 (cross)
-constexpr int GXN = AX + 6, GYN = AY + 6;    // slot cells: 38 x 16 (x), 32 x 22 (y)
-constexpr int NJX = GXN * AY, NJY = AX * GYN;  // 608 x-slot and 704 y-slot cells
-constexpr int NCROSS = HX * AY + AX * 12;      // 704 + 384 staged s values per plane
+constexpr int kSeg = 26;     // cells of a row segment written by one warp
+constexpr int kRows = 8;     // warps (rows) per CTA of k_adj_xz, columns per CTA row of k_adj_y
 
 // periodic image of index a in [0, n): one add or subtract for a in
 // [-n, 2n), a remainder otherwise
@@ -143,29 +143,100 @@ __device__ __forceinline__ R weno5_adj(const R v[5], R dv[5]) {
 // u = the velocity component, mu = the adjoint weight of the cell, inv = 1/dx_d.
 // G[m] is the adjoint of face c-2+m (scaled by dt); the return value is the
 // velocity adjoint dt * mu * (-W), zero where the forward set W to zero.
-template <class R, bool EXACT>
-__device__ __forceinline__ R adv_slots(const R a[7], R u, R mu, R dt, R inv, R G[6]) {
-#pragma unroll
-  for (int m = 0; m < 6; m++) G[m] = R(0);
-  // spatial_derivatives3d.f.in:2756-2812: no derivative where |u| < zero_tol
-  if (fabs(u) < R(Consts<double>::zero_tol)) return R(0);
-  R D[6];  // D(c+f) for f = -2..3
+// FP32 slots with the adjoint weight folded in early: yb = dt mu (-u)/dx
+// multiplies the weights and the beta_k once, so the five face adjoints come
+// out of the derivative formulas directly.
+static __device__ __forceinline__ float adv_slots_f32(const float a[7], float u, float mu, float dt, float inv,
+                                               float G[6]) {
+  const float c13 = 1.f / 3.f, c76 = 7.f / 6.f, c116 = 11.f / 6.f, c16 = 1.f / 6.f, c56 = 5.f / 6.f;
+  const float c1312 = 13.f / 12.f, c136 = 13.f / 6.f;
+  float D[6];
 #pragma unroll
   for (int f = 0; f < 6; f++) D[f] = (a[f + 1] - a[f]) * inv;
-  const bool minus = u > R(0);
-  R v[5], dv[5];
+  const bool minus = u > 0.f;
+  float v[5];
 #pragma unroll
   for (int q = 0; q < 5; q++) v[q] = minus ? D[q] : D[5 - q];
-  const R W = weno5_adj<R, EXACT>(v, dv);
-  const R ybar = dt * mu * (-u) * inv;
-  // minus: v_q on face c-2+q (slot q); plus: v_q on face c+3-q (slot 5-q)
+  float m = v[0] * v[0];
+  int am = 0;
 #pragma unroll
-  for (int m = 0; m < 6; m++) {
-    const R lo = (m < 5) ? dv[m] : R(0);
-    const R hi = (m > 0) ? dv[5 - m] : R(0);
-    G[m] = ybar * (minus ? lo : hi);
+  for (int q = 1; q < 5; q++) {
+    const float sq = v[q] * v[q];
+    const bool take = !(m > sq);  // the running max keeps the earlier value only when larger
+    am = take ? q : am;
+    m = take ? sq : m;
   }
-  return dt * mu * (-W);
+  const float v1 = v[0], v2 = v[1], v3 = v[2], v4 = v[3], v5 = v[4];
+  const float r = __fdividef(1.f, fmaf(1e-6f, m, 1e-36f));
+  const float p1 = fmaf(c13, v1, fmaf(-c76, v2, c116 * v3));
+  const float p2 = fmaf(-c16, v2, fmaf(c56, v3, c13 * v4));
+  const float p3 = fmaf(c13, v3, fmaf(c56, v4, -c16 * v5));
+  const float t1 = fmaf(-2.f, v2, v1 + v3), u1 = fmaf(-4.f, v2, fmaf(3.f, v3, v1));
+  const float t2 = fmaf(-2.f, v3, v2 + v4), u2 = v2 - v4;
+  const float t3 = fmaf(-2.f, v4, v3 + v5), u3 = fmaf(-4.f, v4, fmaf(3.f, v3, v5));
+  const float q1 = fmaf(fmaf(c1312 * t1, t1, 0.25f * u1 * u1), r, 1.f);
+  const float q2 = fmaf(fmaf(c1312 * t2, t2, 0.25f * u2 * u2), r, 1.f);
+  const float q3 = fmaf(fmaf(c1312 * t3, t3, 0.25f * u3 * u3), r, 1.f);
+  const float q12 = q1 * q2, q13 = q1 * q3, q23 = q2 * q3;
+  const float n1 = 0.1f * q23 * q23, n2 = 0.6f * q13 * q13, n3 = 0.3f * q12 * q12;
+  const float is = __fdividef(1.f, n1 + n2 + n3);  // sum <= 3e31 < 2^126
+  const float w1 = n1 * is, w2 = n2 * is, w3 = n3 * is;
+  const float W = fmaf(w1, p1, fmaf(w2, p2, w3 * p3));
+  const float dmu = dt * mu;
+  const float yb = dmu * -u * inv;
+  // beta_k yb = -2 yb w_k (p_k - W) / (S_k + eps), 1/(S_k + eps) = r / (q1 q2 q3) * q_j q_l
+  const float k0 = -2.f * yb * __fdividef(r, q12 * q3);
+  const float b1 = k0 * w1 * (p1 - W) * q23, b2 = k0 * w2 * (p2 - W) * q13, b3 = k0 * w3 * (p3 - W) * q12;
+  const float y1 = yb * w1, y2 = yb * w2, y3 = yb * w3;
+  const float T1 = c136 * t1 * b1, U1 = 0.5f * u1 * b1;
+  const float T2 = c136 * t2 * b2, U2 = 0.5f * u2 * b2;
+  const float T3 = c136 * t3 * b3, U3 = 0.5f * u3 * b3;
+  float g[5];
+  g[0] = fmaf(c13, y1, T1 + U1);
+  g[1] = fmaf(-c76, y1, fmaf(-c16, y2, fmaf(-2.f, T1, fmaf(-4.f, U1, T2 + U2))));
+  g[2] = fmaf(c116, y1, fmaf(c56, y2, fmaf(c13, y3, fmaf(3.f, U1, fmaf(-2.f, T2, fmaf(3.f, U3, T1 + T3))))));
+  g[3] = fmaf(c13, y2, fmaf(c56, y3, fmaf(-2.f, T3, fmaf(-4.f, U3, T2 - U2))));
+  g[4] = fmaf(-c16, y3, T3 + U3);
+  const float de = (b1 + b2 + b3) * 2e-6f;
+#pragma unroll
+  for (int q = 0; q < 5; q++) g[q] = (q == am) ? fmaf(de, v[q], g[q]) : g[q];
+  // spatial_derivatives3d.f.in:2756-2812: no derivative where |u| < zero_tol
+  const bool off = fabsf(u) < 1e-11f;
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    const float lo = (k < 5) ? g[k] : 0.f, hi = (k > 0) ? g[5 - k] : 0.f;
+    G[k] = off ? 0.f : (minus ? lo : hi);
+  }
+  return off ? 0.f : dmu * -W;
+}
+
+template <class R, bool EXACT>
+__device__ __forceinline__ R adv_slots(const R a[7], R u, R mu, R dt, R inv, R G[6]) {
+  if constexpr (!EXACT && sizeof(R) == 4) {
+    return adv_slots_f32(a, u, mu, dt, inv, G);
+  } else {
+#pragma unroll
+    for (int m = 0; m < 6; m++) G[m] = R(0);
+    // spatial_derivatives3d.f.in:2756-2812: no derivative where |u| < zero_tol
+    if (fabs(u) < R(Consts<double>::zero_tol)) return R(0);
+    R D[6];  // D(c+f) for f = -2..3
+#pragma unroll
+    for (int f = 0; f < 6; f++) D[f] = (a[f + 1] - a[f]) * inv;
+    const bool minus = u > R(0);
+    R v[5], dv[5];
+#pragma unroll
+    for (int q = 0; q < 5; q++) v[q] = minus ? D[q] : D[5 - q];
+    const R W = weno5_adj<R, EXACT>(v, dv);
+    const R ybar = dt * mu * (-u) * inv;
+    // minus: v_q on face c-2+q (slot q); plus: v_q on face c+3-q (slot 5-q)
+#pragma unroll
+    for (int m = 0; m < 6; m++) {
+      const R lo = (m < 5) ? dv[m] : R(0);
+      const R hi = (m > 0) ? dv[5 - m] : R(0);
+      G[m] = ybar * (minus ? lo : hi);
+    }
+    return dt * mu * (-W);
+  }
 }
 
 template <class R>
@@ -180,185 +251,183 @@ struct AdjStageArgs {
   R mscale, pscale, qscale;
   R dt;
   R inv[3];
-  int zchunk;
+  int zchunk;         // planes per warp along z (k_adj_xz)
+  int ychunk;         // rows per thread along y (k_adj_y)
 };
 
+// One step of the face-sum ring of a marching thread: add the slots of the
+// cell `lead` (3 ahead of the output cell), and return A(lead - 3) =
+// Vbar(lead - 3) - Vbar(lead - 2).
 template <class R>
-__device__ __forceinline__ long long widx(const Layout &L, int i, int j, int k) {
-  return L.idx(wrapi(i, L.nx), wrapi(j, L.ny), wrapi(k, L.nz));
+__device__ __forceinline__ R ring_step(R F[6], R &prevV, const R G[6]) {
+#pragma unroll
+  for (int m = 0; m < 6; m++) F[m] += G[m];
+  const R A = prevV - F[0];
+  prevV = F[0];
+#pragma unroll
+  for (int m = 0; m < 5; m++) F[m] = F[m + 1];
+  F[5] = R(0);
+  return A;
 }
 
-constexpr int kSmemElems = HY * HX + 6 * AY * GXN + 6 * GYN * AX;
-constexpr int kPer = (NJX + NJY + AX * AY - 1) / (AX * AY);  // slot cells per thread per plane (3)
+// Offset of plane p + c along a periodic axis of n planes and pitch `pitch`,
+// from the offset `o` of plane p (0 <= p < n, -n <= c <= n).
+__device__ __forceinline__ long long plane_add(long long o, int p, int c, int n, long long pitch) {
+  long long r = o + (long long)c * pitch;
+  const int q = p + c;
+  if (q >= n) r -= (long long)n * pitch;
+  else if (q < 0) r += (long long)n * pitch;
+  return r;
+}
 
 template <class R, bool EXACT>
-__global__ void __launch_bounds__(AX * AY) k_adj_stage(AdjStageArgs<R> a) {
-  extern __shared__ __align__(16) unsigned char adj_smem[];
-  R (*sS)[HX] = reinterpret_cast<R (*)[HX]>(adj_smem);
-  R (*sGx)[AY][GXN] = reinterpret_cast<R (*)[AY][GXN]>(adj_smem + sizeof(R) * HY * HX);
-  R (*sGy)[GYN][AX] = reinterpret_cast<R (*)[GYN][AX]>(adj_smem + sizeof(R) * (HY * HX + 6 * AY * GXN));
+__global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? 3 : 1) k_adj_xz(AdjStageArgs<R> a) {
   const Layout &L = a.L;
-  const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + AX * ty;
-  const int x0 = blockIdx.x * AX, y0 = blockIdx.y * AY;
+  const int lane = threadIdx.x;
+  const int j = blockIdx.y * kRows + threadIdx.y;
+  if (j >= L.ny) return;  // whole warp
+  const int xs = blockIdx.x * kSeg;
+  const int x = xs - 3 + lane;
+  const int xw = wrapi(x, L.nx);
+  const bool own = lane >= 3 && lane < 3 + kSeg && x < L.nx;
   const int z0 = blockIdx.z * a.zchunk;
   const int zend = min(z0 + a.zchunk, L.nz);
-  const int i = x0 + tx, j = y0 + ty;
-  const bool mine = i < L.nx && j < L.ny;
-  const R dt = a.dt;
-  // x/y part of the padded index of (wrapped) interior cell (x, y)
-  auto planar = [&](int x, int y) { return (x + fused::GX) + (int)L.py * (y + fused::GY); };
-  // z part for plane z (wrapped)
-  auto zoff = [&](int z) { return L.pz * (long long)(wrapi(z, L.nz) + fused::GZ); };
-
-  // cells this thread stages and computes slots for, in every plane
-  int stg_off[kPer], stg_pos[kPer], job_off[kPer], job_code[kPer];
+  const int nz = L.nz;
+  const R dt = a.dt, msc = a.mscale, ix = a.inv[0], iz = a.inv[2];
+  const long long pz = L.pz;
+  const long long row = (long long)fused::GX + L.py * (j + fused::GY);
+  // x offsets of the x stencil of this lane's cell, s(x-3 .. x+3), relative to the row
+  int xo[7];
 #pragma unroll
-  for (int r = 0; r < kPer; r++) {
-    const int e = tid + r * AX * AY;
-    stg_off[r] = -1;
-    if (e < NCROSS) {
-      int lx, ly;
-      if (e < HX * AY) {
-        ly = 6 + e / HX;
-        lx = e % HX;
-      } else {
-        const int q = e - HX * AY, row = q / AX;
-        ly = row < 6 ? row : row + AY;
-        lx = 6 + q % AX;
-      }
-      stg_off[r] = planar(wrapi(x0 - 6 + lx, L.nx), wrapi(y0 - 6 + ly, L.ny));
-      stg_pos[r] = ly * HX + lx;
-    }
-    job_code[r] = -1;
-    if (e < NJX) {  // x slots of cell (x0 - 3 + lx, y0 + ly)
-      const int ly = e / GXN, lx = e % GXN, cx = x0 - 3 + lx, cy = y0 + ly;
-      job_off[r] = planar(wrapi(cx, L.nx), wrapi(cy, L.ny));
-      const bool own = lx >= 3 && lx < 3 + AX && cx < L.nx && cy < L.ny;
-      job_code[r] = lx | (ly << 6) | (own << 12);
-    } else if (e < NJX + NJY) {  // y slots of cell (x0 + lx, y0 - 3 + ly)
-      const int q = e - NJX, ly = q / AX, lx = q % AX, cx = x0 + lx, cy = y0 - 3 + ly;
-      job_off[r] = planar(wrapi(cx, L.nx), wrapi(cy, L.ny));
-      const bool own = ly >= 3 && ly < 3 + AY && cx < L.nx && cy < L.ny;
-      job_code[r] = lx | (ly << 6) | (own << 12) | (1 << 13);
-    }
-  }
-  const int col = planar(wrapi(i, L.nx), wrapi(j, L.ny));
+  for (int q = 0; q < 7; q++) xo[q] = wrapi(x - 3 + q, L.nx) - xw;
+  const R *s = a.s + row + xw;  // this lane's column; plane offsets are added
+  const R *M = a.M + row + xw;
+  const R *vx = a.vel[0] + row + xw;
+  const R *vz = a.vel[2] + row + xw;
+  // plane cursor: offset of plane kk (wrapped) and its index
+  int zk = wrapi(z0 - 3, nz);
+  long long ok = pz * (long long)(zk + fused::GZ);
 
-  // plane data, loaded one plane ahead: staged s, and mu and the velocity
-  // component of each slot cell
-  R stg[kPer], jm[kPer], jv[kPer];
-  auto load_plane = [&](int k) {
-    const long long zb = zoff(k);
-#pragma unroll
-    for (int r = 0; r < kPer; r++) {
-      if (stg_off[r] >= 0) stg[r] = a.s[zb + stg_off[r]];
-      if (job_code[r] >= 0) {
-        jm[r] = a.M[zb + job_off[r]];
-        jv[r] = (job_code[r] >> 13) ? a.vel[1][zb + job_off[r]] : a.vel[0][zb + job_off[r]];
-      }
-    }
-  };
-  load_plane(z0);
-
-  R win[7];      // s(i, j, kk-3 .. kk+3)
-  R mring[4];    // mu(i, j, kk-3 .. kk)
-  R F[6];        // z-face sums for faces kk-2 .. kk+3
+  R win[7], mring[4], F[6];
   R prevV = R(0);
 #pragma unroll
   for (int q = 0; q < 6; q++) {
-    win[q + 1] = a.s[zoff(z0 - 6 + q) + col];
+    win[q + 1] = s[plane_add(ok, zk, q - 3, nz, pz)];
     F[q] = R(0);
   }
 #pragma unroll
   for (int q = 0; q < 4; q++) mring[q] = R(0);
-  // column values of the next iteration: s(kk+3), M(kk), vel_z(kk)
-  R cs = a.s[zoff(z0) + col], cm = a.M[zoff(z0 - 3) + col], cv = a.vel[2][zoff(z0 - 3) + col];
+  R cs = s[plane_add(ok, zk, 3, nz, pz)], cm = M[ok], cv = vz[ok];
+  R xsn[7], xvn;
+  {
+    const long long o = plane_add(ok, zk, 3, nz, pz);  // plane z0
+#pragma unroll
+    for (int q = 0; q < 7; q++) xsn[q] = s[o + xo[q]];
+    xvn = vx[o];
+  }
 
   for (int kk = z0 - 3; kk < zend + 3; kk++) {
-    // ---- z: slots of cell (i, j, kk) from the column window ----------------
 #pragma unroll
     for (int q = 0; q < 6; q++) win[q] = win[q + 1];
     win[6] = cs;
 #pragma unroll
     for (int q = 0; q < 3; q++) mring[q] = mring[q + 1];
-    mring[3] = a.mscale * cm;
-    const R vz = cv;
-    const long long zk = zoff(kk);
+    mring[3] = msc * cm;
+    const R uz = cv;
+    const long long okk = ok;  // plane kk
+    const int zkk = zk;
+    // advance the cursor to plane kk + 1 and prefetch the next column values
+    ok = plane_add(ok, zk, 1, nz, pz);
+    zk = (zk + 1 == nz) ? 0 : zk + 1;
     if (kk + 1 < zend + 3) {
-      cs = a.s[zoff(kk + 4) + col];
-      cm = a.M[zoff(kk + 1) + col];
-      cv = a.vel[2][zoff(kk + 1) + col];
+      cs = s[plane_add(ok, zk, 3, nz, pz)];
+      cm = M[ok];
+      cv = vz[ok];
     }
-    R Az;
-    {
-      R G[6];
-      const R gz = adv_slots<R, EXACT>(win, vz, mring[3], dt, a.inv[2], G);
-      if (a.gvel[2] && mine && kk >= z0 && kk < zend) a.gvel[2][zk + col] += gz;
-#pragma unroll
-      for (int m = 0; m < 6; m++) F[m] += G[m];
-      Az = prevV - F[0];  // Vbar(kk-3) - Vbar(kk-2)
-      prevV = F[0];
-#pragma unroll
-      for (int m = 0; m < 5; m++) F[m] = F[m + 1];
-      F[5] = R(0);
-    }
+    R G[6];
+    const R gz = adv_slots<R, EXACT>(win, uz, mring[3], dt, iz, G);
+    if (a.gvel[2] && own && kk >= z0 && kk < zend) a.gvel[2][row + xw + okk] += gz;
+    const R Az = ring_step<R>(F, prevV, G);
     const int k = kk - 3;
-    if (k < z0) continue;  // warm-up planes (uniform over the CTA)
+    if (k < z0) continue;
 
-    // ---- x, y: stage plane k of s, slots into shared memory ---------------
-    __syncthreads();  // previous plane's gathers are done
-    R *sflat = &sS[0][0];
+    // x slots of (x, j, k); the warp sums the x faces with shuffles
+    R w7[7];
 #pragma unroll
-    for (int r = 0; r < kPer; r++)
-      if (stg_off[r] >= 0) sflat[stg_pos[r]] = stg[r];
-    R m_cur[kPer], v_cur[kPer];
+    for (int q = 0; q < 7; q++) w7[q] = xsn[q];
+    const R ux = xvn;
+    const long long ob = plane_add(okk, zkk, -3, nz, pz);  // plane k
+    if (k + 1 < zend) {
+      const long long o = plane_add(okk, zkk, -2, nz, pz);
 #pragma unroll
-    for (int r = 0; r < kPer; r++) {
-      m_cur[r] = jm[r];
-      v_cur[r] = jv[r];
+      for (int q = 0; q < 7; q++) xsn[q] = s[o + xo[q]];
+      xvn = vx[o];
     }
-    __syncthreads();
-    if (k + 1 < zend) load_plane(k + 1);  // lands while this plane computes
-    const long long zb = zoff(k);
+    const R gx = adv_slots<R, EXACT>(w7, ux, mring[0], dt, ix, G);
+    const long long c = row + xw + ob;
+    if (a.gvel[0] && own) a.gvel[0][c] += gx;
+    // Vbar(x) = sum_m G_m(x + 2 - m): lane + 2 - m; valid for lanes 3..29
+    R V = R(0);
 #pragma unroll
-    for (int r = 0; r < kPer; r++) {
-      const int code = job_code[r];
-      if (code < 0) continue;
-      const int lx = code & 63, ly = (code >> 6) & 63;
-      const bool own = (code >> 12) & 1, ydir = (code >> 13) & 1;
-      R w7[7], G[6];
-      if (!ydir) {
-#pragma unroll
-        for (int q = 0; q < 7; q++) w7[q] = sS[ly + 6][lx + q];
-      } else {
-#pragma unroll
-        for (int q = 0; q < 7; q++) w7[q] = sS[ly + q][lx + 6];
-      }
-      const R g = adv_slots<R, EXACT>(w7, v_cur[r], a.mscale * m_cur[r], dt, a.inv[ydir], G);
-      if (!ydir) {
-#pragma unroll
-        for (int m = 0; m < 6; m++) sGx[m][ly][lx] = G[m];
-      } else {
-#pragma unroll
-        for (int m = 0; m < 6; m++) sGy[m][ly][lx] = G[m];
-      }
-      if (own && a.gvel[ydir]) a.gvel[ydir][zb + job_off[r]] += g;
-    }
-    __syncthreads();
-
-    // ---- gather and write ---------------------------------------------------
-    if (!mine) continue;
-    R Ax = R(0), Ay = R(0);
-#pragma unroll
-    for (int m = 0; m < 6; m++) {
-      Ax += sGx[m][ty][tx + 5 - m] - sGx[m][ty][tx + 6 - m];
-      Ay += sGy[m][ty + 5 - m][tx] - sGy[m][ty + 6 - m][tx];
-    }
-    const long long c = zb + col;
-    R o = mring[0] + ((Ax + Ay) + Az);
+    for (int m = 0; m < 6; m++) V += __shfl_sync(0xffffffffu, G[m], (lane + 2 - m) & 31);
+    const R Ax = V - __shfl_sync(0xffffffffu, V, (lane + 1) & 31);
+    if (!own) continue;
+    R o = mring[0] + (Ax + Az);
     if (a.P) o += a.pscale * a.P[c];
     if (a.Q) o += a.qscale * a.Q[c];
     a.out[c] = o;
+  }
+}
+
+template <class R, bool EXACT>
+__global__ void __launch_bounds__(32 * kRows) k_adj_y(AdjStageArgs<R> a) {
+  const Layout &L = a.L;
+  const int i = blockIdx.x * 32 + threadIdx.x;
+  const int k = blockIdx.y * kRows + threadIdx.y;
+  if (i >= L.nx || k >= L.nz) return;
+  const int y0 = blockIdx.z * a.ychunk;
+  const int yend = min(y0 + a.ychunk, L.ny);
+  const int ny = L.ny;
+  const R dt = a.dt, msc = a.mscale, iy = a.inv[1];
+  const long long py = L.py;
+  const long long base = (long long)(i + fused::GX) + L.pz * (long long)(k + fused::GZ);
+  const R *s = a.s + base, *M = a.M + base, *vy = a.vel[1] + base;
+  int yk = wrapi(y0 - 3, ny);
+  long long ok = py * (long long)(yk + fused::GY);
+
+  R win[7], mring[4], F[6];
+  R prevV = R(0);
+#pragma unroll
+  for (int q = 0; q < 6; q++) {
+    win[q + 1] = s[plane_add(ok, yk, q - 3, ny, py)];
+    F[q] = R(0);
+  }
+#pragma unroll
+  for (int q = 0; q < 4; q++) mring[q] = R(0);
+  R cs = s[plane_add(ok, yk, 3, ny, py)], cm = M[ok], cv = vy[ok];
+  for (int jj = y0 - 3; jj < yend + 3; jj++) {
+#pragma unroll
+    for (int q = 0; q < 6; q++) win[q] = win[q + 1];
+    win[6] = cs;
+#pragma unroll
+    for (int q = 0; q < 3; q++) mring[q] = mring[q + 1];
+    mring[3] = msc * cm;
+    const R uy = cv;
+    const long long ojj = ok;
+    const int yjj = yk;
+    ok = plane_add(ok, yk, 1, ny, py);
+    yk = (yk + 1 == ny) ? 0 : yk + 1;
+    if (jj + 1 < yend + 3) {
+      cs = s[plane_add(ok, yk, 3, ny, py)];
+      cm = M[ok];
+      cv = vy[ok];
+    }
+    R G[6];
+    const R gy = adv_slots<R, EXACT>(win, uy, mring[3], dt, iy, G);
+    if (a.gvel[1] && jj >= y0 && jj < yend) a.gvel[1][base + ojj] += gy;
+    const R Ay = ring_step<R>(F, prevV, G);
+    if (jj - 3 < y0) continue;
+    a.out[base + plane_add(ojj, yjj, -3, ny, py)] += Ay;
   }
 }
 

@@ -20,53 +20,33 @@ struct AdjSpec {
   double dt, dx, dy, dz, eps;
 };
 
-template <class R, bool EXACT>
-void set_adj_smem() {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_adj_stage<R, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(sizeof(R) * (size_t)kSmemElems));
-    attr = true;
-  }
+// march length per thread: enough threads for about 2048 per SM, and at
+// least 16 cells per march (each march also computes 6 warm-up cells)
+inline int pick_chunk(int n_march, long long threads_per_chunk) {
+  int sms = 152, dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = 2048LL * sms;
+  long long chunks = (want + threads_per_chunk - 1) / threads_per_chunk;
+  if (chunks < 1) chunks = 1;
+  int c = (int)((n_march + chunks - 1) / chunks);
+  if (c < 16) c = 16;
+  if (c > n_march) c = n_march;
+  return c;
 }
 
+// one adjoint stage: x and z faces (writes out), then y faces (adds to out)
 template <class R, bool EXACT>
 void launch_adj_stage(const AdjStageArgs<R> &a) {
   const Layout &L = a.L;
-  const size_t smem = sizeof(R) * (size_t)kSmemElems;
-  set_adj_smem<R, EXACT>();
-  dim3 blk(AX, AY);
-  dim3 grd((unsigned)((L.nx + AX - 1) / AX), (unsigned)((L.ny + AY - 1) / AY),
-           (unsigned)((L.nz + a.zchunk - 1) / a.zchunk));
-  k_adj_stage<R, EXACT><<<grd, blk, smem, stream()>>>(a);
+  dim3 blk(32, kRows);
+  dim3 g1((unsigned)((L.nx + kSeg - 1) / kSeg), (unsigned)((L.ny + kRows - 1) / kRows),
+          (unsigned)((L.nz + a.zchunk - 1) / a.zchunk));
+  k_adj_xz<R, EXACT><<<g1, blk, 0, stream()>>>(a);
   note_launch();
-}
-
-// z planes per CTA: the chunk count c minimising waves(c) * (planes(c) + 6),
-// the time of the slowest SM (each CTA marches its planes plus 6 warm-up
-// planes; waves = ceil(CTAs / resident CTA slots))
-template <class R, bool EXACT>
-int pick_zchunk(const Layout &L) {
-  int sms = 152, dev = 0, per_sm = 1;
-  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  set_adj_smem<R, EXACT>();
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adj_stage<R, EXACT>, AX * AY,
-                                                sizeof(R) * (size_t)kSmemElems);
-  if (per_sm < 1) per_sm = 1;
-  const long long slots = (long long)sms * per_sm;
-  const long long xy = (long long)((L.nx + AX - 1) / AX) * ((L.ny + AY - 1) / AY);
-  int best = L.nz;
-  long long best_cost = -1;
-  for (int c = 1; c <= (L.nz + 7) / 8; c++) {
-    const int z = (L.nz + c - 1) / c;
-    const long long waves = (xy * c + slots - 1) / slots;
-    const long long cost = waves * (z + 6);
-    if (best_cost < 0 || cost < best_cost) {
-      best_cost = cost;
-      best = z;
-    }
-  }
-  return best;
+  dim3 g2((unsigned)((L.nx + 31) / 32), (unsigned)((L.nz + kRows - 1) / kRows),
+          (unsigned)((L.ny + a.ychunk - 1) / a.ychunk));
+  k_adj_y<R, EXACT><<<g2, blk, 0, stream()>>>(a);
+  note_launch();
 }
 
 template <class R, bool EXACT>
@@ -205,7 +185,8 @@ int run(const char *name, const R *phi_user, const Box &gb, const Box &fb, const
     }
     aa.dt = (R)sp.dt;
     aa.inv[0] = fa.inv[0]; aa.inv[1] = fa.inv[1]; aa.inv[2] = fa.inv[2];
-    aa.zchunk = pick_zchunk<R, EXACT>(L);
+    aa.zchunk = pick_chunk(nz, 32LL * ((nx + kSeg - 1) / kSeg) * ny);
+    aa.ychunk = pick_chunk(ny, (long long)nx * nz);
     for (int seg = nck - 1; seg >= 0 && sp.n_steps > 0; seg--) {
       const int s0 = seg * K, s1 = (s0 + K < sp.n_steps) ? s0 + K : sp.n_steps, ns = s1 - s0;
       U[0] = ck[seg];

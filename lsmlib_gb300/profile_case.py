@@ -1,11 +1,15 @@
 """Run one fused call of the level-set hot path on cuda:0, for profilers.
 
   python -m lsmlib_gb300.profile_case --mode reinit --n 256 --iters 1 --precision f32
+  python -m lsmlib_gb300.profile_case --mode adjoint --n 128 --iters 8 --precision f32
 
 Builds the same analytic field as bench.py, moves it to the device, and runs
 `iters` WENO5 / TVD-RK3 iterations (3 stage kernels each) of reinitialization
 or constant-velocity advection, then the mean curvature.  The stage kernels
 are k_stage<float|double, mode>; ncu can select them with -k regex:k_stage.
+Mode adjoint runs the advection objective gradient of bench.adjoint_case
+(`iters` steps, checkpoint every 4): forward stages k_stage_f32 / k_stage,
+adjoint stages k_adj_xz and k_adj_y.
 """
 import argparse
 import os
@@ -19,7 +23,7 @@ sys.path.insert(0, ROOT)
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--mode", choices=["reinit", "advect"], default="reinit")
+    ap.add_argument("--mode", choices=["reinit", "advect", "adjoint"], default="reinit")
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--iters", type=int, default=1)
     ap.add_argument("--precision", choices=["f32", "f64"], default="f32")
@@ -32,8 +36,18 @@ def main():
     B.build()
     L.set_stream(torch.cuda.current_stream().cuda_stream)
     gb, fb = bench.boxes(a.n)
-    phi64, dx = bench.initial_phi(a.n)
     dt = torch.float32 if a.precision == "f32" else torch.float64
+    if a.mode == "adjoint":
+        phi0, vel, tgt, h, tstep = bench.adjoint_case(a.n)
+        ghost = lambda v: torch.from_numpy(np.ascontiguousarray(np.pad(v, 3).T)).cuda().to(dt)
+        J, gp, gv = L.advect_adjoint_weno5_tvdrk3(ghost(phi0), gb, fb, [ghost(v) for v in vel], gb, ghost(tgt), h,
+                                                  tstep, a.iters, 1.5 * h, checkpoint_every=4,
+                                                  precision=a.precision)
+        torch.cuda.synchronize()
+        L.check()
+        print("ok", a.mode, a.n, a.iters, a.precision, "J", J, "launches", L.launch_count())
+        return
+    phi64, dx = bench.initial_phi(a.n)
     phi = torch.from_numpy(np.ascontiguousarray(phi64.T)).cuda().to(dt)
     kappa = torch.zeros_like(phi)
     if a.mode == "reinit":
