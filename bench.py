@@ -480,6 +480,13 @@ def gpu_arm(args, world, rank, local):
         "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
         "fp64": fp64, "fp32_error_vs_fp64": err,
     }
+    if rank == 0 and not args.no_extra:
+        line["other_workloads"] = {
+            "advection_128": sub_advection(stream, dev),
+            "narrow_band_512": sub_narrow_band(stream, dev),
+            "batched_4096": sub_batched(stream, dev),
+            "adjoint_192": sub_adjoint(stream, dev),
+        }
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         v, sec, kind = cpu_sample(n, 1, threads)
@@ -488,6 +495,156 @@ def gpu_arm(args, world, rank, local):
                                           "(%.1f s), k-slabs over %d host threads" % (n, sec, threads)}
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# the other workloads of the hot path, each measured once per run
+# ---------------------------------------------------------------------------
+def _ev(stream):
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _timed(fn, stream):
+    import torch
+    a, b = _ev(stream)
+    torch.cuda.synchronize()
+    a.record(stream)
+    fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b)
+
+
+def sub_advection(stream, dev, n=128, steps=50):
+    """Plain-method advection: 128^3 on [-1, 1]^3, periodic, signed distance
+    to a sphere of radius 0.35 at (0.1, -0.05, 0), constant velocity
+    (1, 0.5, 0.25), WENO5 / TVD-RK3 at CFL 0.5, 50 steps; FP64 parity form
+    and FP32 form, and the FP32 error against FP64."""
+    import torch
+    import lsmlib_gb300 as L
+    gb, fb = boxes(n)
+    dx = 2.0 / n
+    c = -1.0 + (np.arange(-GHOST, n + GHOST) + 0.5) * dx
+    X, Y, Z = np.meshgrid(c, c, c, indexing="ij")
+    phi = np.sqrt((X - 0.1) ** 2 + (Y + 0.05) ** 2 + Z ** 2) - 0.35
+    vel = (1.0, 0.5, 0.25)
+    dt = 0.5 * dx / sum(abs(v) for v in vel)
+    out = {"workload": "advection-weno5-tvdrk3-128, sphere r=0.35, u=(1,0.5,0.25), CFL 0.5, 50 steps, periodic"}
+    res = {}
+    for prec, dtype in (("f64", torch.float64), ("f32", torch.float32)):
+        t = torch.from_numpy(np.ascontiguousarray(phi.T)).to(dev, dtype)
+        L.advect_weno5_tvdrk3(t, gb, fb, dx, dt, 1, vel_const=vel, precision=prec)  # warm-up
+        t.copy_(torch.from_numpy(np.ascontiguousarray(phi.T)).to(dev, dtype))
+        ms = _timed(lambda: L.advect_weno5_tvdrk3(t, gb, fb, dx, dt, steps, vel_const=vel, precision=prec), stream)
+        res[prec] = t.double().cpu().numpy().T[GHOST:-GHOST, GHOST:-GHOST, GHOST:-GHOST]
+        out[prec] = {"ms": ms, "Gcell_updates_per_s": n ** 3 * steps / (ms / 1e3) / 1e9}
+    out["fp32_speedup"] = out["f64"]["ms"] / out["f32"]["ms"]
+    d = np.abs(res["f32"] - res["f64"])
+    out["fp32_error_vs_fp64"] = {"linf": float(d.max()), "l1": float(d.mean())}
+    return out
+
+
+def sub_narrow_band(stream, dev, n=512, steps=100, rebuild=5, n_spheres=64, seed=7):
+    """Narrow band: 512^3 on [-1, 1]^3, signed distance to the union of 64
+    spheres (centres U[-0.8, 0.8]^3, radii U[0.03, 0.10], numpy seed 7),
+    band half-width 6 cells (inner width 3 cells), rebuilt every 5 steps,
+    V_n = 1 - 0.1 kappa, WENO5 + TVD-RK3 on the band, 100 steps, FP32."""
+    import torch
+    import lsmlib_gb300 as L
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(-0.8, 0.8, size=(n_spheres, 3))
+    radii = rng.uniform(0.03, 0.10, size=n_spheres)
+    dx = 2.0 / n
+    gb, fb = boxes(n)
+    c = -1.0 + (torch.arange(-GHOST, n + GHOST, device=dev, dtype=torch.float32) + 0.5) * dx
+    # C-ordered [k][j][i] tensor of the Fortran ghost-box array
+    z, y, x = c.view(-1, 1, 1), c.view(1, -1, 1), c.view(1, 1, -1)
+    phi = torch.full((n + 2 * GHOST,) * 3, 1e30, device=dev, dtype=torch.float32)
+    for (cx, cy, cz), r in zip(centres, radii):
+        phi = torch.minimum(phi, torch.sqrt((x - float(cx)) ** 2 + (y - float(cy)) ** 2 + (z - float(cz)) ** 2)
+                            - float(r))
+    torch.cuda.synchronize()
+    holder = {}
+
+    def run():
+        holder["r"] = L.band_flow_weno5_tvdrk3(phi, gb, fb, dx, steps, rebuild, 6 * dx, 3 * dx, a_n=1.0, b_n=0.1,
+                                               cfl=0.5, precision="f32")
+    ms = _timed(run, stream)
+    dts, bands = holder["r"]
+    band_updates = int(sum(int(b) * min(rebuild, steps - i * rebuild) for i, b in enumerate(bands)))
+    return {"workload": "narrow-band-512, 64 spheres (seed 7), half-width 6dx, rebuild every 5, "
+                        "Vn = 1 - 0.1 kappa, 100 steps, FP32",
+            "ms": ms, "band_cells_first_rebuild": int(bands[0]), "band_cell_updates": band_updates,
+            "Gband_cell_updates_per_s": band_updates / (ms / 1e3) / 1e9,
+            "grid_cell_updates_per_s_equivalent": n ** 3 * steps / (ms / 1e3) / 1e9}
+
+
+def sub_batched(stream, dev, n_grids=4096, steps=30, seed=11):
+    """Batched uneven grids: 4096 grids, sides U{16..96} per axis (numpy seed
+    11), each on [-1, 1]^3 with an ellipsoid level set (semi-axes U[0.2, 0.6],
+    phi = (|x / a| - 1) min(a)), constant velocity U[-1, 1]^3 per grid,
+    periodic, WENO5 / TVD-RK3 at CFL 0.5, 30 steps, FP32; one persistent
+    launch per stage in a CUDA graph against one single-grid launch per grid
+    per stage."""
+    import torch
+    import lsmlib_gb300 as L
+    rng = np.random.default_rng(seed)
+    dims = rng.integers(16, 97, size=(n_grids, 3))
+    axes = rng.uniform(0.2, 0.6, size=(n_grids, 3))
+    vel = rng.uniform(-1.0, 1.0, size=(n_grids, 3))
+    spacing = 2.0 / dims
+    dt = 0.5 / (np.abs(vel) / spacing).sum(axis=1)
+    sizes = np.prod(dims + 2 * GHOST, axis=1)
+    offsets = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    buf = torch.empty(int(sizes.sum()), device=dev, dtype=torch.float32)
+    for g in range(n_grids):
+        nx, ny, nz = (int(v) for v in dims[g])
+        cs = [-1.0 + (torch.arange(-GHOST, m + GHOST, device=dev, dtype=torch.float32) + 0.5) * (2.0 / m)
+              for m in (nx, ny, nz)]
+        z, y, x = cs[2].view(-1, 1, 1), cs[1].view(1, -1, 1), cs[0].view(1, 1, -1)
+        a = axes[g]
+        f = (torch.sqrt((x / a[0]) ** 2 + (y / a[1]) ** 2 + (z / a[2]) ** 2) - 1.0) * float(a.min())
+        buf[offsets[g]:offsets[g] + sizes[g]] = f.reshape(-1)
+    pristine = buf.clone()
+    cells = int(np.prod(dims, axis=1).sum())
+    out = {"workload": "batched-4096 uneven grids (sides U{16..96}, seed 11), ellipsoids, constant velocity, "
+                       "30 steps, FP32", "grids": n_grids, "cells": cells}
+    for name, flags in (("persistent_graph", 0), ("launch_loop", L.BATCH_LOOP)):
+        buf.copy_(pristine)
+        L.advect_batch_weno5_tvdrk3(buf, offsets, dims, vel, spacing, dt, 1, flags=flags)  # tune / warm up
+        buf.copy_(pristine)
+        ms = _timed(lambda: L.advect_batch_weno5_tvdrk3(buf, offsets, dims, vel, spacing, dt, steps, flags=flags),
+                    stream)
+        out[name] = {"ms": ms, "Gcell_updates_per_s": cells * steps / (ms / 1e3) / 1e9}
+    out["speedup_vs_loop"] = out["launch_loop"]["ms"] / out["persistent_graph"]["ms"]
+    return out
+
+
+def sub_adjoint(stream, dev, n=192, steps=40, ckpt=8):
+    """Gradient of J = sum (H(phi_T) - H(phi_target))^2 dx^3 after 40 periodic
+    advection steps at 192^3 (adjoint_case), FP32 state, FP64 objective,
+    checkpoint every 8 steps with recomputation: objective-only time, full
+    gradient time, and the cost of one reverse step (recomputation included)
+    against one forward step."""
+    import torch
+    import lsmlib_gb300 as L
+    phi, vel, tgt, h, dt = adjoint_case(n)
+    gb, fb = boxes(n)
+    dvc = lambda a: torch.from_numpy(np.ascontiguousarray(np.pad(a, GHOST).T)).to(dev, torch.float32)
+    P, V, T = dvc(phi), [dvc(v) for v in vel], dvc(tgt)
+    eps = 1.5 * h
+    run = lambda grads: L.advect_adjoint_weno5_tvdrk3(P, gb, fb, V, gb, T, h, dt, steps, eps, checkpoint_every=ckpt,
+                                                      precision="f32", grads=grads)
+    run(False)
+    run(True)
+    t_f = min(_timed(lambda: run(False), stream) for _ in range(3))
+    t_g = min(_timed(lambda: run(True), stream) for _ in range(3))
+    return {"workload": "adjoint-192: 40 advection steps, sphere r=0.4, velocity field + N(0,0.05) (seed 3), "
+                        "J with H_eps (eps=1.5dx), checkpoint every 8, FP32 state / FP64 objective",
+            "objective_ms": t_f, "gradient_ms": t_g, "forward_step_ms": t_f / steps,
+            "reverse_step_ms": (t_g - t_f) / steps, "reverse_to_forward_step": (t_g - t_f) / t_f}
+
 
 
 # DRAM bytes per fused FP32 reinitialization stage launch at 256^3 from ncu
@@ -503,6 +660,7 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
+    ap.add_argument("--no-extra", action="store_true", help="skip the other workloads")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
