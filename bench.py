@@ -414,6 +414,8 @@ def gpu_arm(args, world, rank, local):
     peak, peak_kind = measured_peaks()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": MEASURED_STAGE_TRAFFIC,
+                "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one stage-2 launch "
+                                "(algorithmic 268.4 MB for that stage; achieved uses the 3-stage mean, 14.67 B/cell)",
                 "kernel": "k_stage<float, REINIT> (fused WENO5 + reinit RHS + TVD-RK3 stage)",
                 "stage_ms": stage_ms, "peak_source": peak_kind}
 
@@ -541,30 +543,40 @@ def sub_advection(stream, dev, n=128, steps=50):
         out[prec] = {"ms": ms, "Gcell_updates_per_s": n ** 3 * steps / (ms / 1e3) / 1e9}
     out["fp32_speedup"] = out["f64"]["ms"] / out["f32"]["ms"]
     d = np.abs(res["f32"] - res["f64"])
-    out["fp32_error_vs_fp64"] = {"linf": float(d.max()), "l1": float(d.mean())}
+    near = np.abs(res["f64"]) < 3 * dx
+    at = np.unravel_index(np.argmax(d), d.shape)
+    out["fp32_error_vs_fp64"] = {"linf": float(d.max()), "l1": float(d.mean()),
+                                 "linf_within_3dx_of_interface": float(d[near].max()),
+                                 "linf_at_cell": [int(v) for v in at]}
     return out
 
 
-def sub_narrow_band(stream, dev, n=512, steps=100, rebuild=5, n_spheres=64, seed=7):
-    """Narrow band: 512^3 on [-1, 1]^3, signed distance to the union of 64
-    spheres (centres U[-0.8, 0.8]^3, radii U[0.03, 0.10], numpy seed 7),
-    band half-width 6 cells (inner width 3 cells), rebuilt every 5 steps,
-    V_n = 1 - 0.1 kappa, WENO5 + TVD-RK3 on the band, 100 steps, FP32."""
+def band_case(dev, n=512, n_spheres=64, seed=7):
+    """Signed distance to the union of 64 spheres (centres U[-0.8, 0.8]^3,
+    radii U[0.03, 0.10], numpy seed 7) on the n^3 cell centres of [-1, 1]^3
+    with 3 ghost cells: a C-ordered FP32 CUDA tensor of the Fortran ghost-box
+    array."""
     import torch
-    import lsmlib_gb300 as L
     rng = np.random.default_rng(seed)
     centres = rng.uniform(-0.8, 0.8, size=(n_spheres, 3))
     radii = rng.uniform(0.03, 0.10, size=n_spheres)
     dx = 2.0 / n
-    gb, fb = boxes(n)
     c = -1.0 + (torch.arange(-GHOST, n + GHOST, device=dev, dtype=torch.float32) + 0.5) * dx
-    # C-ordered [k][j][i] tensor of the Fortran ghost-box array
     z, y, x = c.view(-1, 1, 1), c.view(1, -1, 1), c.view(1, 1, -1)
     phi = torch.full((n + 2 * GHOST,) * 3, 1e30, device=dev, dtype=torch.float32)
     for (cx, cy, cz), r in zip(centres, radii):
         phi = torch.minimum(phi, torch.sqrt((x - float(cx)) ** 2 + (y - float(cy)) ** 2 + (z - float(cz)) ** 2)
                             - float(r))
-    torch.cuda.synchronize()
+    return phi, dx
+
+
+def sub_narrow_band(stream, dev, n=512, steps=100, rebuild=5):
+    """Narrow band: 512^3 on [-1, 1]^3 (band_case), band half-width 6 cells
+    (inner width 3 cells), rebuilt every 5 steps, V_n = 1 - 0.1 kappa,
+    WENO5 + TVD-RK3 on the band, 100 steps, FP32."""
+    import lsmlib_gb300 as L
+    gb, fb = boxes(n)
+    phi, dx = band_case(dev, n)
     holder = {}
 
     def run():
@@ -580,17 +592,15 @@ def sub_narrow_band(stream, dev, n=512, steps=100, rebuild=5, n_spheres=64, seed
             "grid_cell_updates_per_s_equivalent": n ** 3 * steps / (ms / 1e3) / 1e9}
 
 
-def sub_batched(stream, dev, n_grids=4096, steps=30, seed=11):
-    """Batched uneven grids: 4096 grids, sides U{16..96} per axis (numpy seed
-    11), each on [-1, 1]^3 with an ellipsoid level set (semi-axes U[0.2, 0.6],
-    phi = (|x / a| - 1) min(a)), constant velocity U[-1, 1]^3 per grid,
-    periodic, WENO5 / TVD-RK3 at CFL 0.5, 30 steps, FP32; one persistent
-    launch per stage in a CUDA graph against one single-grid launch per grid
-    per stage."""
+def batched_case(dev, n_grids=4096, seed=11, lo=16, hi=96):
+    """4096 grids, sides U{16..96} per axis (numpy seed 11), each on [-1, 1]^3
+    with an ellipsoid level set (semi-axes U[0.2, 0.6], phi = (|x / a| - 1)
+    min(a)) and a constant velocity U[-1, 1]^3, dt at CFL 0.5.  Returns the
+    packed FP32 CUDA buffer (3 ghost cells per grid), offsets, dims,
+    velocities, spacings and dts."""
     import torch
-    import lsmlib_gb300 as L
     rng = np.random.default_rng(seed)
-    dims = rng.integers(16, 97, size=(n_grids, 3))
+    dims = rng.integers(lo, hi + 1, size=(n_grids, 3))
     axes = rng.uniform(0.2, 0.6, size=(n_grids, 3))
     vel = rng.uniform(-1.0, 1.0, size=(n_grids, 3))
     spacing = 2.0 / dims
@@ -606,6 +616,15 @@ def sub_batched(stream, dev, n_grids=4096, steps=30, seed=11):
         a = axes[g]
         f = (torch.sqrt((x / a[0]) ** 2 + (y / a[1]) ** 2 + (z / a[2]) ** 2) - 1.0) * float(a.min())
         buf[offsets[g]:offsets[g] + sizes[g]] = f.reshape(-1)
+    return buf, offsets, dims, vel, spacing, dt
+
+
+def sub_batched(stream, dev, n_grids=4096, steps=30):
+    """Batched uneven grids (batched_case), periodic, WENO5 / TVD-RK3 at CFL
+    0.5, 30 steps, FP32: one persistent launch per stage in a CUDA graph
+    against one single-grid launch per grid per stage."""
+    import lsmlib_gb300 as L
+    buf, offsets, dims, vel, spacing, dt = batched_case(dev, n_grids)
     pristine = buf.clone()
     cells = int(np.prod(dims, axis=1).sum())
     out = {"workload": "batched-4096 uneven grids (sides U{16..96}, seed 11), ellipsoids, constant velocity, "
@@ -647,9 +666,11 @@ def sub_adjoint(stream, dev, n=192, steps=40, ckpt=8):
 
 
 
-# DRAM bytes per fused FP32 reinitialization stage launch at 256^3 from ncu
-# (profiles/ summary); None until captured
-MEASURED_STAGE_TRAFFIC = None
+# DRAM bytes (read + write) of one fused FP32 reinitialization stage launch
+# at 256^3, from one ncu capture of a stage-2 launch (profiles/
+# k_stage_reinit_f32_256.md, packed FP32x2 kernel: 285.6 MB; the stage's
+# algorithmic bytes are 16 B/cell = 268.4 MB)
+MEASURED_STAGE_TRAFFIC = 285.6e6
 
 
 def main():

@@ -2,6 +2,8 @@
 
   python -m lsmlib_gb300.profile_case --mode reinit --n 256 --iters 1 --precision f32
   python -m lsmlib_gb300.profile_case --mode adjoint --n 128 --iters 8 --precision f32
+  python -m lsmlib_gb300.profile_case --mode band --n 256 --iters 10
+  python -m lsmlib_gb300.profile_case --mode batched --n 512 --iters 2
 
 Builds the same analytic field as bench.py, moves it to the device, and runs
 `iters` WENO5 / TVD-RK3 iterations (3 stage kernels each) of reinitialization
@@ -10,6 +12,9 @@ are k_stage<float|double, mode>; ncu can select them with -k regex:k_stage.
 Mode adjoint runs the advection objective gradient of bench.adjoint_case
 (`iters` steps, checkpoint every 4): forward stages k_stage_f32 / k_stage,
 adjoint stages k_adj_xz and k_adj_y.
+Mode band runs `iters` narrow-band curvature-flow steps of bench.band_case
+at n^3 (rebuild every 5 steps, FP32).  Mode batched advects `n` grids of
+bench.batched_case `iters` steps (persistent kernel in a CUDA graph).
 """
 import argparse
 import os
@@ -23,7 +28,7 @@ sys.path.insert(0, ROOT)
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--mode", choices=["reinit", "advect", "adjoint"], default="reinit")
+    ap.add_argument("--mode", choices=["reinit", "advect", "adjoint", "band", "batched"], default="reinit")
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--iters", type=int, default=1)
     ap.add_argument("--precision", choices=["f32", "f64"], default="f32")
@@ -46,6 +51,21 @@ def main():
         torch.cuda.synchronize()
         L.check()
         print("ok", a.mode, a.n, a.iters, a.precision, "J", J, "launches", L.launch_count())
+        return
+    if a.mode == "band":
+        phi, dx = bench.band_case("cuda", a.n)
+        dts, bands = L.band_flow_weno5_tvdrk3(phi, gb, fb, dx, a.iters, 5, 6 * dx, 3 * dx, a_n=1.0, b_n=0.1,
+                                              cfl=0.5, precision="f32")
+        torch.cuda.synchronize()
+        L.check()
+        print("ok", a.mode, a.n, a.iters, "band cells", int(bands[0]), "launches", L.launch_count())
+        return
+    if a.mode == "batched":
+        buf, offsets, dims, vel, spacing, tstep = bench.batched_case("cuda", a.n)
+        L.advect_batch_weno5_tvdrk3(buf, offsets, dims, vel, spacing, tstep, a.iters)
+        torch.cuda.synchronize()
+        L.check()
+        print("ok", a.mode, a.n, "grids", a.iters, "steps", "launches", L.launch_count())
         return
     phi64, dx = bench.initial_phi(a.n)
     phi = torch.from_numpy(np.ascontiguousarray(phi64.T)).cuda().to(dt)
