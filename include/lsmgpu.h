@@ -186,6 +186,34 @@ int lsmgpu_advect_adjoint_weno5_tvdrk3_f32(const float *phi, const int *gb, cons
                                            double heaviside_eps, double *J, float *grad_phi,
                                            float *grad_vel_x, float *grad_vel_y, float *grad_vel_z);
 
+/* Vector-Jacobian products (reverse mode) of the periodic steppers, for any
+ * objective: given grad_out = dJ/dphi_T over gb, return grad_phi =
+ * dJ/dphi (and, for advection, grad_vel_* = dJ/dvel_*), with phi_T the
+ * state after n_steps steps of lsmgpu_advect_weno5_tvdrk3_* /
+ * n_iter iterations of lsmgpu_reinit_weno5_tvdrk3_* (LSMGPU_BC_PERIODIC;
+ * reinitialization in the phi0 sign form, use_phi0_for_sgn = 1, whose sign
+ * source is phi itself, so its sensitivity is part of grad_phi).  phi_out
+ * (optional) receives phi_T over gb.  Checkpointing, derivative conventions
+ * (branch taken at the upwind / Godunov maxima, dt fixed) and memory as for
+ * lsmgpu_advect_adjoint_weno5_tvdrk3_*.  No counterpart in LSMLIB.  Returns
+ * an LSMGPU_* status. */
+int lsmgpu_advect_vjp_weno5_tvdrk3_f64(const double *phi, const int *gb, const int *fb, const double *vel_x,
+                                       const double *vel_y, const double *vel_z, const int *vel_gb, double dx,
+                                       double dy, double dz, double dt, int n_steps, int checkpoint_every,
+                                       const double *grad_out, double *phi_out, double *grad_phi,
+                                       double *grad_vel_x, double *grad_vel_y, double *grad_vel_z);
+int lsmgpu_advect_vjp_weno5_tvdrk3_f32(const float *phi, const int *gb, const int *fb, const float *vel_x,
+                                       const float *vel_y, const float *vel_z, const int *vel_gb, float dx,
+                                       float dy, float dz, float dt, int n_steps, int checkpoint_every,
+                                       const float *grad_out, float *phi_out, float *grad_phi, float *grad_vel_x,
+                                       float *grad_vel_y, float *grad_vel_z);
+int lsmgpu_reinit_vjp_weno5_tvdrk3_f64(const double *phi, const int *gb, const int *fb, double dx, double dy,
+                                       double dz, double dtau, int n_iter, int checkpoint_every,
+                                       const double *grad_out, double *phi_out, double *grad_phi);
+int lsmgpu_reinit_vjp_weno5_tvdrk3_f32(const float *phi, const int *gb, const int *fb, float dx, float dy,
+                                       float dz, float dtau, int n_iter, int checkpoint_every,
+                                       const float *grad_out, float *phi_out, float *grad_phi);
+
 /* Allocation-free CFL-stable advection dt.  No counterpart in LSMLIB: it is
  * lsm3dcomputestableadvectiondt_ (same arguments, same result) for callers
  * that cannot let a library allocate device memory — a solver running inside

@@ -261,3 +261,40 @@ def advect_adjoint_weno5_tvdrk3(phi, gb, fb, vel, vel_gb, phi_target, dx, dt, n_
     if rc != 0:
         raise RuntimeError("lsmgpu advect adjoint failed: %s" % (last_error()[1],))
     return J.value, gphi, gv
+
+
+def advect_vjp_weno5_tvdrk3(phi, gb, fb, vel, vel_gb, grad_out, dx, dt, n_steps, checkpoint_every=8,
+                            precision="f64", dy=None, dz=None, grad_vel=True):
+    """Vector-Jacobian product of n_steps periodic advection steps: returns
+    (phi_T, grad_phi, [grad_vel_x, grad_vel_y, grad_vel_z]) for the upstream
+    gradient grad_out = dJ/dphi_T (new arrays of the kind of `phi`)."""
+    real = ctypes.c_double if precision == "f64" else ctypes.c_float
+    fn = getattr(lib(), "lsmgpu_advect_vjp_weno5_tvdrk3_" + precision)
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p] * 7 + [real] * 4 + [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 6
+    out = _zeros_like(phi)
+    gphi = _zeros_like(phi)
+    gv = [_zeros_like(v) for v in vel] if grad_vel else [None, None, None]
+    rc = fn(_ptr(phi), _box(gb), _box(fb), _ptr(vel[0]), _ptr(vel[1]), _ptr(vel[2]), _box(vel_gb), dx, dy or dx,
+            dz or dx, dt, int(n_steps), int(checkpoint_every), _ptr(grad_out), _ptr(out), _ptr(gphi),
+            _ptr(gv[0]), _ptr(gv[1]), _ptr(gv[2]))
+    if rc != 0:
+        raise RuntimeError("lsmgpu advect vjp failed: %s" % (last_error()[1],))
+    return out, gphi, gv
+
+
+def reinit_vjp_weno5_tvdrk3(phi, gb, fb, grad_out, dx, dtau, n_iter, checkpoint_every=8, precision="f64",
+                            dy=None, dz=None):
+    """Vector-Jacobian product of n_iter periodic reinitialization iterations
+    (phi0 sign form): returns (phi_T, grad_phi) for grad_out = dJ/dphi_T."""
+    real = ctypes.c_double if precision == "f64" else ctypes.c_float
+    fn = getattr(lib(), "lsmgpu_reinit_vjp_weno5_tvdrk3_" + precision)
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p] * 3 + [real] * 4 + [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 3
+    out = _zeros_like(phi)
+    gphi = _zeros_like(phi) if grad_out is not None else None
+    rc = fn(_ptr(phi), _box(gb), _box(fb), dx, dy or dx, dz or dx, dtau, int(n_iter), int(checkpoint_every),
+            _ptr(grad_out), _ptr(out), _ptr(gphi))
+    if rc != 0:
+        raise RuntimeError("lsmgpu reinit vjp failed: %s" % (last_error()[1],))
+    return out, gphi

@@ -143,17 +143,17 @@ __device__ __forceinline__ R weno5_adj(const R v[5], R dv[5]) {
 // u = the velocity component, mu = the adjoint weight of the cell, inv = 1/dx_d.
 // G[m] is the adjoint of face c-2+m (scaled by dt); the return value is the
 // velocity adjoint dt * mu * (-W), zero where the forward set W to zero.
-// FP32 slots with the adjoint weight folded in early: yb = dt mu (-u)/dx
+// FP32 slots with the adjoint weight folded in early: yb = dt mu kap / dx
 // multiplies the weights and the beta_k once, so the five face adjoints come
-// out of the derivative formulas directly.
-static __device__ __forceinline__ float adv_slots_f32(const float a[7], float u, float mu, float dt, float inv,
-                                               float G[6]) {
+// out of the derivative formulas directly.  kap = dL/dW for the WENO5 value W
+// on side `minus`; returns W.
+static __device__ __forceinline__ float lin_slots_f32(const float a[7], float kap, bool minus, float mu, float dt,
+                                                      float inv, float G[6]) {
   const float c13 = 1.f / 3.f, c76 = 7.f / 6.f, c116 = 11.f / 6.f, c16 = 1.f / 6.f, c56 = 5.f / 6.f;
   const float c1312 = 13.f / 12.f, c136 = 13.f / 6.f;
   float D[6];
 #pragma unroll
   for (int f = 0; f < 6; f++) D[f] = (a[f + 1] - a[f]) * inv;
-  const bool minus = u > 0.f;
   float v[5];
 #pragma unroll
   for (int q = 0; q < 5; q++) v[q] = minus ? D[q] : D[5 - q];
@@ -182,8 +182,7 @@ static __device__ __forceinline__ float adv_slots_f32(const float a[7], float u,
   const float is = __fdividef(1.f, n1 + n2 + n3);  // sum <= 3e31 < 2^126
   const float w1 = n1 * is, w2 = n2 * is, w3 = n3 * is;
   const float W = fmaf(w1, p1, fmaf(w2, p2, w3 * p3));
-  const float dmu = dt * mu;
-  const float yb = dmu * -u * inv;
+  const float yb = dt * mu * kap * inv;
   // beta_k yb = -2 yb w_k (p_k - W) / (S_k + eps), 1/(S_k + eps) = r / (q1 q2 q3) * q_j q_l
   const float k0 = -2.f * yb * __fdividef(r, q12 * q3);
   const float b1 = k0 * w1 * (p1 - W) * q23, b2 = k0 * w2 * (p2 - W) * q13, b3 = k0 * w3 * (p3 - W) * q12;
@@ -200,34 +199,31 @@ static __device__ __forceinline__ float adv_slots_f32(const float a[7], float u,
   const float de = (b1 + b2 + b3) * 2e-6f;
 #pragma unroll
   for (int q = 0; q < 5; q++) g[q] = (q == am) ? fmaf(de, v[q], g[q]) : g[q];
-  // spatial_derivatives3d.f.in:2756-2812: no derivative where |u| < zero_tol
-  const bool off = fabsf(u) < 1e-11f;
 #pragma unroll
   for (int k = 0; k < 6; k++) {
     const float lo = (k < 5) ? g[k] : 0.f, hi = (k > 0) ? g[5 - k] : 0.f;
-    G[k] = off ? 0.f : (minus ? lo : hi);
+    G[k] = minus ? lo : hi;
   }
-  return off ? 0.f : dmu * -W;
+  return W;
 }
 
+// Face adjoints G[m] (faces c-2+m, scaled by dt) of one cell along one axis
+// for the linearisation coefficient kap = dL/dW of the WENO5 value W on side
+// `minus` (faces c-2..c+2) or plus (faces c-1..c+3); a[0..6] = s(c-3 .. c+3)
+// along the axis, mu the adjoint weight of the cell, inv = 1/dx_d.  Returns W.
 template <class R, bool EXACT>
-__device__ __forceinline__ R adv_slots(const R a[7], R u, R mu, R dt, R inv, R G[6]) {
+__device__ __forceinline__ R lin_slots(const R a[7], R kap, bool minus, R mu, R dt, R inv, R G[6]) {
   if constexpr (!EXACT && sizeof(R) == 4) {
-    return adv_slots_f32(a, u, mu, dt, inv, G);
+    return lin_slots_f32(a, kap, minus, mu, dt, inv, G);
   } else {
-#pragma unroll
-    for (int m = 0; m < 6; m++) G[m] = R(0);
-    // spatial_derivatives3d.f.in:2756-2812: no derivative where |u| < zero_tol
-    if (fabs(u) < R(Consts<double>::zero_tol)) return R(0);
     R D[6];  // D(c+f) for f = -2..3
 #pragma unroll
     for (int f = 0; f < 6; f++) D[f] = (a[f + 1] - a[f]) * inv;
-    const bool minus = u > R(0);
     R v[5], dv[5];
 #pragma unroll
     for (int q = 0; q < 5; q++) v[q] = minus ? D[q] : D[5 - q];
     const R W = weno5_adj<R, EXACT>(v, dv);
-    const R ybar = dt * mu * (-u) * inv;
+    const R ybar = dt * mu * kap * inv;
     // minus: v_q on face c-2+q (slot q); plus: v_q on face c+3-q (slot 5-q)
 #pragma unroll
     for (int m = 0; m < 6; m++) {
@@ -235,7 +231,35 @@ __device__ __forceinline__ R adv_slots(const R a[7], R u, R mu, R dt, R inv, R G
       const R hi = (m > 0) ? dv[5 - m] : R(0);
       G[m] = ybar * (minus ? lo : hi);
     }
-    return dt * mu * (-W);
+    return W;
+  }
+}
+
+// Linearisation coefficient of one cell along one axis.
+//   ADJ_ADV (advection, L = -sum_d u_d W_d): kap = -u_d, side from the sign of
+//     u_d, none where |u_d| < zero_tol (spatial_derivatives3d.f.in:2756-2812);
+//     the velocity adjoint of the cell is dt mu (-W).
+//   ADJ_LIN: kap and side precomputed per cell (side bits 2d..2d+1: 0 none,
+//     1 plus, 2 minus).
+enum { ADJ_ADV = 0, ADJ_LIN = 1 };
+
+template <class R>
+struct Coef {
+  R k;
+  unsigned char side;
+};
+
+template <class R, bool EXACT, int MODE>
+__device__ __forceinline__ R coef_slots(const R a[7], Coef<R> cf, int d, R mu, R dt, R inv, R G[6]) {
+  if constexpr (MODE == ADJ_ADV) {
+    const R u = cf.k;
+    const bool on = !(fabs(u) < R(Consts<double>::zero_tol));
+    const R W = lin_slots<R, EXACT>(a, on ? -u : R(0), u > R(0), mu, dt, inv, G);
+    return on ? dt * mu * (-W) : R(0);
+  } else {
+    const int sb = (cf.side >> (2 * d)) & 3;
+    lin_slots<R, EXACT>(a, sb ? cf.k : R(0), sb == 2, mu, dt, inv, G);
+    return R(0);
   }
 }
 
@@ -246,14 +270,30 @@ struct AdjStageArgs {
   const R *M;         // adjoint input; mu = mscale * M
   const R *P, *Q;     // optional pointwise terms pscale * P + qscale * Q
   R *out;             // mu + dt L_s^T mu (+ P, Q terms), interior cells
-  const R *vel[3];
-  R *gvel[3];         // velocity adjoint accumulators (nullptr: not wanted)
+  const R *vel[3];     // ADJ_ADV: velocity components
+  R *gvel[3];         // ADJ_ADV: velocity adjoint accumulators (nullptr: not wanted)
+  const R *kap[3];    // ADJ_LIN: dL/dW per axis
+  const unsigned char *side;  // ADJ_LIN: side bits per cell
   R mscale, pscale, qscale;
   R dt;
   R inv[3];
   int zchunk;         // planes per warp along z (k_adj_xz)
   int ychunk;         // rows per thread along y (k_adj_y)
 };
+
+// coefficient of axis d at padded index c
+template <class R, int MODE>
+__device__ __forceinline__ Coef<R> load_coef(const AdjStageArgs<R> &a, int d, long long c) {
+  Coef<R> cf;
+  if constexpr (MODE == ADJ_ADV) {
+    cf.k = a.vel[d][c];
+    cf.side = 0;
+  } else {
+    cf.k = a.kap[d][c];
+    cf.side = a.side[c];
+  }
+  return cf;
+}
 
 // One step of the face-sum ring of a marching thread: add the slots of the
 // cell `lead` (3 ahead of the output cell), and return A(lead - 3) =
@@ -280,7 +320,7 @@ __device__ __forceinline__ long long plane_add(long long o, int p, int c, int n,
   return r;
 }
 
-template <class R, bool EXACT>
+template <class R, bool EXACT, int MODE>
 __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? 3 : 1) k_adj_xz(AdjStageArgs<R> a) {
   const Layout &L = a.L;
   const int lane = threadIdx.x;
@@ -300,10 +340,9 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? 3 : 1) k_adj_xz(A
   int xo[7];
 #pragma unroll
   for (int q = 0; q < 7; q++) xo[q] = wrapi(x - 3 + q, L.nx) - xw;
-  const R *s = a.s + row + xw;  // this lane's column; plane offsets are added
-  const R *M = a.M + row + xw;
-  const R *vx = a.vel[0] + row + xw;
-  const R *vz = a.vel[2] + row + xw;
+  const long long col = row + xw;  // this lane's column; plane offsets are added
+  const R *s = a.s + col;
+  const R *M = a.M + col;
   // plane cursor: offset of plane kk (wrapped) and its index
   int zk = wrapi(z0 - 3, nz);
   long long ok = pz * (long long)(zk + fused::GZ);
@@ -317,13 +356,15 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? 3 : 1) k_adj_xz(A
   }
 #pragma unroll
   for (int q = 0; q < 4; q++) mring[q] = R(0);
-  R cs = s[plane_add(ok, zk, 3, nz, pz)], cm = M[ok], cv = vz[ok];
-  R xsn[7], xvn;
+  R cs = s[plane_add(ok, zk, 3, nz, pz)], cm = M[ok];
+  Coef<R> cv = load_coef<R, MODE>(a, 2, col + ok);
+  R xsn[7];
+  Coef<R> xvn;
   {
     const long long o = plane_add(ok, zk, 3, nz, pz);  // plane z0
 #pragma unroll
     for (int q = 0; q < 7; q++) xsn[q] = s[o + xo[q]];
-    xvn = vx[o];
+    xvn = load_coef<R, MODE>(a, 0, col + o);
   }
 
   for (int kk = z0 - 3; kk < zend + 3; kk++) {
@@ -333,7 +374,7 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? 3 : 1) k_adj_xz(A
 #pragma unroll
     for (int q = 0; q < 3; q++) mring[q] = mring[q + 1];
     mring[3] = msc * cm;
-    const R uz = cv;
+    const Coef<R> uz = cv;
     const long long okk = ok;  // plane kk
     const int zkk = zk;
     // advance the cursor to plane kk + 1 and prefetch the next column values
@@ -342,11 +383,11 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? 3 : 1) k_adj_xz(A
     if (kk + 1 < zend + 3) {
       cs = s[plane_add(ok, zk, 3, nz, pz)];
       cm = M[ok];
-      cv = vz[ok];
+      cv = load_coef<R, MODE>(a, 2, col + ok);
     }
     R G[6];
-    const R gz = adv_slots<R, EXACT>(win, uz, mring[3], dt, iz, G);
-    if (a.gvel[2] && own && kk >= z0 && kk < zend) a.gvel[2][row + xw + okk] += gz;
+    const R gz = coef_slots<R, EXACT, MODE>(win, uz, 2, mring[3], dt, iz, G);
+    if (MODE == ADJ_ADV && a.gvel[2] && own && kk >= z0 && kk < zend) a.gvel[2][col + okk] += gz;
     const R Az = ring_step<R>(F, prevV, G);
     const int k = kk - 3;
     if (k < z0) continue;
@@ -355,17 +396,17 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? 3 : 1) k_adj_xz(A
     R w7[7];
 #pragma unroll
     for (int q = 0; q < 7; q++) w7[q] = xsn[q];
-    const R ux = xvn;
+    const Coef<R> ux = xvn;
     const long long ob = plane_add(okk, zkk, -3, nz, pz);  // plane k
     if (k + 1 < zend) {
       const long long o = plane_add(okk, zkk, -2, nz, pz);
 #pragma unroll
       for (int q = 0; q < 7; q++) xsn[q] = s[o + xo[q]];
-      xvn = vx[o];
+      xvn = load_coef<R, MODE>(a, 0, col + o);
     }
-    const R gx = adv_slots<R, EXACT>(w7, ux, mring[0], dt, ix, G);
-    const long long c = row + xw + ob;
-    if (a.gvel[0] && own) a.gvel[0][c] += gx;
+    const R gx = coef_slots<R, EXACT, MODE>(w7, ux, 0, mring[0], dt, ix, G);
+    const long long c = col + ob;
+    if (MODE == ADJ_ADV && a.gvel[0] && own) a.gvel[0][c] += gx;
     // Vbar(x) = sum_m G_m(x + 2 - m): lane + 2 - m; valid for lanes 3..29
     R V = R(0);
 #pragma unroll
@@ -379,7 +420,7 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? 3 : 1) k_adj_xz(A
   }
 }
 
-template <class R, bool EXACT>
+template <class R, bool EXACT, int MODE>
 __global__ void __launch_bounds__(32 * kRows) k_adj_y(AdjStageArgs<R> a) {
   const Layout &L = a.L;
   const int i = blockIdx.x * 32 + threadIdx.x;
@@ -391,7 +432,7 @@ __global__ void __launch_bounds__(32 * kRows) k_adj_y(AdjStageArgs<R> a) {
   const R dt = a.dt, msc = a.mscale, iy = a.inv[1];
   const long long py = L.py;
   const long long base = (long long)(i + fused::GX) + L.pz * (long long)(k + fused::GZ);
-  const R *s = a.s + base, *M = a.M + base, *vy = a.vel[1] + base;
+  const R *s = a.s + base, *M = a.M + base;
   int yk = wrapi(y0 - 3, ny);
   long long ok = py * (long long)(yk + fused::GY);
 
@@ -404,7 +445,8 @@ __global__ void __launch_bounds__(32 * kRows) k_adj_y(AdjStageArgs<R> a) {
   }
 #pragma unroll
   for (int q = 0; q < 4; q++) mring[q] = R(0);
-  R cs = s[plane_add(ok, yk, 3, ny, py)], cm = M[ok], cv = vy[ok];
+  R cs = s[plane_add(ok, yk, 3, ny, py)], cm = M[ok];
+  Coef<R> cv = load_coef<R, MODE>(a, 1, base + ok);
   for (int jj = y0 - 3; jj < yend + 3; jj++) {
 #pragma unroll
     for (int q = 0; q < 6; q++) win[q] = win[q + 1];
@@ -412,7 +454,7 @@ __global__ void __launch_bounds__(32 * kRows) k_adj_y(AdjStageArgs<R> a) {
 #pragma unroll
     for (int q = 0; q < 3; q++) mring[q] = mring[q + 1];
     mring[3] = msc * cm;
-    const R uy = cv;
+    const Coef<R> uy = cv;
     const long long ojj = ok;
     const int yjj = yk;
     ok = plane_add(ok, yk, 1, ny, py);
@@ -420,15 +462,92 @@ __global__ void __launch_bounds__(32 * kRows) k_adj_y(AdjStageArgs<R> a) {
     if (jj + 1 < yend + 3) {
       cs = s[plane_add(ok, yk, 3, ny, py)];
       cm = M[ok];
-      cv = vy[ok];
+      cv = load_coef<R, MODE>(a, 1, base + ok);
     }
     R G[6];
-    const R gy = adv_slots<R, EXACT>(win, uy, mring[3], dt, iy, G);
-    if (a.gvel[1] && jj >= y0 && jj < yend) a.gvel[1][base + ojj] += gy;
+    const R gy = coef_slots<R, EXACT, MODE>(win, uy, 1, mring[3], dt, iy, G);
+    if (MODE == ADJ_ADV && a.gvel[1] && jj >= y0 && jj < yend) a.gvel[1][base + ojj] += gy;
     const R Ay = ring_step<R>(F, prevV, G);
     if (jj - 3 < y0) continue;
     a.out[base + plane_add(ojj, yjj, -3, ny, py)] += Ay;
   }
+}
+
+// Linearisation of the reinitialization RHS (phi0 sign form, use_phi0_for_sgn
+// = 1; reinitialization3d.f.in:217-256) at state s, one thread per interior
+// cell.  L = sgn (1 - |grad s|_G), sgn = phi0 / sqrt(phi0^2 + dx^2),
+// |grad s|_G^2 = sum_d max(u_d, w_d)^2 with u, w from the WENO5 plus/minus
+// values.  Per axis the derivative follows the branch the forward's maxima
+// take to exactly one of the two WENO5 values (or none): kap_d = dL/dW and
+// the side bits.  The sign source's sensitivity dL/dphi0 = (1 - |grad s|_G)
+// dx^2 / (phi0^2 + dx^2)^(3/2) is accumulated (times dt mu) into gp0.
+template <class R, bool EXACT>
+__global__ void __launch_bounds__(256) k_reinit_lin(const R *s, const R *phi0, const R *M, R mscale, R dt,
+                                                    R dx_sq, R ix, R iy, R iz, Layout L, R *kx, R *ky, R *kz,
+                                                    unsigned char *side, R *gp0) {
+  const int i = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= L.nx || j >= L.ny || k >= L.nz) return;
+  const long long c = L.idx(i, j, k);
+  const long long st[3] = {1, L.py, L.pz};
+  const R inv[3] = {ix, iy, iz};
+  const R pc = phi0[c];
+  R kap[3] = {R(0), R(0), R(0)};
+  unsigned char sb = 0;
+  const bool live = EXACT ? (fabs(pc) >= Consts<double>::zero_tol) : !(fabs(pc) < R(1e-11));
+  if (live) {
+    R star[3], sel[3];
+    int which[3];
+    for (int d = 0; d < 3; d++) {
+      R v[6];  // scaled D1(c-2 .. c+3)
+#pragma unroll
+      for (int f = -2; f <= 3; f++) v[f + 2] = (s[c + f * st[d]] - s[c + (f - 1) * st[d]]) * inv[d];
+      const R gp = fused::weno<R, EXACT>(v[5], v[4], v[3], v[2], v[1]);
+      const R gm = fused::weno<R, EXACT>(v[0], v[1], v[2], v[3], v[4]);
+      R u, w, du, dw;
+      if (pc > R(0)) {
+        u = rmax(-gp, R(0)); du = (-gp > R(0)) ? R(-1) : R(0);
+        w = rmax(gm, R(0));  dw = (gm > R(0)) ? R(1) : R(0);
+      } else {
+        u = rmax(gp, R(0));  du = (gp > R(0)) ? R(1) : R(0);
+        w = rmax(-gm, R(0)); dw = (-gm > R(0)) ? R(-1) : R(0);
+      }
+      if (u > w) {
+        star[d] = u; sel[d] = du; which[d] = du != R(0) ? 1 : 0;
+      } else {
+        star[d] = w; sel[d] = dw; which[d] = dw != R(0) ? 2 : 0;
+      }
+    }
+    const R n2 = star[0] * star[0] + star[1] * star[1] + star[2] * star[2];
+    const R nrm = sqrt(n2);
+    const R den = pc * pc + dx_sq;
+    const R sq = sqrt(den);
+    const R sgn = pc / sq;
+    const R mu = mscale * M[c];
+    gp0[c] += dt * mu * (R(1) - nrm) * dx_sq / (den * sq);
+    if (nrm > R(0)) {
+      for (int d = 0; d < 3; d++) {
+        if (!which[d]) continue;
+        kap[d] = -sgn * star[d] / nrm * sel[d];
+        sb |= (unsigned char)(which[d] << (2 * d));
+      }
+    }
+  }
+  kx[c] = kap[0];
+  ky[c] = kap[1];
+  kz[c] = kap[2];
+  side[c] = sb;
+}
+
+template <class R>
+__global__ void k_add_interior(R *dst, const R *src, Layout L) {
+  const int i = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= L.nx || j >= L.ny || k >= L.nz) return;
+  const long long c = L.idx(i, j, k);
+  dst[c] += src[c];
 }
 
 // Objective terms per interior cell (in FP64): h = H(phi_T) - H(phi_target),

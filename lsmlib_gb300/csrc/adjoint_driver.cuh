@@ -1,10 +1,13 @@
-// Host driver of the advection adjoint: forward sweep with checkpoints,
-// objective, then per checkpoint segment a forward recomputation that keeps
-// every stage state and the reverse sweep over it.
+// Host driver of the adjoints (periodic advection; periodic reinitialization
+// in the phi0 sign form): forward sweep with checkpoints, the objective or the
+// caller's dJ/dphi_T, then per checkpoint segment a forward recomputation that
+// keeps every stage state and the reverse sweep over it.
 //
 // Memory (padded layout, E elements per field): 3 forward fields, one
 // checkpoint per `ckpt` steps, 3*ckpt - 1 segment stage states, 3 adjoint
-// fields, 3 velocity fields, 3 velocity accumulators and the target.
+// fields; advection: 3 velocity fields and 3 velocity accumulators;
+// reinitialization: 3 linearisation coefficients, side bits and the sign
+// source's accumulator.
 #pragma once
 
 #include <vector>
@@ -15,9 +18,25 @@
 namespace lsmgpu {
 namespace adj {
 
+enum { ADJ_MODE_ADVECT = 0, ADJ_MODE_REINIT = 1 };
+
 struct AdjSpec {
+  int mode;          // ADJ_MODE_ADVECT / ADJ_MODE_REINIT (phi0 sign form)
   int n_steps, ckpt;
   double dt, dx, dy, dz, eps;
+};
+
+// Arrays of one call (host or device; any output may be null)
+template <class R>
+struct AdjIO {
+  const R *phi;          // initial state over gb (fill-box values used)
+  const R *vel[3];       // advection velocity over vb
+  const R *tgt;          // objective target over gb (objective form)
+  const R *grad_out;     // dJ/dphi_T over gb (vector-Jacobian form)
+  double *J;             // objective value (objective form)
+  R *phi_out;            // final state over gb
+  R *gphi;               // dJ/dphi over gb
+  R *gvel[3];            // dJ/dvel over vb
 };
 
 // march length per thread: enough threads for about 2048 per SM, and at
@@ -34,68 +53,75 @@ inline int pick_chunk(int n_march, long long threads_per_chunk) {
   return c;
 }
 
-// one adjoint stage: x and z faces (writes out), then y faces (adds to out)
-template <class R, bool EXACT>
+// one reverse stage: x and z faces (writes out), then y faces (adds to out)
+template <class R, bool EXACT, int MODE>
 void launch_adj_stage(const AdjStageArgs<R> &a) {
   const Layout &L = a.L;
   dim3 blk(32, kRows);
   dim3 g1((unsigned)((L.nx + kSeg - 1) / kSeg), (unsigned)((L.ny + kRows - 1) / kRows),
           (unsigned)((L.nz + a.zchunk - 1) / a.zchunk));
-  k_adj_xz<R, EXACT><<<g1, blk, 0, stream()>>>(a);
+  k_adj_xz<R, EXACT, MODE><<<g1, blk, 0, stream()>>>(a);
   note_launch();
   dim3 g2((unsigned)((L.nx + 31) / 32), (unsigned)((L.nz + kRows - 1) / kRows),
           (unsigned)((L.ny + a.ychunk - 1) / a.ychunk));
-  k_adj_y<R, EXACT><<<g2, blk, 0, stream()>>>(a);
+  k_adj_y<R, EXACT, MODE><<<g2, blk, 0, stream()>>>(a);
   note_launch();
 }
 
 template <class R, bool EXACT>
-int run(const char *name, const R *phi_user, const Box &gb, const Box &fb, const R *const vel_user[3],
-        const Box &vb, const R *tgt_user, const AdjSpec &sp, double *J_user, R *gphi_user,
-        R *const gvel_user[3]) {
+int run(const char *name, const Box &gb, const Box &fb, const Box &vb, const AdjSpec &sp, const AdjIO<R> &io) {
   using fused::StageArgs;
+  const bool advect = sp.mode == ADJ_MODE_ADVECT;
   Call call(name);
   if (!gb.contains(fb, 3, 3, 3)) call.fail("ghost box must hold 3 ghost cells around the fill box");
-  if (!vb.contains(fb, 0, 0, 0)) call.fail("velocity ghost box does not cover the fill box");
+  if (advect && !vb.contains(fb, 0, 0, 0)) call.fail("velocity ghost box does not cover the fill box");
   const int nx = (int)fb.n(0), ny = (int)fb.n(1), nz = (int)fb.n(2);
   if (fb.empty() || nx < 6 || ny < 6 || nz < 6) call.fail("fill box must be at least 6 cells per axis");
   if (!call.ok()) return LSMGPU_ERR_BOUNDS;
-  const int ngv = (gvel_user[0] != nullptr) + (gvel_user[1] != nullptr) + (gvel_user[2] != nullptr);
-  if (sp.n_steps < 0 || sp.ckpt < 1 || !(sp.eps > 0.0) || (ngv != 0 && ngv != 3) ||
-      (ngv == 3 && !gphi_user)) {
+  const int ngv = advect ? (io.gvel[0] != nullptr) + (io.gvel[1] != nullptr) + (io.gvel[2] != nullptr) : 0;
+  const bool objective = io.tgt != nullptr;
+  if (sp.n_steps < 0 || sp.ckpt < 1 || (objective && !(sp.eps > 0.0)) || (ngv != 0 && ngv != 3) ||
+      (ngv == 3 && !io.gphi) || (io.gphi && !objective && !io.grad_out)) {
     set_error(LSMGPU_ERR_ARGUMENT,
-              "%s: need n_steps >= 0, checkpoint_every >= 1, heaviside_eps > 0, and velocity gradients "
-              "either all three (with grad_phi) or none",
+              "%s: need n_steps >= 0, checkpoint_every >= 1, heaviside_eps > 0, a gradient source, and "
+              "velocity gradients either all three (with grad_phi) or none",
               name);
     return LSMGPU_ERR_ARGUMENT;
   }
-  const bool want_grad = gphi_user != nullptr, want_gvel = ngv == 3;
+  const bool want_grad = io.gphi != nullptr, want_gvel = ngv == 3;
 
-  const R *phi_d = call.in(phi_user, gb.size());
-  const R *tgt_d = call.in(tgt_user, gb.size());
-  const R *vel_d[3];
-  for (int d = 0; d < 3; d++) vel_d[d] = call.in(vel_user[d], vb.size());
-  R *gphi_d = want_grad ? call.out(gphi_user, gb.size()) : nullptr;
+  const R *phi_d = call.in(io.phi, gb.size());
+  const R *tgt_d = objective ? call.in(io.tgt, gb.size()) : nullptr;
+  const R *gout_d = (!objective && want_grad) ? call.in(io.grad_out, gb.size()) : nullptr;
+  const R *vel_d[3] = {nullptr, nullptr, nullptr};
+  if (advect)
+    for (int d = 0; d < 3; d++) vel_d[d] = call.in(io.vel[d], vb.size());
+  R *gphi_d = want_grad ? call.out(io.gphi, gb.size()) : nullptr;
   R *gvel_d[3] = {nullptr, nullptr, nullptr};
   if (want_gvel)
-    for (int d = 0; d < 3; d++) gvel_d[d] = call.out(gvel_user[d], vb.size());
-  double *J_d = J_user ? call.scalar_out(J_user) : nullptr;
+    for (int d = 0; d < 3; d++) gvel_d[d] = call.out(io.gvel[d], vb.size());
+  R *phi_out_d = io.phi_out ? call.inout(io.phi_out, gb.size()) : nullptr;
+  double *J_d = (objective && io.J) ? call.scalar_out(io.J) : nullptr;
 
   const Layout L = fused::make_layout(nx, ny, nz);
   const long long ne = L.elems();
   const int K = sp.ckpt;
   const int nck = sp.n_steps > 0 ? (sp.n_steps + K - 1) / K : 1;
-  R *X = call.temp<R>(ne), *T1 = call.temp<R>(ne), *T2 = call.temp<R>(ne), *TG = call.temp<R>(ne);
-  R *V[3];
-  for (int d = 0; d < 3; d++) V[d] = call.temp<R>(ne);
+  R *X = call.temp<R>(ne), *T1 = call.temp<R>(ne), *T2 = call.temp<R>(ne);
+  R *TG = objective ? call.temp<R>(ne) : nullptr;
+  R *V[3] = {nullptr, nullptr, nullptr};
+  if (advect)
+    for (int d = 0; d < 3; d++) V[d] = call.temp<R>(ne);
   std::vector<R *> ck(nck);
   for (int c = 0; c < nck; c++) ck[c] = call.temp<R>(ne);
   const long long ncell = (long long)nx * ny * nz;
   const int nblk = (int)((ncell + kObjThreads - 1) / kObjThreads);
-  double *partial = call.temp<double>(nblk);
-  double *Jdev = call.temp<double>(1);
+  double *partial = objective ? call.temp<double>(nblk) : nullptr;
+  double *Jdev = objective ? call.temp<double>(1) : nullptr;
   int *err = call.temp<int>(1);
   R *LA = nullptr, *LB = nullptr, *LC = nullptr, *GV[3] = {nullptr, nullptr, nullptr};
+  R *KAP[3] = {nullptr, nullptr, nullptr}, *GP0 = nullptr;
+  unsigned char *SIDE = nullptr;
   std::vector<R *> U;
   if (want_grad) {
     LA = call.temp<R>(ne);
@@ -103,6 +129,11 @@ int run(const char *name, const R *phi_user, const Box &gb, const Box &fb, const
     LC = call.temp<R>(ne);
     if (want_gvel)
       for (int d = 0; d < 3; d++) GV[d] = call.temp<R>(ne);
+    if (!advect) {
+      for (int d = 0; d < 3; d++) KAP[d] = call.temp<R>(ne);
+      SIDE = call.temp<unsigned char>(ne);
+      GP0 = call.temp<R>(ne);
+    }
     U.assign(3 * K, nullptr);
     for (int m = 1; m < 3 * K; m++) U[m] = call.temp<R>(ne);
   }
@@ -110,16 +141,17 @@ int run(const char *name, const R *phi_user, const Box &gb, const Box &fb, const
 
   cudaStream_t s = stream();
   cudaMemsetAsync(err, 0, sizeof(int), s);
+  dim3 pblk(32, 4, 2);
+  dim3 pgrd((unsigned)((nx + 7 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));
+  LSMGPU_LAUNCH(fused::k_pack<R>, pgrd, pblk, 0, ck[0], L, view(phi_d, gb), gb, fb.lo[0], fb.lo[1], fb.lo[2]);
+  if (objective)
+    LSMGPU_LAUNCH(fused::k_pack<R>, pgrd, pblk, 0, TG, L, view(tgt_d, gb), gb, fb.lo[0], fb.lo[1], fb.lo[2]);
+  for (int d = 0; d < 3 && advect; d++)
+    LSMGPU_LAUNCH(fused::k_pack<R>, pgrd, pblk, 0, V[d], L, view(vel_d[d], vb), vb, fb.lo[0], fb.lo[1], fb.lo[2]);
   {
-    dim3 blk(32, 4, 2);
-    dim3 grd((unsigned)((nx + 7 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));
-    LSMGPU_LAUNCH(fused::k_pack<R>, grd, blk, 0, ck[0], L, view(phi_d, gb), gb, fb.lo[0], fb.lo[1], fb.lo[2]);
-    LSMGPU_LAUNCH(fused::k_pack<R>, grd, blk, 0, TG, L, view(tgt_d, gb), gb, fb.lo[0], fb.lo[1], fb.lo[2]);
-    for (int d = 0; d < 3; d++)
-      LSMGPU_LAUNCH(fused::k_pack<R>, grd, blk, 0, V[d], L, view(vel_d[d], vb), vb, fb.lo[0], fb.lo[1], fb.lo[2]);
     dim3 gf((unsigned)((nx + 6 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));
     // the initial state is the periodic extension of the fill-box values
-    LSMGPU_LAUNCH(k_fill_periodic<R>, gf, blk, 0, ck[0], L);
+    LSMGPU_LAUNCH(k_fill_periodic<R>, gf, pblk, 0, ck[0], L);
   }
   cudaMemcpyAsync(X, ck[0], (size_t)ne * sizeof(R), cudaMemcpyDeviceToDevice, s);
 
@@ -141,20 +173,27 @@ int run(const char *name, const R *phi_user, const Box &gb, const Box &fb, const
   fa.inv[1] = R(1.0) / (R)sp.dy;
   fa.inv[2] = R(1.0) / (R)sp.dz;
   fa.dt = (R)sp.dt;
+  {
+    const R m = rmax(rmax((R)sp.dx, (R)sp.dy), (R)sp.dz);
+    fa.dx_sq = m * m;
+  }
+  fa.phi0 = ck[0];  // reinitialization sign source: the initial state
+  fa.use0 = 1;
   fa.periodic = 1;
   fa.err = err;
+  auto stage = [&](const CUtensorMap &t, R *out, int st) {
+    fa.stage = st;
+    fa.out = out;
+    if (advect) fused::launch_stage<R, fused::ADV_FIELD, EXACT>(t, fa);
+    else fused::launch_stage<R, fused::REINIT, EXACT>(t, fa);
+  };
   // one forward TVD-RK3 step: src -> o1 -> o2 -> dst (dst may be src)
   auto fwd_step = [&](const CUtensorMap &t_src, R *src, const CUtensorMap &t_o1, R *o1,
                       const CUtensorMap &t_o2, R *o2, R *dst) {
     fa.phi_n = src;
-    fa.stage = 1; fa.out = o1;
-    fused::launch_stage<R, fused::ADV_FIELD, EXACT>(t_src, fa);
-    fa.stage = 2; fa.out = o2;
-    fused::launch_stage<R, fused::ADV_FIELD, EXACT>(t_o1, fa);
-    if (dst) {
-      fa.stage = 3; fa.out = dst;
-      fused::launch_stage<R, fused::ADV_FIELD, EXACT>(t_o2, fa);
-    }
+    stage(t_src, o1, 1);
+    stage(t_o1, o2, 2);
+    if (dst) stage(t_o2, dst, 3);
   };
 
   // ---- forward sweep with checkpoints ----------------------------------------
@@ -163,14 +202,26 @@ int run(const char *name, const R *phi_user, const Box &gb, const Box &fb, const
     if ((n + 1) % K == 0 && (n + 1) < sp.n_steps)
       cudaMemcpyAsync(ck[(n + 1) / K], X, (size_t)ne * sizeof(R), cudaMemcpyDeviceToDevice, s);
   }
-  const double vol = sp.dx * sp.dy * sp.dz;
-  LSMGPU_LAUNCH(k_objective<R>, dim3((unsigned)nblk), dim3(kObjThreads), 0, X, TG, L, sp.eps, vol, LA, partial);
-  LSMGPU_LAUNCH(k_objective_fold, dim3(1), dim3(1024), 0, partial, nblk, vol, J_d ? J_d : Jdev);
+  if (phi_out_d) {
+    dim3 blk(32, 4, 2);
+    dim3 grd((unsigned)((nx + 6 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));
+    LSMGPU_LAUNCH(fused::k_unpack<R>, grd, blk, 0, view(phi_out_d, gb), gb, X, L, fb.lo[0], fb.lo[1], fb.lo[2]);
+  }
+  if (objective) {
+    const double vol = sp.dx * sp.dy * sp.dz;
+    LSMGPU_LAUNCH(k_objective<R>, dim3((unsigned)nblk), dim3(kObjThreads), 0, X, TG, L, sp.eps, vol, LA,
+                  partial);
+    LSMGPU_LAUNCH(k_objective_fold, dim3(1), dim3(1024), 0, partial, nblk, vol, J_d ? J_d : Jdev);
+  } else if (want_grad) {
+    // dJ/dphi_T given by the caller
+    LSMGPU_LAUNCH(fused::k_pack<R>, pgrd, pblk, 0, LA, L, view(gout_d, gb), gb, fb.lo[0], fb.lo[1], fb.lo[2]);
+  }
 
   // ---- reverse sweep ------------------------------------------------------------
   if (want_grad) {
     if (want_gvel)
       for (int d = 0; d < 3; d++) cudaMemsetAsync(GV[d], 0, (size_t)ne * sizeof(R), s);
+    if (GP0) cudaMemsetAsync(GP0, 0, (size_t)ne * sizeof(R), s);
     std::vector<CUtensorMap> tU(3 * K);
     for (int m = 1; m < 3 * K; m++)
       if (!tmap(U[m], &tU[m])) {
@@ -182,11 +233,24 @@ int run(const char *name, const R *phi_user, const Box &gb, const Box &fb, const
     for (int d = 0; d < 3; d++) {
       aa.vel[d] = V[d];
       aa.gvel[d] = GV[d];
+      aa.kap[d] = KAP[d];
     }
+    aa.side = SIDE;
     aa.dt = (R)sp.dt;
     aa.inv[0] = fa.inv[0]; aa.inv[1] = fa.inv[1]; aa.inv[2] = fa.inv[2];
     aa.zchunk = pick_chunk(nz, 32LL * ((nx + kSeg - 1) / kSeg) * ny);
     aa.ychunk = pick_chunk(ny, (long long)nx * nz);
+    const dim3 cgrid((unsigned)((nx + 31) / 32), (unsigned)((ny + 7) / 8), (unsigned)nz), cblk(32, 8);
+    // one reverse stage at forward state `st`
+    auto rstage = [&]() {
+      if (advect) {
+        launch_adj_stage<R, EXACT, ADJ_ADV>(aa);
+      } else {
+        LSMGPU_LAUNCH((k_reinit_lin<R, EXACT>), cgrid, cblk, 0, aa.s, (const R *)ck[0], aa.M, aa.mscale, aa.dt,
+                      fa.dx_sq, aa.inv[0], aa.inv[1], aa.inv[2], L, KAP[0], KAP[1], KAP[2], SIDE, GP0);
+        launch_adj_stage<R, EXACT, ADJ_LIN>(aa);
+      }
+    };
     for (int seg = nck - 1; seg >= 0 && sp.n_steps > 0; seg--) {
       const int s0 = seg * K, s1 = (s0 + K < sp.n_steps) ? s0 + K : sp.n_steps, ns = s1 - s0;
       U[0] = ck[seg];
@@ -200,14 +264,15 @@ int run(const char *name, const R *phi_user, const Box &gb, const Box &fb, const
       for (int m = ns - 1; m >= 0; m--) {
         aa.s = U[3 * m + 2]; aa.M = LA; aa.mscale = R(2.0 / 3.0);
         aa.P = nullptr; aa.Q = nullptr; aa.out = LB;
-        launch_adj_stage<R, EXACT>(aa);
+        rstage();
         aa.s = U[3 * m + 1]; aa.M = LB; aa.mscale = R(0.25); aa.out = LC;
-        launch_adj_stage<R, EXACT>(aa);
+        rstage();
         aa.s = U[3 * m]; aa.M = LC; aa.mscale = R(1.0);
         aa.P = LA; aa.pscale = R(1.0 / 3.0); aa.Q = LB; aa.qscale = R(0.75); aa.out = LA;
-        launch_adj_stage<R, EXACT>(aa);
+        rstage();
       }
     }
+    if (GP0) LSMGPU_LAUNCH(k_add_interior<R>, cgrid, cblk, 0, LA, (const R *)GP0, L);
     Grid3 gg = cover(gb);
     LSMGPU_LAUNCH(k_unpack_interior<R>, gg.grid, gg.block, 0, view(gphi_d, gb), gb, LA, L, fb.lo[0], fb.lo[1],
                   fb.lo[2]);

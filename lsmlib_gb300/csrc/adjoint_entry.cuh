@@ -29,13 +29,68 @@ extern "C" int LSMGPU_ACAT(lsmgpu_advect_adjoint_weno5_tvdrk3_, LSMGPU_ADJ_SUFFI
     return LSMGPU_ERR_ARGUMENT;
   }
   adj::AdjSpec sp{};
+  sp.mode = adj::ADJ_MODE_ADVECT;
   sp.n_steps = n_steps;
   sp.ckpt = checkpoint_every;
   sp.dt = dt; sp.dx = dx; sp.dy = dy; sp.dz = dz;
   sp.eps = heaviside_eps;
-  const LSMGPU_ADJ_R *vel[3] = {vel_x, vel_y, vel_z};
-  LSMGPU_ADJ_R *gvel[3] = {grad_vel_x, grad_vel_y, grad_vel_z};
-  return adj::run<LSMGPU_ADJ_R, LSMGPU_ADJ_EXACT>("lsmgpu_advect_adjoint_weno5_tvdrk3", phi, adj_box6(gb),
-                                                  adj_box6(fb), vel, adj_box6(vel_gb), phi_target, sp, J,
-                                                  grad_phi, gvel);
+  adj::AdjIO<LSMGPU_ADJ_R> io{};
+  io.phi = phi;
+  io.vel[0] = vel_x; io.vel[1] = vel_y; io.vel[2] = vel_z;
+  io.tgt = phi_target;
+  io.J = J;
+  io.gphi = grad_phi;
+  io.gvel[0] = grad_vel_x; io.gvel[1] = grad_vel_y; io.gvel[2] = grad_vel_z;
+  return adj::run<LSMGPU_ADJ_R, LSMGPU_ADJ_EXACT>("lsmgpu_advect_adjoint_weno5_tvdrk3", adj_box6(gb), adj_box6(fb),
+                                                  adj_box6(vel_gb), sp, io);
+}
+
+extern "C" int LSMGPU_ACAT(lsmgpu_advect_vjp_weno5_tvdrk3_, LSMGPU_ADJ_SUFFIX)(
+    const LSMGPU_ADJ_R *phi, const int *gb, const int *fb, const LSMGPU_ADJ_R *vel_x,
+    const LSMGPU_ADJ_R *vel_y, const LSMGPU_ADJ_R *vel_z, const int *vel_gb, LSMGPU_ADJ_R dx, LSMGPU_ADJ_R dy,
+    LSMGPU_ADJ_R dz, LSMGPU_ADJ_R dt, int n_steps, int checkpoint_every, const LSMGPU_ADJ_R *grad_out,
+    LSMGPU_ADJ_R *phi_out, LSMGPU_ADJ_R *grad_phi, LSMGPU_ADJ_R *grad_vel_x, LSMGPU_ADJ_R *grad_vel_y,
+    LSMGPU_ADJ_R *grad_vel_z) {
+  clear_error();
+  if (!phi || !gb || !fb || !vel_x || !vel_y || !vel_z || !vel_gb || (grad_phi && !grad_out)) {
+    set_error(LSMGPU_ERR_ARGUMENT, "lsmgpu_advect_vjp_weno5_tvdrk3: null argument");
+    return LSMGPU_ERR_ARGUMENT;
+  }
+  adj::AdjSpec sp{};
+  sp.mode = adj::ADJ_MODE_ADVECT;
+  sp.n_steps = n_steps;
+  sp.ckpt = checkpoint_every;
+  sp.dt = dt; sp.dx = dx; sp.dy = dy; sp.dz = dz;
+  adj::AdjIO<LSMGPU_ADJ_R> io{};
+  io.phi = phi;
+  io.vel[0] = vel_x; io.vel[1] = vel_y; io.vel[2] = vel_z;
+  io.grad_out = grad_out;
+  io.phi_out = phi_out;
+  io.gphi = grad_phi;
+  io.gvel[0] = grad_vel_x; io.gvel[1] = grad_vel_y; io.gvel[2] = grad_vel_z;
+  return adj::run<LSMGPU_ADJ_R, LSMGPU_ADJ_EXACT>("lsmgpu_advect_vjp_weno5_tvdrk3", adj_box6(gb), adj_box6(fb),
+                                                  adj_box6(vel_gb), sp, io);
+}
+
+extern "C" int LSMGPU_ACAT(lsmgpu_reinit_vjp_weno5_tvdrk3_, LSMGPU_ADJ_SUFFIX)(
+    const LSMGPU_ADJ_R *phi, const int *gb, const int *fb, LSMGPU_ADJ_R dx, LSMGPU_ADJ_R dy, LSMGPU_ADJ_R dz,
+    LSMGPU_ADJ_R dtau, int n_iter, int checkpoint_every, const LSMGPU_ADJ_R *grad_out, LSMGPU_ADJ_R *phi_out,
+    LSMGPU_ADJ_R *grad_phi) {
+  clear_error();
+  if (!phi || !gb || !fb || (grad_phi && !grad_out)) {
+    set_error(LSMGPU_ERR_ARGUMENT, "lsmgpu_reinit_vjp_weno5_tvdrk3: null argument");
+    return LSMGPU_ERR_ARGUMENT;
+  }
+  adj::AdjSpec sp{};
+  sp.mode = adj::ADJ_MODE_REINIT;
+  sp.n_steps = n_iter;
+  sp.ckpt = checkpoint_every;
+  sp.dt = dtau; sp.dx = dx; sp.dy = dy; sp.dz = dz;
+  adj::AdjIO<LSMGPU_ADJ_R> io{};
+  io.phi = phi;
+  io.grad_out = grad_out;
+  io.phi_out = phi_out;
+  io.gphi = grad_phi;
+  return adj::run<LSMGPU_ADJ_R, LSMGPU_ADJ_EXACT>("lsmgpu_reinit_vjp_weno5_tvdrk3", adj_box6(gb), adj_box6(fb),
+                                                  Box{}, sp, io);
 }

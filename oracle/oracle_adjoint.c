@@ -1,6 +1,6 @@
 /*
- * Reverse-mode gradient of the periodic WENO5 / TVD-RK3 advection objective,
- * FP64, on the CPU.
+ * Reverse-mode gradients of periodic WENO5 / TVD-RK3 advection and
+ * reinitialization, FP64, on the CPU.
  *
  * TEST INFRASTRUCTURE ONLY: this is the checker for the GPU adjoint.  Nothing
  * in lsmlib_gb300/ includes or links it.
@@ -12,6 +12,9 @@
  *                              (level_set_evolution3d.f.in:38, :113-116)
  *   TVD RK3 stages             tvd_runge_kutta3d.f:78, :403-404, :490-492
  *   periodic ghost fill after every stage (and of the initial state)
+ * and, for reinitialization, HJ WENO5 plus/minus with the reinitialization
+ * RHS in its phi0 sign form (lsm3dComputeReinitializationEqnRHS,
+ * reinitialization3d.f.in:217-256) in place of the advection terms,
  * with every operation in the order the oracle's dense routines use, so the
  * forward states are bit-identical to the oracle's LSMLIB composition.  The
  * objective is
@@ -183,16 +186,184 @@ static void adv_rhs_adjoint(const pgrid *g, const double *s, const double *const
   }
 }
 
+/* reinitialization RHS, phi0 sign form (use_phi0_for_sgn = 1), in the
+ * operation order of lsm3dcomputereinitializationeqnrhs_
+ * (reinitialization3d.f.in:217-256) with HJ WENO5 plus/minus derivatives */
+static void reinit_rhs(const pgrid *g, const double *s, const double *phi0, double dx_sq, double *rhs) {
+  FOR_BOX(0, g->n[0] - 1, 0, g->n[1] - 1, 0, g->n[2] - 1) {
+    const long c = pidx(g, i, j, k);
+    double gp[3], gm[3], star[3];
+    for (int d = 0; d < 3; d++) {
+      double v[5];
+      int face[5];
+      upwind_stencil(g, s, i, j, k, d, 0, v, face);
+      gp[d] = weno5_d(v, NULL);
+      upwind_stencil(g, s, i, j, k, d, 1, v, face);
+      gm[d] = weno5_d(v, NULL);
+    }
+    const double pc = phi0[c];
+    for (int d = 0; d < 3; d++) {
+      double u, w;
+      if (pc > 0.0) {
+        u = fmax2(-gp[d], 0.0);
+        w = fmax2(gm[d], 0.0);
+      } else {
+        u = fmax2(gp[d], 0.0);
+        w = fmax2(-gm[d], 0.0);
+      }
+      star[d] = fmax2(u, w);
+    }
+    double out = 0.0;
+    if (fabs(pc) >= ORACLE_ZERO_TOL) {
+      const double n2 = star[0] * star[0] + star[1] * star[1] + star[2] * star[2];
+      const double sgn = pc / sqrt(pc * pc + dx_sq);
+      out = sgn * (1.0 - sqrt(n2));
+    }
+    rhs[c] = out;
+  }
+}
+
+/* acc_s += dt * (dL/ds)^T mu ; acc_p0 += dt * (dL/dphi0)^T mu  (L = reinit RHS).
+ * Per axis the Godunov selection passes the derivative to one of the two
+ * WENO5 values (the branch the forward max takes); sgn = phi0/sqrt(phi0^2 +
+ * dx^2) gives d sgn/d phi0 = dx^2 / (phi0^2 + dx^2)^(3/2). */
+static void reinit_rhs_adjoint(const pgrid *g, const double *s, const double *phi0, double dx_sq, const double *mu,
+                               double dt, double *acc_s, double *acc_p0) {
+  FOR_BOX(0, g->n[0] - 1, 0, g->n[1] - 1, 0, g->n[2] - 1) {
+    const long c = pidx(g, i, j, k);
+    const double pc = phi0[c];
+    if (!(fabs(pc) >= ORACLE_ZERO_TOL)) continue;
+    double vp[3][5], vm[3][5], gp[3], gm[3], star[3];
+    int fp[3][5], fm[3][5];
+    int which[3]; /* 0: none, 1: plus side, 2: minus side */
+    double sel[3];  /* d star / d (selected WENO value) */
+    for (int d = 0; d < 3; d++) {
+      upwind_stencil(g, s, i, j, k, d, 0, vp[d], fp[d]);
+      gp[d] = weno5_d(vp[d], NULL);
+      upwind_stencil(g, s, i, j, k, d, 1, vm[d], fm[d]);
+      gm[d] = weno5_d(vm[d], NULL);
+      double u, w, du, dw;
+      if (pc > 0.0) {
+        u = fmax2(-gp[d], 0.0); du = (-gp[d] > 0.0) ? -1.0 : 0.0;
+        w = fmax2(gm[d], 0.0);  dw = (gm[d] > 0.0) ? 1.0 : 0.0;
+      } else {
+        u = fmax2(gp[d], 0.0);  du = (gp[d] > 0.0) ? 1.0 : 0.0;
+        w = fmax2(-gm[d], 0.0); dw = (-gm[d] > 0.0) ? -1.0 : 0.0;
+      }
+      if (u > w) {
+        star[d] = u; which[d] = du != 0.0 ? 1 : 0; sel[d] = du;
+      } else {
+        star[d] = w; which[d] = dw != 0.0 ? 2 : 0; sel[d] = dw;
+      }
+    }
+    const double n2 = star[0] * star[0] + star[1] * star[1] + star[2] * star[2];
+    const double nrm = sqrt(n2);
+    const double den = pc * pc + dx_sq;
+    const double sgn = pc / sqrt(den);
+    if (acc_p0) acc_p0[c] += dt * mu[c] * (1.0 - nrm) * dx_sq / (den * sqrt(den));
+    if (!(nrm > 0.0)) continue;
+    for (int d = 0; d < 3; d++) {
+      if (!which[d]) continue;
+      const double kap = -sgn * star[d] / nrm * sel[d]; /* dL / d(selected WENO value) */
+      const double *v = which[d] == 1 ? vp[d] : vm[d];
+      const int *face = which[d] == 1 ? fp[d] : fm[d];
+      double dv[5];
+      weno5_d(v, dv);
+      const double ybar = dt * mu[c] * kap * g->inv[d];
+      for (int q = 0; q < 5; q++) {
+        int a[3] = {i, j, k}, b[3] = {i, j, k};
+        a[d] += face[q];
+        b[d] += face[q] - 1;
+        const double wq = ybar * dv[q];
+        acc_s[pidx(g, a[0], a[1], a[2])] += wq;
+        acc_s[pidx(g, b[0], b[1], b[2])] -= wq;
+      }
+    }
+  }
+}
+
+typedef struct {
+  int reinit;                  /* 0: advection, 1: reinitialization (phi0 form) */
+  const double *const *vel;    /* advection velocity fields */
+  const double *phi0;          /* reinitialization sign source */
+  double dx_sq;
+} rhs_t;
+
+static void rhs_eval(const rhs_t *r, const pgrid *g, const double *s, double *rhs) {
+  if (r->reinit) reinit_rhs(g, s, r->phi0, r->dx_sq, rhs);
+  else adv_rhs(g, s, r->vel, rhs);
+}
+
+static void rhs_adj(const rhs_t *r, const pgrid *g, const double *s, const double *mu, double dt, double *acc_s,
+                    double *const acc_v[3], double *acc_p0) {
+  if (r->reinit) reinit_rhs_adjoint(g, s, r->phi0, r->dx_sq, mu, dt, acc_s, acc_p0);
+  else adv_rhs_adjoint(g, s, r->vel, mu, dt, acc_s, acc_v);
+}
+
 /* one TVD-RK3 step u -> out, keeping u1 and u2 */
-static void rk3_step(const pgrid *g, const double *u, const double *const vel[3], double dt, double *u1,
-                     double *u2, double *out, double *rhs) {
+static void rk3_step(const rhs_t *r, const pgrid *g, const double *u, double dt, double *u1, double *u2,
+                     double *out, double *rhs) {
   const long n = (long)g->n[0] * g->n[1] * g->n[2];
-  adv_rhs(g, u, vel, rhs);
+  rhs_eval(r, g, u, rhs);
   for (long c = 0; c < n; c++) u1[c] = u[c] + dt * rhs[c];
-  adv_rhs(g, u1, vel, rhs);
+  rhs_eval(r, g, u1, rhs);
   for (long c = 0; c < n; c++) u2[c] = 0.75 * u[c] + 0.25 * (u1[c] + dt * rhs[c]);
-  adv_rhs(g, u2, vel, rhs);
+  rhs_eval(r, g, u2, rhs);
   for (long c = 0; c < n; c++) out[c] = 1.0 / 3.0 * u[c] + 2.0 / 3.0 * (u2[c] + dt * rhs[c]);
+}
+
+/* Forward n_steps from phi0 (whole trajectory kept in traj); then, when lam
+ * is not NULL, the reverse sweep from lam = dJ/dphi_T, leaving dJ/dphi_0 in
+ * lam and the velocity gradients in acc_v (advection) or adding the sign
+ * sensitivity to lam (reinitialization: phi0 is also the sign source). */
+static void run(const rhs_t *r, const pgrid *g, double dt, int n_steps, double *traj, double *lam,
+                double *const acc_v[3]) {
+  const long n = (long)g->n[0] * g->n[1] * g->n[2];
+  double *u1 = (double *)malloc(sizeof(double) * n), *u2 = (double *)malloc(sizeof(double) * n);
+  double *rhs = (double *)malloc(sizeof(double) * n);
+  for (int st = 0; st < n_steps; st++)
+    rk3_step(r, g, traj + (size_t)st * n, dt, u1, u2, traj + (size_t)(st + 1) * n, rhs);
+  if (lam) {
+    double *lu1 = (double *)malloc(sizeof(double) * n), *lu2 = (double *)malloc(sizeof(double) * n);
+    double *ln = (double *)malloc(sizeof(double) * n), *mu = (double *)malloc(sizeof(double) * n);
+    double *p0 = r->reinit ? (double *)calloc((size_t)n, sizeof(double)) : NULL;
+    if (acc_v)
+      for (int d = 0; d < 3; d++) memset(acc_v[d], 0, sizeof(double) * n);
+    for (int st = n_steps - 1; st >= 0; st--) {
+      const double *u = traj + (size_t)st * n;
+      double *tmp = traj + (size_t)(st + 1) * n; /* recomputed, identical */
+      rk3_step(r, g, u, dt, u1, u2, tmp, rhs);
+      /* stage 3: out = u/3 + 2/3 (u2 + dt L(u2)) */
+      for (long c = 0; c < n; c++) {
+        ln[c] = lam[c] / 3.0;
+        mu[c] = 2.0 / 3.0 * lam[c];
+        lu2[c] = mu[c];
+      }
+      rhs_adj(r, g, u2, mu, dt, lu2, acc_v, p0);
+      /* stage 2: u2 = 3/4 u + 1/4 (u1 + dt L(u1)) */
+      for (long c = 0; c < n; c++) {
+        ln[c] += 0.75 * lu2[c];
+        mu[c] = 0.25 * lu2[c];
+        lu1[c] = mu[c];
+      }
+      rhs_adj(r, g, u1, mu, dt, lu1, acc_v, p0);
+      /* stage 1: u1 = u + dt L(u) */
+      for (long c = 0; c < n; c++) ln[c] += lu1[c];
+      rhs_adj(r, g, u, lu1, dt, ln, acc_v, p0);
+      memcpy(lam, ln, sizeof(double) * n);
+    }
+    if (p0)
+      for (long c = 0; c < n; c++) lam[c] += p0[c];
+    free(lu1); free(lu2); free(ln); free(mu); free(p0);
+  }
+  free(u1); free(u2); free(rhs);
+}
+
+static pgrid mk_pgrid(int nx, int ny, int nz, double dx, double dy, double dz) {
+  pgrid g;
+  g.n[0] = nx; g.n[1] = ny; g.n[2] = nz;
+  g.inv[0] = 1.0 / dx; g.inv[1] = 1.0 / dy; g.inv[2] = 1.0 / dz;
+  return g;
 }
 
 /* Objective J and (when g_phi is not NULL) its gradient with respect to the
@@ -203,20 +374,15 @@ double oracle_advect_objective_adjoint(int nx, int ny, int nz, double dx, double
                                        const double *vel_x, const double *vel_y, const double *vel_z,
                                        const double *phi_target, double *phi_final, double *g_phi,
                                        double *g_vel_x, double *g_vel_y, double *g_vel_z) {
-  pgrid g;
-  g.n[0] = nx; g.n[1] = ny; g.n[2] = nz;
-  g.inv[0] = 1.0 / dx; g.inv[1] = 1.0 / dy; g.inv[2] = 1.0 / dz;
+  const pgrid g = mk_pgrid(nx, ny, nz, dx, dy, dz);
   const long n = (long)nx * ny * nz;
   const double *const vel[3] = {vel_x, vel_y, vel_z};
+  const rhs_t r = {0, vel, NULL, 0.0};
   double *traj = (double *)malloc(sizeof(double) * n * (size_t)(n_steps + 1));
-  double *u1 = (double *)malloc(sizeof(double) * n), *u2 = (double *)malloc(sizeof(double) * n);
-  double *rhs = (double *)malloc(sizeof(double) * n);
   memcpy(traj, phi0, sizeof(double) * n);
-  for (int s = 0; s < n_steps; s++)
-    rk3_step(&g, traj + (size_t)s * n, vel, dt, u1, u2, traj + (size_t)(s + 1) * n, rhs);
+  run(&r, &g, dt, n_steps, traj, NULL, NULL);
   const double *phiT = traj + (size_t)n_steps * n;
   if (phi_final) memcpy(phi_final, phiT, sizeof(double) * n);
-
   const double vol = dx * dy * dz;
   double sum = 0.0;
   double *lam = (double *)calloc((size_t)n, sizeof(double));
@@ -226,40 +392,49 @@ double oracle_advect_objective_adjoint(int nx, int ny, int nz, double dx, double
     lam[c] = 2.0 * h * oracle_delta(phiT[c], heaviside_eps) * vol;
   }
   const double J = sum * vol;
-
   if (g_phi) {
-    double *lu1 = (double *)malloc(sizeof(double) * n), *lu2 = (double *)malloc(sizeof(double) * n);
-    double *ln = (double *)malloc(sizeof(double) * n), *mu = (double *)malloc(sizeof(double) * n);
     double *const acc_v[3] = {g_vel_x, g_vel_y, g_vel_z};
-    const int want_v = g_vel_x && g_vel_y && g_vel_z;
-    if (want_v)
-      for (int d = 0; d < 3; d++) memset(acc_v[d], 0, sizeof(double) * n);
-    for (int s = n_steps - 1; s >= 0; s--) {
-      const double *u = traj + (size_t)s * n;
-      double *tmp = traj + (size_t)(s + 1) * n; /* the next state is no longer needed */
-      rk3_step(&g, u, vel, dt, u1, u2, tmp, rhs);
-      /* stage 3: out = u/3 + 2/3 (u2 + dt L(u2)) */
-      for (long c = 0; c < n; c++) {
-        ln[c] = lam[c] / 3.0;
-        mu[c] = 2.0 / 3.0 * lam[c];
-        lu2[c] = mu[c];
-      }
-      adv_rhs_adjoint(&g, u2, vel, mu, dt, lu2, want_v ? acc_v : NULL);
-      /* stage 2: u2 = 3/4 u + 1/4 (u1 + dt L(u1)) */
-      for (long c = 0; c < n; c++) {
-        ln[c] += 0.75 * lu2[c];
-        mu[c] = 0.25 * lu2[c];
-        lu1[c] = mu[c];
-      }
-      adv_rhs_adjoint(&g, u1, vel, mu, dt, lu1, want_v ? acc_v : NULL);
-      /* stage 1: u1 = u + dt L(u) */
-      for (long c = 0; c < n; c++) ln[c] += lu1[c];
-      adv_rhs_adjoint(&g, u, vel, lu1, dt, ln, want_v ? acc_v : NULL);
-      memcpy(lam, ln, sizeof(double) * n);
-    }
+    memcpy(traj, phi0, sizeof(double) * n);
+    run(&r, &g, dt, n_steps, traj, lam, (g_vel_x && g_vel_y && g_vel_z) ? acc_v : NULL);
     memcpy(g_phi, lam, sizeof(double) * n);
-    free(lu1); free(lu2); free(ln); free(mu);
   }
-  free(lam); free(traj); free(u1); free(u2); free(rhs);
+  free(lam);
+  free(traj);
   return J;
+}
+
+/* Vector-Jacobian product of n_steps periodic advection steps:
+ * g_phi = (d phi_T / d phi)^T grad_out, g_vel_d = (d phi_T / d vel_d)^T grad_out. */
+void oracle_advect_vjp(int nx, int ny, int nz, double dx, double dy, double dz, double dt, int n_steps,
+                       const double *phi, const double *vel_x, const double *vel_y, const double *vel_z,
+                       const double *grad_out, double *phi_final, double *g_phi, double *g_vel_x,
+                       double *g_vel_y, double *g_vel_z) {
+  const pgrid g = mk_pgrid(nx, ny, nz, dx, dy, dz);
+  const long n = (long)nx * ny * nz;
+  const double *const vel[3] = {vel_x, vel_y, vel_z};
+  const rhs_t r = {0, vel, NULL, 0.0};
+  double *traj = (double *)malloc(sizeof(double) * n * (size_t)(n_steps + 1));
+  memcpy(traj, phi, sizeof(double) * n);
+  memcpy(g_phi, grad_out, sizeof(double) * n);
+  double *const acc_v[3] = {g_vel_x, g_vel_y, g_vel_z};
+  run(&r, &g, dt, n_steps, traj, g_phi, (g_vel_x && g_vel_y && g_vel_z) ? acc_v : NULL);
+  if (phi_final) memcpy(phi_final, traj + (size_t)n_steps * n, sizeof(double) * n);
+  free(traj);
+}
+
+/* Vector-Jacobian product of n_steps periodic reinitialization iterations
+ * (phi0 sign form: the sign source is the initial phi, so its sensitivity is
+ * part of the gradient); pseudo-time step dtau, dx_sq = max(dx, dy, dz)^2. */
+void oracle_reinit_vjp(int nx, int ny, int nz, double dx, double dy, double dz, double dtau, int n_steps,
+                       const double *phi, const double *grad_out, double *phi_final, double *g_phi) {
+  const pgrid g = mk_pgrid(nx, ny, nz, dx, dy, dz);
+  const long n = (long)nx * ny * nz;
+  double m = fmax2(fmax2(dx, dy), dz);
+  const rhs_t r = {1, NULL, phi, m * m};
+  double *traj = (double *)malloc(sizeof(double) * n * (size_t)(n_steps + 1));
+  memcpy(traj, phi, sizeof(double) * n);
+  memcpy(g_phi, grad_out, sizeof(double) * n);
+  run(&r, &g, dtau, n_steps, traj, g_phi, NULL);
+  if (phi_final) memcpy(phi_final, traj + (size_t)n_steps * n, sizeof(double) * n);
+  free(traj);
 }

@@ -41,3 +41,32 @@ class AdvectObjective(torch.autograd.Function):
         gp, gx, gy, gz = ctx.saved_tensors
         s = gJ.to(gp.dtype)
         return gp * s, gx * s, gy * s, gz * s, None, None, None, None, None, None
+
+
+class Reinit(torch.autograd.Function):
+    """phi -> phi_T after `n_iter` periodic reinitialization iterations (phi0
+    sign form); backward through the C-ABI vector-Jacobian product."""
+
+    @staticmethod
+    def forward(ctx, phi, spacing, dtau, n_iter, ckpt):
+        precision = "f64" if phi.dtype == torch.float64 else "f32"
+        nx, ny, nz = phi.shape
+        gb = (-3, nx + 2, -3, ny + 2, -3, nz + 2)
+        fb = (0, nx - 1, 0, ny - 1, 0, nz - 1)
+        g = _ghosted(phi.detach())
+        out, _ = L.reinit_vjp_weno5_tvdrk3(g, gb, fb, None, spacing[0], dtau, n_iter, checkpoint_every=ckpt,
+                                           precision=precision, dy=spacing[1], dz=spacing[2])
+        torch.cuda.synchronize()
+        ctx.save_for_backward(phi.detach())
+        ctx.args = (spacing, dtau, n_iter, ckpt, precision, gb, fb)
+        return _interior(out)
+
+    @staticmethod
+    def backward(ctx, gout):
+        (phi,) = ctx.saved_tensors
+        spacing, dtau, n_iter, ckpt, precision, gb, fb = ctx.args
+        _, gp = L.reinit_vjp_weno5_tvdrk3(_ghosted(phi), gb, fb, _ghosted(gout.contiguous()), spacing[0], dtau,
+                                          n_iter, checkpoint_every=ckpt, precision=precision, dy=spacing[1],
+                                          dz=spacing[2])
+        torch.cuda.synchronize()
+        return _interior(gp), None, None, None, None

@@ -315,3 +315,210 @@ def test_adjoint_argument_errors(gpu_lib):
         L.advect_adjoint_weno5_tvdrk3(P, gb, (0, 4, 0, 11, 0, 11), V, gb, T, sp[0], dt, 3, 0.1)
     with pytest.raises(RuntimeError, match="3 ghost cells"):
         L.advect_adjoint_weno5_tvdrk3(P, (0, 17, -3, 14, -3, 14), fb, V, gb, T, sp[0], dt, 3, 0.1)
+
+
+# ---------------------------------------------------------------------------
+# vector-Jacobian products (advection and reinitialization), CPU oracle
+# ---------------------------------------------------------------------------
+def _vjp_fns():
+    lib = H.oracle()
+    P = ctypes.c_void_p
+    fa = lib.oracle_advect_vjp
+    fa.restype = None
+    fa.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [ctypes.c_int] + [P] * 9
+    fr = lib.oracle_reinit_vjp
+    fr.restype = None
+    fr.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [ctypes.c_int] + [P] * 4
+    return fa, fr
+
+
+def oracle_advect_vjp(phi, vel, gout, sp, dt, steps, grads=True):
+    fa, _ = _vjp_fns()
+    phi = np.asfortranarray(phi, dtype=np.float64)
+    vel = [np.asfortranarray(v, dtype=np.float64) for v in vel]
+    gout = np.asfortranarray(gout, dtype=np.float64)
+    fin = np.zeros_like(phi, order="F")
+    gp = np.zeros_like(phi, order="F")
+    gv = [np.zeros_like(phi, order="F") for _ in range(3)]
+    fa(*phi.shape, *[float(x) for x in sp], float(dt), int(steps), _p(phi), *[_p(v) for v in vel], _p(gout),
+       _p(fin), _p(gp), *[_p(g) for g in gv])
+    return fin, gp, gv
+
+
+def oracle_reinit_vjp(phi, gout, sp, dtau, steps):
+    _, fr = _vjp_fns()
+    phi = np.asfortranarray(phi, dtype=np.float64)
+    gout = np.asfortranarray(gout, dtype=np.float64)
+    fin = np.zeros_like(phi, order="F")
+    gp = np.zeros_like(phi, order="F")
+    fr(*phi.shape, *[float(x) for x in sp], float(dtau), int(steps), _p(phi), _p(gout), _p(fin), _p(gp))
+    return fin, gp
+
+
+def reinit_case(dims, seed=5):
+    """A non-distance level set (the reinitialization workload's form) on
+    (nx, ny, nz) cells of [-1, 1]^3 with a smooth random perturbation."""
+    sp = tuple(2.0 / n for n in dims)
+    c = [-1.0 + (np.arange(n) + 0.5) * h for n, h in zip(dims, sp)]
+    X, Y, Z = np.meshgrid(*c, indexing="ij")
+    r = np.sqrt(X * X + Y * Y + Z * Z)
+    phi = (r - 0.5) * (0.1 + (X - 0.3) ** 2 + (Y - 0.3) ** 2 + (Z + 0.2) ** 2)
+    return np.asfortranarray(phi), sp, 0.5 * min(sp)
+
+
+def test_oracle_reinit_forward_is_the_lsmlib_sequence():
+    dims = (12, 10, 14)
+    phi, sp, dtau = reinit_case(dims)
+    fin, _ = oracle_reinit_vjp(phi, np.zeros(dims), sp, dtau, 3)
+    gb, fb = boxes(dims)
+    g = ghosted(phi)
+    O.periodic_fill(g, gb, fb)
+    want = O.tvdrk3_run(H.oracle(), "reinit", g, gb, fb, sp, dtau, 3, L.BC_PERIODIC, use0=1)
+    assert H.same(fin, want[3:-3, 3:-3, 3:-3])
+
+
+def test_oracle_advect_vjp_matches_objective_gradient():
+    """The VJP with grad_out = dJ/dphi_T reproduces the objective gradient."""
+    dims = (12, 10, 14)
+    phi, vel, tgt, sp, dt = adjoint_case(dims)
+    eps = 1.5 * sp[0]
+    J, fin, gp, gv = oracle_adjoint(phi, vel, tgt, sp, dt, 3, eps)
+    lib = H.oracle()
+    for name in ("oracle_heaviside", "oracle_delta"):
+        getattr(lib, name).restype = ctypes.c_double
+        getattr(lib, name).argtypes = [ctypes.c_double, ctypes.c_double]
+    vol = sp[0] * sp[1] * sp[2]
+    hv = np.vectorize(lambda x: lib.oracle_heaviside(x, eps))
+    dl = np.vectorize(lambda x: lib.oracle_delta(x, eps))
+    lam = np.asfortranarray(2.0 * (hv(fin) - hv(tgt)) * dl(fin) * vol)
+    _, gp2, gv2 = oracle_advect_vjp(phi, vel, lam, sp, dt, 3)
+    assert rel(gp2, gp) <= 1e-14
+    for a, b in zip(gv2, gv):
+        assert rel(a, b) <= 1e-14
+
+
+def test_oracle_reinit_vjp_matches_finite_differences():
+    dims = (12, 10, 14)
+    phi, sp, dtau = reinit_case(dims)
+    steps = 3
+    rng = np.random.default_rng(9)
+    gout = np.asfortranarray(rng.standard_normal(dims))
+    _, gp = oracle_reinit_vjp(phi, gout, sp, dtau, steps)
+    F = lambda p: float(np.sum(gout * oracle_reinit_vjp(p, np.zeros(dims), sp, dtau, steps)[0]))
+    h = 1e-6
+    for _ in range(4):
+        (d,) = smooth_unit(rng, dims)
+        fd = (F(phi + h * d) - F(phi - h * d)) / (2 * h)
+        an = float(np.sum(gp * d))
+        assert abs(fd - an) <= 1e-6 * max(abs(fd), 1e-3 * np.linalg.norm(gp)), (fd, an)
+
+
+def gpu_reinit_vjp(phi, gout, sp, dtau, steps, precision="f64", ckpt=8):
+    real = np.float64 if precision == "f64" else np.float32
+    gb, fb = boxes(phi.shape)
+    out, gp = L.reinit_vjp_weno5_tvdrk3(ghosted(phi, real), gb, fb, None if gout is None else ghosted(gout, real),
+                                        sp[0], dtau, steps, checkpoint_every=ckpt, precision=precision,
+                                        dy=sp[1], dz=sp[2])
+    inner = (slice(3, -3),) * 3
+    return out[inner].astype(np.float64), None if gp is None else gp[inner].astype(np.float64)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dims,steps,ckpt", [((20, 18, 16), 5, 2), ((16, 16, 16), 3, 8)])
+def test_reinit_vjp_f64_matches_oracle(dims, steps, ckpt, gpu_lib):
+    phi, sp, dtau = reinit_case(dims)
+    rng = np.random.default_rng(21)
+    gout = np.asfortranarray(rng.standard_normal(dims))
+    fin_w, gw = oracle_reinit_vjp(phi, gout, sp, dtau, steps)
+    fin, gp = gpu_reinit_vjp(phi, gout, sp, dtau, steps, "f64", ckpt)
+    assert H.same(fin, fin_w)
+    assert rel(gp, gw) <= 1e-11
+
+
+@pytest.mark.gpu
+def test_reinit_vjp_f32_against_fp64_oracle(gpu_lib):
+    dims = (24, 20, 18)
+    phi, sp, dtau = reinit_case(dims)
+    rng = np.random.default_rng(22)
+    gout = np.asfortranarray(rng.standard_normal(dims))
+    fin_w, gw = oracle_reinit_vjp(phi, gout, sp, dtau, 4)
+    fin, gp = gpu_reinit_vjp(phi, gout, sp, dtau, 4, "f32", 2)
+    assert np.max(np.abs(fin - fin_w)) <= 1e-5
+    assert np.linalg.norm(gp - gw) <= 1e-3 * np.linalg.norm(gw), np.linalg.norm(gp - gw) / np.linalg.norm(gw)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_reinit_vjp_checkpoint_spacing_changes_nothing(precision, gpu_lib):
+    dims = (20, 18, 16)
+    phi, sp, dtau = reinit_case(dims)
+    gout = np.asfortranarray(np.random.default_rng(23).standard_normal(dims))
+    base = gpu_reinit_vjp(phi, gout, sp, dtau, 7, precision, 7)
+    for ckpt in (1, 3, 50):
+        fin, gp = gpu_reinit_vjp(phi, gout, sp, dtau, 7, precision, ckpt)
+        assert np.array_equal(fin, base[0]) and np.array_equal(gp, base[1])
+
+
+@pytest.mark.gpu
+def test_reinit_vjp_matches_central_differences(gpu_lib):
+    """20 reinitialization iterations at 48^3 (the headline workload's field
+    and dtau = 0.5 dx): FP64 and FP32 VJPs against FP64 central differences
+    of <grad_out, phi_T> along smooth random unit directions.  The Godunov
+    and sign maxima make the map piecewise smooth, so the step is h = 1e-5:
+    measured, the differences converge to the FP64 VJP (relative error 7e-5 to
+    8e-4 at h = 1e-3, 6e-6 to 3e-5 at 1e-4, 3e-8 to 2e-7 at 1e-5) as steps
+    stop crossing switching points.  FP32 carries its own rounding (up to 2e-4
+    relative on these directions)."""
+    n = 48
+    phi, sp, dtau = reinit_case((n, n, n))
+    rng = np.random.default_rng(24)
+    gout = np.asfortranarray(rng.standard_normal(phi.shape))
+    _, g64 = gpu_reinit_vjp(phi, gout, sp, dtau, 20, "f64", 8)
+    _, g32 = gpu_reinit_vjp(phi, gout, sp, dtau, 20, "f32", 8)
+    F = lambda p: float(np.sum(gout * gpu_reinit_vjp(p, None, sp, dtau, 20, "f64")[0]))
+    h = 1e-5
+    for _ in range(3):
+        (d,) = smooth_unit(rng, phi.shape)
+        fd = (F(phi + h * d) - F(phi - h * d)) / (2 * h)
+        assert abs(np.sum(g64 * d) - fd) <= 1e-6 * abs(fd), (np.sum(g64 * d), fd)
+        assert abs(np.sum(g32 * d) - fd) <= 1e-3 * abs(fd), (np.sum(g32 * d), fd)
+
+
+@pytest.mark.gpu
+def test_advect_vjp_matches_objective_gradient(gpu_lib):
+    dims = (20, 18, 16)
+    phi, vel, tgt, sp, dt = adjoint_case(dims)
+    eps = 1.5 * sp[0]
+    J, fin, gw, gvw = oracle_adjoint(phi, vel, tgt, sp, dt, 5, eps)
+    lib = H.oracle()
+    for name in ("oracle_heaviside", "oracle_delta"):
+        getattr(lib, name).restype = ctypes.c_double
+        getattr(lib, name).argtypes = [ctypes.c_double, ctypes.c_double]
+    vol = sp[0] * sp[1] * sp[2]
+    hv = np.vectorize(lambda x: lib.oracle_heaviside(x, eps))
+    dl = np.vectorize(lambda x: lib.oracle_delta(x, eps))
+    lam = np.asfortranarray(2.0 * (hv(fin) - hv(tgt)) * dl(fin) * vol)
+    gb, fb = boxes(dims)
+    out, gp, gv = L.advect_vjp_weno5_tvdrk3(ghosted(phi), gb, fb, [ghosted(v) for v in vel], gb, ghosted(lam),
+                                            sp[0], dt, 5, checkpoint_every=2, dy=sp[1], dz=sp[2])
+    inner = (slice(3, -3),) * 3
+    assert H.same(out[inner], fin)
+    assert rel(gp[inner], gw) <= 1e-11
+    for a, b in zip(gv, gvw):
+        assert rel(a[inner], b) <= 1e-11
+
+
+@pytest.mark.gpu
+def test_reinit_autograd_function(gpu_lib):
+    import torch
+    from tests.adjoint_autograd import Reinit
+    dims = (16, 16, 16)
+    phi, sp, dtau = reinit_case(dims)
+    w = np.asfortranarray(np.random.default_rng(25).standard_normal(dims))
+    fin, gp = gpu_reinit_vjp(phi, w, sp, dtau, 4, "f64", 2)
+    p = torch.tensor(phi, dtype=torch.float64, device="cuda", requires_grad=True)
+    out = Reinit.apply(p, sp, dtau, 4, 2)
+    loss = (out * torch.tensor(w, dtype=torch.float64, device="cuda")).sum()
+    loss.backward()
+    assert np.array_equal(out.detach().cpu().numpy(), fin)
+    assert np.array_equal(p.grad.cpu().numpy(), gp)
