@@ -252,6 +252,13 @@ __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
+// 2^-floor(log2 x) for a positive normal float x, from the exponent bits (no
+// reciprocal instruction).  x * pow2_recip(x) lies in [1, 2).
+__device__ __forceinline__ float pow2_recip(float x) {
+  return __int_as_float(0x7f000000 - (__float_as_int(x) & 0x7f800000));
+}
+__device__ __forceinline__ float2 pow2_recip2(float2 x) { return make_float2(pow2_recip(x.x), pow2_recip(x.y)); }
+
 // WENO5-JS on two cells at once, the epsilon-scaled weight form of
 // weno5_fast with the common factors folded: smoothness and epsilon are both
 // scaled by 12 (only S/eps enters the weights) and the candidate stencils by
@@ -276,8 +283,13 @@ __device__ __forceinline__ float2 weno5_x2(float2 v1, float2 v2, float2 v3, floa
   t = fma2(sp(-2.f), v4, add2(v3, v5));
   u = fma2(sp(-4.f), v4, fma2(sp(3.f), v3, v5));
   const float2 S3 = fma2(mul2(sp(13.f), t), t, mul2(mul2(sp(3.f), u), u));
-  const float2 r = make_float2(__fdividef(1.f, eps.x), __fdividef(1.f, eps.y));
-  float2 w1 = fma2(S1, r, sp(1.f)), w2 = fma2(S2, r, sp(1.f)), w3 = fma2(S3, r, sp(1.f));
+  // q_k = (S_k + eps) 2^-e with 2^e <= eps < 2^(e+1): the weights only see
+  // ratios of the q_k, so any common scale of S + eps gives the same weights
+  // as (S_k / eps + 1); with eps 2^-e in [1, 2), 1 <= q_k < 7e7 and the
+  // products below stay under 3e30
+  const float2 r = pow2_recip2(eps);
+  const float2 e = mul2(eps, r);
+  float2 w1 = fma2(S1, r, e), w2 = fma2(S2, r, e), w3 = fma2(S3, r, e);
   w1 = mul2(w1, w1);
   w2 = mul2(w2, w2);
   w3 = mul2(w3, w3);
@@ -287,6 +299,60 @@ __device__ __forceinline__ float2 weno5_x2(float2 v1, float2 v2, float2 v3, floa
   const float2 num = fma2(n1, P1, fma2(n2, P2, mul2(n3, P3)));
   const float2 den = mul2(sp(6.f), add2(add2(n1, n2), n3));
   return make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
+}
+
+// Both one-sided WENO5 values of one axis for two cells: minus side on
+// D(c-2 .. c+2), plus side on D(c+3 .. c-1), given D[0..5] = D(c-2 .. c+3).
+// The two sides share two of their three candidate stencils (plus P2 = minus
+// P3, plus P3 = minus P2), the second differences t of their middle and outer
+// smoothness indicators (plus t2 = minus t3, plus t3 = minus t2), and four of
+// the five squared differences of the epsilon maximum; each is computed once.
+__device__ __forceinline__ void weno5_pm_x2(const float2 D[6], float2 &gp, float2 &gm) {
+  float2 sq[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) sq[i] = mul2(D[i], D[i]);
+  const float cx = fmaxf(fmaxf(sq[1].x, sq[2].x), fmaxf(sq[3].x, sq[4].x));
+  const float cy = fmaxf(fmaxf(sq[1].y, sq[2].y), fmaxf(sq[3].y, sq[4].y));
+  const float2 em = fma2(sp(12e-6f), make_float2(fmaxf(cx, sq[0].x), fmaxf(cy, sq[0].y)), sp(12e-36f));
+  const float2 ep = fma2(sp(12e-6f), make_float2(fmaxf(cx, sq[5].x), fmaxf(cy, sq[5].y)), sp(12e-36f));
+  const float2 rm = pow2_recip2(em), rp = pow2_recip2(ep);
+  const float2 emr = mul2(em, rm), epr = mul2(ep, rp);
+  // 6 * candidate stencils
+  const float2 P1m = fma2(sp(2.f), D[0], fma2(sp(-7.f), D[1], mul2(sp(11.f), D[2])));
+  const float2 A = fma2(sp(-1.f), D[1], fma2(sp(5.f), D[2], mul2(sp(2.f), D[3])));  // minus P2, plus P3
+  const float2 B = fma2(sp(2.f), D[2], fma2(sp(5.f), D[3], mul2(sp(-1.f), D[4])));  // minus P3, plus P2
+  const float2 P1p = fma2(sp(2.f), D[5], fma2(sp(-7.f), D[4], mul2(sp(11.f), D[3])));
+  // second differences t and the asymmetric parts u of the indicators
+  const float2 t1m = fma2(sp(-2.f), D[1], add2(D[0], D[2]));
+  const float2 t2 = fma2(sp(-2.f), D[2], add2(D[1], D[3]));  // minus t2, plus t3
+  const float2 t3 = fma2(sp(-2.f), D[3], add2(D[2], D[4]));  // minus t3, plus t2
+  const float2 t1p = fma2(sp(-2.f), D[4], add2(D[5], D[3]));
+  const float2 u1m = fma2(sp(-4.f), D[1], fma2(sp(3.f), D[2], D[0]));
+  const float2 u2m = fma2(sp(-1.f), D[3], D[1]);
+  const float2 u3m = fma2(sp(-4.f), D[3], fma2(sp(3.f), D[2], D[4]));
+  const float2 u1p = fma2(sp(-4.f), D[4], fma2(sp(3.f), D[3], D[5]));
+  const float2 u2p = fma2(sp(-1.f), D[2], D[4]);
+  const float2 u3p = fma2(sp(-4.f), D[2], fma2(sp(3.f), D[3], D[1]));
+  // 12 * smoothness indicators: 13 t^2 + 3 u^2
+  const float2 T1m = mul2(mul2(sp(13.f), t1m), t1m), T2 = mul2(mul2(sp(13.f), t2), t2);
+  const float2 T3 = mul2(mul2(sp(13.f), t3), t3), T1p = mul2(mul2(sp(13.f), t1p), t1p);
+  const float2 q1m = fma2(fma2(mul2(sp(3.f), u1m), u1m, T1m), rm, emr);
+  const float2 q2m = fma2(fma2(mul2(sp(3.f), u2m), u2m, T2), rm, emr);
+  const float2 q3m = fma2(fma2(mul2(sp(3.f), u3m), u3m, T3), rm, emr);
+  const float2 q1p = fma2(fma2(mul2(sp(3.f), u1p), u1p, T1p), rp, epr);
+  const float2 q2p = fma2(fma2(mul2(sp(3.f), u2p), u2p, T3), rp, epr);
+  const float2 q3p = fma2(fma2(mul2(sp(3.f), u3p), u3p, T2), rp, epr);
+  auto combine = [](float2 q1, float2 q2, float2 q3, float2 P1, float2 P2, float2 P3) {
+    const float2 q23 = mul2(q2, q3), q13 = mul2(q1, q3), q12 = mul2(q1, q2);
+    const float2 n1 = mul2(mul2(sp(0.1f), q23), q23);
+    const float2 n2 = mul2(mul2(sp(0.6f), q13), q13);
+    const float2 n3 = mul2(mul2(sp(0.3f), q12), q12);
+    const float2 num = fma2(n1, P1, fma2(n2, P2, mul2(n3, P3)));
+    const float2 den = mul2(sp(6.f), add2(add2(n1, n2), n3));
+    return make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
+  };
+  gm = combine(q1m, q2m, q3m, P1m, A, B);
+  gp = combine(q1p, q2p, q3p, P1p, B, A);
 }
 
 // Computes one 32 x 8 x TZ_ tile whose haloed input (40 x 14 x (TZ_ + 6)) is
@@ -318,8 +384,8 @@ __device__ __forceinline__ void f32_tile(const float *tile, const StageArgs<floa
 #pragma unroll
         for (int f = -2; f <= 3; f++)
           v[f + 2] = mul2(make_float2(c0[f * st[d]] - c0[(f - 1) * st[d]], c1[f * st[d]] - c1[(f - 1) * st[d]]), inv[d]);
-        const float2 p = weno5_x2(v[5], v[4], v[3], v[2], v[1]);
-        const float2 m = weno5_x2(v[0], v[1], v[2], v[3], v[4]);
+        float2 p, m;
+        weno5_pm_x2(v, p, m);
         gp0[d] = p.x; gp1[d] = p.y;
         gm0[d] = m.x; gm1[d] = m.y;
       }
