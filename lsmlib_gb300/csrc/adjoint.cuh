@@ -50,6 +50,7 @@ using fused::Layout;
 
 constexpr int kSeg = 26;     // cells of a row segment written by one warp
 constexpr int kRows = 8;     // warps (rows) per CTA of k_adj_xz, columns per CTA row of k_adj_y
+constexpr int kRowMax = 256; // longest x row k_adj_xz_row takes (one CTA per row)
 
 // periodic image of index a in [0, n): one add or subtract for a in
 // [-n, 2n), a remainder otherwise
@@ -412,6 +413,117 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? 3 : 1) k_adj_xz(A
 #pragma unroll
     for (int m = 0; m < 6; m++) V += __shfl_sync(0xffffffffu, G[m], (lane + 2 - m) & 31);
     const R Ax = V - __shfl_sync(0xffffffffu, V, (lane + 1) & 31);
+    if (!own) continue;
+    R o = mring[0] + (Ax + Az);
+    if (a.P) o += a.pscale * a.P[c];
+    if (a.Q) o += a.qscale * a.Q[c];
+    a.out[c] = o;
+  }
+}
+
+// Row form of k_adj_xz for rows of at most kRowMax cells: a CTA of
+// ceil(nx/32) warps owns a whole x row (every cell of it written, no halo
+// lanes) and marches along z; per output plane each lane puts its x slots in
+// shared memory (two buffers, one barrier per plane) and sums its two x faces
+// from its neighbours' slots with periodic wrap.
+template <class R, bool EXACT, int MODE>
+__global__ void __launch_bounds__(kRowMax, sizeof(R) == 4 ? 3 : 1) k_adj_xz_row(AdjStageArgs<R> a) {
+  extern __shared__ __align__(16) unsigned char xr_smem[];
+  const Layout &L = a.L;
+  const int nx = L.nx, nz = L.nz;
+  const int npad = blockDim.y * 32;
+  R *buf = reinterpret_cast<R *>(xr_smem);  // [2][6][npad]
+  const int lane = threadIdx.x;
+  const int x = threadIdx.y * 32 + lane;
+  const bool own = x < nx;
+  const int j = blockIdx.x;
+  const int z0 = blockIdx.y * a.zchunk;
+  const int zend = min(z0 + a.zchunk, nz);
+  const R dt = a.dt, msc = a.mscale, ix = a.inv[0], iz = a.inv[2];
+  const long long pz = L.pz;
+  const long long row = (long long)fused::GX + L.py * (j + fused::GY);
+  const int xc = own ? x : nx - 1;  // idle lanes shadow the last cell
+  int xo[7], xn[7];  // stencil offsets relative to the cell; wrapped neighbour cells x-3 .. x+3
+#pragma unroll
+  for (int q = 0; q < 7; q++) {
+    xn[q] = wrapi(xc - 3 + q, nx);
+    xo[q] = xn[q] - xc;
+  }
+  const long long col = row + xc;
+  const R *s = a.s + col;
+  const R *M = a.M + col;
+  int zk = wrapi(z0 - 3, nz);
+  long long ok = pz * (long long)(zk + fused::GZ);
+
+  R win[7], mring[4], F[6];
+  R prevV = R(0);
+#pragma unroll
+  for (int q = 0; q < 6; q++) {
+    win[q + 1] = s[plane_add(ok, zk, q - 3, nz, pz)];
+    F[q] = R(0);
+  }
+#pragma unroll
+  for (int q = 0; q < 4; q++) mring[q] = R(0);
+  R cs = s[plane_add(ok, zk, 3, nz, pz)], cm = M[ok];
+  Coef<R> cv = load_coef<R, MODE>(a, 2, col + ok);
+  R xsn[7];
+  Coef<R> xvn;
+  {
+    const long long o = plane_add(ok, zk, 3, nz, pz);  // plane z0
+#pragma unroll
+    for (int q = 0; q < 7; q++) xsn[q] = s[o + xo[q]];
+    xvn = load_coef<R, MODE>(a, 0, col + o);
+  }
+  int b = 0;
+  for (int kk = z0 - 3; kk < zend + 3; kk++) {
+#pragma unroll
+    for (int q = 0; q < 6; q++) win[q] = win[q + 1];
+    win[6] = cs;
+#pragma unroll
+    for (int q = 0; q < 3; q++) mring[q] = mring[q + 1];
+    mring[3] = msc * cm;
+    const Coef<R> uz = cv;
+    const long long okk = ok;
+    const int zkk = zk;
+    ok = plane_add(ok, zk, 1, nz, pz);
+    zk = (zk + 1 == nz) ? 0 : zk + 1;
+    if (kk + 1 < zend + 3) {
+      cs = s[plane_add(ok, zk, 3, nz, pz)];
+      cm = M[ok];
+      cv = load_coef<R, MODE>(a, 2, col + ok);
+    }
+    R G[6];
+    const R gz = coef_slots<R, EXACT, MODE>(win, uz, 2, mring[3], dt, iz, G);
+    if (MODE == ADJ_ADV && a.gvel[2] && own && kk >= z0 && kk < zend) a.gvel[2][col + okk] += gz;
+    const R Az = ring_step<R>(F, prevV, G);
+    const int k = kk - 3;
+    if (k < z0) continue;  // uniform over the CTA
+
+    R w7[7];
+#pragma unroll
+    for (int q = 0; q < 7; q++) w7[q] = xsn[q];
+    const Coef<R> ux = xvn;
+    const long long ob = plane_add(okk, zkk, -3, nz, pz);  // plane k
+    if (k + 1 < zend) {
+      const long long o = plane_add(okk, zkk, -2, nz, pz);
+#pragma unroll
+      for (int q = 0; q < 7; q++) xsn[q] = s[o + xo[q]];
+      xvn = load_coef<R, MODE>(a, 0, col + o);
+    }
+    const R gx = coef_slots<R, EXACT, MODE>(w7, ux, 0, mring[0], dt, ix, G);
+    const long long c = col + ob;
+    if (MODE == ADJ_ADV && a.gvel[0] && own) a.gvel[0][c] += gx;
+    R *bb = buf + b * 6 * npad;
+    if (own) {
+#pragma unroll
+      for (int m = 0; m < 6; m++) bb[m * npad + x] = G[m];
+    }
+    __syncthreads();
+    // Vbar(x) - Vbar(x+1) = sum_m G_m(x + 2 - m) - G_m(x + 3 - m)
+    R Ax = R(0);
+#pragma unroll
+    for (int m = 0; m < 6; m++) Ax += bb[m * npad + xn[5 - m]] - bb[m * npad + xn[6 - m]];
+    b ^= 1;
     if (!own) continue;
     R o = mring[0] + (Ax + Az);
     if (a.P) o += a.pscale * a.P[c];

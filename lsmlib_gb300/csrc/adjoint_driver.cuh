@@ -39,12 +39,12 @@ struct AdjIO {
   R *gvel[3];            // dJ/dvel over vb
 };
 
-// march length per thread: enough threads for about 2048 per SM, and at
-// least 16 cells per march (each march also computes 6 warm-up cells)
-inline int pick_chunk(int n_march, long long threads_per_chunk) {
+// march length per thread: enough chunks for `per_sm` threads per SM (each
+// march also computes 6 cells before its first output), at least 16 cells
+inline int pick_chunk(int n_march, long long threads_per_chunk, int per_sm) {
   int sms = 152, dev = 0;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long want = 2048LL * sms;
+  const long long want = (long long)per_sm * sms;
   long long chunks = (want + threads_per_chunk - 1) / threads_per_chunk;
   if (chunks < 1) chunks = 1;
   int c = (int)((n_march + chunks - 1) / chunks);
@@ -58,9 +58,23 @@ template <class R, bool EXACT, int MODE>
 void launch_adj_stage(const AdjStageArgs<R> &a) {
   const Layout &L = a.L;
   dim3 blk(32, kRows);
-  dim3 g1((unsigned)((L.nx + kSeg - 1) / kSeg), (unsigned)((L.ny + kRows - 1) / kRows),
-          (unsigned)((L.nz + a.zchunk - 1) / a.zchunk));
-  k_adj_xz<R, EXACT, MODE><<<g1, blk, 0, stream()>>>(a);
+  if (L.nx <= kRowMax) {
+    // one CTA per x row
+    const int w = (L.nx + 31) / 32;
+    const size_t smem = 2 * 6 * (size_t)w * 32 * sizeof(R);
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_adj_xz_row<R, EXACT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(2 * 6 * kRowMax * sizeof(R)));
+      attr = true;
+    }
+    dim3 g1((unsigned)L.ny, (unsigned)((L.nz + a.zchunk - 1) / a.zchunk));
+    k_adj_xz_row<R, EXACT, MODE><<<g1, dim3(32, w), smem, stream()>>>(a);
+  } else {
+    dim3 g1((unsigned)((L.nx + kSeg - 1) / kSeg), (unsigned)((L.ny + kRows - 1) / kRows),
+            (unsigned)((L.nz + a.zchunk - 1) / a.zchunk));
+    k_adj_xz<R, EXACT, MODE><<<g1, blk, 0, stream()>>>(a);
+  }
   note_launch();
   dim3 g2((unsigned)((L.nx + 31) / 32), (unsigned)((L.nz + kRows - 1) / kRows),
           (unsigned)((L.ny + a.ychunk - 1) / a.ychunk));
@@ -238,8 +252,11 @@ int run(const char *name, const Box &gb, const Box &fb, const Box &vb, const Adj
     aa.side = SIDE;
     aa.dt = (R)sp.dt;
     aa.inv[0] = fa.inv[0]; aa.inv[1] = fa.inv[1]; aa.inv[2] = fa.inv[2];
-    aa.zchunk = pick_chunk(nz, 32LL * ((nx + kSeg - 1) / kSeg) * ny);
-    aa.ychunk = pick_chunk(ny, (long long)nx * nz);
+    // thread targets per SM measured best at 192^3 (more chunks than resident
+    // threads: latency hiding outweighs the extra warm-up cells)
+    aa.zchunk = pick_chunk(nz, nx <= kRowMax ? 32LL * ((nx + 31) / 32) * ny : 32LL * ((nx + kSeg - 1) / kSeg) * ny,
+                           2048);
+    aa.ychunk = pick_chunk(ny, (long long)nx * nz, 4096);
     const dim3 cgrid((unsigned)((nx + 31) / 32), (unsigned)((ny + 7) / 8), (unsigned)nz), cblk(32, 8);
     // one reverse stage at forward state `st`
     auto rstage = [&]() {

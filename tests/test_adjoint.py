@@ -171,8 +171,10 @@ def test_oracle_adjoint_matches_finite_differences():
 # GPU
 # ---------------------------------------------------------------------------
 @pytest.mark.gpu
-@pytest.mark.parametrize("dims,steps,ckpt", [((20, 18, 16), 7, 3), ((16, 16, 16), 4, 8), ((40, 9, 33), 2, 1)])
+@pytest.mark.parametrize("dims,steps,ckpt", [((20, 18, 16), 7, 3), ((16, 16, 16), 4, 8), ((40, 9, 33), 2, 1),
+                                             ((264, 7, 6), 2, 1)])
 def test_adjoint_f64_matches_oracle(dims, steps, ckpt, gpu_lib):
+    """(264, 7, 6): rows longer than one CTA takes, the segmented x kernel."""
     phi, vel, tgt, sp, dt = adjoint_case(dims)
     eps = 1.5 * sp[0]
     Jw, _, gw, gvw = oracle_adjoint(phi, vel, tgt, sp, dt, steps, eps)
