@@ -49,7 +49,7 @@ void lsm3ddeterminenarrowband_(const R *phi, BOXARG(g), unsigned char *narrow_ba
   int ob[4];
   long long n0 = 0;
   if (!band_build<R>(call, phd, gb, nbd, nbb, ix, iy, iz, *nlo_index, *nhi_index, outer, *nlo_index_outer,
-                     *nhi_index_outer, *width, *width_inner, *level, lo, hi, ob, &n0))
+                     *nhi_index_outer, *width, *width_inner, *level, lo, hi, ob, &n0, new_claims(call, nbb)))
     return;
   // an empty band writes only level 0 (localization3d.f:289-292)
   const int nwrite = n0 > 0 ? *level + 1 : 1;
@@ -76,7 +76,9 @@ void lsm3dmarknarrowbandneighbors_(unsigned char *narrow_band, BOXARG(nb), int *
   std::vector<int> lo(*level + 1), hi(*level + 1);
   get_ints(lo.data(), n_lo, *level + 1);
   get_ints(hi.data(), n_hi, *level + 1);
-  if (!bfs_levels(call, view(nbd, nbb), nbb, ix, iy, iz, *nlo_index, *nhi_index, lo, hi, *level)) return;
+  if (!bfs_levels(call, view(nbd, nbb), nbb, ix, iy, iz, *nlo_index, *nhi_index, lo, hi, *level,
+                  new_claims(call, nbb)))
+    return;
   put_ints(n_lo, lo.data(), *level + 1);
   put_ints(n_hi, hi.data(), *level + 1);
   call.finish();
@@ -107,17 +109,20 @@ void lsm3ddeterminenarrowbandfrommask_(const R *mask, BOXARG(g), unsigned char *
   z.mode = (*use_mask_sign > 0) ? 1 : 2;
   const long long n = gb.size();
   long long tot[3];
-  if (!compact(call, CountOnly<Level0>{z}, n, tot)) return;
+  Compaction c0;
+  if (!c0.count(call, z, n, tot)) return;
   if (tot[0] > cap) {
     set_error(LSMGPU_ERR_CAPACITY, "lsm3ddeterminenarrowbandfrommask_: band exceeds the index arrays");
     return;
   }
-  LSMGPU_LAUNCH(k_mark0, (unsigned)((n + 255) / 256), 256, 0, z, n);
-  if (!compact(call, z, n, tot)) return;
+  LSMGPU_LAUNCH(k_mark0, dim3((unsigned)((gb.n(0) + 31) / 32), (unsigned)((gb.n(1) + 7) / 8), (unsigned)gb.n(2)),
+                dim3(32, 8), 0, z);
+  c0.emit(z);
   std::vector<int> lo(*level + 1, -1), hi(*level + 1, -1);
   lo[0] = *nlo_index;
   hi[0] = (int)(*nlo_index + tot[0] - 1);
-  if (!bfs_levels(call, z.nb, nbb, ix, iy, iz, *nlo_index, *nhi_index, lo, hi, *level)) return;
+  if (!bfs_levels(call, z.nb, nbb, ix, iy, iz, *nlo_index, *nhi_index, lo, hi, *level, new_claims(call, nbb)))
+    return;
   put_ints(n_lo, lo.data(), *level + 1);
   put_ints(n_hi, hi.data(), *level + 1);
   call.finish();

@@ -26,7 +26,7 @@ namespace {
 typedef double R;
 typedef unsigned char U8;
 constexpr int SCAN_BLOCK = 256;
-constexpr int SCAN_ITEMS = 16;  // elements per thread
+constexpr int SCAN_ITEMS = 32;  // elements per thread
 constexpr long long SCAN_TILE = (long long)SCAN_BLOCK * SCAN_ITEMS;
 
 #define BOXARG(b) const int *b##_ilo, const int *b##_ihi, const int *b##_jlo, const int *b##_jhi, const int *b##_klo, const int *b##_khi
@@ -36,31 +36,37 @@ constexpr long long SCAN_TILE = (long long)SCAN_BLOCK * SCAN_ITEMS;
 // A "classifier" F provides  __device__ int flags(long long e) returning bits
 // 0..2 for element e, and __device__ void emit(long long e, int bits,
 // long long r0, long long r1, long long r2) called with each counter's rank.
+// A block takes SCAN_TILE consecutive elements; warp w takes the WARP_SPAN
+// elements from w * WARP_SPAN in SCAN_ITEMS rounds of 32 consecutive elements
+// (coalesced loads), and ranks inside a round come from warp ballots, so the
+// ranks follow element order.
+constexpr int SCAN_WARPS = SCAN_BLOCK / 32;
+constexpr int WARP_SPAN = 32 * SCAN_ITEMS;
+
 template <class F>
-__global__ void k_scan_count(F f, long long n, int *counts) {
-  __shared__ int s[3][SCAN_BLOCK];
-  const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)threadIdx.x * SCAN_ITEMS;
+__global__ void __launch_bounds__(SCAN_BLOCK) k_scan_count(F f, long long n, int *counts) {
+  __shared__ int s[3][SCAN_WARPS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)w * WARP_SPAN + lane;
   int c0 = 0, c1 = 0, c2 = 0;
   for (int q = 0; q < SCAN_ITEMS; q++) {
-    const long long e = base + q;
-    if (e < n) {
-      const int b = f.flags(e);
-      c0 += b & 1;
-      c1 += (b >> 1) & 1;
-      c2 += (b >> 2) & 1;
-    }
+    const long long e = base + 32LL * q;
+    const int b = (e < n) ? f.flags(e) : 0;
+    c0 += __popc(__ballot_sync(0xffffffffu, b & 1));
+    c1 += __popc(__ballot_sync(0xffffffffu, b & 2));
+    c2 += __popc(__ballot_sync(0xffffffffu, b & 4));
   }
-  s[0][threadIdx.x] = c0;
-  s[1][threadIdx.x] = c1;
-  s[2][threadIdx.x] = c2;
+  if (lane == 0) {
+    s[0][w] = c0;
+    s[1][w] = c1;
+    s[2][w] = c2;
+  }
   __syncthreads();
-  for (int st = SCAN_BLOCK / 2; st > 0; st >>= 1) {
-    if ((int)threadIdx.x < st)
-      for (int r = 0; r < 3; r++) s[r][threadIdx.x] += s[r][threadIdx.x + st];
-    __syncthreads();
+  if (threadIdx.x < 3) {
+    int t = 0;
+    for (int u = 0; u < SCAN_WARPS; u++) t += s[threadIdx.x][u];
+    counts[3 * blockIdx.x + threadIdx.x] = t;
   }
-  if (threadIdx.x == 0)
-    for (int r = 0; r < 3; r++) counts[3 * blockIdx.x + r] = s[r][0];
 }
 
 // exclusive scan of the per-block counts (one block; serial chunks per
@@ -94,65 +100,83 @@ __global__ void k_scan_blocks(int *counts, int nblocks, long long *offsets, long
     }
 }
 
+// The classifier's flags are evaluated twice (count pass, rank pass); an
+// emit may change the data a later flags call reads only for elements whose
+// flags it has already been given (the breadth-first classifier marks the
+// cell its winner claimed), so both passes see the same flags.
 template <class F>
-__global__ void k_scan_emit(F f, long long n, const long long *offsets) {
-  __shared__ int s[3][SCAN_BLOCK];
-  const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)threadIdx.x * SCAN_ITEMS;
-  int bits[SCAN_ITEMS];
+__global__ void __launch_bounds__(SCAN_BLOCK) k_scan_emit(F f, long long n, const long long *offsets) {
+  __shared__ int s[3][SCAN_WARPS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)w * WARP_SPAN + lane;
   int c[3] = {0, 0, 0};
   for (int q = 0; q < SCAN_ITEMS; q++) {
-    const long long e = base + q;
-    bits[q] = (e < n) ? f.flags(e) : 0;
-    for (int r = 0; r < 3; r++) c[r] += (bits[q] >> r) & 1;
+    const long long e = base + 32LL * q;
+    const int b = (e < n) ? f.flags(e) : 0;
+#pragma unroll
+    for (int r = 0; r < 3; r++) c[r] += __popc(__ballot_sync(0xffffffffu, (b >> r) & 1));
   }
-  for (int r = 0; r < 3; r++) s[r][threadIdx.x] = c[r];
+  if (lane == 0)
+    for (int r = 0; r < 3; r++) s[r][w] = c[r];
   __syncthreads();
-  // inclusive Hillis-Steele scan over the block's thread totals
-  for (int st = 1; st < SCAN_BLOCK; st <<= 1) {
-    int v[3] = {0, 0, 0};
-    if ((int)threadIdx.x >= st)
-      for (int r = 0; r < 3; r++) v[r] = s[r][threadIdx.x - st];
-    __syncthreads();
-    for (int r = 0; r < 3; r++) s[r][threadIdx.x] += v[r];
-    __syncthreads();
+  long long run[3];
+  for (int r = 0; r < 3; r++) {
+    long long o = offsets[3 * blockIdx.x + r];
+    for (int u = 0; u < w; u++) o += s[r][u];
+    run[r] = o;
   }
-  long long rank[3];
-  for (int r = 0; r < 3; r++) rank[r] = offsets[3 * blockIdx.x + r] + s[r][threadIdx.x] - c[r];
+  const unsigned below = (1u << lane) - 1u;
   for (int q = 0; q < SCAN_ITEMS; q++) {
-    const long long e = base + q;
-    if (e >= n) break;
-    if (bits[q]) f.emit(e, bits[q], rank[0], rank[1], rank[2]);
-    for (int r = 0; r < 3; r++) rank[r] += (bits[q] >> r) & 1;
+    const long long e = base + 32LL * q;
+    const int b = (e < n) ? f.flags(e) : 0;
+    const unsigned m0 = __ballot_sync(0xffffffffu, b & 1);
+    const unsigned m1 = __ballot_sync(0xffffffffu, b & 2);
+    const unsigned m2 = __ballot_sync(0xffffffffu, b & 4);
+    if (b) f.emit(e, b, run[0] + __popc(m0 & below), run[1] + __popc(m1 & below), run[2] + __popc(m2 & below));
+    run[0] += __popc(m0);
+    run[1] += __popc(m1);
+    run[2] += __popc(m2);
   }
 }
 
-// counts only (no emission), for capacity checks before anything is written
-template <class F>
-struct CountOnly {
-  F f;
-  __device__ int flags(long long e) const { return f.flags(e); }
-  __device__ void emit(long long, int, long long, long long, long long) const {}
+// Ordered compaction in two calls: count() runs the per-block counts and the
+// scan and returns the three totals (synchronous, so capacities can be
+// checked before anything is written); emit() then writes every element's
+// ranks using the same offsets.
+struct Compaction {
+  long long n = 0, nb = 0;
+  int *counts = nullptr;
+  long long *offs = nullptr, *tot = nullptr;
+
+  template <class F>
+  bool count(Call &call, F f, long long n_, long long totals_out[3]) {
+    n = n_;
+    nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    totals_out[0] = totals_out[1] = totals_out[2] = 0;
+    if (nb == 0) return true;
+    counts = call.temp<int>(3 * nb);
+    offs = call.temp<long long>(3 * nb);
+    tot = call.temp<long long>(3);
+    if (!call.ok()) return false;
+    LSMGPU_LAUNCH(k_scan_count<F>, (unsigned)nb, SCAN_BLOCK, 0, f, n, counts);
+    LSMGPU_LAUNCH(k_scan_blocks, 1, 1024, 0, counts, (int)nb, offs, tot);
+    return cuda_ok(cudaMemcpyAsync(totals_out, tot, 3 * sizeof(long long), cudaMemcpyDeviceToHost, stream()),
+                   "cudaMemcpyAsync(totals)") &&
+           cuda_ok(cudaStreamSynchronize(stream()), "cudaStreamSynchronize");
+  }
+
+  template <class F>
+  void emit(F f) const {
+    if (nb > 0) LSMGPU_LAUNCH(k_scan_emit<F>, (unsigned)nb, SCAN_BLOCK, 0, f, n, offs);
+  }
 };
 
-// runs the compaction; returns the three totals (synchronous)
+// count + emit in one go; returns the three totals
 template <class F>
 bool compact(Call &call, F f, long long n, long long totals_out[3]) {
-  const long long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
-  if (nb == 0) {
-    totals_out[0] = totals_out[1] = totals_out[2] = 0;
-    return true;
-  }
-  int *counts = call.temp<int>(3 * nb);
-  long long *offs = call.temp<long long>(3 * nb);
-  long long *tot = call.temp<long long>(3);
-  if (!call.ok()) return false;
-  LSMGPU_LAUNCH(k_scan_count<F>, (unsigned)nb, SCAN_BLOCK, 0, f, n, counts);
-  LSMGPU_LAUNCH(k_scan_blocks, 1, 1024, 0, counts, (int)nb, offs, tot);
-  LSMGPU_LAUNCH(k_scan_emit<F>, (unsigned)nb, SCAN_BLOCK, 0, f, n, offs);
-  if (!cuda_ok(cudaMemcpyAsync(totals_out, tot, 3 * sizeof(long long), cudaMemcpyDeviceToHost, stream()),
-               "cudaMemcpyAsync(totals)") ||
-      !cuda_ok(cudaStreamSynchronize(stream()), "cudaStreamSynchronize"))
-    return false;
+  Compaction c;
+  if (!c.count(call, f, n, totals_out)) return false;
+  c.emit(f);
   return true;
 }
 
@@ -174,14 +198,39 @@ struct Level0T {
     j = gb.lo[1] + (int)(r / nx);
     i = gb.lo[0] + (int)(r % nx);
   }
+  // FP32 fields compare in FP32 against thresholds rounded so each decision
+  // equals the FP64 one: for a float a, (double)a < width <=> a <= width_lt
+  // (the largest float below width) and (double)a >= width_inner <=>
+  // a >= inner_ge (the smallest float not below width_inner)
+  float width_lt, inner_ge;
   __device__ int flags(long long e) const {
-    const R v = (R)phi.p[e];
-    if (mode == 1) return v >= R(0) ? 1 : 0;
-    if (mode == 2) return v <= R(0) ? 1 : 0;
-    const R a = fabs(v);
-    if (!(a < width)) return 0;
-    if (a >= width_inner) return v <= R(0) ? 3 : 5;
-    return 1;
+    if constexpr (sizeof(T) == 4) {
+      const float v = (float)phi.p[e];
+      if (mode == 1) return v >= 0.f ? 1 : 0;
+      if (mode == 2) return v <= 0.f ? 1 : 0;
+      const float a = fabsf(v);
+      if (!(a <= width_lt)) return 0;
+      if (a >= inner_ge) return v <= 0.f ? 3 : 5;
+      return 1;
+    } else {
+      const R v = (R)phi.p[e];
+      if (mode == 1) return v >= R(0) ? 1 : 0;
+      if (mode == 2) return v <= R(0) ? 1 : 0;
+      const R a = fabs(v);
+      if (!(a < width)) return 0;
+      if (a >= width_inner) return v <= R(0) ? 3 : 5;
+      return 1;
+    }
+  }
+  void set_widths(double w, double wi) {
+    width = w;
+    width_inner = wi;
+    float f = (float)w;
+    if ((double)f >= w) f = nextafterf(f, -INFINITY);
+    width_lt = f;
+    float g = (float)wi;
+    if ((double)g < wi) g = nextafterf(g, INFINITY);
+    inner_ge = g;
   }
   __device__ void emit(long long e, int bits, long long r0, long long r1, long long r2) const {
     int i, j, k;
@@ -197,21 +246,25 @@ struct Level0T {
 
 typedef Level0T<R> Level0;
 
-// every cell of phi's ghost box gets its level-0 mark (1 in the band, 0 out)
+// every cell of phi's ghost box gets its level-0 mark (1 in the band, 0 out);
+// one thread per cell, x fastest (grid: x in 32s, y in 8s, z per block)
 template <class T>
-__global__ void k_mark0(Level0T<T> z, long long n) {
-  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n) return;
-  int i, j, k;
-  z.cell(e, i, j, k);
-  z.nb(i, j, k) = (z.flags(e) & 1) ? 1 : 0;
+__global__ void k_mark0(Level0T<T> z) {
+  const int i = z.gb.lo[0] + (int)(blockIdx.x * 32 + threadIdx.x);
+  const int j = z.gb.lo[1] + (int)(blockIdx.y * 8 + threadIdx.y);
+  const int k = z.gb.lo[2] + (int)blockIdx.z;
+  if (i > z.gb.hi[0] || j > z.gb.hi[1]) return;
+  z.nb(i, j, k) = (z.flags(z.phi.off(i, j, k)) & 1) ? 1 : 0;
 }
+
+// claim value of an unclaimed cell (a byte pattern, so a memset sets it)
+constexpr int kUnclaimed = 0x7f7f7f7f;
 
 // ---- breadth-first levels --------------------------------------------------------
 struct Bfs {
   View<U8> nb;
   Box nbb;
-  int *claim;             // over the nb box, INT_MAX where unclaimed
+  int *claim;             // over the nb box, kUnclaimed where unclaimed
   int *ix, *iy, *iz;      // list arrays, element 0 = entry nlo_index
   int nlo;                // list base
   int plo;                // first parent entry of this level
@@ -239,6 +292,8 @@ struct Bfs {
     const long long o = cidx(a, b, c);
     return (nb.p[o] == 0 && claim[o] == (int)t) ? 1 : 0;
   }
+  // lists the winner, marks its cell with the level and releases the claim
+  // (a cell has exactly one winner, so only this call changes that cell)
   __device__ void emit(long long t, int, long long r0, long long, long long) const {
     int a, b, c;
     nbr(t, a, b, c);
@@ -246,6 +301,9 @@ struct Bfs {
     ix[pos] = a;
     iy[pos] = b;
     iz[pos] = c;
+    const long long o = cidx(a, b, c);
+    nb.p[o] = mark;
+    claim[o] = kUnclaimed;
   }
 };
 
@@ -258,26 +316,19 @@ __global__ void k_bfs_claim(Bfs f, long long n) {
   if (f.nb.p[o] == 0) atomicMin(&f.claim[o], (int)t);
 }
 
-// after the compaction: mark the new cells and release their claims
-__global__ void k_bfs_mark(Bfs f, long long n) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  int a, b, c;
-  if (!f.nbr(t, a, b, c)) return;
-  const long long o = f.cidx(a, b, c);
-  if (f.nb.p[o] == 0 && f.claim[o] == (int)t) {
-    f.nb.p[o] = f.mark;
-    f.claim[o] = INT_MAX;
-  }
+// claim array over the nb box, every entry kUnclaimed; bfs_levels leaves it so
+int *new_claims(Call &call, const Box &nbb) {
+  int *claim = call.temp<int>(nbb.size());
+  if (call.ok()) cudaMemsetAsync(claim, 0x7f, (size_t)nbb.size() * sizeof(int), stream());
+  return claim;
 }
 
 // Breadth-first levels 1..level from the lists already holding levels
 // 0..(start-1); lo/hi are host copies of n_lo/n_hi, updated in place.
+// `claim` (over the nb box) must hold kUnclaimed everywhere and is returned so.
 bool bfs_levels(Call &call, View<U8> nb, const Box &nbb, int *ix, int *iy, int *iz, int nlo, int nhi,
-                std::vector<int> &lo, std::vector<int> &hi, int level) {
-  int *claim = call.temp<int>(nbb.size());
-  if (!call.ok()) return false;
-  cudaMemsetAsync(claim, 0x7f, (size_t)nbb.size() * sizeof(int), stream());
+                std::vector<int> &lo, std::vector<int> &hi, int level, int *claim) {
+  if (!claim) return false;
   long long count = (long long)hi[0] + 1;
   for (int lv = 1; lv <= level; lv++) {
     // an empty parent level (-1, -1) yields an empty level; the reference
@@ -285,7 +336,7 @@ bool bfs_levels(Call &call, View<U8> nb, const Box &nbb, int *ix, int *iy, int *
     const long long np = (lo[lv - 1] >= 0 && hi[lv - 1] >= lo[lv - 1]) ? (long long)hi[lv - 1] - lo[lv - 1] + 1 : 0;
     long long added = 0;
     if (np > 0) {
-      if (6 * np >= INT_MAX) {
+      if (6 * np >= kUnclaimed) {
         set_error(LSMGPU_ERR_CAPACITY, "narrow band level too large for 32-bit candidate keys");
         return false;
       }
@@ -293,20 +344,16 @@ bool bfs_levels(Call &call, View<U8> nb, const Box &nbb, int *ix, int *iy, int *
       const long long n = 6 * np;
       const unsigned g = (unsigned)((n + 255) / 256);
       LSMGPU_LAUNCH(k_bfs_claim, g, 256, 0, f, n);
-      // the compaction writes list entries count .. count+added-1; check the
-      // capacity against the worst case first
-      if (count + n - 1 > nhi) {
-        // exact count needed: count winners first
-        long long tot[3];
-        if (!compact(call, CountOnly<Bfs>{f}, n, tot)) return false;
-        if (count + tot[0] - 1 > nhi) {
-          set_error(LSMGPU_ERR_CAPACITY, "narrow band lists exceed nhi_index");
-          return false;
-        }
-      }
+      // the compaction writes list entries count .. count+added-1; the
+      // counts are checked against the capacity before anything is written
       long long tot[3];
-      if (!compact(call, f, n, tot)) return false;
-      LSMGPU_LAUNCH(k_bfs_mark, g, 256, 0, f, n);
+      Compaction cw;
+      if (!cw.count(call, f, n, tot)) return false;
+      if (count + tot[0] - 1 > nhi) {
+        set_error(LSMGPU_ERR_CAPACITY, "narrow band lists exceed nhi_index");
+        return false;
+      }
+      cw.emit(f);
       added = tot[0];
     }
     if (added > 0) {
@@ -356,7 +403,8 @@ void put_ints(int *dst, const int *src, int n) {
 template <class T>
 bool band_build(Call &call, const T *phi, const Box &gb, U8 *nbd, const Box &nbb, int *ix, int *iy, int *iz,
                 int nlo, int nhi, int *outer, int nlo_outer, int nhi_outer, double width, double width_inner,
-                int level, std::vector<int> &lo, std::vector<int> &hi, int ob[4], long long *level0_count) {
+                int level, std::vector<int> &lo, std::vector<int> &hi, int ob[4], long long *level0_count,
+                int *claim) {
   const long long cap = (long long)nhi - nlo + 1;
   const long long ocap = (long long)nhi_outer - nlo_outer + 1;
   Level0T<T> z;
@@ -365,8 +413,7 @@ bool band_build(Call &call, const T *phi, const Box &gb, U8 *nbd, const Box &nbb
   z.gb = gb;
   z.nx = gb.n(0);
   z.nxy = gb.n(0) * gb.n(1);
-  z.width = width;
-  z.width_inner = width_inner;
+  z.set_widths(width, width_inner);
   z.ix = ix; z.iy = iy; z.iz = iz;
   z.outer = outer;
   z.nlo = nlo;
@@ -375,14 +422,16 @@ bool band_build(Call &call, const T *phi, const Box &gb, U8 *nbd, const Box &nbb
   z.mode = 0;
   const long long n = gb.size();
   long long tot[3];
-  if (!compact(call, CountOnly<Level0T<T>>{z}, n, tot)) return false;
+  Compaction c0;
+  if (!c0.count(call, z, n, tot)) return false;
   if (tot[0] > cap || tot[1] + tot[2] > ocap) {
     set_error(LSMGPU_ERR_CAPACITY, "narrow band (%lld cells) or outer layer (%lld) exceeds the index arrays", tot[0],
               tot[1] + tot[2]);
     return false;
   }
-  LSMGPU_LAUNCH(k_mark0<T>, (unsigned)((n + 255) / 256), 256, 0, z, n);
-  if (!compact(call, z, n, tot)) return false;
+  LSMGPU_LAUNCH(k_mark0<T>, dim3((unsigned)((gb.n(0) + 31) / 32), (unsigned)((gb.n(1) + 7) / 8), (unsigned)gb.n(2)),
+                dim3(32, 8), 0, z);
+  c0.emit(z);
   lo.assign(level + 1, -1);
   hi.assign(level + 1, -1);
   lo[0] = nlo;
@@ -394,7 +443,7 @@ bool band_build(Call &call, const T *phi, const Box &gb, U8 *nbd, const Box &nbb
     ob[3] = (int)(nlo_outer + tot[1] - 1);
     ob[0] = (int)(nhi_outer - tot[2] + 1);
     ob[1] = nhi_outer;
-    if (!bfs_levels(call, z.nb, nbb, ix, iy, iz, nlo, nhi, lo, hi, level)) return false;
+    if (!bfs_levels(call, z.nb, nbb, ix, iy, iz, nlo, nhi, lo, hi, level, claim)) return false;
   } else {
     hi[0] = nlo;  // localization3d.f:289-292
   }

@@ -201,6 +201,18 @@ __global__ void k_band_stage(BandArgs<R> a) {
   a.out(i, j, k) = rk_update<R>(a.stage, a.phin(i, j, k), us, *a.dt, r);
 }
 
+// phi -> u1, u2 at the listed cells
+template <class R>
+__global__ void k_copy_band(const R *phi, R *u1, R *u2, View<const R> v, const int *ix, const int *iy, const int *iz,
+                            int n) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= n) return;
+  const long long o = v.off(ix[l], iy[l], iz[l]);
+  const R p = phi[o];
+  u1[o] = p;
+  u2[o] = p;
+}
+
 template <class R, bool EXACT>
 int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n, R b_n, R cfl, R gamma, R beta,
         int n_steps, int rebuild_every, double *dt_log, long long *band_log) {
@@ -218,6 +230,7 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
   R *dt = call.temp<R>(1);
   unsigned long long *key = call.temp<unsigned long long>(1);
   double *dtl = dt_log ? call.temp<double>(n_steps) : nullptr;
+  int *claim = new_claims(call, gb);  // reused by every rebuild (left unclaimed)
   if (!call.ok()) return lsmgpu_get_last_error(nullptr, 0);
   cudaStream_t s = stream();
   const int level = 3;
@@ -228,14 +241,19 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
     if (step % rebuild_every == 0) {
       long long c0 = 0;
       if (!band_build<R>(call, phi, gb, nb, gb, ix, iy, iz, 0, (int)(n - 1), outer, 0, (int)(n - 1), (double)gamma,
-                         (double)beta, level, lo, hi, ob, &c0))
+                         (double)beta, level, lo, hi, ob, &c0, claim))
         return lsmgpu_get_last_error(nullptr, 0);
       n0 = (int)c0;
       if (band_log) band_log[nrebuild] = c0;
       nrebuild++;
-      // stage fields hold phi^n off the updated cells
-      cudaMemcpyAsync(u1, phi, n * sizeof(R), cudaMemcpyDeviceToDevice, s);
-      cudaMemcpyAsync(u2, phi, n * sizeof(R), cudaMemcpyDeviceToDevice, s);
+      // stage fields hold phi^n on band levels 1..3 (every cell a level-0
+      // stencil reads); level-0 cells are overwritten by each stage
+      int nlist = 0;
+      for (int lv = 0; lv <= level; lv++)
+        if (hi[lv] + 1 > nlist) nlist = hi[lv] + 1;
+      if (n0 > 0 && nlist > 0)
+        LSMGPU_LAUNCH(k_copy_band<R>, (unsigned)((nlist + 255) / 256), 256, 0, (const R *)phi, u1, u2,
+                      view((const R *)phi, gb), ix, iy, iz, nlist);
     }
     if (n0 == 0) continue;
     BandArgs<R> a{};
