@@ -115,7 +115,8 @@ void lsm3ddeterminenarrowbandfrommask_(const R *mask, BOXARG(g), unsigned char *
     set_error(LSMGPU_ERR_CAPACITY, "lsm3ddeterminenarrowbandfrommask_: band exceeds the index arrays");
     return;
   }
-  LSMGPU_LAUNCH(k_mark0, dim3((unsigned)((gb.n(0) + 31) / 32), (unsigned)((gb.n(1) + 7) / 8), (unsigned)gb.n(2)),
+  LSMGPU_LAUNCH(k_mark0, dim3((unsigned)((gb.n(0) + 31) / 32), (unsigned)((gb.n(1) + 7) / 8),
+                             (unsigned)((gb.n(2) + kMarkZ - 1) / kMarkZ)),
                 dim3(32, 8), 0, z);
   c0.emit(z);
   std::vector<int> lo(*level + 1, -1), hi(*level + 1, -1);

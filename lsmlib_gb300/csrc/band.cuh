@@ -43,15 +43,32 @@ constexpr long long SCAN_TILE = (long long)SCAN_BLOCK * SCAN_ITEMS;
 constexpr int SCAN_WARPS = SCAN_BLOCK / 32;
 constexpr int WARP_SPAN = 32 * SCAN_ITEMS;
 
+// Classifiers split flags(e) into load(e) (the memory read) and
+// classify(value, e); the kernels issue all of a thread's loads before the
+// ballots (a ballot orders the memory operations around it, so loads and
+// ballots interleaved one element at a time would expose each load's
+// latency).
+template <class F>
+__device__ __forceinline__ void load_round(const F &f, long long base, long long n, typename F::V v[SCAN_ITEMS]) {
+#pragma unroll
+  for (int q = 0; q < SCAN_ITEMS; q++) {
+    const long long e = base + 32LL * q;
+    if (e < n) v[q] = f.load(e);
+  }
+}
+
 template <class F>
 __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_count(F f, long long n, int *counts) {
   __shared__ int s[3][SCAN_WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)w * WARP_SPAN + lane;
+  typename F::V v[SCAN_ITEMS];
+  load_round(f, base, n, v);
   int c0 = 0, c1 = 0, c2 = 0;
+#pragma unroll
   for (int q = 0; q < SCAN_ITEMS; q++) {
     const long long e = base + 32LL * q;
-    const int b = (e < n) ? f.flags(e) : 0;
+    const int b = (e < n) ? f.classify(v[q], e) : 0;
     c0 += __popc(__ballot_sync(0xffffffffu, b & 1));
     c1 += __popc(__ballot_sync(0xffffffffu, b & 2));
     c2 += __popc(__ballot_sync(0xffffffffu, b & 4));
@@ -100,21 +117,24 @@ __global__ void k_scan_blocks(int *counts, int nblocks, long long *offsets, long
     }
 }
 
-// The classifier's flags are evaluated twice (count pass, rank pass); an
-// emit may change the data a later flags call reads only for elements whose
-// flags it has already been given (the breadth-first classifier marks the
-// cell its winner claimed), so both passes see the same flags.
+// An emit may change data a classify call reads (the breadth-first
+// classifier marks the cell its winner claimed), but only for a cell whose one
+// winner it is, so every element's flags in this pass equal the count pass's.
 template <class F>
 __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_emit(F f, long long n, const long long *offsets) {
   __shared__ int s[3][SCAN_WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)w * WARP_SPAN + lane;
+  typename F::V v[SCAN_ITEMS];
+  load_round(f, base, n, v);
+  int bits[SCAN_ITEMS];
   int c[3] = {0, 0, 0};
+#pragma unroll
   for (int q = 0; q < SCAN_ITEMS; q++) {
     const long long e = base + 32LL * q;
-    const int b = (e < n) ? f.flags(e) : 0;
+    bits[q] = (e < n) ? f.classify(v[q], e) : 0;
 #pragma unroll
-    for (int r = 0; r < 3; r++) c[r] += __popc(__ballot_sync(0xffffffffu, (b >> r) & 1));
+    for (int r = 0; r < 3; r++) c[r] += __popc(__ballot_sync(0xffffffffu, (bits[q] >> r) & 1));
   }
   if (lane == 0)
     for (int r = 0; r < 3; r++) s[r][w] = c[r];
@@ -126,13 +146,14 @@ __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_emit(F f, long long n, cons
     run[r] = o;
   }
   const unsigned below = (1u << lane) - 1u;
+#pragma unroll
   for (int q = 0; q < SCAN_ITEMS; q++) {
-    const long long e = base + 32LL * q;
-    const int b = (e < n) ? f.flags(e) : 0;
-    const unsigned m0 = __ballot_sync(0xffffffffu, b & 1);
-    const unsigned m1 = __ballot_sync(0xffffffffu, b & 2);
-    const unsigned m2 = __ballot_sync(0xffffffffu, b & 4);
-    if (b) f.emit(e, b, run[0] + __popc(m0 & below), run[1] + __popc(m1 & below), run[2] + __popc(m2 & below));
+    const unsigned m0 = __ballot_sync(0xffffffffu, bits[q] & 1);
+    const unsigned m1 = __ballot_sync(0xffffffffu, bits[q] & 2);
+    const unsigned m2 = __ballot_sync(0xffffffffu, bits[q] & 4);
+    if (bits[q])
+      f.emit(base + 32LL * q, bits[q], run[0] + __popc(m0 & below), run[1] + __popc(m1 & below),
+             run[2] + __popc(m2 & below));
     run[0] += __popc(m0);
     run[1] += __popc(m1);
     run[2] += __popc(m2);
@@ -203,9 +224,12 @@ struct Level0T {
   // (the largest float below width) and (double)a >= width_inner <=>
   // a >= inner_ge (the smallest float not below width_inner)
   float width_lt, inner_ge;
-  __device__ int flags(long long e) const {
+  typedef T V;
+  __device__ T load(long long e) const { return phi.p[e]; }
+  __device__ int flags(long long e) const { return classify(phi.p[e], e); }
+  __device__ int classify(T raw, long long) const {
     if constexpr (sizeof(T) == 4) {
-      const float v = (float)phi.p[e];
+      const float v = (float)raw;
       if (mode == 1) return v >= 0.f ? 1 : 0;
       if (mode == 2) return v <= 0.f ? 1 : 0;
       const float a = fabsf(v);
@@ -213,7 +237,7 @@ struct Level0T {
       if (a >= inner_ge) return v <= 0.f ? 3 : 5;
       return 1;
     } else {
-      const R v = (R)phi.p[e];
+      const R v = (R)raw;
       if (mode == 1) return v >= R(0) ? 1 : 0;
       if (mode == 2) return v <= R(0) ? 1 : 0;
       const R a = fabs(v);
@@ -247,14 +271,21 @@ struct Level0T {
 typedef Level0T<R> Level0;
 
 // every cell of phi's ghost box gets its level-0 mark (1 in the band, 0 out);
-// one thread per cell, x fastest (grid: x in 32s, y in 8s, z per block)
+// threads along x and y, each walking kMarkZ planes
+constexpr int kMarkZ = 16;
 template <class T>
 __global__ void k_mark0(Level0T<T> z) {
   const int i = z.gb.lo[0] + (int)(blockIdx.x * 32 + threadIdx.x);
   const int j = z.gb.lo[1] + (int)(blockIdx.y * 8 + threadIdx.y);
-  const int k = z.gb.lo[2] + (int)blockIdx.z;
+  const int k0 = z.gb.lo[2] + (int)blockIdx.z * kMarkZ;
   if (i > z.gb.hi[0] || j > z.gb.hi[1]) return;
-  z.nb(i, j, k) = (z.flags(z.phi.off(i, j, k)) & 1) ? 1 : 0;
+  T v[kMarkZ];  // all loads before the stores (the arrays may alias for the compiler)
+#pragma unroll
+  for (int q = 0; q < kMarkZ; q++)
+    if (k0 + q <= z.gb.hi[2]) v[q] = z.phi.p[z.phi.off(i, j, k0 + q)];
+#pragma unroll
+  for (int q = 0; q < kMarkZ; q++)
+    if (k0 + q <= z.gb.hi[2]) z.nb(i, j, k0 + q) = (z.classify(v[q], 0) & 1) ? 1 : 0;
 }
 
 // claim value of an unclaimed cell (a byte pattern, so a memset sets it)
@@ -286,6 +317,9 @@ struct Bfs {
     return true;
   }
   __device__ long long cidx(int a, int b, int c) const { return nb.off(a, b, c); }
+  typedef int V;
+  __device__ int load(long long) const { return 0; }
+  __device__ int classify(int, long long t) const { return flags(t); }
   __device__ int flags(long long t) const {
     int a, b, c;
     if (!nbr(t, a, b, c)) return 0;
@@ -429,7 +463,9 @@ bool band_build(Call &call, const T *phi, const Box &gb, U8 *nbd, const Box &nbb
               tot[1] + tot[2]);
     return false;
   }
-  LSMGPU_LAUNCH(k_mark0<T>, dim3((unsigned)((gb.n(0) + 31) / 32), (unsigned)((gb.n(1) + 7) / 8), (unsigned)gb.n(2)),
+  LSMGPU_LAUNCH(k_mark0<T>,
+                dim3((unsigned)((gb.n(0) + 31) / 32), (unsigned)((gb.n(1) + 7) / 8),
+                     (unsigned)((gb.n(2) + kMarkZ - 1) / kMarkZ)),
                 dim3(32, 8), 0, z);
   c0.emit(z);
   lo.assign(level + 1, -1);
