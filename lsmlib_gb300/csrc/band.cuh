@@ -62,16 +62,27 @@ __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_count(F f, long long n, int
   __shared__ int s[3][SCAN_WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)w * WARP_SPAN + lane;
-  typename F::V v[SCAN_ITEMS];
-  load_round(f, base, n, v);
   int c0 = 0, c1 = 0, c2 = 0;
+  if constexpr (F::kPrefetch) {
+    typename F::V v[SCAN_ITEMS];
+    load_round(f, base, n, v);
 #pragma unroll
-  for (int q = 0; q < SCAN_ITEMS; q++) {
-    const long long e = base + 32LL * q;
-    const int b = (e < n) ? f.classify(v[q], e) : 0;
-    c0 += __popc(__ballot_sync(0xffffffffu, b & 1));
-    c1 += __popc(__ballot_sync(0xffffffffu, b & 2));
-    c2 += __popc(__ballot_sync(0xffffffffu, b & 4));
+    for (int q = 0; q < SCAN_ITEMS; q++) {
+      const long long e = base + 32LL * q;
+      const int b = (e < n) ? f.classify(v[q], e) : 0;
+      if (e < n) f.counted(e, b);
+      c0 += __popc(__ballot_sync(0xffffffffu, b & 1));
+      c1 += __popc(__ballot_sync(0xffffffffu, b & 2));
+      c2 += __popc(__ballot_sync(0xffffffffu, b & 4));
+    }
+  } else {
+    for (int q = 0; q < SCAN_ITEMS; q++) {
+      const long long e = base + 32LL * q;
+      const int b = (e < n) ? f.flags(e) : 0;
+      c0 += __popc(__ballot_sync(0xffffffffu, b & 1));
+      c1 += __popc(__ballot_sync(0xffffffffu, b & 2));
+      c2 += __popc(__ballot_sync(0xffffffffu, b & 4));
+    }
   }
   if (lane == 0) {
     s[0][w] = c0;
@@ -125,16 +136,25 @@ __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_emit(F f, long long n, cons
   __shared__ int s[3][SCAN_WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)w * WARP_SPAN + lane;
-  typename F::V v[SCAN_ITEMS];
-  load_round(f, base, n, v);
-  int bits[SCAN_ITEMS];
   int c[3] = {0, 0, 0};
+  int bits[F::kPrefetch ? SCAN_ITEMS : 1];
+  if constexpr (F::kPrefetch) {
+    typename F::V v[SCAN_ITEMS];
+    load_round(f, base, n, v);
 #pragma unroll
-  for (int q = 0; q < SCAN_ITEMS; q++) {
-    const long long e = base + 32LL * q;
-    bits[q] = (e < n) ? f.classify(v[q], e) : 0;
+    for (int q = 0; q < SCAN_ITEMS; q++) {
+      const long long e = base + 32LL * q;
+      bits[q] = (e < n) ? f.classify(v[q], e) : 0;
 #pragma unroll
-    for (int r = 0; r < 3; r++) c[r] += __popc(__ballot_sync(0xffffffffu, (bits[q] >> r) & 1));
+      for (int r = 0; r < 3; r++) c[r] += __popc(__ballot_sync(0xffffffffu, (bits[q] >> r) & 1));
+    }
+  } else {
+    for (int q = 0; q < SCAN_ITEMS; q++) {
+      const long long e = base + 32LL * q;
+      const int b = (e < n) ? f.flags(e) : 0;
+#pragma unroll
+      for (int r = 0; r < 3; r++) c[r] += __popc(__ballot_sync(0xffffffffu, (b >> r) & 1));
+    }
   }
   if (lane == 0)
     for (int r = 0; r < 3; r++) s[r][w] = c[r];
@@ -148,12 +168,14 @@ __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_emit(F f, long long n, cons
   const unsigned below = (1u << lane) - 1u;
 #pragma unroll
   for (int q = 0; q < SCAN_ITEMS; q++) {
-    const unsigned m0 = __ballot_sync(0xffffffffu, bits[q] & 1);
-    const unsigned m1 = __ballot_sync(0xffffffffu, bits[q] & 2);
-    const unsigned m2 = __ballot_sync(0xffffffffu, bits[q] & 4);
-    if (bits[q])
-      f.emit(base + 32LL * q, bits[q], run[0] + __popc(m0 & below), run[1] + __popc(m1 & below),
-             run[2] + __popc(m2 & below));
+    const long long e = base + 32LL * q;
+    int b;
+    if constexpr (F::kPrefetch) b = bits[q];
+    else b = (e < n) ? f.flags(e) : 0;
+    const unsigned m0 = __ballot_sync(0xffffffffu, b & 1);
+    const unsigned m1 = __ballot_sync(0xffffffffu, b & 2);
+    const unsigned m2 = __ballot_sync(0xffffffffu, b & 4);
+    if (b) f.emit(e, b, run[0] + __popc(m0 & below), run[1] + __popc(m1 & below), run[2] + __popc(m2 & below));
     run[0] += __popc(m0);
     run[1] += __popc(m1);
     run[2] += __popc(m2);
@@ -214,6 +236,14 @@ struct Level0T {
   int nlo, nlo_outer, nhi_outer;
   int mode;               // 0: |phi| < width, 1: mask >= 0, 2: mask <= 0
   __device__ void cell(long long e, int &i, int &j, int &k) const {
+    if (nxy * (gb.hi[2] - gb.lo[2] + 1) <= 0x7fffffffLL) {  // 32-bit division when the box allows
+      const unsigned u = (unsigned)e, uxy = (unsigned)nxy, ux = (unsigned)nx;
+      const unsigned kk = u / uxy, r = u - kk * uxy, jj = r / ux;
+      k = gb.lo[2] + (int)kk;
+      j = gb.lo[1] + (int)jj;
+      i = gb.lo[0] + (int)(r - jj * ux);
+      return;
+    }
     k = gb.lo[2] + (int)(e / nxy);
     const long long r = e % nxy;
     j = gb.lo[1] + (int)(r / nx);
@@ -224,6 +254,11 @@ struct Level0T {
   // (the largest float below width) and (double)a >= width_inner <=>
   // a >= inner_ge (the smallest float not below width_inner)
   float width_lt, inner_ge;
+  U8 *mark_lin = nullptr;   // when set (nb box == phi's box): level-0 marks written by the count pass
+  static constexpr bool kPrefetch = true;
+  __device__ void counted(long long e, int bits) const {
+    if (mark_lin) mark_lin[e] = (bits & 1) ? 1 : 0;
+  }
   typedef T V;
   __device__ T load(long long e) const { return phi.p[e]; }
   __device__ int flags(long long e) const { return classify(phi.p[e], e); }
@@ -317,9 +352,11 @@ struct Bfs {
     return true;
   }
   __device__ long long cidx(int a, int b, int c) const { return nb.off(a, b, c); }
+  static constexpr bool kPrefetch = false;  // dependent gathers; the one-pass form keeps registers low
   typedef int V;
   __device__ int load(long long) const { return 0; }
   __device__ int classify(int, long long t) const { return flags(t); }
+  __device__ void counted(long long, int) const {}
   __device__ int flags(long long t) const {
     int a, b, c;
     if (!nbr(t, a, b, c)) return 0;
@@ -438,7 +475,7 @@ template <class T>
 bool band_build(Call &call, const T *phi, const Box &gb, U8 *nbd, const Box &nbb, int *ix, int *iy, int *iz,
                 int nlo, int nhi, int *outer, int nlo_outer, int nhi_outer, double width, double width_inner,
                 int level, std::vector<int> &lo, std::vector<int> &hi, int ob[4], long long *level0_count,
-                int *claim) {
+                int *claim, bool fuse_marks = false) {
   const long long cap = (long long)nhi - nlo + 1;
   const long long ocap = (long long)nhi_outer - nlo_outer + 1;
   Level0T<T> z;
@@ -456,17 +493,25 @@ bool band_build(Call &call, const T *phi, const Box &gb, U8 *nbd, const Box &nbb
   z.mode = 0;
   const long long n = gb.size();
   long long tot[3];
+  // fused marks: the count pass writes every cell's level-0 mark (the nb
+  // array has phi's box); only for callers that own the arrays, since the
+  // marks are then written before the capacity check
+  const bool fused = fuse_marks && nbb.lo[0] == gb.lo[0] && nbb.hi[0] == gb.hi[0] && nbb.lo[1] == gb.lo[1] &&
+                     nbb.hi[1] == gb.hi[1] && nbb.lo[2] == gb.lo[2] && nbb.hi[2] == gb.hi[2];
+  if (fused) z.mark_lin = nbd;
   Compaction c0;
   if (!c0.count(call, z, n, tot)) return false;
+  z.mark_lin = nullptr;
   if (tot[0] > cap || tot[1] + tot[2] > ocap) {
     set_error(LSMGPU_ERR_CAPACITY, "narrow band (%lld cells) or outer layer (%lld) exceeds the index arrays", tot[0],
               tot[1] + tot[2]);
     return false;
   }
-  LSMGPU_LAUNCH(k_mark0<T>,
-                dim3((unsigned)((gb.n(0) + 31) / 32), (unsigned)((gb.n(1) + 7) / 8),
-                     (unsigned)((gb.n(2) + kMarkZ - 1) / kMarkZ)),
-                dim3(32, 8), 0, z);
+  if (!fused)
+    LSMGPU_LAUNCH(k_mark0<T>,
+                  dim3((unsigned)((gb.n(0) + 31) / 32), (unsigned)((gb.n(1) + 7) / 8),
+                       (unsigned)((gb.n(2) + kMarkZ - 1) / kMarkZ)),
+                  dim3(32, 8), 0, z);
   c0.emit(z);
   lo.assign(level + 1, -1);
   hi.assign(level + 1, -1);

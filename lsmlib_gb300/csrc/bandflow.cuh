@@ -241,7 +241,7 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
     if (step % rebuild_every == 0) {
       long long c0 = 0;
       if (!band_build<R>(call, phi, gb, nb, gb, ix, iy, iz, 0, (int)(n - 1), outer, 0, (int)(n - 1), (double)gamma,
-                         (double)beta, level, lo, hi, ob, &c0, claim))
+                         (double)beta, level, lo, hi, ob, &c0, claim, true))
         return lsmgpu_get_last_error(nullptr, 0);
       n0 = (int)c0;
       if (band_log) band_log[nrebuild] = c0;
