@@ -79,14 +79,12 @@ __device__ __forceinline__ R weno_local(R v1, R v2, R v3, R v4, R v5) {
   }
 }
 
-// the RHS of one level-0 cell, before the cut-off; also the cell's H/dx for dt
-template <class R, bool EXACT>
-__device__ __forceinline__ R cell_rhs(const BandArgs<R> &a, int i, int j, int k, R &h_over_dx) {
-  const R *c = a.src.p + a.src.off(i, j, k);
-  const long long s[3] = {1, a.src.s1, a.src.s2};
+// normal speed Vn = a_n - b_n kappa at a level-0 cell: central gradient,
+// |grad phi| with zero_tol clamps, mean curvature
+// (spatial_derivatives3d_local.f.in:825-839, :1251-1272; curvature3d_local.f.in)
+template <class R>
+__device__ __forceinline__ R cell_vn(const BandArgs<R> &a, const R *c, const long long s[3]) {
   const R dx = a.dx;
-  // central gradient, |grad phi| with zero_tol clamps, mean curvature
-  // (spatial_derivatives3d_local.f.in:825-839, :1251-1272; curvature3d_local.f.in)
   const R f = R(0.5) / dx;
   const R g0 = (c[s[0]] - c[-s[0]]) * f, g1 = (c[s[1]] - c[-s[1]]) * f, g2 = (c[s[2]] - c[-s[2]]) * f;
   const R tol = Consts<double>::zero_tol;
@@ -105,9 +103,34 @@ __device__ __forceinline__ R cell_rhs(const BandArgs<R> &a, int i, int j, int k,
   const R yz = (c[s[1] + s[2]] - c[s[1] - s[2]] - c[-s[1] + s[2]] + c[-s[1] - s[2]]) * fxy;
   const R den = mag * mag * mag;
   const R kappa = (den < tol) ? R(0) : curv_numerator(xx, yy, zz, xy, xz, yz, g0, g1, g2) / den;
-  const R vn = a.a_n - a.b_n * kappa;
+  return a.a_n - a.b_n * kappa;
+}
+
+// Godunov normal-velocity term (level_set_evolution3d_local.f.in:236-273) from
+// the WENO5 plus/minus derivatives, and the cell's H/dx
+// (math_utils3d_local.f.in:396-414)
+template <class R>
+__device__ __forceinline__ R godunov_rhs(const BandArgs<R> &a, R vn, const R gp[3], const R gm[3], R &h_over_dx) {
+  const R tol = Consts<double>::zero_tol;
+  const R sq = godunov_normal_sq<R>(vn > R(0), gp, gm);
+  R rhs = R(0);
+  if (fabs(vn) >= tol) rhs = rhs - vn * sqrt(sq);
+  const R dx = a.dx, inv = R(1.0) / dx;
+  const R mx2 = dx * dx;
+  const R cx = rmax(fabs(gp[0]), fabs(gm[0])), cy = rmax(fabs(gp[1]), fabs(gm[1])), cz = rmax(fabs(gp[2]), fabs(gm[2]));
+  const R ng = sqrt(cx * cx + cy * cy + cz * cz + mx2);
+  h_over_dx = (ng > tol) ? fabs(vn) / ng * (cx * inv + cy * inv + cz * inv) : R(-1.0);
+  return rhs;
+}
+
+// the RHS of one level-0 cell, before the cut-off; also the cell's H/dx for dt
+template <class R, bool EXACT>
+__device__ __forceinline__ R cell_rhs(const BandArgs<R> &a, int i, int j, int k, R &h_over_dx) {
+  const R *c = a.src.p + a.src.off(i, j, k);
+  const long long s[3] = {1, a.src.s1, a.src.s2};
+  const R vn = cell_vn<R>(a, c, s);
   // HJ WENO5 plus/minus from the band values of src
-  const R inv = R(1.0) / dx;
+  const R inv = R(1.0) / a.dx;
   R gp[3], gm[3];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
@@ -117,16 +140,34 @@ __device__ __forceinline__ R cell_rhs(const BandArgs<R> &a, int i, int j, int k,
     gp[d] = weno_local<R, EXACT>(v[5], v[4], v[3], v[2], v[1]);
     gm[d] = weno_local<R, EXACT>(v[0], v[1], v[2], v[3], v[4]);
   }
-  // Godunov normal-velocity term (level_set_evolution3d_local.f.in:236-273)
-  const R sq = godunov_normal_sq<R>(vn > R(0), gp, gm);
-  R rhs = R(0);
-  if (fabs(vn) >= tol) rhs = rhs - vn * sqrt(sq);
-  // H/dx of math_utils3d_local.f.in:396-414
-  const R mx2 = dx * dx;
-  const R cx = rmax(fabs(gp[0]), fabs(gm[0])), cy = rmax(fabs(gp[1]), fabs(gm[1])), cz = rmax(fabs(gp[2]), fabs(gm[2]));
-  const R ng = sqrt(cx * cx + cy * cy + cz * cz + mx2);
-  h_over_dx = (ng > tol) ? fabs(vn) / ng * (cx * inv + cy * inv + cz * inv) : R(-1.0);
-  return rhs;
+  return godunov_rhs<R>(a, vn, gp, gm, h_over_dx);
+}
+
+// FP32 RHS of two level-0 cells (padded offsets o0, o1): the six WENO5
+// reconstructions run on the pair in Blackwell's packed FP32x2 arithmetic,
+// both sides of an axis together; curvature and the Godunov term per cell
+static __device__ __forceinline__ float2 cell_rhs_x2(const BandArgs<float> &a, long long o0, long long o1, float2 &hd) {
+  const float *c0 = a.src.p + o0, *c1 = a.src.p + o1;
+  const long long s[3] = {1, a.src.s1, a.src.s2};
+  const float vn0 = cell_vn<float>(a, c0, s), vn1 = cell_vn<float>(a, c1, s);
+  const float2 inv = fused::sp(1.0f / a.dx);
+  float gp0[3], gm0[3], gp1[3], gm1[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    float2 v[6];
+#pragma unroll
+    for (int q = -2; q <= 3; q++)
+      v[q + 2] = fused::mul2(make_float2(c0[q * s[d]] - c0[(q - 1) * s[d]], c1[q * s[d]] - c1[(q - 1) * s[d]]), inv);
+    float2 p, m;
+    fused::weno5_pm_x2(v, p, m);
+    gp0[d] = p.x; gp1[d] = p.y;
+    gm0[d] = m.x; gm1[d] = m.y;
+  }
+  float h0, h1;
+  const float r0 = godunov_rhs<float>(a, vn0, gp0, gm0, h0);
+  const float r1 = godunov_rhs<float>(a, vn1, gp1, gm1, h1);
+  hd = make_float2(h0, h1);
+  return make_float2(r0, r1);
 }
 
 // cubic cut-off between beta and gamma (localization3d.f:527-553)
@@ -201,6 +242,43 @@ __global__ void k_band_stage(BandArgs<R> a) {
   a.out(i, j, k) = rk_update<R>(a.stage, a.phin(i, j, k), us, *a.dt, r);
 }
 
+// FP32 forms of k_band_rhs and k_band_stage on pairs of consecutive list
+// entries (the second of an odd tail repeats the first and is not written)
+static __global__ void k_band_rhs_x2(BandArgs<float> a) {
+  const int l0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  double h = -1.0e308;
+  if (l0 < a.n0) {
+    const bool two = l0 + 1 < a.n0;
+    const int l1 = two ? l0 + 1 : l0;
+    const long long o0 = a.src.off(a.ix[l0], a.iy[l0], a.iz[l0]), o1 = a.src.off(a.ix[l1], a.iy[l1], a.iz[l1]);
+    float2 hd;
+    const float2 r = cell_rhs_x2(a, o0, o1, hd);
+    h = (double)hd.x;
+    a.rhs[l0] = cutoff<float>(r.x, a.src.p[o0], a.beta, a.gamma);
+    if (two) {
+      h = fmax(h, (double)hd.y);
+      a.rhs[l1] = cutoff<float>(r.y, a.src.p[o1], a.beta, a.gamma);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(a.key, okey(h));
+}
+
+static __global__ void k_band_stage_x2(BandArgs<float> a) {
+  const int l0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (l0 >= a.n0) return;
+  const bool two = l0 + 1 < a.n0;
+  const int l1 = two ? l0 + 1 : l0;
+  const long long o0 = a.src.off(a.ix[l0], a.iy[l0], a.iz[l0]), o1 = a.src.off(a.ix[l1], a.iy[l1], a.iz[l1]);
+  float2 hd;
+  const float2 r = cell_rhs_x2(a, o0, o1, hd);
+  const float dt = *a.dt;
+  const float us0 = a.src.p[o0], us1 = a.src.p[o1];
+  const float n0v = a.phin.p[o0], n1v = a.phin.p[o1];
+  a.out.p[o0] = rk_update<float>(a.stage, n0v, us0, dt, cutoff<float>(r.x, us0, a.beta, a.gamma));
+  if (two) a.out.p[o1] = rk_update<float>(a.stage, n1v, us1, dt, cutoff<float>(r.y, us1, a.beta, a.gamma));
+}
+
 // phi -> u1, u2 at the listed cells
 template <class R>
 __global__ void k_copy_band(const R *phi, R *u1, R *u2, View<const R> v, const int *ix, const int *iy, const int *iz,
@@ -264,13 +342,16 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
     a.dt = dt;
     a.key = key;
     const unsigned blocks = (unsigned)((n0 + 127) / 128);
+    const unsigned blocks2 = (unsigned)((n0 + 255) / 256);  // pairs of entries
+    constexpr bool packed = !EXACT && sizeof(R) == 4;
     // stage 1
     a.src = view((const R *)phi, gb);
     a.phin = a.src;
     a.out = view(u1, gb);
     a.stage = 1;
     cudaMemsetAsync(key, 0, sizeof(unsigned long long), s);
-    LSMGPU_LAUNCH((k_band_rhs<R, EXACT>), blocks, 128, 0, a);
+    if constexpr (packed) LSMGPU_LAUNCH(k_band_rhs_x2, blocks2, 128, 0, a);
+    else LSMGPU_LAUNCH((k_band_rhs<R, EXACT>), blocks, 128, 0, a);
     LSMGPU_LAUNCH(k_band_dt<R>, 1, 1, 0, key, dt, cfl, dtl ? dtl + step : nullptr);
     LSMGPU_LAUNCH(k_band_update1<R>, blocks, 128, 0, a);
     // stage 2
@@ -278,12 +359,14 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
     a.out = view(u2, gb);
     a.phin = view((const R *)phi, gb);
     a.stage = 2;
-    LSMGPU_LAUNCH((k_band_stage<R, EXACT>), blocks, 128, 0, a);
+    if constexpr (packed) LSMGPU_LAUNCH(k_band_stage_x2, blocks2, 128, 0, a);
+    else LSMGPU_LAUNCH((k_band_stage<R, EXACT>), blocks, 128, 0, a);
     // stage 3 (in place on phi: each cell reads only its own phi^n)
     a.src = view((const R *)u2, gb);
     a.out = view(phi, gb);
     a.stage = 3;
-    LSMGPU_LAUNCH((k_band_stage<R, EXACT>), blocks, 128, 0, a);
+    if constexpr (packed) LSMGPU_LAUNCH(k_band_stage_x2, blocks2, 128, 0, a);
+    else LSMGPU_LAUNCH((k_band_stage<R, EXACT>), blocks, 128, 0, a);
   }
   if (dt_log) cudaMemcpyAsync(dt_log, dtl, sizeof(double) * n_steps, cudaMemcpyDeviceToHost, s);
   call.finish();

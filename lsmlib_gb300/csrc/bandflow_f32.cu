@@ -1,5 +1,5 @@
-// FP32 form of the fused narrow-band curvature flow (fast WENO weights);
-// the band's distance test runs in FP64.
+// FP32 form of the fused narrow-band curvature flow (fast WENO weights on
+// packed cell pairs); the band's distance test gives the FP64 decisions.
 #include "bandflow.cuh"
 
 extern "C" int lsmgpu_band_flow_weno5_tvdrk3_f32(float *phi, const int *gb, const int *fb, float dx, float a_n,
