@@ -646,7 +646,7 @@ def sub_batched(stream, dev, n_grids=4096, steps=30):
 
 def sub_adjoint(stream, dev, n=192, steps=40, ckpt=8):
     """Gradient of J = sum (H(phi_T) - H(phi_target))^2 dx^3 after 40 periodic
-    advection steps at 192^3 (adjoint_case), FP32 state, FP64 objective,
+    advection steps at 192^3 (adjoint_case), FP32 state, FP64 objective sum,
     checkpoint every 8 steps with recomputation: objective-only time, full
     gradient time, and the cost of one reverse step (recomputation included)
     against one forward step."""
@@ -664,7 +664,7 @@ def sub_adjoint(stream, dev, n=192, steps=40, ckpt=8):
     t_f = min(_timed(lambda: run(False), stream) for _ in range(3))
     t_g = min(_timed(lambda: run(True), stream) for _ in range(3))
     return {"workload": "adjoint-192: 40 advection steps, sphere r=0.4, velocity field + N(0,0.05) (seed 3), "
-                        "J with H_eps (eps=1.5dx), checkpoint every 8, FP32 state / FP64 objective",
+                        "J with H_eps (eps=1.5dx), checkpoint every 8, FP32 state / FP64 objective accumulation",
             "objective_ms": t_f, "gradient_ms": t_g, "forward_step_ms": t_f / steps,
             "reverse_step_ms": (t_g - t_f) / steps, "reverse_to_forward_step": (t_g - t_f) / t_f}
 

@@ -178,7 +178,7 @@ int lsmgpu_advect_adjoint_weno5_tvdrk3_f64(const double *phi, const int *gb, con
                                            double dz, double dt, int n_steps, int checkpoint_every,
                                            double heaviside_eps, double *J, double *grad_phi,
                                            double *grad_vel_x, double *grad_vel_y, double *grad_vel_z);
-/* FP32 state and adjoint fields; FP64 objective. */
+/* FP32 state and adjoint fields; H and delta of the objective evaluated in FP32, its sum in FP64. */
 int lsmgpu_advect_adjoint_weno5_tvdrk3_f32(const float *phi, const int *gb, const int *fb,
                                            const float *vel_x, const float *vel_y, const float *vel_z,
                                            const int *vel_gb, const float *phi_target, float dx, float dy,

@@ -679,6 +679,18 @@ static __device__ __forceinline__ double delta_fn(double x, double eps) {
 
 constexpr int kObjThreads = 256;
 
+// FP32 forms of H and delta for FP32 states (the sums stay FP64)
+static __device__ __forceinline__ float heaviside_f(float x, float eps) {
+  if (x < -eps) return 0.f;
+  if (x > eps) return 1.f;
+  return 0.5f * (1.f + x / eps + (1.f / 3.14159265358979f) * sinf(3.14159265358979f * x / eps));
+}
+static __device__ __forceinline__ float delta_f(float x, float eps) {
+  if (x < -eps) return 0.f;
+  if (x > eps) return 0.f;
+  return 0.5f / eps * (1.f + cosf(3.14159265358979f * x / eps));
+}
+
 template <class R>
 __global__ void __launch_bounds__(kObjThreads) k_objective(const R *phiT, const R *tgt, Layout L, double eps,
                                                            double vol, R *lam, double *partial) {
@@ -690,10 +702,20 @@ __global__ void __launch_bounds__(kObjThreads) k_objective(const R *phiT, const 
     const int j = (int)((e / L.nx) % L.ny);
     const int k = (int)(e / ((long long)L.nx * L.ny));
     const long long c = L.idx(i, j, k);
-    const double p = (double)phiT[c];
-    const double h = heaviside(p, eps) - heaviside((double)tgt[c], eps);
+    double h, dl;
+    if constexpr (sizeof(R) == 4) {
+      // FP32 state: H and delta in FP32 (FP64 sin/cos would dominate the
+      // forward pass on this GPU), h^2 and the sum in FP64
+      const float p = (float)phiT[c], ef = (float)eps;
+      h = (double)(heaviside_f(p, ef) - heaviside_f((float)tgt[c], ef));
+      dl = (double)delta_f(p, ef);
+    } else {
+      const double p = (double)phiT[c];
+      h = heaviside(p, eps) - heaviside((double)tgt[c], eps);
+      dl = delta_fn(p, eps);
+    }
     h2 = h * h;
-    if (lam) lam[c] = (R)(2.0 * h * delta_fn(p, eps) * vol);
+    if (lam) lam[c] = (R)(2.0 * h * dl * vol);
   }
   for (int o = 16; o > 0; o >>= 1) h2 += __shfl_xor_sync(0xffffffffu, h2, o);
   __shared__ double ws[kObjThreads / 32];

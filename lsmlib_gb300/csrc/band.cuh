@@ -132,7 +132,10 @@ __global__ void k_scan_blocks(int *counts, int nblocks, long long *offsets, long
 // classifier marks the cell its winner claimed), but only for a cell whose one
 // winner it is, so every element's flags in this pass equal the count pass's.
 template <class F>
-__global__ void __launch_bounds__(SCAN_BLOCK) k_scan_emit(F f, long long n, const long long *offsets) {
+__global__ void __launch_bounds__(SCAN_BLOCK) k_scan_emit(F f, long long n, const long long *offsets,
+                                                           const int *counts) {
+  // a tile the count pass found empty has nothing to emit
+  if ((counts[3 * blockIdx.x] | counts[3 * blockIdx.x + 1] | counts[3 * blockIdx.x + 2]) == 0) return;
   __shared__ int s[3][SCAN_WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)w * WARP_SPAN + lane;
@@ -210,7 +213,7 @@ struct Compaction {
 
   template <class F>
   void emit(F f) const {
-    if (nb > 0) LSMGPU_LAUNCH(k_scan_emit<F>, (unsigned)nb, SCAN_BLOCK, 0, f, n, offs);
+    if (nb > 0) LSMGPU_LAUNCH(k_scan_emit<F>, (unsigned)nb, SCAN_BLOCK, 0, f, n, offs, counts);
   }
 };
 
