@@ -260,44 +260,44 @@ __device__ __forceinline__ float pow2_recip(float x) {
 __device__ __forceinline__ float2 pow2_recip2(float2 x) { return make_float2(pow2_recip(x.x), pow2_recip(x.y)); }
 
 // WENO5-JS on two cells at once, the epsilon-scaled weight form of
-// weno5_fast with the common factors folded: smoothness and epsilon are both
-// scaled by 12 (only S/eps enters the weights) and the candidate stencils by
-// 6 (divided out with the normalisation).
+// weno5_fast with the common factors folded: only S/eps enters the weights,
+// so the smoothness indicators are kept as 4 S and epsilon as 12 eps (the
+// factor 3 goes into the scale), and the weights as 10 d_k prod q_j^2.
 __device__ __forceinline__ float2 weno5_x2(float2 v1, float2 v2, float2 v3, float2 v4, float2 v5) {
   const float2 q1s = mul2(v1, v1), q2s = mul2(v2, v2), q3s = mul2(v3, v3), q4s = mul2(v4, v4), q5s = mul2(v5, v5);
   float2 m;
   m.x = fmaxf(fmaxf(fmaxf(q1s.x, q2s.x), fmaxf(q3s.x, q4s.x)), q5s.x);
   m.y = fmaxf(fmaxf(fmaxf(q1s.y, q2s.y), fmaxf(q3s.y, q4s.y)), q5s.y);
-  const float2 eps = fma2(sp(12e-6f), m, sp(12e-36f));
-  // 6 * candidate stencils
-  const float2 P1 = fma2(sp(2.f), v1, fma2(sp(-7.f), v2, mul2(sp(11.f), v3)));
-  const float2 P2 = fma2(sp(-1.f), v2, fma2(sp(5.f), v3, mul2(sp(2.f), v4)));
-  const float2 P3 = fma2(sp(2.f), v3, fma2(sp(5.f), v4, mul2(sp(-1.f), v5)));
-  // 12 * smoothness indicators: 13 t^2 + 3 u^2
+  const float2 eps = fma2(sp(12e-6f), m, sp(12e-36f));  // 12 eps
+  const float c13 = 1.f / 3.f, c76 = 7.f / 6.f, c116 = 11.f / 6.f, c16 = 1.f / 6.f, c56 = 5.f / 6.f;
+  const float2 P1 = fma2(sp(c13), v1, fma2(sp(-c76), v2, mul2(sp(c116), v3)));
+  const float2 P2 = fma2(sp(-c16), v2, fma2(sp(c56), v3, mul2(sp(c13), v4)));
+  const float2 P3 = fma2(sp(c13), v3, fma2(sp(c56), v4, mul2(sp(-c16), v5)));
+  // 4 * smoothness indicators: 13/3 t^2 + u^2
+  const float c133 = 13.f / 3.f;
   float2 t = fma2(sp(-2.f), v2, add2(v1, v3));
   float2 u = fma2(sp(-4.f), v2, fma2(sp(3.f), v3, v1));
-  const float2 S1 = fma2(mul2(sp(13.f), t), t, mul2(mul2(sp(3.f), u), u));
+  const float2 S1 = fma2(u, u, mul2(mul2(sp(c133), t), t));
   t = fma2(sp(-2.f), v3, add2(v2, v4));
   u = fma2(sp(-1.f), v4, v2);
-  const float2 S2 = fma2(mul2(sp(13.f), t), t, mul2(mul2(sp(3.f), u), u));
+  const float2 S2 = fma2(u, u, mul2(mul2(sp(c133), t), t));
   t = fma2(sp(-2.f), v4, add2(v3, v5));
   u = fma2(sp(-4.f), v4, fma2(sp(3.f), v3, v5));
-  const float2 S3 = fma2(mul2(sp(13.f), t), t, mul2(mul2(sp(3.f), u), u));
+  const float2 S3 = fma2(u, u, mul2(mul2(sp(c133), t), t));
   // q_k = (S_k + eps) 2^-e with 2^e <= eps < 2^(e+1): the weights only see
   // ratios of the q_k, so any common scale of S + eps gives the same weights
   // as (S_k / eps + 1); with eps 2^-e in [1, 2), 1 <= q_k < 7e7 and the
-  // products below stay under 3e30
+  // products below stay under 1e32
   const float2 r = pow2_recip2(eps);
-  const float2 e = mul2(eps, r);
-  float2 w1 = fma2(S1, r, e), w2 = fma2(S2, r, e), w3 = fma2(S3, r, e);
-  w1 = mul2(w1, w1);
-  w2 = mul2(w2, w2);
-  w3 = mul2(w3, w3);
-  const float2 n1 = mul2(sp(0.1f), mul2(w2, w3));
-  const float2 n2 = mul2(sp(0.6f), mul2(w1, w3));
-  const float2 n3 = mul2(sp(0.3f), mul2(w1, w2));
+  const float2 e = mul2(eps, r), r3 = mul2(sp(3.f), r);
+  const float2 q1 = fma2(S1, r3, e), q2 = fma2(S2, r3, e), q3 = fma2(S3, r3, e);
+  const float2 q23 = mul2(q2, q3), q13 = mul2(q1, q3), q12 = mul2(q1, q2);
+  // 10 d_k prod_{j != k} q_j^2 (the common factor cancels)
+  const float2 n1 = mul2(q23, q23);
+  const float2 n2 = mul2(mul2(sp(6.f), q13), q13);
+  const float2 n3 = mul2(mul2(sp(3.f), q12), q12);
   const float2 num = fma2(n1, P1, fma2(n2, P2, mul2(n3, P3)));
-  const float2 den = mul2(sp(6.f), add2(add2(n1, n2), n3));
+  const float2 den = add2(add2(n1, n2), n3);
   return make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
 }
 
@@ -313,15 +313,18 @@ __device__ __forceinline__ void weno5_pm_x2(const float2 D[6], float2 &gp, float
   for (int i = 0; i < 6; i++) sq[i] = mul2(D[i], D[i]);
   const float cx = fmaxf(fmaxf(sq[1].x, sq[2].x), fmaxf(sq[3].x, sq[4].x));
   const float cy = fmaxf(fmaxf(sq[1].y, sq[2].y), fmaxf(sq[3].y, sq[4].y));
+  // 12 eps of each side, its power-of-two scale r and 12 eps r in [1, 2)
   const float2 em = fma2(sp(12e-6f), make_float2(fmaxf(cx, sq[0].x), fmaxf(cy, sq[0].y)), sp(12e-36f));
   const float2 ep = fma2(sp(12e-6f), make_float2(fmaxf(cx, sq[5].x), fmaxf(cy, sq[5].y)), sp(12e-36f));
   const float2 rm = pow2_recip2(em), rp = pow2_recip2(ep);
   const float2 emr = mul2(em, rm), epr = mul2(ep, rp);
-  // 6 * candidate stencils
-  const float2 P1m = fma2(sp(2.f), D[0], fma2(sp(-7.f), D[1], mul2(sp(11.f), D[2])));
-  const float2 A = fma2(sp(-1.f), D[1], fma2(sp(5.f), D[2], mul2(sp(2.f), D[3])));  // minus P2, plus P3
-  const float2 B = fma2(sp(2.f), D[2], fma2(sp(5.f), D[3], mul2(sp(-1.f), D[4])));  // minus P3, plus P2
-  const float2 P1p = fma2(sp(2.f), D[5], fma2(sp(-7.f), D[4], mul2(sp(11.f), D[3])));
+  const float2 rm3 = mul2(sp(3.f), rm), rp3 = mul2(sp(3.f), rp);
+  // candidate stencils
+  const float c13 = 1.f / 3.f, c76 = 7.f / 6.f, c116 = 11.f / 6.f, c16 = 1.f / 6.f, c56 = 5.f / 6.f;
+  const float2 P1m = fma2(sp(c13), D[0], fma2(sp(-c76), D[1], mul2(sp(c116), D[2])));
+  const float2 A = fma2(sp(-c16), D[1], fma2(sp(c56), D[2], mul2(sp(c13), D[3])));  // minus p2, plus p3
+  const float2 B = fma2(sp(c13), D[2], fma2(sp(c56), D[3], mul2(sp(-c16), D[4])));  // minus p3, plus p2
+  const float2 P1p = fma2(sp(c13), D[5], fma2(sp(-c76), D[4], mul2(sp(c116), D[3])));
   // second differences t and the asymmetric parts u of the indicators
   const float2 t1m = fma2(sp(-2.f), D[1], add2(D[0], D[2]));
   const float2 t2 = fma2(sp(-2.f), D[2], add2(D[1], D[3]));  // minus t2, plus t3
@@ -333,22 +336,24 @@ __device__ __forceinline__ void weno5_pm_x2(const float2 D[6], float2 &gp, float
   const float2 u1p = fma2(sp(-4.f), D[4], fma2(sp(3.f), D[3], D[5]));
   const float2 u2p = fma2(sp(-1.f), D[2], D[4]);
   const float2 u3p = fma2(sp(-4.f), D[2], fma2(sp(3.f), D[3], D[1]));
-  // 12 * smoothness indicators: 13 t^2 + 3 u^2
-  const float2 T1m = mul2(mul2(sp(13.f), t1m), t1m), T2 = mul2(mul2(sp(13.f), t2), t2);
-  const float2 T3 = mul2(mul2(sp(13.f), t3), t3), T1p = mul2(mul2(sp(13.f), t1p), t1p);
-  const float2 q1m = fma2(fma2(mul2(sp(3.f), u1m), u1m, T1m), rm, emr);
-  const float2 q2m = fma2(fma2(mul2(sp(3.f), u2m), u2m, T2), rm, emr);
-  const float2 q3m = fma2(fma2(mul2(sp(3.f), u3m), u3m, T3), rm, emr);
-  const float2 q1p = fma2(fma2(mul2(sp(3.f), u1p), u1p, T1p), rp, epr);
-  const float2 q2p = fma2(fma2(mul2(sp(3.f), u2p), u2p, T3), rp, epr);
-  const float2 q3p = fma2(fma2(mul2(sp(3.f), u3p), u3p, T2), rp, epr);
-  auto combine = [](float2 q1, float2 q2, float2 q3, float2 P1, float2 P2, float2 P3) {
+  // 4 * smoothness indicators, 13/3 t^2 + u^2 (times 3 r below gives 12 S r)
+  const float c133 = 13.f / 3.f;
+  const float2 T1m = mul2(mul2(sp(c133), t1m), t1m), T2 = mul2(mul2(sp(c133), t2), t2);
+  const float2 T3 = mul2(mul2(sp(c133), t3), t3), T1p = mul2(mul2(sp(c133), t1p), t1p);
+  const float2 q1m = fma2(fma2(u1m, u1m, T1m), rm3, emr);
+  const float2 q2m = fma2(fma2(u2m, u2m, T2), rm3, emr);
+  const float2 q3m = fma2(fma2(u3m, u3m, T3), rm3, emr);
+  const float2 q1p = fma2(fma2(u1p, u1p, T1p), rp3, epr);
+  const float2 q2p = fma2(fma2(u2p, u2p, T3), rp3, epr);
+  const float2 q3p = fma2(fma2(u3p, u3p, T2), rp3, epr);
+  // weights 10 d_k prod_{j != k} q_j^2 (the common factor cancels)
+  auto combine = [](float2 q1, float2 q2, float2 q3, float2 p1, float2 p2, float2 p3) {
     const float2 q23 = mul2(q2, q3), q13 = mul2(q1, q3), q12 = mul2(q1, q2);
-    const float2 n1 = mul2(mul2(sp(0.1f), q23), q23);
-    const float2 n2 = mul2(mul2(sp(0.6f), q13), q13);
-    const float2 n3 = mul2(mul2(sp(0.3f), q12), q12);
-    const float2 num = fma2(n1, P1, fma2(n2, P2, mul2(n3, P3)));
-    const float2 den = mul2(sp(6.f), add2(add2(n1, n2), n3));
+    const float2 n1 = mul2(q23, q23);
+    const float2 n2 = mul2(mul2(sp(6.f), q13), q13);
+    const float2 n3 = mul2(mul2(sp(3.f), q12), q12);
+    const float2 num = fma2(n1, p1, fma2(n2, p2, mul2(n3, p3)));
+    const float2 den = add2(add2(n1, n2), n3);  // <= 1e32 < 2^126
     return make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
   };
   gm = combine(q1m, q2m, q3m, P1m, A, B);
@@ -380,10 +385,11 @@ __device__ __forceinline__ void f32_tile(const float *tile, const StageArgs<floa
       float gp0[3], gp1[3], gm0[3], gm1[3];
 #pragma unroll
       for (int d = 0; d < 3; d++) {
-        float2 v[6];  // scaled D1(c-2 .. c+3) for both cells
+        float2 a7[7], v[6];  // phi / dx at c-3 .. c+3; scaled D1(c-2 .. c+3) for both cells
 #pragma unroll
-        for (int f = -2; f <= 3; f++)
-          v[f + 2] = mul2(make_float2(c0[f * st[d]] - c0[(f - 1) * st[d]], c1[f * st[d]] - c1[(f - 1) * st[d]]), inv[d]);
+        for (int q = -3; q <= 3; q++) a7[q + 3] = mul2(make_float2(c0[q * st[d]], c1[q * st[d]]), inv[d]);
+#pragma unroll
+        for (int f = 0; f < 6; f++) v[f] = fma2(sp(-1.f), a7[f], a7[f + 1]);
         float2 p, m;
         weno5_pm_x2(v, p, m);
         gp0[d] = p.x; gp1[d] = p.y;
@@ -407,11 +413,11 @@ __device__ __forceinline__ void f32_tile(const float *tile, const StageArgs<floa
         // stencil D1(c+3..c-1) otherwise (spatial_derivatives3d.f.in:2756-2812);
         // the six differences are loaded at fixed offsets and the lane's
         // stencil is selected in registers
-        float2 D[6];
+        float2 a7[7], D[6];
 #pragma unroll
-        for (int f = -2; f <= 3; f++)
-          D[f + 2] = mul2(make_float2(c0[f * st[d]] - c0[(f - 1) * st[d]], c1[f * st[d]] - c1[(f - 1) * st[d]]),
-                          inv[d]);
+        for (int q = -3; q <= 3; q++) a7[q + 3] = mul2(make_float2(c0[q * st[d]], c1[q * st[d]]), inv[d]);
+#pragma unroll
+        for (int f = 0; f < 6; f++) D[f] = fma2(sp(-1.f), a7[f], a7[f + 1]);
         const bool b0 = vel0[d] > 0.f, b1 = vel1[d] > 0.f;
         float2 v[5];
 #pragma unroll
