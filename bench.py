@@ -423,7 +423,9 @@ def gpu_arm(args, world, rank, local):
                 "frac": achieved / peak, "traffic": MEASURED_STAGE_TRAFFIC,
                 "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one stage-2 launch "
                                 "(algorithmic 268.4 MB for that stage; achieved uses the 3-stage mean, 14.67 B/cell)",
-                "kernel": "k_stage<float, REINIT> (fused WENO5 + reinit RHS + TVD-RK3 stage)",
+                "kernel": "k_stage_f32<REINIT> (fused WENO5 + reinit RHS + TVD-RK3 stage, packed FP32x2)",
+                "note": "the kernel is bound by the FP32 FMA pipe, not by DRAM (ncu: sm__pipe_fma_cycles_active "
+                        "74%, DRAM traffic 1.06x algorithmic); see profiles/k_stage_reinit_f32_256.md",
                 "stage_ms": stage_ms, "peak_source": peak_kind}
 
     # end to end through the C ABI with host (pinned) buffers

@@ -151,7 +151,7 @@ __device__ __forceinline__ R weno5_adj(const R v[5], R dv[5]) {
 static __device__ __forceinline__ float lin_slots_f32(const float a[7], float kap, bool minus, float mu, float dt,
                                                       float inv, float G[6]) {
   const float c13 = 1.f / 3.f, c76 = 7.f / 6.f, c116 = 11.f / 6.f, c16 = 1.f / 6.f, c56 = 5.f / 6.f;
-  const float c1312 = 13.f / 12.f, c136 = 13.f / 6.f;
+  const float c136 = 13.f / 6.f;
   float D[6];
 #pragma unroll
   for (int f = 0; f < 6; f++) D[f] = (a[f + 1] - a[f]) * inv;
@@ -168,19 +168,26 @@ static __device__ __forceinline__ float lin_slots_f32(const float a[7], float ka
     m = take ? sq : m;
   }
   const float v1 = v[0], v2 = v[1], v3 = v[2], v4 = v[3], v5 = v[4];
-  const float r = __fdividef(1.f, fmaf(1e-6f, m, 1e-36f));
+  // q_k = (S_k + eps) r with r = 2^-e, 2^e <= eps < 2^(e+1) (exponent bits,
+  // no reciprocal): the weights see only ratios of the q_k, and
+  // 1/(S_k + eps) = r / q_k; S_k is kept as 4 S_k = 13/3 t^2 + u^2
+  const float eps = fmaf(1e-6f, m, 1e-36f);
+  const float r = fused::pow2_recip(eps);
+  const float e = eps * r, r4 = 0.25f * r;
   const float p1 = fmaf(c13, v1, fmaf(-c76, v2, c116 * v3));
   const float p2 = fmaf(-c16, v2, fmaf(c56, v3, c13 * v4));
   const float p3 = fmaf(c13, v3, fmaf(c56, v4, -c16 * v5));
   const float t1 = fmaf(-2.f, v2, v1 + v3), u1 = fmaf(-4.f, v2, fmaf(3.f, v3, v1));
   const float t2 = fmaf(-2.f, v3, v2 + v4), u2 = v2 - v4;
   const float t3 = fmaf(-2.f, v4, v3 + v5), u3 = fmaf(-4.f, v4, fmaf(3.f, v3, v5));
-  const float q1 = fmaf(fmaf(c1312 * t1, t1, 0.25f * u1 * u1), r, 1.f);
-  const float q2 = fmaf(fmaf(c1312 * t2, t2, 0.25f * u2 * u2), r, 1.f);
-  const float q3 = fmaf(fmaf(c1312 * t3, t3, 0.25f * u3 * u3), r, 1.f);
+  const float c133 = 13.f / 3.f;
+  const float q1 = fmaf(fmaf(u1, u1, c133 * t1 * t1), r4, e);
+  const float q2 = fmaf(fmaf(u2, u2, c133 * t2 * t2), r4, e);
+  const float q3 = fmaf(fmaf(u3, u3, c133 * t3 * t3), r4, e);
   const float q12 = q1 * q2, q13 = q1 * q3, q23 = q2 * q3;
-  const float n1 = 0.1f * q23 * q23, n2 = 0.6f * q13 * q13, n3 = 0.3f * q12 * q12;
-  const float is = __fdividef(1.f, n1 + n2 + n3);  // sum <= 3e31 < 2^126
+  // 10 d_k prod_{j != k} q_j^2 (the common factor cancels in the weights)
+  const float n1 = q23 * q23, n2 = 6.f * q13 * q13, n3 = 3.f * q12 * q12;
+  const float is = __fdividef(1.f, n1 + n2 + n3);  // sum <= 1e32 < 2^126
   const float w1 = n1 * is, w2 = n2 * is, w3 = n3 * is;
   const float W = fmaf(w1, p1, fmaf(w2, p2, w3 * p3));
   const float yb = dt * mu * kap * inv;
