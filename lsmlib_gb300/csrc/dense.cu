@@ -325,10 +325,16 @@ __device__ __forceinline__ void block_max_commit(R v, unsigned long long *key) {
 // mode 0: advection (math_utils3d.f.in:309-315)
 // mode 1: normal velocity field (:421-438), mode 2: constant normal velocity (:537-556)
 // mode 3: max |f1 - f2| (:56-71)
+// The control-volume variants (math_utils3d.f.in:852-1416) take a cell only
+// when control_vol > 0 (cv_sgn > 0) or control_vol < 0 (cv_sgn < 0); cv_sgn 0
+// takes every cell.  Max-norm seeds with the (ilo, jlo, klo) corner whatever
+// its control volume (:908-909), so mode 3 always takes that cell.
 struct RedArgs {
   View<const R> a, b, c;         // vel_x,y,z | (unused) | f1,f2
   View<const R> pxp, pyp, pzp, pxm, pym, pzm;
   View<const R> vn;
+  View<const R> cv;
+  int cv_sgn;
   R vn_const, ix, iy, iz, max_dx_sq;
 };
 
@@ -338,7 +344,12 @@ __global__ void k_reduce_max(RedArgs A, Box ib, unsigned long long *key) {
   const int j = ib.lo[1] + blockIdx.y * blockDim.y + threadIdx.y;
   const int k = ib.lo[2] + blockIdx.z * blockDim.z + threadIdx.z;
   R v = R(-1.0e308);
-  if (i <= ib.hi[0] && j <= ib.hi[1] && k <= ib.hi[2]) {
+  bool take = i <= ib.hi[0] && j <= ib.hi[1] && k <= ib.hi[2];
+  if (take && A.cv_sgn != 0 && !(MODE == 3 && i == ib.lo[0] && j == ib.lo[1] && k == ib.lo[2])) {
+    const R c = A.cv(i, j, k);
+    take = A.cv_sgn > 0 ? c > R(0) : c < R(0);
+  }
+  if (take) {
     if (MODE == 0) {
       v = fabs(A.a(i, j, k)) * A.ix + fabs(A.b(i, j, k)) * A.iy + fabs(A.c(i, j, k)) * A.iz;
     } else if (MODE == 3) {
@@ -711,12 +722,17 @@ void lsm3dcomputestableadvectiondt_(R *dt, const R *vel_x, const R *vel_y, const
 static void normal_dt(const char *name, bool const_vn, R *dt, const R *vn, const Box &vb, R vn_const,
                       const R *pxp, const R *pyp, const R *pzp, const Box &pb, const R *pxm,
                       const R *pym, const R *pzm, const Box &mb, const Box &ib, R dx, R dy, R dz,
-                      R cfl) {
+                      R cfl, const R *cv = nullptr, const Box &cb = Box{}, int cv_sgn = 0) {
   Call call(name);
-  if (!pb.contains(ib, 0, 0, 0) || !mb.contains(ib, 0, 0, 0) || (!const_vn && !vb.contains(ib, 0, 0, 0)))
+  if (!pb.contains(ib, 0, 0, 0) || !mb.contains(ib, 0, 0, 0) || (!const_vn && !vb.contains(ib, 0, 0, 0)) ||
+      (cv_sgn != 0 && !cb.contains(ib, 0, 0, 0)))
     call.fail("ghost box does not cover the index box");
   if (!call.ok()) return;
   RedArgs A{};
+  if (cv_sgn != 0) {
+    A.cv = view((const R *)call.in(cv, cb.size()), cb);
+    A.cv_sgn = cv_sgn;
+  }
   const long long np = pb.size(), nm = mb.size();
   A.pxp = view((const R *)call.in(pxp, np), pb); A.pyp = view((const R *)call.in(pyp, np), pb);
   A.pzp = view((const R *)call.in(pzp, np), pb);
@@ -751,6 +767,68 @@ void lsm3dcomputestableconstnormalveldt_(R *dt, const R *vel_n, const R *phi_x_p
   normal_dt("lsm3dcomputestableconstnormalveldt_", true, dt, nullptr, Box{}, *vel_n, phi_x_plus,
             phi_y_plus, phi_z_plus, BOXOF(p), phi_x_minus, phi_y_minus, phi_z_minus, BOXOF(m), IBOX, *dx,
             *dy, *dz, *cfl_number);
+}
+
+
+// ---- control-volume variants (math_utils3d.f.in:852-1416) ------------------------
+#define CVARGS const R *control_vol, BOXARG(c), const int *control_vol_sgn
+#define CVSGN (*control_vol_sgn > 0 ? 1 : -1)
+
+void lsm3dmaxnormdiffcontrolvolume_(R *max_norm_diff, const R *field1, BOXARG(a), const R *field2, BOXARG(b),
+                                    CVARGS, IBARGS) {
+  Call call("lsm3dmaxnormdiffcontrolvolume_");
+  Box ab = BOXOF(a), bb = BOXOF(b), cb = BOXOF(c), ib = IBOX;
+  Box corner = ib;
+  corner.hi[0] = corner.lo[0]; corner.hi[1] = corner.lo[1]; corner.hi[2] = corner.lo[2];
+  if (!ab.contains(corner, 0, 0, 0) || !bb.contains(corner, 0, 0, 0) || !ab.contains(ib, 0, 0, 0) ||
+      !bb.contains(ib, 0, 0, 0) || !cb.contains(ib, 0, 0, 0))
+    call.fail("ghost box does not cover the index box");
+  if (!call.ok()) return;
+  RedArgs A{};
+  A.a = view((const R *)call.in(field1, ab.size()), ab);
+  A.b = view((const R *)call.in(field2, bb.size()), bb);
+  A.cv = view((const R *)call.in(control_vol, cb.size()), cb);
+  A.cv_sgn = CVSGN;
+  if (!call.ok()) return;
+  reduce_max<3>(call, A, ib.empty() ? corner : ib, max_norm_diff, R(0), R(-1.0e308));
+}
+
+void lsm3dcomputestableadvectiondtcontrolvolume_(R *dt, const R *vel_x, const R *vel_y, const R *vel_z,
+                                                 BOXARG(v), CVARGS, IBARGS, DXP, const R *cfl_number) {
+  Call call("lsm3dcomputestableadvectiondtcontrolvolume_");
+  Box vb = BOXOF(v), cb = BOXOF(c), ib = IBOX;
+  if (!vb.contains(ib, 0, 0, 0) || !cb.contains(ib, 0, 0, 0)) call.fail("ghost box does not cover the index box");
+  if (!call.ok()) return;
+  RedArgs A{};
+  const long long n = vb.size();
+  A.a = view((const R *)call.in(vel_x, n), vb);
+  A.b = view((const R *)call.in(vel_y, n), vb);
+  A.c = view((const R *)call.in(vel_z, n), vb);
+  A.cv = view((const R *)call.in(control_vol, cb.size()), cb);
+  A.cv_sgn = CVSGN;
+  A.ix = R(1.0) / *dx; A.iy = R(1.0) / *dy; A.iz = R(1.0) / *dz;
+  if (!call.ok()) return;
+  reduce_max<0>(call, A, ib, dt, *cfl_number, R(-1.0));
+}
+
+void lsm3dcomputestablenormalveldtcontrolvolume_(R *dt, const R *vel_n, BOXARG(v), const R *phi_x_plus,
+                                                 const R *phi_y_plus, const R *phi_z_plus, BOXARG(p),
+                                                 const R *phi_x_minus, const R *phi_y_minus,
+                                                 const R *phi_z_minus, BOXARG(m), CVARGS, IBARGS, DXP,
+                                                 const R *cfl_number) {
+  normal_dt("lsm3dcomputestablenormalveldtcontrolvolume_", false, dt, vel_n, BOXOF(v), R(0), phi_x_plus,
+            phi_y_plus, phi_z_plus, BOXOF(p), phi_x_minus, phi_y_minus, phi_z_minus, BOXOF(m), IBOX, *dx, *dy,
+            *dz, *cfl_number, control_vol, BOXOF(c), CVSGN);
+}
+
+void lsm3dcomputestableconstnormalveldtcontrolvolume_(R *dt, const R *vel_n, const R *phi_x_plus,
+                                                      const R *phi_y_plus, const R *phi_z_plus, BOXARG(p),
+                                                      const R *phi_x_minus, const R *phi_y_minus,
+                                                      const R *phi_z_minus, BOXARG(m), CVARGS, IBARGS, DXP,
+                                                      const R *cfl_number) {
+  normal_dt("lsm3dcomputestableconstnormalveldtcontrolvolume_", true, dt, nullptr, Box{}, *vel_n, phi_x_plus,
+            phi_y_plus, phi_z_plus, BOXOF(p), phi_x_minus, phi_y_minus, phi_z_minus, BOXOF(m), IBOX, *dx, *dy,
+            *dz, *cfl_number, control_vol, BOXOF(c), CVSGN);
 }
 
 }  // extern "C"

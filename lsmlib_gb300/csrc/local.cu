@@ -713,8 +713,11 @@ void lsm3dcomputemeancurvatureorder2local_(R *kappa, BOXARG(k), const R *phi, BO
 // ---- reductions over lists ----------------------------------------------------
 // mode 0: advection dt, 1: normal velocity dt (skips norm_grad_phi <= tol),
 // 2: constant normal velocity dt, 3: max |f1 - f2|
+// cv_sgn != 0 (control-volume variants, math_utils3d_local.f.in:98, :432):
+// take a cell only when control_vol > 0 (cv_sgn > 0) or < 0 (cv_sgn < 0)
 struct LRed {
-  View<const R> a, b, c, xp, yp, zp, xm, ym, zm, vn;
+  View<const R> a, b, c, xp, yp, zp, xm, ym, zm, vn, cv;
+  int cv_sgn;
   R vc, ix, iy, iz, mdx2;
 };
 
@@ -725,7 +728,9 @@ __global__ void k_list_max(LRed A, Gate g, List L, int lo, int hi, unsigned long
   if (l <= hi) {
     const long long e = l - L.decl;
     const int i = L.ix[e], j = L.iy[e], k = L.iz[e];
-    if (g(i, j, k)) {
+    bool take = g(i, j, k);
+    if (take && A.cv_sgn != 0) take = A.cv_sgn > 0 ? A.cv(i, j, k) > R(0) : A.cv(i, j, k) < R(0);
+    if (take) {
       if (MODE == 0) {
         v = fabs(A.a(i, j, k)) * A.ix + fabs(A.b(i, j, k)) * A.iy + fabs(A.c(i, j, k)) * A.iz;
       } else if (MODE == 3) {
@@ -813,6 +818,42 @@ void lsm3dcomputestablenormalveldtlocal_(R *dt, const R *vel_n, BOXARG(v), const
   normal_dt_local("lsm3dcomputestablenormalveldtlocal_", 1, dt, vel_n, BOXOF(v), R(0), phi_x_plus, phi_y_plus,
                   phi_z_plus, BOXOF(p), phi_x_minus, phi_y_minus, phi_z_minus, BOXOF(m), *dx, *dy, *dz,
                   *cfl_number, true, LPASS);
+}
+
+// starts at 0 and takes listed cells with a negative control volume: the
+// routine has no control_vol_sgn argument (math_utils3d_local.f.in:98-190)
+void lsm3dmaxnormdiffcontrolvolumelocal_(R *max_norm_diff, const R *field1, BOXARG(a), const R *field2,
+                                         BOXARG(b), const R *control_vol, BOXARG(c), LTAIL) {
+  LSETUP("lsm3dmaxnormdiffcontrolvolumelocal_")
+  LRed A{};
+  A.a = lc.in(field1, BOXOF(a));
+  A.b = lc.in(field2, BOXOF(b));
+  A.cv = lc.in(control_vol, BOXOF(c));
+  A.cv_sgn = -1;
+  g.safe = isect(isect(BOXOF(a), BOXOF(b)), BOXOF(c));
+  list_max<3>(lc, A, g, L, *nlo, *nhi, max_norm_diff, R(0.0), 1, R(0));
+}
+
+// math_utils3d_local.f.in:432-624 (norm_grad_phi <= zero_tol skipped, :138)
+void lsm3dcomputestablenormalveldtcontrolvolumelocal_(R *dt, const R *vel_n, BOXARG(v), const R *phi_x_plus,
+                                                      const R *phi_y_plus, const R *phi_z_plus, BOXARG(p),
+                                                      const R *phi_x_minus, const R *phi_y_minus,
+                                                      const R *phi_z_minus, BOXARG(m), const R *control_vol,
+                                                      BOXARG(c), const int *control_vol_sgn, DXP,
+                                                      const R *cfl_number, LTAIL) {
+  LSETUP("lsm3dcomputestablenormalveldtcontrolvolumelocal_")
+  const Box vb = BOXOF(v), pb = BOXOF(p), mb = BOXOF(m), cb = BOXOF(c);
+  LRed A{};
+  A.xp = lc.in(phi_x_plus, pb); A.yp = lc.in(phi_y_plus, pb); A.zp = lc.in(phi_z_plus, pb);
+  A.xm = lc.in(phi_x_minus, mb); A.ym = lc.in(phi_y_minus, mb); A.zm = lc.in(phi_z_minus, mb);
+  A.vn = lc.in(vel_n, vb);
+  A.cv = lc.in(control_vol, cb);
+  A.cv_sgn = *control_vol_sgn > 0 ? 1 : -1;
+  g.safe = isect(isect(isect(pb, mb), vb), cb);
+  A.ix = R(1.0) / *dx; A.iy = R(1.0) / *dy; A.iz = R(1.0) / *dz;
+  const R mx = rmax(rmax(*dx, *dy), *dz);
+  A.mdx2 = mx * mx;
+  list_max<1>(lc, A, g, L, *nlo, *nhi, dt, R(-1.0), 0, *cfl_number);
 }
 
 // LSMLIB's routine (math_utils3d_local.f.in:628-752) reads two unassigned

@@ -569,6 +569,52 @@ void lsm3dcomputestablenormalveldtlocal_(real_t *dt, const real_t *vn, A3(v), co
   *dt = *cfl / (best + ORACLE_TINY);
 }
 
+/* lsm3dMaxNormDiffControlVolumeLOCAL (math_utils3d_local.f.in:98-190): starts
+ * at 0 and takes listed cells whose control volume is negative (the routine
+ * has no control_vol_sgn argument) */
+void lsm3dmaxnormdiffcontrolvolumelocal_(real_t *out, const real_t *f1, A3(a), const real_t *f2, A3(b),
+                                         const real_t *cv, A3(c), LOCAL_TAIL) {
+  gbox A = B3(a), B = B3(b), C = B3(c), NB = NBBOX;
+  real_t m = 0.0;
+  FOR_LIST(*nlo, *nlo, *nhi) {
+    if (!GATE || !(inb(&A, i, j, k) && inb(&B, i, j, k) && inb(&C, i, j, k))) continue;
+    if (!(cv[at(&C, i, j, k)] < 0.0)) continue;
+    real_t d = fabs(f1[at(&A, i, j, k)] - f2[at(&B, i, j, k)]);
+    if (d > m) m = d;
+  }
+  *out = m;
+}
+
+/* lsm3dComputeStableNormalVelDtControlVolumeLOCAL (math_utils3d_local.f.in:
+ * 432-624): control_vol > 0 for control_vol_sgn > 0, else control_vol < 0;
+ * cells with norm_grad_phi <= zero_tol are skipped (:138, :171) */
+void lsm3dcomputestablenormalveldtcontrolvolumelocal_(real_t *dt, const real_t *vn, A3(v), const real_t *pxp,
+                                                      const real_t *pyp, const real_t *pzp, A3(p),
+                                                      const real_t *pxm, const real_t *pym,
+                                                      const real_t *pzm, A3(m), const real_t *cv, A3(c),
+                                                      const int *sgn, DX_ARGS, const real_t *cfl,
+                                                      LOCAL_TAIL) {
+  gbox V = B3(v), P = B3(p), M = B3(m), C = B3(c), NB = NBBOX;
+  real_t mx = fmax2(fmax2(*dx, *dy), *dz);
+  real_t max_dx_sq = mx * mx;
+  real_t inv[3] = {1.0 / *dx, 1.0 / *dy, 1.0 / *dz}, best = -1.0;
+  FOR_LIST(*nlo, *nlo, *nhi) {
+    if (!GATE || !(inb(&V, i, j, k) && inb(&P, i, j, k) && inb(&M, i, j, k) && inb(&C, i, j, k))) continue;
+    real_t c = cv[at(&C, i, j, k)];
+    if (!(*sgn > 0 ? c > 0.0 : c < 0.0)) continue;
+    long a = at(&P, i, j, k), b = at(&M, i, j, k);
+    real_t cx = fmax2(fabs(pxp[a]), fabs(pxm[b]));
+    real_t cy = fmax2(fabs(pyp[a]), fabs(pym[b]));
+    real_t cz = fmax2(fabs(pzp[a]), fabs(pzm[b]));
+    real_t ng = sqrt(cx * cx + cy * cy + cz * cz + max_dx_sq);
+    if (ng > ORACLE_ZERO_TOL) {
+      real_t h = fabs(vn[at(&V, i, j, k)]) / ng * (cx * inv[0] + cy * inv[1] + cz * inv[2]);
+      if (h > best) best = h;
+    }
+  }
+  *dt = *cfl / (best + ORACLE_TINY);
+}
+
 /* lsm3dComputeStableConstNormalVelDtLOCAL (math_utils3d_local.f.in:628-752)
  * reads two local variables it never assigns (abs_vel_n, norm_grad_phi).
  * The oracle implements the evident intent, the dense routine's formula
