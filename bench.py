@@ -494,6 +494,7 @@ def gpu_arm(args, world, rank, local):
             "narrow_band_512": sub_narrow_band(stream, dev),
             "batched_4096": sub_batched(stream, dev),
             "adjoint_192": sub_adjoint(stream, dev),
+            "geometry_512": sub_geometry(stream, dev),
         }
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -670,6 +671,65 @@ def sub_adjoint(stream, dev, n=192, steps=40, ckpt=8):
             "objective_ms": t_f, "gradient_ms": t_g, "forward_step_ms": t_f / steps,
             "reverse_step_ms": (t_g - t_f) / steps, "reverse_to_forward_step": (t_g - t_f) / t_f}
 
+
+
+def sub_geometry(stream, dev, n=512, reps=10):
+    """Geometry reductions through the drop-in C entry points on device
+    arrays (FP64): volume of {phi < 0}, area of {phi = 0} and the count of
+    phi < 0 cells over the 512^3 box of a sphere's signed distance (radius
+    0.5, 3 ghost cells, smoothing width 1.5 dx) with its exact gradient.
+    Each call returns its scalar to the host, so a call's time includes that
+    copy.  Algorithmic bytes: phi once (8 B/cell), plus the gradient (24 B)
+    at the cells inside the smoothing band for the area."""
+    import torch
+    import lsmlib_gb300 as L
+    lib = L.lib()
+    dx = 2.0 / n
+    c = -1.0 + (torch.arange(-GHOST, n + GHOST, device=dev, dtype=torch.float64) + 0.5) * dx
+    z, y, x = c.view(-1, 1, 1), c.view(1, -1, 1), c.view(1, 1, -1)
+    d = torch.sqrt(x * x + y * y + z * z).clamp_min(1e-12)
+    phi = d - 0.5
+    grads = [(x / d).contiguous(), (y / d).contiguous(), (z / d).contiguous()]
+    del d
+    eps = 1.5 * dx
+    gb = (-GHOST, n - 1 + GHOST) * 3
+    ib = (0, n - 1) * 3
+    band = int((phi[GHOST:-GHOST, GHOST:-GHOST, GHOST:-GHOST].abs() < eps).sum())
+    cells = n ** 3
+    peak, src = measured_peaks()
+    out = {"workload": "geometry-512: sphere r=0.5 signed distance on [-1, 1]^3, FP64, eps = 1.5 dx, "
+                       "device arrays, scalar result copied to the host per call",
+           "band_cells": band}
+
+    def vals(sym):
+        arrays = {"phi": phi, "phi_x": grads[0], "phi_y": grads[1], "phi_z": grads[2]}
+        scalars = {"dx": dx, "dy": dx, "dz": dx, "epsilon": eps, "volume": 0.0, "area": 0.0, "count": 0}
+        v = {}
+        for name, kind, is_arr, _w in L.ABI[sym]["args"]:
+            if is_arr:
+                v[name] = arrays[name]
+            elif name in scalars:
+                v[name] = scalars[name]
+            else:
+                b = ib if name.endswith("_ib") else gb
+                v[name] = b[["ilo", "ihi", "jlo", "jhi", "klo", "khi"].index(name[:3])]
+        return v
+
+    cases = (("volume", "lsm3dvolumeregionphilessthanzero_", 8.0 * cells),
+             ("area", "lsm3dsurfaceareazerolevelset_", 8.0 * cells + 24.0 * band),
+             ("count", "lsm3dvoxelcountlessthanzero_", 8.0 * cells))
+    for key, sym, nbytes in cases:
+        v = vals(sym)
+        res = L.invoke(lib, sym, v)   # warm-up
+        L.check(lib)
+        ms = min(_timed(lambda: [L.invoke(lib, sym, v) for _ in range(reps)], stream) for _ in range(3)) / reps
+        gbs = nbytes / (ms / 1e3) / 1e9
+        out[key] = {"entry": sym, "ms_per_call": ms, "result": res[L.ABI[sym]["args"][0][0]],
+                    "Gcells_per_s": cells / (ms / 1e3) / 1e9, "algorithmic_GBps": gbs,
+                    "hbm_frac": gbs / peak, "peak_source": src}
+    out["volume"]["exact"] = 4.0 / 3.0 * np.pi * 0.5 ** 3
+    out["area"]["exact"] = 4.0 * np.pi * 0.5 ** 2
+    return out
 
 
 # DRAM bytes (read + write) of one fused FP32 reinitialization stage launch

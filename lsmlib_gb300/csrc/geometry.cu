@@ -5,20 +5,26 @@
 // symbol names and argument lists.
 //
 // Sums.  The reference adds its terms serially in (k, j, i) order.  Here one
-// warp owns one (j, k) row of the index box: lane l adds the row's terms at
+// warp owns one (j, k) row of the index box: lane l takes the row's cells at
 // i = ilo + l, ilo + l + 32, ... in increasing i, a fixed shuffle tree adds
-// the 32 lane totals, and one block adds the row totals with compensated
-// (two-sum) arithmetic in a fixed order.  The result depends only on the data
-// and the box, not on the launch or the run, and its rounding error is far
-// below the serial sum's.  Each term keeps the reference's operation order
-// (this unit is compiled without FMA contraction), so terms made of +, -, *,
-// / and sqrt are bit-identical; sin and cos are CUDA's (within 2 ulp), so
-// terms inside the smoothing band |phi| < epsilon can differ in the last
-// bits.  Voxel counts are sums of ones and exact.
+// the lanes, a block adds its 16 rows in order, and one block adds the block
+// partials in a fixed order (two-sum for the last tree).  The result depends
+// only on the data and the box, not on the launch or the run, and its
+// rounding error is far below the serial sum's.  Each term keeps the
+// reference's operation order (this unit is compiled without FMA
+// contraction), so terms made of +, -, *, / and sqrt are bit-identical; sin
+// and cos are CUDA's (within 2 ulp), so terms inside the smoothing band
+// |phi| < epsilon can differ in the last bits.  Voxel counts are integers.
 //
-// Memory: each row is read once, coalesced along x, with four 32-cell
-// segments per lane in flight; F and the gradient are read only for cells
-// whose term needs them, as the reference does.
+// Arithmetic: GB300's FP64 rate is a small fraction of its FP32 rate, so a
+// cell's class (outside, full, smoothing band) is decided on integers, full
+// cells are counted (or, for the integrals, their F summed) and scaled by dV
+// once, and only band cells evaluate their FP64 term; partial sums that are
+// zero skip their FP64 additions.  Memory: each row is read once, coalesced
+// along x, with four 32-cell segments per lane in flight; F and the gradient
+// are read only for cells whose term needs them, as the reference does.
+#include <cstring>
+
 #include "lsmgpu_common.cuh"
 #include "stencil_math.cuh"
 #include "../../include/lsmgpu_toolbox3d.h"
@@ -60,6 +66,8 @@ struct SumArgs {
   View<const R> px, py, pz;  // gradient
   View<const R> cv;          // control volume
   int cv_sgn;                // 0: every cell; > 0: control_vol > 0; < 0: control_vol < 0
+  int eps_bits_ok;           // epsilon is positive and finite: classify on bit patterns
+  unsigned long long eps_bits;
   R eps, inv_eps, dv;
 };
 
@@ -68,73 +76,184 @@ __device__ __forceinline__ R grad_norm(const SumArgs &A, int i, int j, int k) {
   return sqrt(x * x + y * y + z * z);
 }
 
-// the term cell (i, j, k) adds, given its phi value p (reference line numbers
-// in the kind list above; factor order as written there)
+// GB300 runs FP64 arithmetic at a small fraction of its FP32 rate, so the
+// comparisons that decide a cell's class are made on the IEEE bit pattern
+// (sign and magnitude as integers), which orders finite doubles exactly as
+// the reference's FP64 comparisons do (-0 equals +0, NaN compares false).
+constexpr unsigned long long kMag = 0x7fffffffffffffffULL, kInf = 0x7ff0000000000000ULL;
+
+enum CellClass { C_NONE = 0, C_FULL = 1, C_BAND = 2 };
+
+// b: the bit pattern of phi; EB: epsilon is positive and finite
+template <int K, bool EB>
+__device__ __forceinline__ int classify(const SumArgs &A, unsigned long long b) {
+  if (K == ABS_DIFF) return C_BAND;  // every cell (a NaN propagates, as in the reference)
+  const unsigned long long m = b & kMag;
+  const bool neg = (b >> 63) != 0;
+  if (m > kInf) return C_NONE;  // NaN: every comparison of the reference is false
+  if (K == COUNT_GT) return (!neg && m != 0) ? C_FULL : C_NONE;
+  if (K == COUNT_LT) return (neg && m != 0) ? C_FULL : C_NONE;
+  if (K == AREA_DELTA) return (!neg && m != 0) ? C_BAND : C_NONE;
+  if (EB) {
+    const unsigned long long e = A.eps_bits;
+    if (K == VOL_LT || K == INT_LT) {  // p < -eps; -eps <= p < eps
+      if (neg && m > e) return C_FULL;
+      return ((neg && m <= e) || (!neg && m < e)) ? C_BAND : C_NONE;
+    }
+    if (K == VOL_GT || K == INT_GT) {  // p > eps; -eps < p <= eps
+      if (!neg && m > e) return C_FULL;
+      return ((!neg && m <= e) || (neg && m < e)) ? C_BAND : C_NONE;
+    }
+    return m < e ? C_BAND : C_NONE;  // AREA, SURF_INT: |p| < eps
+  }
+  // epsilon zero, negative or not finite: the reference's comparisons as written
+  const R p = __longlong_as_double((long long)b);
+  if (K == VOL_LT || K == INT_LT) return p < -A.eps ? C_FULL : (p < A.eps ? C_BAND : C_NONE);
+  if (K == VOL_GT || K == INT_GT) return p > A.eps ? C_FULL : (p > -A.eps ? C_BAND : C_NONE);
+  return fabs(p) < A.eps ? C_BAND : C_NONE;
+}
+
+__device__ __forceinline__ bool cv_takes(int sgn, unsigned long long b) {
+  const unsigned long long m = b & kMag;
+  if (m == 0 || m > kInf) return false;  // zero or NaN
+  return sgn > 0 ? (b >> 63) == 0 : (b >> 63) != 0;
+}
+
+__device__ __forceinline__ bool nonzero(R v) { return (__double_as_longlong(v) & (long long)kMag) != 0; }
+
+// the term of a smoothing-band cell, given its phi value p (reference line
+// numbers in the kind list above; factor order as written there).  A full
+// cell adds dV (volumes), F dV (integrals) or 1 (counts): those are counted
+// (or their F summed) and scaled once, further up.
 template <int K>
-__device__ __forceinline__ R cell_term(const SumArgs &A, R p, int i, int j, int k) {
+__device__ __forceinline__ R band_term(const SumArgs &A, R p, int i, int j, int k) {
   if (K == VOL_LT || K == INT_LT) {
     const R q = p / A.eps;
-    if (p < -A.eps) return K == VOL_LT ? A.dv : A.f(i, j, k) * A.dv;
-    if (p < A.eps) {
-      const R omh = R(0.5) * (R(1) - q - kOneOverPi * sin(kPi * q));
-      return K == VOL_LT ? omh * A.dv : omh * A.f(i, j, k) * A.dv;
-    }
-    return R(0);
+    const R omh = R(0.5) * (R(1) - q - kOneOverPi * sin(kPi * q));
+    return K == VOL_LT ? omh * A.dv : omh * A.f(i, j, k) * A.dv;
   }
   if (K == VOL_GT || K == INT_GT) {
     const R q = p / A.eps;
-    if (p > A.eps) return K == VOL_GT ? A.dv : A.f(i, j, k) * A.dv;
-    if (p > -A.eps) {
-      const R h = R(0.5) * (R(1) + q + kOneOverPi * sin(kPi * q));
-      return K == VOL_GT ? h * A.dv : h * A.f(i, j, k) * A.dv;
-    }
-    return R(0);
+    const R h = R(0.5) * (R(1) + q + kOneOverPi * sin(kPi * q));
+    return K == VOL_GT ? h * A.dv : h * A.f(i, j, k) * A.dv;
   }
   if (K == AREA || K == SURF_INT) {
-    if (!(fabs(p) < A.eps)) return R(0);
     const R delta = R(0.5) * A.inv_eps * (R(1) + cos(kPi * p * A.inv_eps));
     const R ng = grad_norm(A, i, j, k);
     return K == AREA ? delta * ng * A.dv : delta * ng * A.f(i, j, k) * A.dv;
   }
-  if (K == AREA_DELTA) return p > R(0) ? p * grad_norm(A, i, j, k) * A.dv : R(0);
-  if (K == ABS_DIFF) return fabs(p - A.f(i, j, k));
-  if (K == COUNT_GT) return p > R(0) ? R(1) : R(0);
-  return p < R(0) ? R(1) : R(0);  // COUNT_LT
+  if (K == AREA_DELTA) return p * grad_norm(A, i, j, k) * A.dv;
+  return fabs(p - A.f(i, j, k));  // ABS_DIFF
 }
 
-constexpr int kRowWarps = 8;  // rows per block
-constexpr int kSeg = 4;       // 32-cell segments per lane in flight
+// fixed-order sum over the 32 lanes (lane 0 holds it); skipped, and zero,
+// when every lane holds zero, which costs no FP64 work
+__device__ __forceinline__ R warp_sum(R v) {
+  if (!__any_sync(0xffffffffu, nonzero(v))) return R(0);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
 
-template <int K>
-__global__ void __launch_bounds__(32 * kRowWarps) k_row_sums(SumArgs A, Box ib, long long nrows, R *rows) {
-  const long long r = (long long)blockIdx.x * kRowWarps + (threadIdx.x >> 5);
-  if (r >= nrows) return;  // whole warps leave together
-  const int lane = threadIdx.x & 31;
-  const long long ny = ib.n(1);
-  const int j = ib.lo[1] + (int)(r % ny), k = ib.lo[2] + (int)(r / ny);
-  const int nx = (int)ib.n(0);
-  const R *prow = &A.phi(ib.lo[0], j, k);
-  const R *crow = A.cv_sgn ? &A.cv(ib.lo[0], j, k) : nullptr;
-  R acc = R(0);
-  for (int x0 = 0; x0 < nx; x0 += 32 * kSeg) {
-    R p[kSeg], c[kSeg];
+constexpr int kRowWarps = 16;  // rows per block, one warp each
+constexpr int kSeg = 4;        // 32-cell segments per lane in flight
+
+// One warp per (j, k) row of the index box, one partial per block of 16
+// rows: the number of full cells (an integer) and the FP64 rest, which is
+// (sum of F over full cells) * dV for the integrals plus the band terms.
+// Band cells are scattered (a few per 32-cell segment), so a warp queues
+// them in shared memory (value and i) and evaluates their FP64 terms 32 at a
+// time with every lane busy; the order of the queue is fixed by the data.
+template <int K, bool EB>
+__global__ void __launch_bounds__(32 * kRowWarps) k_row_sums(SumArgs A, Box ib, long long nrows,
+                                                              unsigned long long *part_n, R *part_v) {
+  __shared__ unsigned sn[kRowWarps];
+  __shared__ R sv[kRowWarps];
+  __shared__ unsigned long long qp[kRowWarps][64];
+  __shared__ int qx[kRowWarps][64];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long r = (long long)blockIdx.x * kRowWarps + w;
+  constexpr bool kFullF = (K == INT_LT || K == INT_GT);
+  constexpr bool kQueue = (K != ABS_DIFF);  // every cell of ABS_DIFF is a term: no divergence
+  unsigned nfull = 0;
+  R band = R(0), ffull = R(0);
+  if (r < nrows) {
+    const long long ny = ib.n(1);
+    const int j = ib.lo[1] + (int)(r % ny), k = ib.lo[2] + (int)(r / ny);
+    const int nx = (int)ib.n(0), i0 = ib.lo[0];
+    // rows are read as bit patterns: the hot loop does no FP64 arithmetic
+    const unsigned long long *prow = (const unsigned long long *)&A.phi(i0, j, k);
+    const unsigned long long *crow = A.cv_sgn ? (const unsigned long long *)&A.cv(i0, j, k) : nullptr;
+    int qn = 0;  // queued band cells (the same in every lane)
+    for (int x0 = 0; x0 < nx; x0 += 32 * kSeg) {
+      unsigned long long p[kSeg], c[kSeg];
 #pragma unroll
-    for (int u = 0; u < kSeg; u++) {
-      const int x = x0 + 32 * u + lane;
-      p[u] = x < nx ? __ldg(prow + x) : R(0);
-      c[u] = (crow && x < nx) ? __ldg(crow + x) : R(0);
+      for (int u = 0; u < kSeg; u++) {
+        const int x = x0 + 32 * u + lane;
+        p[u] = x < nx ? __ldg(prow + x) : 0ull;
+        c[u] = (crow && x < nx) ? __ldg(crow + x) : 0ull;
+      }
+#pragma unroll
+      for (int u = 0; u < kSeg; u++) {
+        const int x = x0 + 32 * u + lane;
+        const bool ok = x < nx && (!A.cv_sgn || cv_takes(A.cv_sgn, c[u]));
+        const int cls = ok ? classify<K, EB>(A, p[u]) : C_NONE;
+        if (cls == C_FULL) {
+          if (kFullF)
+            ffull += A.f(i0 + x, j, k);
+          else
+            nfull++;
+        }
+        if (!kQueue) {
+          if (cls == C_BAND) band += band_term<K>(A, __longlong_as_double((long long)p[u]), i0 + x, j, k);
+          continue;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, cls == C_BAND);
+        if (m == 0u) continue;
+        if (cls == C_BAND) {
+          const int slot = qn + __popc(m & ((1u << lane) - 1u));
+          qp[w][slot] = p[u];
+          qx[w][slot] = x;
+        }
+        qn += __popc(m);
+        if (qn >= 32) {
+          __syncwarp();
+          band += band_term<K>(A, __longlong_as_double((long long)qp[w][lane]), i0 + qx[w][lane], j, k);
+          __syncwarp();
+          if (lane < qn - 32) {
+            qp[w][lane] = qp[w][32 + lane];
+            qx[w][lane] = qx[w][32 + lane];
+          }
+          __syncwarp();
+          qn -= 32;
+        }
+      }
     }
-#pragma unroll
-    for (int u = 0; u < kSeg; u++) {
-      const int x = x0 + 32 * u + lane;
-      bool take = x < nx;
-      if (take && A.cv_sgn) take = A.cv_sgn > 0 ? c[u] > R(0) : c[u] < R(0);
-      if (take) acc += cell_term<K>(A, p[u], ib.lo[0] + x, j, k);
+    if (kQueue && qn > 0) {
+      __syncwarp();
+      if (lane < qn) band += band_term<K>(A, __longlong_as_double((long long)qp[w][lane]), i0 + qx[w][lane], j, k);
     }
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if (lane == 0) rows[r] = acc;
+  const unsigned n_w = __reduce_add_sync(0xffffffffu, nfull);
+  R v_w = warp_sum(band);
+  if (kFullF) {
+    const R f_w = warp_sum(ffull);
+    if (lane == 0 && nonzero(f_w)) v_w = f_w * A.dv + v_w;
+  }
+  if (lane == 0) {
+    sn[w] = n_w;
+    sv[w] = v_w;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const unsigned n = lane < kRowWarps ? sn[lane] : 0u;
+    const R v = warp_sum(lane < kRowWarps ? sv[lane] : R(0));
+    const unsigned nb = __reduce_add_sync(0xffffffffu, n);
+    if (lane == 0) {
+      part_n[blockIdx.x] = nb;
+      part_v[blockIdx.x] = v;
+    }
+  }
 }
 
 // s + e = a + b exactly (Knuth's two-sum)
@@ -146,46 +265,58 @@ __device__ __forceinline__ void two_sum(R a, R b, R &s, R &e) {
 
 constexpr int kFinal = 1024;
 
-// Adds the row totals in a fixed order: thread t takes rows t, t + 1024, ...
-// with a running two-sum, then a fixed tree combines the threads.  Writes the
-// routine's scalar result: the sum, the mean (ABS_DIFF) or the count.
-__global__ void __launch_bounds__(kFinal) k_sum_rows(const R *rows, long long nrows, int kind, R npts, R *out,
-                                                     int *count) {
+// Adds the block partials in a fixed order: thread t takes partials t,
+// t + 1024, ... (integers exactly, FP64 values in order, zeros skipped), a
+// fixed tree combines the threads (FP64 with two-sum).  Writes the routine's
+// scalar: count * unit + rest, the mean (ABS_DIFF) or the count.
+__global__ void __launch_bounds__(kFinal) k_sum_parts(const unsigned long long *part_n, const R *part_v,
+                                                      long long nparts, int kind, R unit, R npts, R *out,
+                                                      int *count) {
+  __shared__ unsigned long long hn[kFinal];
   __shared__ R hs[kFinal], he[kFinal];
-  R s = R(0), e = R(0);
-  for (long long r = threadIdx.x; r < nrows; r += kFinal) {
-    R t, d;
-    two_sum(s, rows[r], t, d);
-    s = t;
-    e += d;
+  unsigned long long n = 0;
+  R s = R(0);
+  for (long long b = threadIdx.x; b < nparts; b += kFinal) {
+    n += part_n[b];
+    const R v = part_v[b];
+    if (nonzero(v)) s += v;
   }
+  hn[threadIdx.x] = n;
   hs[threadIdx.x] = s;
-  he[threadIdx.x] = e;
+  he[threadIdx.x] = R(0);
   __syncthreads();
   for (int h = kFinal / 2; h > 0; h >>= 1) {
     if (threadIdx.x < h) {
-      R t, d;
-      two_sum(hs[threadIdx.x], hs[threadIdx.x + h], t, d);
-      hs[threadIdx.x] = t;
-      he[threadIdx.x] += he[threadIdx.x + h] + d;
+      hn[threadIdx.x] += hn[threadIdx.x + h];
+      const R a = hs[threadIdx.x], b = hs[threadIdx.x + h], eb = he[threadIdx.x + h];
+      if (nonzero(b)) {
+        R t, d;
+        two_sum(a, b, t, d);
+        hs[threadIdx.x] = t;
+        he[threadIdx.x] += d;
+      }
+      if (nonzero(eb)) he[threadIdx.x] += eb;
     }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const R total = hs[0] + he[0];
+    const R rest = hs[0] + he[0];
     if (kind == COUNT_GT || kind == COUNT_LT)
-      *count = (int)total;
+      *count = (int)hn[0];
     else if (kind == ABS_DIFF)
-      *out = npts > R(0) ? total / npts : R(0);
+      *out = npts > R(0) ? rest / npts : R(0);
     else
-      *out = total;
+      *out = (R)hn[0] * unit + rest;
   }
 }
 
 template <int K>
-void launch_rows(const SumArgs &A, const Box &ib, long long nrows, R *rows) {
-  LSMGPU_LAUNCH(k_row_sums<K>, (unsigned)((nrows + kRowWarps - 1) / kRowWarps), 32 * kRowWarps, 0, A, ib, nrows,
-                rows);
+void launch_rows(const SumArgs &A, const Box &ib, long long nrows, long long nparts, unsigned long long *pn,
+                 R *pv) {
+  if (A.eps_bits_ok)
+    LSMGPU_LAUNCH((k_row_sums<K, true>), (unsigned)nparts, 32 * kRowWarps, 0, A, ib, nrows, pn, pv);
+  else
+    LSMGPU_LAUNCH((k_row_sums<K, false>), (unsigned)nparts, 32 * kRowWarps, 0, A, ib, nrows, pn, pv);
 }
 
 // Runs one reduction.  Arrays in `need` must cover the index box.
@@ -204,6 +335,12 @@ struct SumCall {
     A.cv_sgn = sgn > 0 ? 1 : -1;
   }
   void cell_volume(R dx, R dy, R dz) { A.dv = dx * dy * dz; }
+  void epsilon(R eps) {
+    A.eps = eps;
+    A.inv_eps = R(1.0) / eps;
+    A.eps_bits_ok = eps > R(0) && eps <= 1.7976931348623157e308;
+    memcpy(&A.eps_bits, &eps, sizeof(eps));
+  }
   void run(int kind, R *out, int *count) {
     if (!call.ok()) return;
     R *dout = nullptr;
@@ -213,24 +350,25 @@ struct SumCall {
     else
       dout = call.scalar_out(out);
     const long long nrows = ib.empty() ? 0 : ib.n(1) * ib.n(2);
-    R *rows = call.temp<R>(nrows > 0 ? nrows : 1);
+    const long long nparts = (nrows + kRowWarps - 1) / kRowWarps;
+    unsigned long long *pn = call.temp<unsigned long long>(nparts > 0 ? nparts : 1);
+    R *pv = call.temp<R>(nparts > 0 ? nparts : 1);
     if (!call.ok()) return;
-    if (nrows > 0) {
+    if (nparts > 0) {
       switch (kind) {
-        case VOL_LT: launch_rows<VOL_LT>(A, ib, nrows, rows); break;
-        case VOL_GT: launch_rows<VOL_GT>(A, ib, nrows, rows); break;
-        case AREA: launch_rows<AREA>(A, ib, nrows, rows); break;
-        case AREA_DELTA: launch_rows<AREA_DELTA>(A, ib, nrows, rows); break;
-        case INT_LT: launch_rows<INT_LT>(A, ib, nrows, rows); break;
-        case INT_GT: launch_rows<INT_GT>(A, ib, nrows, rows); break;
-        case SURF_INT: launch_rows<SURF_INT>(A, ib, nrows, rows); break;
-        case ABS_DIFF: launch_rows<ABS_DIFF>(A, ib, nrows, rows); break;
-        case COUNT_GT: launch_rows<COUNT_GT>(A, ib, nrows, rows); break;
-        default: launch_rows<COUNT_LT>(A, ib, nrows, rows); break;
+        case VOL_LT: launch_rows<VOL_LT>(A, ib, nrows, nparts, pn, pv); break;
+        case VOL_GT: launch_rows<VOL_GT>(A, ib, nrows, nparts, pn, pv); break;
+        case AREA: launch_rows<AREA>(A, ib, nrows, nparts, pn, pv); break;
+        case AREA_DELTA: launch_rows<AREA_DELTA>(A, ib, nrows, nparts, pn, pv); break;
+        case INT_LT: launch_rows<INT_LT>(A, ib, nrows, nparts, pn, pv); break;
+        case INT_GT: launch_rows<INT_GT>(A, ib, nrows, nparts, pn, pv); break;
+        case SURF_INT: launch_rows<SURF_INT>(A, ib, nrows, nparts, pn, pv); break;
+        case ABS_DIFF: launch_rows<ABS_DIFF>(A, ib, nrows, nparts, pn, pv); break;
+        case COUNT_GT: launch_rows<COUNT_GT>(A, ib, nrows, nparts, pn, pv); break;
+        default: launch_rows<COUNT_LT>(A, ib, nrows, nparts, pn, pv); break;
       }
     }
-    const R npts = (R)ib.size();
-    LSMGPU_LAUNCH(k_sum_rows, 1, kFinal, 0, rows, nrows, kind, npts, dout, dcount);
+    LSMGPU_LAUNCH(k_sum_parts, 1, kFinal, 0, pn, pv, nparts, kind, A.dv, (R)ib.size(), dout, dcount);
     call.finish();
   }
 };
@@ -332,7 +470,7 @@ static void volume_integral(const char *name, int kind, R *int_F, const R *F, co
   s.A.phi = s.in(phi, pb);
   if (cv) s.control_volume(cv, cb, sgn);
   s.cell_volume(dx, dy, dz);
-  s.A.eps = eps;
+  s.epsilon(eps);
   s.run(kind, int_F, nullptr);
 }
 
@@ -359,8 +497,7 @@ static void surface_integral(const char *name, R *int_F, const R *F, const Box &
   s.A.pz = s.in(phi_z, gb);
   if (cv) s.control_volume(cv, cb, sgn);
   s.cell_volume(dx, dy, dz);
-  s.A.eps = eps;
-  s.A.inv_eps = R(1.0) / eps;
+  s.epsilon(eps);
   s.run(SURF_INT, int_F, nullptr);
 }
 
@@ -470,7 +607,7 @@ static void volume_region(const char *name, int kind, R *volume, const R *phi, c
   s.A.phi = s.in(phi, pb);
   if (cv) s.control_volume(cv, cb, sgn);
   s.cell_volume(dx, dy, dz);
-  s.A.eps = eps;
+  s.epsilon(eps);
   s.run(kind, volume, nullptr);
 }
 
@@ -506,10 +643,7 @@ static void surface_area(const char *name, bool delta_form, R *area, const R *ph
   s.A.pz = s.in(phi_z, gb);
   if (cv) s.control_volume(cv, cb, sgn);
   s.cell_volume(dx, dy, dz);
-  if (!delta_form) {
-    s.A.eps = eps;
-    s.A.inv_eps = R(1.0) / eps;
-  }
+  if (!delta_form) s.epsilon(eps);
   s.run(delta_form ? AREA_DELTA : AREA, area, nullptr);
 }
 

@@ -1,0 +1,272 @@
+#!/usr/bin/env python3
+"""Maintainer tool: regenerate include/lsmgpu_toolbox3d.h and
+lsmlib_gb300/abi.json for the drop-in entry points this library implements.
+
+The argument lists come from the signature dump that oracle/f77ref.py writes
+when it translates the reference's Fortran (oracle/_ref/sigs.json, produced
+by `python -m oracle.build`), so every declaration has the reference
+routine's exact argument order; the C-header line cited beside each comes
+from the reference tree's own headers (searched under /root/reference/src).
+
+    python -m lsmlib_gb300.gen_abi
+"""
+import json
+import os
+import re
+import subprocess
+
+REF = "/root/reference"
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+# symbol -> (header group, one-line description)
+DESC = {
+    # spatial derivatives
+    "lsm3dhjeno1_": ("deriv", "first-order HJ ENO plus/minus gradients"),
+    "lsm3dhjeno2_": ("deriv", "second-order HJ ENO plus/minus gradients"),
+    "lsm3dhjeno3_": ("deriv", "third-order HJ ENO plus/minus gradients"),
+    "lsm3dhjweno5_": ("deriv", "fifth-order HJ WENO plus/minus gradients"),
+    "lsm3dupwindhjeno1_": ("deriv", "first-order upwind HJ ENO gradient for a velocity field"),
+    "lsm3dupwindhjeno2_": ("deriv", "second-order upwind HJ ENO gradient"),
+    "lsm3dupwindhjeno3_": ("deriv", "third-order upwind HJ ENO gradient"),
+    "lsm3dupwindhjweno5_": ("deriv", "fifth-order upwind HJ WENO gradient"),
+    "lsm3dcentralgradorder2_": ("deriv", "second-order central gradient"),
+    "lsm3dcentralgradorder4_": ("deriv", "fourth-order central gradient"),
+    "lsm3dlaplacianorder2_": ("deriv", "second-order Laplacian"),
+    "lsm3dgradientmagnitude_": ("deriv", "|grad phi| with the reference's 1e-8 clamps"),
+    # RK
+    "lsm3drk1step_": ("rk", "forward Euler step u_next = u + dt*L"),
+    "lsm3dtvdrk2stage1_": ("rk", "TVD RK2 stage 1 (an Euler step)"),
+    "lsm3dtvdrk2stage2_": ("rk", "TVD RK2 stage 2: 0.5*(u + u1 + dt*L)"),
+    "lsm3dtvdrk3stage1_": ("rk", "TVD RK3 stage 1 (an Euler step)"),
+    "lsm3dtvdrk3stage2_": ("rk", "TVD RK3 stage 2: 0.75*u + 0.25*(u1 + dt*L)"),
+    "lsm3dtvdrk3stage3_": ("rk", "TVD RK3 stage 3: u/3 + 2/3*(u2 + dt*L)"),
+    # LSE
+    "lsm3dzerooutlevelseteqnrhs_": ("lse", "zero the level set equation RHS over its ghost box"),
+    "lsm3daddadvectiontermtolserhs_": ("lse", "rhs -= u . grad(phi)"),
+    "lsm3daddnormalveltermtolserhs_": ("lse", "rhs -= Vn |grad phi| (Godunov), Vn a field"),
+    "lsm3daddconstnormalveltermtolserhs_": ("lse", "rhs -= Vn |grad phi| (Godunov), Vn constant"),
+    "lsm3daddconstcurvtermtolserhs_": ("lse", "rhs += b * kappa |grad phi| from first and second derivatives"),
+    # reinit / curvature
+    "lsm3dcomputereinitializationeqnrhs_": ("reinit", "reinitialization RHS sgn(phi)(1 - |grad phi|), Godunov"),
+    "lsm3dcomputemeancurvatureorder2_": ("geom", "second-order mean curvature"),
+    # reductions
+    "lsm3dmaxnormdiff_": ("red", "max |field1 - field2| over an index box"),
+    "lsm3dcomputestableadvectiondt_": ("red", "CFL-stable dt for advection"),
+    "lsm3dcomputestablenormalveldt_": ("red", "CFL-stable dt for a normal velocity field"),
+    "lsm3dcomputestableconstnormalveldt_": ("red", "CFL-stable dt for a constant normal velocity"),
+    "lsm3daveabsdiff_": ("red", "mean |field1 - field2| over an index box"),
+    "lsm3dvoxelcountgreaterthanzero_": ("red", "number of cells with phi > 0"),
+    "lsm3dvoxelcountlessthanzero_": ("red", "number of cells with phi < 0"),
+    "lsm3dvolumeintegralphilessthanzero_": ("red", "integral of F over {phi < 0} with a smoothed Heaviside"),
+    "lsm3dvolumeintegralphigreaterthanzero_": ("red", "integral of F over {phi > 0} with a smoothed Heaviside"),
+    "lsm3dsurfaceintegral_": ("red", "integral of F over {phi = 0} with a smoothed delta"),
+    "lsm3dmaxnormdiffcontrolvolume_": ("red", "max |field1 - field2| over cells of one control-volume sign (seeded with the box corner)"),
+    "lsm3dcomputestableadvectiondtcontrolvolume_": ("red", "CFL-stable advection dt over cells of one control-volume sign"),
+    "lsm3dcomputestablenormalveldtcontrolvolume_": ("red", "CFL-stable normal-velocity dt over cells of one control-volume sign"),
+    "lsm3dcomputestableconstnormalveldtcontrolvolume_": ("red", "CFL-stable constant normal-velocity dt over cells of one control-volume sign"),
+    "lsm3dvolumeintegralphilessthanzerocontrolvolume_": ("red", "volume integral over {phi < 0} restricted to one control-volume sign"),
+    "lsm3dvolumeintegralphigreaterthanzerocontrolvolume_": ("red", "volume integral over {phi > 0} restricted to one control-volume sign"),
+    "lsm3dsurfaceintegralcontrolvolume_": ("red", "surface integral restricted to one control-volume sign"),
+    "lsm3dvoxelcountgreaterthanzerocontrolvolume_": ("red", "number of cells with phi > 0 and the selected control-volume sign"),
+    "lsm3dvoxelcountlessthanzerocontrolvolume_": ("red", "number of cells with phi < 0 and the selected control-volume sign"),
+    # geometry
+    "lsm3dcomputeunitnormal_": ("geo", "unit normal grad phi / |grad phi| ((1,0,0) where |grad phi| < zero_tol)"),
+    "lsm3dcomputesignedunitnormal_": ("geo", "sgn(phi) grad phi / |grad phi| with the smoothed sign"),
+    "lsm3dcomputemeancurvature_": ("geo", "mean curvature from first and second derivatives"),
+    "lsm3dvolumeregionphilessthanzero_": ("geo", "volume of {phi < 0} with a smoothed Heaviside"),
+    "lsm3dvolumeregionphigreaterthanzero_": ("geo", "volume of {phi > 0} with a smoothed Heaviside"),
+    "lsm3dsurfaceareazerolevelset_": ("geo", "area of {phi = 0} with a smoothed delta"),
+    "lsm3dsurfaceareazerolevelsetdelta_": ("geo", "area of {phi = 0} from a precomputed delta function"),
+    "lsm3dvolumeregionphilessthanzerocontrolvolume_": ("geo", "volume of {phi < 0} over one control-volume sign"),
+    "lsm3dvolumeregionphigreaterthanzerocontrolvolume_": ("geo", "volume of {phi > 0} over one control-volume sign"),
+    "lsm3dsurfaceareazerolevelsetcontrolvolume_": ("geo", "area of {phi = 0} over one control-volume sign"),
+    "lsm3dsurfaceareazerolevelsetdeltacontrolvolume_": ("geo", "area of {phi = 0} from a delta function over one control-volume sign"),
+    # extra dense
+    "lsm3dcentralhessian_": ("deriv", "second-order central Hessian"),
+    "lsm3daveragegradphi_": ("deriv", "average of plus and minus gradients"),
+    "lsm3dphiupwindgradf_": ("deriv", "gradient of F upwinded by the local extremum of phi"),
+    "lsm3daddconstprecomputedcurvtermtolserhs_": ("lse", "rhs += b * kappa * |grad phi| (loops k,j from the fill box to the ghost box end and i over the ghost box, as the reference does)"),
+    "lsm3daddexternalandnormalveltermtolserhs_": ("lse", "rhs -= u . grad(phi) + Vn |grad phi| with the combined Godunov upwinding (same loop bounds as the reference)"),
+    # boundary conditions
+    "lsm3dlinearextrapolation_": ("bc", "linear extrapolation into the ghost cells of one face"),
+    "lsm3dsignedlinearextrapolation_": ("bc", "signed linear extrapolation into the ghost cells of one face"),
+    "lsm3dcopyextrapolation_": ("bc", "copy extrapolation into the ghost cells of one face"),
+    "lsm3dhomogeneousneumanneno1_": ("bc", "homogeneous Neumann fill for ENO1 (copy extrapolation)"),
+    "lsm3dhomogeneousneumanneno2_": ("bc", "homogeneous Neumann fill for ENO2 (copy extrapolation)"),
+    "lsm3dhomogeneousneumanneno3_": ("bc", "homogeneous Neumann fill for ENO3 (copy extrapolation)"),
+    "lsm3dhomogeneousneumannweno5_": ("bc", "homogeneous Neumann fill for WENO5 (copy extrapolation)"),
+    # local derivatives
+    "lsm3dcomputednlocal_": ("local", "n-th undivided differences over an index list"),
+    "lsm3dhjeno1local_": ("local", "HJ ENO1 plus/minus gradients on level-0 band cells"),
+    "lsm3dhjeno2local_": ("local", "HJ ENO2 plus/minus gradients on level-0 band cells"),
+    "lsm3dhjeno3local_": ("local", "HJ ENO3 plus/minus gradients on level-0 band cells"),
+    "lsm3dhjweno5local_": ("local", "HJ WENO5 plus/minus gradients on level-0 band cells"),
+    "lsm3dcentralgradorder2local_": ("local", "second-order central gradient on band cells"),
+    "lsm3dcentralgradorder4local_": ("local", "fourth-order central gradient on band cells"),
+    "lsm3dlaplacianorder2local_": ("local", "second-order Laplacian on band cells"),
+    "lsm3dcomputeavegradphilocal_": ("local", "average |grad phi| over band cells"),
+    "lsm3dgradientmagnitudelocal_": ("local", "|grad phi| on band cells (zero_tol clamps)"),
+    # local RK
+    "lsm3drk1steplocal_": ("local", "Euler step on band cells"),
+    "lsm3dtvdrk2stage1local_": ("local", "TVD RK2 stage 1 on band cells"),
+    "lsm3dtvdrk2stage2local_": ("local", "TVD RK2 stage 2 on band cells"),
+    "lsm3dtvdrk3stage1local_": ("local", "TVD RK3 stage 1 on band cells"),
+    "lsm3dtvdrk3stage2local_": ("local", "TVD RK3 stage 2 on band cells"),
+    "lsm3dtvdrk3stage3local_": ("local", "TVD RK3 stage 3 on band cells"),
+    # local LSE
+    "lsm3dzerooutlevelseteqnrhslocal_": ("local", "zero the RHS on listed cells"),
+    "lsm3daddadvectiontermtolserhslocal_": ("local", "advection term on band cells"),
+    "lsm3daddnormalveltermtolserhslocal_": ("local", "normal velocity term (field) on band cells"),
+    "lsm3daddconstnormalveltermtolserhslocal_": ("local", "normal velocity term (constant) on band cells"),
+    "lsm3daddconstcurvtermtolserhslocal_": ("local", "curvature term on band cells"),
+    "lsm3dcomputereinitializationeqnrhslocal_": ("local", "reinitialization RHS on band cells"),
+    "lsm3dcomputemeancurvatureorder2local_": ("local", "second-order mean curvature on band cells"),
+    "lsm3dmaxnormdifflocal_": ("local", "max |field1 - field2| over band cells (starts at 0)"),
+    "lsm3dcomputestableadvectiondtlocal_": ("local", "CFL-stable advection dt over band cells"),
+    "lsm3dcomputestablenormalveldtlocal_": ("local", "CFL-stable normal-velocity dt over band cells"),
+    "lsm3dmaxnormdiffcontrolvolumelocal_": ("local", "max |field1 - field2| over band cells with a negative control volume (starts at 0)"),
+    "lsm3dcomputestablenormalveldtcontrolvolumelocal_": ("local", "CFL-stable normal-velocity dt over band cells of one control-volume sign"),
+    "lsm3dcomputestableconstnormalveldtlocal_": ("local", "CFL-stable constant normal-velocity dt over band cells (the reference routine reads two unassigned variables; this computes the dense routine's formula)"),
+    # band construction
+    "lsm3ddeterminenarrowband_": ("band", "build the narrow band: level-0 list in sweep order, outer lists, BFS levels"),
+    "lsm3dmarknarrowbandneighbors_": ("band", "breadth-first neighbour levels of a narrow band"),
+    "lsm3dmarknarrowbandboundarylayer_": ("band", "mark the one-cell faces of a fill box"),
+    "lsm3ddeterminenarrowbandfrommask_": ("band", "build a narrow band from the sign of a mask"),
+    "lsm3dmultiplycutofflserhslocal_": ("band", "cubic cut-off of the RHS between beta and gamma"),
+    "lsm3dcheckouternarrowbandlayer_": ("band", "1 when the outer band layer holds both signs of phi"),
+    "lsm3dimposemasklocal_": ("band", "dest = max(mask, src) on listed cells"),
+    "lsm3dcopydatalocal_": ("band", "dest = src on listed cells"),
+}
+
+
+# entry points LSMLIB lacks in 3D, with argument lists following the 2D
+# *_local routines (spatial_derivatives2d_local.f.in:498, :816)
+def _box(n):
+    return [[f"{a}_{n}_gb", "int", False, False] for a in ("ilo", "ihi", "jlo", "jhi", "klo", "khi")]
+
+
+_PM = ([["phi_x_plus", "real", True, True], ["phi_y_plus", "real", True, True], ["phi_z_plus", "real", True, True]]
+       + _box("grad_phi_plus") +
+       [["phi_x_minus", "real", True, True], ["phi_y_minus", "real", True, True], ["phi_z_minus", "real", True, True]]
+       + _box("grad_phi_minus") + [["phi", "real", True, False]] + _box("phi"))
+_TAIL_IDX = ([["dx", "real", False, False], ["dy", "real", False, False], ["dz", "real", False, False],
+              ["index_x", "int", True, False], ["index_y", "int", True, False], ["index_z", "int", True, False]]
+             + [[f"{a}_index{l}", "int", False, False] for l in range(4) for a in ("nlo", "nhi")]
+             + [["narrow_band", "int1", True, False]] + _box("nb") + [["mark_fb", "int1", False, False]])
+NEW_SIGS = {
+    "lsm3dhjweno5local_": {"src": "NEW (pattern: src/toolbox/lsm_spatial_derivatives2d_local.f.in:816)",
+                           "args": _PM + [["d1", "real", True, True]] + _box("d1") + _TAIL_IDX +
+                                   [["mark_d1", "int1", False, False]]},
+    "lsm3dhjeno3local_": {"src": "NEW (pattern: src/toolbox/lsm_spatial_derivatives2d_local.f.in:498)",
+                          "args": _PM + [["d1", "real", True, True]] + _box("d1") + [["d2", "real", True, True]]
+                                  + _box("d2") + [["d3", "real", True, True]] + _box("d3") + _TAIL_IDX +
+                                  [["mark_d1", "int1", False, False], ["mark_d2", "int1", False, False],
+                                   ["mark_d3", "int1", False, False]]},
+}
+
+GROUP_TITLE = {
+    "deriv": "Spatial derivatives (src/toolbox/lsm_spatial_derivatives3d)",
+    "rk": "TVD Runge-Kutta stages (src/toolbox/lsm_tvd_runge_kutta3d)",
+    "lse": "Level set equation right-hand sides (src/toolbox/lsm_level_set_evolution3d)",
+    "reinit": "Reinitialization (src/reinitialization/lsm_reinitialization3d)",
+    "geom": "Curvature (src/geometry/lsm_curvature3d)",
+    "red": "Reductions (src/toolbox/lsm_math_utils3d)",
+    "geo": "Geometry: normals, curvature, volumes and areas (src/geometry/lsm_geometry3d_fort)",
+    "local": "Narrow-band (index-list) variants (*_local)",
+    "band": "Narrow-band construction and utilities (src/toolbox/lsm_localization3d)",
+    "bc": "Boundary conditions (src/boundary_conditions/lsm_boundary_conditions3d)",
+}
+
+
+def header_line(sym):
+    """(header path, line) of the C declaration whose LSM3D_* macro names sym."""
+    out = subprocess.run(["grep", "-rn", "--include=*.h", sym, REF + "/src"],
+                         capture_output=True, text=True).stdout
+    for line in out.splitlines():
+        path, ln, text = line.split(":", 2)
+        m = re.match(r"\s*#define\s+(\w+)", text)
+        macro = m.group(1) if m else None
+        if not macro:
+            # continuation style: '#define X \' on the previous line
+            prev = open(path).read().splitlines()[int(ln) - 2]
+            m = re.match(r"\s*#define\s+(\w+)", prev)
+            macro = m.group(1) if m else None
+        if not macro:
+            continue
+        txt = open(path).read().splitlines()
+        for i, t in enumerate(txt, 1):
+            if re.match(r"\s*void\s+" + macro + r"\s*\(", t):
+                return os.path.relpath(path, REF), i
+        return os.path.relpath(path, REF), int(ln)
+    return None, None
+
+
+def ctype(kind, is_arr, written):
+    base = {"real": "double", "int": "int", "int1": "unsigned char", "logical": "int",
+            "double": "double"}[kind]
+    return ("" if written else "const ") + base + " *"
+
+
+def main():
+    sigs = json.load(open(os.path.join(REPO, "oracle", "_ref", "sigs.json")))
+    abi, groups = {}, {}
+    for s in DESC:
+        if s in NEW_SIGS:
+            abi[s] = {"ref": NEW_SIGS[s]["src"], "header": None, "args": NEW_SIGS[s]["args"]}
+        else:
+            sg = sigs[s]
+            src, line = sg["src"].split(":")
+            hpath, hline = header_line(s)
+            abi[s] = {"ref": f"{os.path.relpath(src, REF)}:{line}",
+                      "header": f"{hpath}:{hline}" if hpath else None, "args": sg["args"]}
+        groups.setdefault(DESC[s][0], []).append(s)
+    with open(os.path.join(REPO, "lsmlib_gb300", "abi.json"), "w") as f:
+        json.dump(abi, f, indent=1)
+    lines = [
+        "/*",
+        " * lsmgpu drop-in entry points for LSMLIB's 3D toolbox.",
+        " *",
+        " * Every function below has the symbol name and argument list of the LSMLIB",
+        " * Fortran routine it replaces (the name gfortran exports, which LSMLIB's C",
+        " * headers #define their LSM3D_* macros to), so a program built against",
+        " * LSMLIB's headers links against liblsmgpu.so unchanged.  All arguments are",
+        " * pointers, arrays are column-major over the ghost box given by the six",
+        " * bounds that follow them, and real numbers are double (LSMLIB's default",
+        " * FP64 build).  Pointer, scratch and error rules: see lsmgpu.h.",
+        " *",
+        " * Each declaration cites the reference routine (Fortran file:line) and the",
+        " * C declaration it mirrors (header file:line), relative to the LSMLIB tree.",
+        " */",
+        "#ifndef LSMGPU_TOOLBOX3D_H",
+        "#define LSMGPU_TOOLBOX3D_H",
+        "",
+        "#ifdef __cplusplus",
+        'extern "C" {',
+        "#endif",
+        "",
+    ]
+    for g, members in groups.items():
+        lines += ["/* " + "-" * 70 + " */", "/* " + GROUP_TITLE[g] + " */", "/* " + "-" * 70 + " */", ""]
+        for s in members:
+            a = abi[s]
+            lines.append(f"/* {DESC[s][1]}.")
+            if a["ref"].startswith("NEW"):
+                lines.append(" * No 3D counterpart in LSMLIB; arguments follow the 2D routine "
+                             + a["ref"][len("NEW (pattern: "):-1] + ".")
+            else:
+                lines.append(f" * Replaces {a['ref']}" + (f"; C declaration {a['header']}." if a["header"] else "."))
+            lines.append(" */")
+            lines.append(f"void {s}(")
+            args = a["args"]
+            for i, (nm, kind, is_arr, written) in enumerate(args):
+                sep = "," if i < len(args) - 1 else ");"
+                lines.append(f"  {ctype(kind, is_arr, written)}{nm}{sep}")
+            lines.append("")
+    lines += ["#ifdef __cplusplus", "}", "#endif", "", "#endif /* LSMGPU_TOOLBOX3D_H */", ""]
+    with open(os.path.join(REPO, "include", "lsmgpu_toolbox3d.h"), "w") as f:
+        f.write("\n".join(lines))
+    print(len(abi), "entry points")
+
+
+if __name__ == "__main__":
+    main()

@@ -4,6 +4,7 @@
   python -m lsmlib_gb300.profile_case --mode adjoint --n 128 --iters 8 --precision f32
   python -m lsmlib_gb300.profile_case --mode band --n 256 --iters 10
   python -m lsmlib_gb300.profile_case --mode batched --n 512 --iters 2
+  python -m lsmlib_gb300.profile_case --mode geometry --n 256 --iters 1
 
 Builds the same analytic field as bench.py, moves it to the device, and runs
 `iters` WENO5 / TVD-RK3 iterations (3 stage kernels each) of reinitialization
@@ -15,6 +16,8 @@ adjoint stages k_adj_xz and k_adj_y.
 Mode band runs `iters` narrow-band curvature-flow steps of bench.band_case
 at n^3 (rebuild every 5 steps, FP32).  Mode batched advects `n` grids of
 bench.batched_case `iters` steps (persistent kernel in a CUDA graph).
+Mode geometry runs bench.sub_geometry at n^3 with `iters` calls per entry
+(volume, area, count; kernels k_row_sums and k_sum_parts).
 """
 import argparse
 import os
@@ -28,7 +31,7 @@ sys.path.insert(0, ROOT)
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--mode", choices=["reinit", "advect", "adjoint", "band", "batched"], default="reinit")
+    ap.add_argument("--mode", choices=["reinit", "advect", "adjoint", "band", "batched", "geometry"], default="reinit")
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--iters", type=int, default=1)
     ap.add_argument("--precision", choices=["f32", "f64"], default="f32")
@@ -51,6 +54,11 @@ def main():
         torch.cuda.synchronize()
         L.check()
         print("ok", a.mode, a.n, a.iters, a.precision, "J", J, "launches", L.launch_count())
+        return
+    if a.mode == "geometry":
+        r = bench.sub_geometry(torch.cuda.current_stream(), "cuda", n=a.n, reps=a.iters)
+        L.check()
+        print("ok", a.mode, a.n, {k: v["ms_per_call"] for k, v in r.items() if isinstance(v, dict)})
         return
     if a.mode == "band":
         phi, dx = bench.band_case("cuda", a.n)

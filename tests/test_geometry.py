@@ -270,3 +270,21 @@ def test_gpu_sphere_properties_128(gpu_lib):
         vals = geo_vals(sym, c)
         want = H.run(H.oracle(), sym, vals)[1][out_scalar(sym)]
         assert_sum_close(sym, run(sym), want, abs(want), 128 ** 3)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("eps", [0.0, -0.3, 0.05, 3.0])
+def test_gpu_sums_any_epsilon(eps, gpu_lib):
+    """Positive finite epsilons classify cells on bit patterns; zero and
+    negative ones take the reference's comparisons as written."""
+    for sym in ("lsm3dvolumeregionphilessthanzero_", "lsm3dvolumeregionphigreaterthanzero_",
+                "lsm3dvolumeintegralphilessthanzero_", "lsm3dsurfaceareazerolevelset_"):
+        vals = case(sym, 11, eps=eps)
+        k = out_scalar(sym)
+        want = H.run(H.oracle(), sym, vals)[1][k]
+        got = H.run(gpu_lib, sym, vals)[1][k]
+        L.check(gpu_lib)
+        if not np.isfinite(want):
+            assert H.same(want, got), "%s eps %g: %r vs %r" % (sym, eps, want, got)
+            continue
+        assert_sum_close(sym, got, want, abs_scale(H.oracle(), sym, vals), n_cells(vals))
