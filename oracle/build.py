@@ -5,7 +5,9 @@
   multiply-add alters a rounding.
 * oracle/_ref/liblsmref.so — LSMLIB's own Fortran kernels, translated to C by
   f77ref.py from the reference source tree (when it is present) and compiled
-  the same way.  The translated C (oracle/_ref/lsmref.c) is kept out of
+  the same way.
+* oracle/_ref/liblsmrefio.so — LSMLIB's own Grid / data-array file code
+  (src/utils, C), compiled from the reference tree when it is present.  The translated C (oracle/_ref/lsmref.c) is kept out of
   version control; where the reference tree is absent, an existing
   lsmref.c is compiled as is.
 
@@ -79,9 +81,39 @@ def build_ref():
     return out
 
 
+# The reference's on-disk format code (C), compiled from its own files.
+REF_IO_SOURCES = ["utils/lsm_grid.c", "utils/lsm_data_arrays.c", "utils/lsm_file.c"]
+
+# The values the reference's build writes into lsmlib_config.h for its
+# double-precision configuration (include/lsmlib_config.h.in).
+REF_IO_CONFIG = """#define LSMLIB_DOUBLE_PRECISION
+#define LSMLIB_REAL double
+#define LSMLIB_ZERO_TOL 1.e-11
+#define LSMLIB_REAL_MAX 1.7976931348623157e308
+#define LSMLIB_REAL_MIN 2.2250738585072014e-308
+#define LSMLIB_REAL_EPSILON 2.2204460492503131e-16
+"""
+
+
+def build_ref_io():
+    """Compile the reference's Grid / data-array file code
+    (oracle/_ref/liblsmrefio.so) when the reference tree is present."""
+    if not os.path.isdir(REFERENCE_TREE):
+        return None
+    os.makedirs(REF_DIR, exist_ok=True)
+    with open(os.path.join(REF_DIR, "lsmlib_config.h"), "w") as f:
+        f.write(REF_IO_CONFIG)
+    srcs = [os.path.join(REFERENCE_TREE, "src", s) for s in REF_IO_SOURCES]
+    out = os.path.join(REF_DIR, "liblsmrefio.so")
+    _run([_cc(), "-O2", "-fPIC", "-shared", "-w", "-I", REF_DIR,
+          "-I", os.path.join(REFERENCE_TREE, "src", "utils"), "-o", out] + srcs + ["-lm"])
+    return out
+
+
 def build():
     o = build_oracle()
     r = build_ref()
+    build_ref_io()
     return o, r
 
 
