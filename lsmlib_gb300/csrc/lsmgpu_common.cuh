@@ -16,6 +16,14 @@
 
 namespace lsmgpu {
 
+// Dimension of the drop-in call running on this host thread: 3 normally; 2
+// or 1 while a 2D / 1D entry point (lifted.cu) runs the 3D routine on its
+// arrays, which are then 3D arrays with one cell along the missing axes.  In
+// that state every view has stride 0 along those axes (a stencil reaching
+// along them reads the centre cell, so its differences are exactly 0) and a
+// stencil's reach along them is not required of the ghost boxes.
+extern thread_local int g_lift_dims;
+
 // ---------------------------------------------------------------------------
 // index spaces
 // ---------------------------------------------------------------------------
@@ -30,6 +38,8 @@ struct Box {
   // true when `o` (grown by `g` cells per side along each axis) fits in this box
   __host__ bool contains(const Box &o, int gx, int gy, int gz) const {
     if (o.empty()) return true;
+    if (g_lift_dims < 3) gz = 0;
+    if (g_lift_dims < 2) gy = 0;
     return o.lo[0] - gx >= lo[0] && o.hi[0] + gx <= hi[0] && o.lo[1] - gy >= lo[1] &&
            o.hi[1] + gy <= hi[1] && o.lo[2] - gz >= lo[2] && o.hi[2] + gz <= hi[2];
   }
@@ -47,13 +57,17 @@ inline Box isect(const Box &a, const Box &b) {
   return r;
 }
 // the cells c of b for which c - lo_reach .. c + hi_reach (per axis) stay in b
+// (no reach is required along the missing axes of a 2D / 1D call)
 inline Box inner(const Box &b, int rx0, int rx1, int ry0, int ry1, int rz0, int rz1) {
+  if (g_lift_dims < 3) rz0 = rz1 = 0;
+  if (g_lift_dims < 2) ry0 = ry1 = 0;
   Box r = b;
   r.lo[0] += rx0; r.hi[0] -= rx1;
   r.lo[1] += ry0; r.hi[1] -= ry1;
   r.lo[2] += rz0; r.hi[2] -= rz1;
   return r;
 }
+// (empty along a missing axis of a 2D / 1D call: work along it is skipped)
 inline Box inner_axis(const Box &b, int axis, int lo_reach, int hi_reach) {
   Box r = b;
   r.lo[axis] += lo_reach;
@@ -88,8 +102,8 @@ inline View<T> view(T *p, const Box &b) {
   View<T> v;
   v.p = p;
   v.lo0 = b.lo[0]; v.lo1 = b.lo[1]; v.lo2 = b.lo[2];
-  v.s1 = b.n(0);
-  v.s2 = b.n(0) * b.n(1);
+  v.s1 = g_lift_dims < 2 ? 0 : b.n(0);
+  v.s2 = g_lift_dims < 3 ? 0 : b.n(0) * b.n(1);
   return v;
 }
 

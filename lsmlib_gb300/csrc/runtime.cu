@@ -13,6 +13,8 @@
 
 namespace lsmgpu {
 
+thread_local int g_lift_dims = 3;
+
 namespace {
 
 thread_local int g_err = LSMGPU_OK;

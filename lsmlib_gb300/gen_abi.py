@@ -1,6 +1,16 @@
 #!/usr/bin/env python3
-"""Maintainer tool: regenerate include/lsmgpu_toolbox3d.h and
-lsmlib_gb300/abi.json for the drop-in entry points this library implements.
+"""Maintainer tool: regenerate include/lsmgpu_toolbox{3d,2d,1d}.h,
+lsmlib_gb300/abi.json and lsmlib_gb300/csrc/lifted.cu for the drop-in entry
+points this library implements.
+
+The 2D and 1D entry points run the 3D routines on their arrays (see
+csrc/lift.cuh); lifted.cu holds one generated wrapper per routine that maps
+its arguments onto the 3D routine's by position: missing array components
+become stand-in buffers, missing k (and j) bounds 0, a missing dz (and dy)
+the caller's dx (1 where the routine multiplies a cell volume).  A 2D / 1D
+routine is lifted when its 3D counterpart is implemented, every one of its
+arguments finds its place and its arithmetic is the 3D routine's with the
+missing terms removed (NOT_LIFTED lists the exceptions).
 
 The argument lists come from the signature dump that oracle/f77ref.py writes
 when it translates the reference's Fortran (oracle/_ref/sigs.json, produced
@@ -207,6 +217,157 @@ def ctype(kind, is_arr, written):
     return ("" if written else "const ") + base + " *"
 
 
+BOUND = re.compile(r"^(ilo|ihi|jlo|jhi|klo|khi)_")
+
+# 2D / 1D routines whose arithmetic or loop bounds are not the 3D routine's
+# with the missing terms removed: the 1D normal-velocity dt is |vn| / dx
+# (math_utils1d.f.in); the 2D external-plus-normal velocity term loops over
+# the fill box where the 3D routine loops from the fill box to the ghost box
+# end (level_set_evolution3d.f.in:620); the 1D signed extrapolation takes the
+# sign from the second fill-box cell (boundary_conditions1d.f), the 3D one
+# from the first.
+NOT_LIFTED = {"lsm1dcomputestablenormalveldt_", "lsm1dcomputestablenormalveldtcontrolvolume_",
+              "lsm2daddexternalandnormalveltermtolserhs_", "lsm1dsignedlinearextrapolation_"}
+
+# 3D routines whose dz (and dy) multiply a cell volume: lifted with 1 there
+VOLUME_FACTOR = re.compile(r"volumeintegral|volumeregion|surfaceintegral|surfacearea")
+
+
+def missing_component(name, dims):
+    """True for an array argument that is a z (1D: y or z) component:
+    phi_z_plus, vel_z, phi_xz, index_z, ..."""
+    gone = "z" if dims == 2 else "yz"
+    return any(re.fullmatch(r"[xyz]+", t) and any(c in t for c in gone) for t in name.split("_")[1:])
+
+
+def lift_map(sym2, dims, abi3, sigs):
+    """Argument expressions of the 3D call for the 2D / 1D routine sym2 and
+    the Lift registrations, or None when the arguments do not map."""
+    sym3 = "lsm3d" + sym2[5:]
+    if sym3 not in abi3 or sym2 not in sigs or sym2 in NOT_LIFTED:
+        return None
+    spacing = "&L_.one" if VOLUME_FACTOR.search(sym3) else "dx"
+    a3, a2 = abi3[sym3]["args"], sigs[sym2]["args"]
+    names2 = [a[0] for a in a2]
+    out, j = [], 0
+    for name, kind, is_arr, written in a3:
+        m = BOUND.match(name)
+        if is_arr:
+            if name in names2:
+                if j >= len(a2) or a2[j][0] != name:
+                    return None
+                out.append(name)
+                j += 1
+            elif not missing_component(name, dims):
+                return None
+            elif written:
+                if kind not in ("real", "double"):
+                    return None
+                out.append("L_.junk()")
+            else:
+                out.append({"real": "L_.zero()", "double": "L_.zero()", "int": "L_.zero_int()"}.get(kind))
+                if out[-1] is None:
+                    return None
+        elif m:
+            axis = m.group(1)[0]
+            if (dims == 2 and axis == "k") or (dims == 1 and axis in "jk"):
+                out.append("&L_.k0")
+            else:
+                if j >= len(a2) or not BOUND.match(a2[j][0]) or a2[j][0][:3] != m.group(1):
+                    return None
+                out.append(a2[j][0])
+                j += 1
+        else:
+            if j < len(a2) and a2[j][0] == name:
+                out.append(name)
+                j += 1
+            elif (name == "dz" and dims <= 2) or (name == "dy" and dims == 1):
+                out.append(spacing)
+            else:
+                return None
+    if j != len(a2):
+        return None
+    regs = []
+    for q, (name, kind, is_arr, written) in enumerate(a2):
+        if name.startswith("ilo_"):
+            if dims == 2:
+                regs.append("L_.box(%s, %s, %s, %s);" % tuple(a2[q + t][0] for t in range(4)))
+            else:
+                regs.append("L_.box(%s, %s);" % (a2[q][0], a2[q + 1][0]))
+        if name.startswith("nlo_index") and q + 1 < len(a2) and a2[q + 1][0].startswith("nhi_index"):
+            regs.append("L_.list(%s, %s);" % (name, a2[q + 1][0]))
+    return {"sym3": sym3, "args": out, "regs": regs}
+
+
+def write_lifted(abi, lifted):
+    lines = [
+        "// GENERATED by lsmlib_gb300/gen_abi.py -- do not edit.",
+        "//",
+        "// LSMLIB's 2D and 1D drop-in routines, each running the 3D routine on its",
+        "// arrays with the missing axes lifted (lift.cuh).  Each wrapper cites the",
+        "// reference routine it replaces; its declaration is in",
+        "// include/lsmgpu_toolbox2d.h or include/lsmgpu_toolbox1d.h.",
+        '#include "lift.cuh"',
+        '#include "../../include/lsmgpu_toolbox3d.h"',
+        '#include "../../include/lsmgpu_toolbox2d.h"',
+        '#include "../../include/lsmgpu_toolbox1d.h"',
+        "",
+        "using lsmgpu::Lift;",
+        "",
+        'extern "C" {',
+        "",
+    ]
+    for sym2, (dims, mp) in lifted.items():
+        params = ", ".join(ctype(k, a, w) + n for n, k, a, w in abi[sym2]["args"])
+        lines.append("// %s" % abi[sym2]["ref"])
+        lines.append("void %s(%s) {" % (sym2, params))
+        lines.append('  Lift L_(%d, "%s");' % (dims, sym2))
+        for r in mp["regs"]:
+            lines.append("  " + r)
+        lines.append("  if (!L_.ready()) return;")
+        lines.append("  %s(%s);" % (mp["sym3"], ", ".join(mp["args"])))
+        lines.append("}")
+        lines.append("")
+    lines += ['}  // extern "C"', ""]
+    with open(os.path.join(REPO, "lsmlib_gb300", "csrc", "lifted.cu"), "w") as f:
+        f.write("\n".join(lines))
+
+
+def write_header(path, guard, title, syms, abi, desc):
+    lines = [
+        "/*",
+        " * lsmgpu drop-in entry points for LSMLIB's %s toolbox." % title,
+        " *",
+        " * Same conventions as lsmgpu_toolbox3d.h: LSMLIB's symbol names and",
+        " * argument lists, column-major arrays over the ghost box given by the",
+        " * bounds that follow them, double precision.  Each routine runs the 3D",
+        " * kernels on its arrays (one cell along the missing axes, stride 0) and",
+        " * matches the reference routine bit for bit.",
+        " */",
+        "#ifndef %s" % guard,
+        "#define %s" % guard,
+        "",
+        "#ifdef __cplusplus",
+        'extern "C" {',
+        "#endif",
+        "",
+    ]
+    for s in syms:
+        a = abi[s]
+        lines.append("/* %s." % desc[s])
+        lines.append(f" * Replaces {a['ref']}" + (f"; C declaration {a['header']}." if a["header"] else "."))
+        lines.append(" */")
+        lines.append(f"void {s}(")
+        args = a["args"]
+        for i, (nm, kind, is_arr, written) in enumerate(args):
+            sep = "," if i < len(args) - 1 else ");"
+            lines.append(f"  {ctype(kind, is_arr, written)}{nm}{sep}")
+        lines.append("")
+    lines += ["#ifdef __cplusplus", "}", "#endif", "", "#endif /* %s */" % guard, ""]
+    with open(path, "w") as f:
+        f.write("\n".join(lines))
+
+
 def main():
     sigs = json.load(open(os.path.join(REPO, "oracle", "_ref", "sigs.json")))
     abi, groups = {}, {}
@@ -220,6 +381,27 @@ def main():
             abi[s] = {"ref": f"{os.path.relpath(src, REF)}:{line}",
                       "header": f"{hpath}:{hline}" if hpath else None, "args": sg["args"]}
         groups.setdefault(DESC[s][0], []).append(s)
+    # 2D and 1D routines lifted onto the 3D ones
+    lifted, desc2 = {}, {}
+    for s in sorted(sigs):
+        dims = 2 if s.startswith("lsm2d") else (1 if s.startswith("lsm1d") else 0)
+        if not dims:
+            continue
+        mp = lift_map(s, dims, abi, sigs)
+        if mp is None:
+            continue
+        sg = sigs[s]
+        src, line = sg["src"].split(":")
+        hpath, hline = header_line(s)
+        abi[s] = {"ref": f"{os.path.relpath(src, REF)}:{line}",
+                  "header": f"{hpath}:{hline}" if hpath else None, "args": sg["args"], "lifted_from": mp["sym3"]}
+        lifted[s] = (dims, mp)
+        desc2[s] = "%dD form: %s" % (dims, DESC[mp["sym3"]][1])
+    write_lifted(abi, lifted)
+    for dims in (2, 1):
+        syms = [s for s in lifted if lifted[s][0] == dims]
+        write_header(os.path.join(REPO, "include", "lsmgpu_toolbox%dd.h" % dims), "LSMGPU_TOOLBOX%dD_H" % dims,
+                     "%dD" % dims, syms, abi, desc2)
     with open(os.path.join(REPO, "lsmlib_gb300", "abi.json"), "w") as f:
         json.dump(abi, f, indent=1)
     lines = [
@@ -265,7 +447,7 @@ def main():
     lines += ["#ifdef __cplusplus", "}", "#endif", "", "#endif /* LSMGPU_TOOLBOX3D_H */", ""]
     with open(os.path.join(REPO, "include", "lsmgpu_toolbox3d.h"), "w") as f:
         f.write("\n".join(lines))
-    print(len(abi), "entry points")
+    print(len(abi), "entry points,", len(lifted), "lifted 2D / 1D")
 
 
 if __name__ == "__main__":

@@ -41,6 +41,20 @@ REF_SOURCES = [
     "toolbox/lsm_calculus_toolbox3d.f.in",
     "geometry/lsm_geometry3d_fort.f.in",
     "toolbox/lsm_spatial_derivatives2d_local.f.in",
+    # 2D and 1D forms of the dense hot-path routines
+    "toolbox/lsm_spatial_derivatives2d.f.in",
+    "toolbox/lsm_tvd_runge_kutta2d.f",
+    "toolbox/lsm_level_set_evolution2d.f.in",
+    "reinitialization/lsm_reinitialization2d.f.in",
+    "geometry/lsm_curvature2d.f.in",
+    "toolbox/lsm_math_utils2d.f.in",
+    "boundary_conditions/lsm_boundary_conditions2d.f",
+    "toolbox/lsm_spatial_derivatives1d.f.in",
+    "toolbox/lsm_tvd_runge_kutta1d.f",
+    "toolbox/lsm_level_set_evolution1d.f.in",
+    "reinitialization/lsm_reinitialization1d.f.in",
+    "toolbox/lsm_math_utils1d.f.in",
+    "boundary_conditions/lsm_boundary_conditions1d.f",
 ]
 
 CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-std=gnu99",

@@ -1,0 +1,226 @@
+"""LSMLIB's 2D and 1D routines (include/lsmgpu_toolbox2d.h, _1d.h), which run
+the 3D kernels with the missing axes lifted (stride 0, see csrc/lift.cuh).
+
+CPU: the principle, on the oracle — the 3D routine applied to data copied
+along the missing axes returns, on the middle plane, exactly what the
+reference's own 2D / 1D routine returns (its mechanical translation,
+oracle/_ref).  GPU: every lifted entry point against the reference's 2D / 1D
+routine on seeded inputs — bit for bit; sums (volumes, integrals, the band
+average) within (n + 16) 2^-53 S, S the sum of |term|, as in test_geometry.
+"""
+import re
+
+import numpy as np
+import pytest
+
+import lsmlib_gb300 as L
+from tests import harness as H
+from tests.test_geometry import SUMS
+
+LIFTED = sorted(s for s, v in L.ABI.items() if "lifted_from" in v)
+DIMS = {s: int(s[3]) for s in LIFTED}
+GB = {2: (-3, 12, -3, 10), 1: (-3, 14)}
+FB = {2: (0, 9, 0, 7), 1: (0, 11)}
+BOUND = re.compile(r"^(ilo|ihi|jlo|jhi)_(.*)$")
+SCRATCH = ("d1", "d2", "d3")   # dense routines accept their scratch and leave it alone
+VOLUME = re.compile(r"volumeintegral|volumeregion|surfaceintegral|surfacearea")
+U = 2.0 ** -53
+
+
+def is_local(sym):
+    return any(a[0] == "index_x" or a[0] == "narrow_band" for a in L.ABI[sym]["args"])
+
+
+def is_bc(sym):
+    return "extrapolation" in sym or "neumann" in sym
+
+
+def tolerant(sym):
+    base = L.ABI[sym]["lifted_from"]
+    return base in SUMS or base == "lsm3dcomputeavegradphilocal_"
+
+
+def shape(d):
+    return tuple(GB[d][2 * q + 1] - GB[d][2 * q] + 1 for q in range(d))
+
+
+def field(rng, d):
+    n = shape(d)
+    t = sum(np.linspace(0, 3 - q, n[q]).reshape([-1 if p == q else 1 for p in range(d)]) for q in range(d))
+    return np.asfortranarray(np.sin(t) + 0.3 * rng.standard_normal(n))
+
+
+def lists(rng, d, phi):
+    """Every fill-box cell, in memory order, split into four levels by |phi|
+    rank; narrow_band holds level + 1 there (a few boundary marks of 120)."""
+    fb, gb = FB[d], GB[d]
+    cells = [c for c in np.ndindex(*[fb[2 * q + 1] - fb[2 * q] + 1 for q in range(d)][::-1])]
+    cells = [tuple(fb[2 * q] + c[d - 1 - q] for q in range(d)) for c in cells]   # x fastest
+    mag = np.array([abs(phi[tuple(c[q] - gb[2 * q] for q in range(d))]) for c in cells])
+    level = np.minimum((np.argsort(np.argsort(mag, kind="stable"), kind="stable") * 4) // len(cells), 3)
+    order = sorted(range(len(cells)), key=lambda m: (level[m], m))
+    nb = np.zeros(shape(d), dtype=np.uint8, order="F")
+    ix, iy, bounds = [], [], []
+    for lev in range(4):
+        members = [m for m in order if level[m] == lev]
+        bounds.append((len(ix), len(ix) + len(members) - 1))
+        for m in members:
+            c = cells[m]
+            ix.append(c[0])
+            if d == 2:
+                iy.append(c[1])
+            nb[tuple(c[q] - gb[2 * q] for q in range(d))] = lev + 1
+    nb[rng.random(nb.shape) < 0.03] = 120
+    return np.array(ix, np.int32), np.array(iy, np.int32), bounds, nb
+
+
+def case(sym, seed, face=0):
+    d = DIMS[sym]
+    rng = np.random.default_rng(seed)
+    args = L.ABI[sym]["args"]
+    sc = dict(H.DEFAULT_SCALARS)
+    sc.update({"bdry_location_idx": face, "n": 2, "dir": 1 + seed % d, "beta": 0.15, "gamma": 0.3,
+               "grad_phi_ave": -1.0, "dt": 0.01, "mark_fb": 2, "mark_d1": 4, "mark_d2": 4, "mark_d3": 4})
+    vals = {}
+    phi = field(rng, d)
+    if is_local(sym):
+        ix, iy, bounds, nb = lists(rng, d, phi)
+        vals.update({"index_x": ix, "index_y": iy, "narrow_band": nb})
+        sc.update({"nlo_index": bounds[0][0], "nhi_index": bounds[3][1]})
+        for lev in range(4):
+            sc["nlo_index%d" % lev], sc["nhi_index%d" % lev] = bounds[lev]
+        if any(a[0] == "nlo_index0" for a in args):
+            sc.update({"mark_fb": 1, "mark_d1": 4, "mark_d2": 3, "mark_d3": 2})
+    for name, kind, is_arr, written in args:
+        m = BOUND.match(name)
+        if m:
+            grp = m.group(2)
+            b = FB[d] if (grp in ("fb", "ib") or grp.endswith("_fb")) else GB[d]
+            vals[name] = b[["ilo", "ihi", "jlo", "jhi"].index(m.group(1))]
+        elif is_arr and name not in vals:
+            if kind == "real" and not written:
+                a = phi.copy(order="F") if name == "phi" else field(rng, d)
+                if name.startswith("vel"):
+                    a[rng.random(a.shape) < 0.1] = 0.0
+                if name == "grad_phi_mag":
+                    a = np.abs(a)
+                vals[name] = a
+            elif kind == "real":
+                vals[name] = np.asfortranarray(rng.standard_normal(shape(d)))
+            else:
+                raise KeyError("%s: no case for array %s" % (sym, name))
+        elif not is_arr:
+            vals[name] = sc[name]
+    return vals
+
+
+def compare(sym, a1, s1, a2, s2, scale=None, n=0):
+    for name in H.written_names(sym):
+        if name in SCRATCH and not is_local(sym):
+            continue
+        if name in a1:
+            assert H.same(a1[name], a2[name]), "%s: %s differs, max |diff| %g" % (
+                sym, name, np.nanmax(np.abs(a1[name] - a2[name])))
+        elif scale is not None:
+            tol = (n + 16) * U * scale
+            assert abs(s1[name] - s2[name]) <= tol, (sym, name, s1[name], s2[name])
+        else:
+            assert H.same(s1[name], s2[name]), "%s: %s %r vs %r" % (sym, name, s1[name], s2[name])
+
+
+@pytest.fixture(scope="module")
+def ref():
+    r = H.reference()
+    if r is None:
+        pytest.skip("reference translation not available")
+    return r
+
+
+def test_every_lifted_routine_has_a_reference_routine(ref):
+    assert len(LIFTED) >= 100
+    for s in LIFTED:
+        assert hasattr(ref, s), s
+
+
+# ---- CPU: the 3D oracle on data copied along the missing axes ---------------------------
+
+DENSE = [s for s in LIFTED if not is_local(s) and not is_bc(s)]
+
+
+def lifted_3d_call(sym, vals, copies=7):
+    """Arguments of the 3D routine for a 2D / 1D call: arrays copied `copies`
+    times along each missing axis, boxes 0:copies-1 there (fill boxes the
+    middle cell), zero arrays for the missing components, dz (dy) = dx, or 1
+    where the routine multiplies a cell volume."""
+    d = DIMS[sym]
+    sym3 = L.ABI[sym]["lifted_from"]
+    mid = copies // 2
+    out = {}
+    for name, kind, is_arr, written in L.ABI[sym3]["args"]:
+        m = re.match(r"^(ilo|ihi|jlo|jhi|klo|khi)_(.*)$", name)
+        if m:
+            axis = "ijk".index(m.group(1)[0])
+            if axis < d:
+                key = [a[0] for a in L.ABI[sym]["args"] if a[0].startswith(m.group(1)[:3])
+                       and BOUND.match(a[0]).group(2) in (m.group(2), "fb" if m.group(2).endswith("fb") else None)]
+                out[name] = vals[key[0]] if key else vals[name]
+            else:
+                grp = m.group(2)
+                fill = grp in ("fb", "ib") or grp.endswith("_fb")
+                out[name] = mid if fill else (0 if m.group(1)[1:] == "lo" else copies - 1)
+        elif is_arr:
+            a = vals.get(name)
+            if a is None:
+                a = np.zeros(shape(d))
+            a = np.asarray(a)
+            for _ in range(3 - d):
+                a = np.repeat(a[..., None], copies, axis=-1)
+            out[name] = np.asfortranarray(a)
+        else:
+            out[name] = vals[name] if name in vals else (1.0 if VOLUME.search(sym3) else vals["dx"])
+    return sym3, out
+
+
+@pytest.mark.parametrize("sym", DENSE)
+def test_lift_principle_on_the_oracle(sym, ref):
+    vals = case(sym, 3)
+    a_ref, s_ref = H.run(ref, sym, vals)
+    sym3, v3 = lifted_3d_call(sym, vals)
+    a3, s3 = H.run(H.oracle(), sym3, v3)
+    d = DIMS[sym]
+    mid = (slice(None),) * d + (3,) * (3 - d)
+    for name in H.written_names(sym):
+        if name in SCRATCH:
+            continue
+        if name in a_ref:
+            got = a3[name][mid]
+            fb, gb = FB[d], GB[d]
+            sel = tuple(slice(fb[2 * q] - gb[2 * q], fb[2 * q + 1] - gb[2 * q] + 1) for q in range(d))
+            assert H.same(a_ref[name][sel], got[sel]), "%s: %s" % (sym, name)
+        elif tolerant(sym):
+            assert abs(s_ref[name] - s3[name]) <= 1e-12 * max(1.0, abs(s_ref[name])), (sym, name)
+        else:
+            assert H.same(s_ref[name], s3[name]), (sym, name, s_ref[name], s3[name])
+
+
+# ---- GPU: every lifted routine against the reference's -----------------------------------
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("sym", LIFTED)
+def test_lifted_gpu_matches_reference(sym, ref, gpu_lib):
+    faces = range(2 * DIMS[sym]) if is_bc(sym) else [0]
+    for face in faces:
+        for seed in (0, 1):
+            vals = case(sym, seed, face)
+            a1, s1 = H.run(ref, sym, vals)
+            a2, s2 = H.run(gpu_lib, sym, vals)
+            L.check(gpu_lib)
+            scale, n = None, 0
+            if tolerant(sym):
+                v = dict(vals)
+                if "f" in v:
+                    v["f"] = np.abs(v["f"]).copy(order="F")
+                out = [a[0] for a in L.ABI[sym]["args"] if not a[2] and a[3]][0]
+                scale = abs(H.run(ref, sym, v)[1][out])
+                n = int(np.prod(shape(DIMS[sym])))
+            compare(sym, a1, s1, a2, s2, scale, n)

@@ -21,13 +21,13 @@ FB = (0, 19, 0, 17, 0, 17)
 DX = 0.1
 LEVEL = 3
 
-LOCAL = [s for s in L.ABI if any(a[0] == "index_x" for a in L.ABI[s]["args"])
+LOCAL = [s for s in L.ABI if s.startswith("lsm3d") and any(a[0] == "index_x" for a in L.ABI[s]["args"])
          and s not in ("lsm3ddeterminenarrowband_", "lsm3dmarknarrowbandneighbors_",
                        "lsm3ddeterminenarrowbandfrommask_", "lsm3dcheckouternarrowbandlayer_")]
 # LSMLIB's lsm3dComputeStableConstNormalVelDtLOCAL reads unassigned locals;
 # the oracle implements the dense formula and is pinned against it below
 REF_UNDEFINED = {"lsm3dcomputestableconstnormalveldtlocal_"}
-BC = [s for s in L.ABI if "extrapolation" in s or "neumann" in s]
+BC = [s for s in L.ABI if s.startswith("lsm3d") and ("extrapolation" in s or "neumann" in s)]
 NEW_3D = {"lsm3dhjeno3local_", "lsm3dhjweno5local_"}
 
 

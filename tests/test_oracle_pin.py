@@ -12,7 +12,8 @@ import pytest
 import lsmlib_gb300 as L
 from tests import harness as H
 
-DENSE = [s for s in L.ABI if not any(a[0] in ("index_x", "narrow_band") for a in L.ABI[s]["args"])
+DENSE = [s for s in L.ABI if s.startswith("lsm3d")
+         and not any(a[0] in ("index_x", "narrow_band") for a in L.ABI[s]["args"])
          and "extrapolation" not in s and "neumann" not in s]
 
 
