@@ -40,6 +40,38 @@ void lsm2daddadvectiontermtolserhs_(
   const int *jlo_fb,
   const int *jhi_fb);
 
+/* 2D form: advection term on band cells.
+ * Replaces src/toolbox/lsm_level_set_evolution2d_local.f.in:55; C declaration src/toolbox/lsm_level_set_evolution2d_local.h:106.
+ */
+void lsm2daddadvectiontermtolserhslocal_(
+  double *lse_rhs,
+  const int *ilo_lse_rhs_gb,
+  const int *ihi_lse_rhs_gb,
+  const int *jlo_lse_rhs_gb,
+  const int *jhi_lse_rhs_gb,
+  const double *phi_x,
+  const double *phi_y,
+  const int *ilo_grad_phi_gb,
+  const int *ihi_grad_phi_gb,
+  const int *jlo_grad_phi_gb,
+  const int *jhi_grad_phi_gb,
+  const double *vel_x,
+  const double *vel_y,
+  const int *ilo_vel_gb,
+  const int *ihi_vel_gb,
+  const int *jlo_vel_gb,
+  const int *jhi_vel_gb,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
 /* 2D form: rhs += b * kappa |grad phi| from first and second derivatives.
  * Replaces src/toolbox/lsm_level_set_evolution2d.f.in:273; C declaration src/toolbox/lsm_level_set_evolution2d.h:243.
  */
@@ -68,6 +100,40 @@ void lsm2daddconstcurvtermtolserhs_(
   const int *jlo_fb,
   const int *jhi_fb);
 
+/* 2D form: curvature term on band cells.
+ * Replaces src/toolbox/lsm_level_set_evolution2d_local.f.in:320; C declaration src/toolbox/lsm_level_set_evolution2d_local.h:289.
+ */
+void lsm2daddconstcurvtermtolserhslocal_(
+  double *lse_rhs,
+  const int *ilo_lse_rhs_gb,
+  const int *ihi_lse_rhs_gb,
+  const int *jlo_lse_rhs_gb,
+  const int *jhi_lse_rhs_gb,
+  const double *phi_x,
+  const double *phi_y,
+  const int *ilo_grad_phi_gb,
+  const int *ihi_grad_phi_gb,
+  const int *jlo_grad_phi_gb,
+  const int *jhi_grad_phi_gb,
+  const double *phi_xx,
+  const double *phi_xy,
+  const double *phi_yy,
+  const int *ilo_grad2_phi_gb,
+  const int *ihi_grad2_phi_gb,
+  const int *jlo_grad2_phi_gb,
+  const int *jhi_grad2_phi_gb,
+  const double *b,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
 /* 2D form: rhs -= Vn |grad phi| (Godunov), Vn constant.
  * Replaces src/toolbox/lsm_level_set_evolution2d.f.in:189; C declaration src/toolbox/lsm_level_set_evolution2d.h:193.
  */
@@ -94,6 +160,39 @@ void lsm2daddconstnormalveltermtolserhs_(
   const int *ihi_fb,
   const int *jlo_fb,
   const int *jhi_fb);
+
+/* 2D form: normal velocity term (constant) on band cells.
+ * Replaces src/toolbox/lsm_level_set_evolution2d_local.f.in:227; C declaration src/toolbox/lsm_level_set_evolution2d_local.h:226.
+ */
+void lsm2daddconstnormalveltermtolserhslocal_(
+  double *lse_rhs,
+  const int *ilo_lse_rhs_gb,
+  const int *ihi_lse_rhs_gb,
+  const int *jlo_lse_rhs_gb,
+  const int *jhi_lse_rhs_gb,
+  const double *phi_x_plus,
+  const double *phi_y_plus,
+  const int *ilo_grad_phi_plus_gb,
+  const int *ihi_grad_phi_plus_gb,
+  const int *jlo_grad_phi_plus_gb,
+  const int *jhi_grad_phi_plus_gb,
+  const double *phi_x_minus,
+  const double *phi_y_minus,
+  const int *ilo_grad_phi_minus_gb,
+  const int *ihi_grad_phi_minus_gb,
+  const int *jlo_grad_phi_minus_gb,
+  const int *jhi_grad_phi_minus_gb,
+  const double *vel_n,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
 
 /* 2D form: rhs += b * kappa * |grad phi| (loops k,j from the fill box to the ghost box end and i over the ghost box, as the reference does).
  * Replaces src/toolbox/lsm_level_set_evolution2d.f.in:345; C declaration src/toolbox/lsm_level_set_evolution2d.h:288.
@@ -150,6 +249,43 @@ void lsm2daddnormalveltermtolserhs_(
   const int *ihi_fb,
   const int *jlo_fb,
   const int *jhi_fb);
+
+/* 2D form: normal velocity term (field) on band cells.
+ * Replaces src/toolbox/lsm_level_set_evolution2d_local.f.in:126; C declaration src/toolbox/lsm_level_set_evolution2d_local.h:163.
+ */
+void lsm2daddnormalveltermtolserhslocal_(
+  double *lse_rhs,
+  const int *ilo_lse_rhs_gb,
+  const int *ihi_lse_rhs_gb,
+  const int *jlo_lse_rhs_gb,
+  const int *jhi_lse_rhs_gb,
+  const double *phi_x_plus,
+  const double *phi_y_plus,
+  const int *ilo_grad_phi_plus_gb,
+  const int *ihi_grad_phi_plus_gb,
+  const int *jlo_grad_phi_plus_gb,
+  const int *jhi_grad_phi_plus_gb,
+  const double *phi_x_minus,
+  const double *phi_y_minus,
+  const int *ilo_grad_phi_minus_gb,
+  const int *ihi_grad_phi_minus_gb,
+  const int *jlo_grad_phi_minus_gb,
+  const int *jhi_grad_phi_minus_gb,
+  const double *vel_n,
+  const int *ilo_vel_gb,
+  const int *ihi_vel_gb,
+  const int *jlo_vel_gb,
+  const int *jhi_vel_gb,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
 
 /* 2D form: mean |field1 - field2| over an index box.
  * Replaces src/toolbox/lsm_math_utils2d.f.in:69; C declaration src/toolbox/lsm_math_utils2d.h:121.
@@ -321,6 +457,28 @@ void lsm2dcentralhessian_(
   const double *dx,
   const double *dy);
 
+/* 2D form: 1 when the outer band layer holds both signs of phi.
+ * Replaces src/toolbox/lsm_localization2d.f:693; C declaration src/toolbox/lsm_localization2d.h:403.
+ */
+void lsm2dcheckouternarrowbandlayer_(
+  int *change_sign,
+  const double *phi,
+  const int *ilo_gb,
+  const int *ihi_gb,
+  const int *jlo_gb,
+  const int *jhi_gb,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const int *index_outer,
+  const int *nlo_index_outer,
+  const int *nhi_index_outer,
+  const int *nlo_outer_plus,
+  const int *nhi_outer_plus,
+  const int *nlo_outer_minus,
+  const int *nhi_outer_minus);
+
 /* 2D form: average |grad phi| over band cells.
  * Replaces src/toolbox/lsm_spatial_derivatives2d_local.f.in:1616; C declaration src/toolbox/lsm_spatial_derivatives2d_local.h:555.
  */
@@ -399,6 +557,40 @@ void lsm2dcomputemeancurvatureorder2_(
   const double *dx,
   const double *dy);
 
+/* 2D form: second-order mean curvature on band cells.
+ * Replaces src/geometry/lsm_curvature2d_local.f.in:15; C declaration src/geometry/lsm_curvature2d_local.h:64.
+ */
+void lsm2dcomputemeancurvatureorder2local_(
+  double *kappa,
+  const int *ilo_kappa_gb,
+  const int *ihi_kappa_gb,
+  const int *jlo_kappa_gb,
+  const int *jhi_kappa_gb,
+  const double *phi,
+  const int *ilo_phi_gb,
+  const int *ihi_phi_gb,
+  const int *jlo_phi_gb,
+  const int *jhi_phi_gb,
+  const double *phi_x,
+  const double *phi_y,
+  const double *grad_phi_mag,
+  const int *ilo_grad_phi_gb,
+  const int *ihi_grad_phi_gb,
+  const int *jlo_grad_phi_gb,
+  const int *jhi_grad_phi_gb,
+  const double *dx,
+  const double *dy,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
 /* 2D form: reinitialization RHS sgn(phi)(1 - |grad phi|), Godunov.
  * Replaces src/reinitialization/lsm_reinitialization2d.f.in:48; C declaration src/reinitialization/lsm_reinitialization2d.h:78.
  */
@@ -437,6 +629,51 @@ void lsm2dcomputereinitializationeqnrhs_(
   const double *dx,
   const double *dy,
   const int *use_phi0_for_sgn);
+
+/* 2D form: reinitialization RHS on band cells.
+ * Replaces src/reinitialization/lsm_reinitialization2d_local.f.in:49; C declaration src/reinitialization/lsm_reinitialization2d_local.h:41.
+ */
+void lsm2dcomputereinitializationeqnrhslocal_(
+  double *reinit_rhs,
+  const int *ilo_rhs_gb,
+  const int *ihi_rhs_gb,
+  const int *jlo_rhs_gb,
+  const int *jhi_rhs_gb,
+  const double *phi,
+  const int *ilo_phi_gb,
+  const int *ihi_phi_gb,
+  const int *jlo_phi_gb,
+  const int *jhi_phi_gb,
+  const double *phi0,
+  const int *ilo_phi0_gb,
+  const int *ihi_phi0_gb,
+  const int *jlo_phi0_gb,
+  const int *jhi_phi0_gb,
+  const double *phi_x_plus,
+  const double *phi_y_plus,
+  const int *ilo_grad_phi_plus_gb,
+  const int *ihi_grad_phi_plus_gb,
+  const int *jlo_grad_phi_plus_gb,
+  const int *jhi_grad_phi_plus_gb,
+  const double *phi_x_minus,
+  const double *phi_y_minus,
+  const int *ilo_grad_phi_minus_gb,
+  const int *ihi_grad_phi_minus_gb,
+  const int *jlo_grad_phi_minus_gb,
+  const int *jhi_grad_phi_minus_gb,
+  const double *dx,
+  const double *dy,
+  const int *use_phi0_for_sgn,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
 
 /* 2D form: CFL-stable dt for advection.
  * Replaces src/toolbox/lsm_math_utils2d.f.in:218; C declaration src/toolbox/lsm_math_utils2d.h:204.
@@ -481,6 +718,31 @@ void lsm2dcomputestableadvectiondtcontrolvolume_(
   const double *dx,
   const double *dy,
   const double *cfl_number);
+
+/* 2D form: CFL-stable advection dt over band cells.
+ * Replaces src/toolbox/lsm_math_utils2d_local.f.in:165; C declaration src/toolbox/lsm_math_utils2d_local.h:146.
+ */
+void lsm2dcomputestableadvectiondtlocal_(
+  double *dt,
+  const double *vel_x,
+  const double *vel_y,
+  const int *ilo_vel_gb,
+  const int *ihi_vel_gb,
+  const int *jlo_vel_gb,
+  const int *jhi_vel_gb,
+  const double *dx,
+  const double *dy,
+  const double *cfl_number,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
 
 /* 2D form: CFL-stable dt for a constant normal velocity.
  * Replaces src/toolbox/lsm_math_utils2d.f.in:382; C declaration src/toolbox/lsm_math_utils2d.h:297.
@@ -539,6 +801,38 @@ void lsm2dcomputestableconstnormalveldtcontrolvolume_(
   const double *dx,
   const double *dy,
   const double *cfl_number);
+
+/* 2D form: CFL-stable constant normal-velocity dt over band cells (the reference routine reads two unassigned variables; this computes the dense routine's formula).
+ * Replaces src/toolbox/lsm_math_utils2d_local.f.in:360; C declaration src/toolbox/lsm_math_utils2d_local.h:257.
+ */
+void lsm2dcomputestableconstnormalveldtlocal_(
+  double *dt,
+  const double *vel_n,
+  const double *phi_x_plus,
+  const double *phi_y_plus,
+  const int *ilo_grad_phi_plus_gb,
+  const int *ihi_grad_phi_plus_gb,
+  const int *jlo_grad_phi_plus_gb,
+  const int *jhi_grad_phi_plus_gb,
+  const double *phi_x_minus,
+  const double *phi_y_minus,
+  const int *ilo_grad_phi_minus_gb,
+  const int *ihi_grad_phi_minus_gb,
+  const int *jlo_grad_phi_minus_gb,
+  const int *jhi_grad_phi_minus_gb,
+  const double *dx,
+  const double *dy,
+  const double *cfl_number,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
 
 /* 2D form: CFL-stable dt for a normal velocity field.
  * Replaces src/toolbox/lsm_math_utils2d.f.in:285; C declaration src/toolbox/lsm_math_utils2d.h:245.
@@ -605,6 +899,61 @@ void lsm2dcomputestablenormalveldtcontrolvolume_(
   const double *dx,
   const double *dy,
   const double *cfl_number);
+
+/* 2D form: CFL-stable normal-velocity dt over band cells.
+ * Replaces src/toolbox/lsm_math_utils2d_local.f.in:246; C declaration src/toolbox/lsm_math_utils2d_local.h:196.
+ */
+void lsm2dcomputestablenormalveldtlocal_(
+  double *dt,
+  const double *vel_n,
+  const int *ilo_vel_gb,
+  const int *ihi_vel_gb,
+  const int *jlo_vel_gb,
+  const int *jhi_vel_gb,
+  const double *phi_x_plus,
+  const double *phi_y_plus,
+  const int *ilo_grad_phi_plus_gb,
+  const int *ihi_grad_phi_plus_gb,
+  const int *jlo_grad_phi_plus_gb,
+  const int *jhi_grad_phi_plus_gb,
+  const double *phi_x_minus,
+  const double *phi_y_minus,
+  const int *ilo_grad_phi_minus_gb,
+  const int *ihi_grad_phi_minus_gb,
+  const int *jlo_grad_phi_minus_gb,
+  const int *jhi_grad_phi_minus_gb,
+  const double *dx,
+  const double *dy,
+  const double *cfl_number,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
+/* 2D form: dest = src on listed cells.
+ * Replaces src/toolbox/lsm_localization2d.f:833; C declaration src/toolbox/lsm_localization2d.h:491.
+ */
+void lsm2dcopydatalocal_(
+  double *dest,
+  const int *ilo_dest_gb,
+  const int *ihi_dest_gb,
+  const int *jlo_dest_gb,
+  const int *jhi_dest_gb,
+  const double *src,
+  const int *ilo_src_gb,
+  const int *ihi_src_gb,
+  const int *jlo_src_gb,
+  const int *jhi_src_gb,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index);
 
 /* 2D form: copy extrapolation into the ghost cells of one face.
  * Replaces src/boundary_conditions/lsm_boundary_conditions2d.f:264; C declaration src/boundary_conditions/lsm_boundary_conditions2d.h:129.
@@ -1004,6 +1353,30 @@ void lsm2dhomogeneousneumannweno5_(
   const int *jhi_fb,
   const int *bdry_location_idx);
 
+/* 2D form: dest = max(mask, src) on listed cells.
+ * Replaces src/toolbox/lsm_localization2d.f:778; C declaration src/toolbox/lsm_localization2d.h:421.
+ */
+void lsm2dimposemasklocal_(
+  double *dest,
+  const int *ilo_dest_gb,
+  const int *ihi_dest_gb,
+  const int *jlo_dest_gb,
+  const int *jhi_dest_gb,
+  const double *src,
+  const int *ilo_src_gb,
+  const int *ihi_src_gb,
+  const int *jlo_src_gb,
+  const int *jhi_src_gb,
+  const double *mask,
+  const int *ilo_mask_gb,
+  const int *ihi_mask_gb,
+  const int *jlo_mask_gb,
+  const int *jhi_mask_gb,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index);
+
 /* 2D form: second-order Laplacian.
  * Replaces src/toolbox/lsm_spatial_derivatives2d.f.in:2091; C declaration src/toolbox/lsm_spatial_derivatives2d.h:643.
  */
@@ -1067,6 +1440,21 @@ void lsm2dlinearextrapolation_(
   const int *jhi_fb,
   const int *bdry_location_idx);
 
+/* 2D form: mark the one-cell faces of a fill box.
+ * Replaces src/toolbox/lsm_localization2d.f:486; C declaration src/toolbox/lsm_localization2d.h:283.
+ */
+void lsm2dmarknarrowbandboundarylayer_(
+  unsigned char *narrow_band,
+  const int *ilo_gb,
+  const int *ihi_gb,
+  const int *jlo_gb,
+  const int *jhi_gb,
+  const int *ilo_fb,
+  const int *ihi_fb,
+  const int *jlo_fb,
+  const int *jhi_fb,
+  const unsigned char *mark_boundary_layer);
+
 /* 2D form: max |field1 - field2| over an index box.
  * Replaces src/toolbox/lsm_math_utils2d.f.in:15; C declaration src/toolbox/lsm_math_utils2d.h:90.
  */
@@ -1112,6 +1500,55 @@ void lsm2dmaxnormdiffcontrolvolume_(
   const int *ihi_ib,
   const int *jlo_ib,
   const int *jhi_ib);
+
+/* 2D form: max |field1 - field2| over band cells (starts at 0).
+ * Replaces src/toolbox/lsm_math_utils2d_local.f.in:16; C declaration src/toolbox/lsm_math_utils2d_local.h:64.
+ */
+void lsm2dmaxnormdifflocal_(
+  double *max_norm_diff,
+  const double *field1,
+  const int *ilo_field1_gb,
+  const int *ihi_field1_gb,
+  const int *jlo_field1_gb,
+  const int *jhi_field1_gb,
+  const double *field2,
+  const int *ilo_field2_gb,
+  const int *ihi_field2_gb,
+  const int *jlo_field2_gb,
+  const int *jhi_field2_gb,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
+/* 2D form: cubic cut-off of the RHS between beta and gamma.
+ * Replaces src/toolbox/lsm_localization2d.f:621; C declaration src/toolbox/lsm_localization2d.h:367.
+ */
+void lsm2dmultiplycutofflserhslocal_(
+  const double *phi,
+  double *lse_rhs,
+  const int *ilo_gb,
+  const int *ihi_gb,
+  const int *jlo_gb,
+  const int *jhi_gb,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb,
+  const double *beta,
+  const double *gamma);
 
 /* 2D form: gradient of F upwinded by the local extremum of phi.
  * Replaces src/toolbox/lsm_spatial_derivatives2d.f.in:2166; C declaration src/toolbox/lsm_spatial_derivatives2d.h:690.
@@ -1169,6 +1606,37 @@ void lsm2drk1step_(
   const int *jlo_fb,
   const int *jhi_fb,
   const double *dt);
+
+/* 2D form: Euler step on band cells.
+ * Replaces src/toolbox/lsm_tvd_runge_kutta2d_local.f:33; C declaration src/toolbox/lsm_tvd_runge_kutta2d_local.h:35.
+ */
+void lsm2drk1steplocal_(
+  double *u_next,
+  const int *ilo_u_next_gb,
+  const int *ihi_u_next_gb,
+  const int *jlo_u_next_gb,
+  const int *jhi_u_next_gb,
+  const double *u_cur,
+  const int *ilo_u_cur_gb,
+  const int *ihi_u_cur_gb,
+  const int *jlo_u_cur_gb,
+  const int *jhi_u_cur_gb,
+  const double *rhs,
+  const int *ilo_rhs_gb,
+  const int *ihi_rhs_gb,
+  const int *jlo_rhs_gb,
+  const int *jhi_rhs_gb,
+  const double *dt,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
 
 /* 2D form: signed linear extrapolation into the ghost cells of one face.
  * Replaces src/boundary_conditions/lsm_boundary_conditions2d.f:149; C declaration src/boundary_conditions/lsm_boundary_conditions2d.h:107.
@@ -1274,6 +1742,37 @@ void lsm2dtvdrk2stage1_(
   const int *jhi_fb,
   const double *dt);
 
+/* 2D form: TVD RK2 stage 1 on band cells.
+ * Replaces src/toolbox/lsm_tvd_runge_kutta2d_local.f:123; C declaration src/toolbox/lsm_tvd_runge_kutta2d_local.h:64.
+ */
+void lsm2dtvdrk2stage1local_(
+  double *u_stage1,
+  const int *ilo_u_stage1_gb,
+  const int *ihi_u_stage1_gb,
+  const int *jlo_u_stage1_gb,
+  const int *jhi_u_stage1_gb,
+  const double *u_cur,
+  const int *ilo_u_cur_gb,
+  const int *ihi_u_cur_gb,
+  const int *jlo_u_cur_gb,
+  const int *jhi_u_cur_gb,
+  const double *rhs,
+  const int *ilo_rhs_gb,
+  const int *ihi_rhs_gb,
+  const int *jlo_rhs_gb,
+  const int *jhi_rhs_gb,
+  const double *dt,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
 /* 2D form: TVD RK2 stage 2: 0.5*(u + u1 + dt*L).
  * Replaces src/toolbox/lsm_tvd_runge_kutta2d.f:160; C declaration src/toolbox/lsm_tvd_runge_kutta2d.h:138.
  */
@@ -1304,6 +1803,42 @@ void lsm2dtvdrk2stage2_(
   const int *jhi_fb,
   const double *dt);
 
+/* 2D form: TVD RK2 stage 2 on band cells.
+ * Replaces src/toolbox/lsm_tvd_runge_kutta2d_local.f:212; C declaration src/toolbox/lsm_tvd_runge_kutta2d_local.h:93.
+ */
+void lsm2dtvdrk2stage2local_(
+  double *u_next,
+  const int *ilo_u_next_gb,
+  const int *ihi_u_next_gb,
+  const int *jlo_u_next_gb,
+  const int *jhi_u_next_gb,
+  const double *u_stage1,
+  const int *ilo_u_stage1_gb,
+  const int *ihi_u_stage1_gb,
+  const int *jlo_u_stage1_gb,
+  const int *jhi_u_stage1_gb,
+  const double *u_cur,
+  const int *ilo_u_cur_gb,
+  const int *ihi_u_cur_gb,
+  const int *jlo_u_cur_gb,
+  const int *jhi_u_cur_gb,
+  const double *rhs,
+  const int *ilo_rhs_gb,
+  const int *ihi_rhs_gb,
+  const int *jlo_rhs_gb,
+  const int *jhi_rhs_gb,
+  const double *dt,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
 /* 2D form: TVD RK3 stage 1 (an Euler step).
  * Replaces src/toolbox/lsm_tvd_runge_kutta2d.f:232; C declaration src/toolbox/lsm_tvd_runge_kutta2d.h:184.
  */
@@ -1328,6 +1863,37 @@ void lsm2dtvdrk3stage1_(
   const int *jlo_fb,
   const int *jhi_fb,
   const double *dt);
+
+/* 2D form: TVD RK3 stage 1 on band cells.
+ * Replaces src/toolbox/lsm_tvd_runge_kutta2d_local.f:308; C declaration src/toolbox/lsm_tvd_runge_kutta2d_local.h:127.
+ */
+void lsm2dtvdrk3stage1local_(
+  double *u_stage1,
+  const int *ilo_u_stage1_gb,
+  const int *ihi_u_stage1_gb,
+  const int *jlo_u_stage1_gb,
+  const int *jhi_u_stage1_gb,
+  const double *u_cur,
+  const int *ilo_u_cur_gb,
+  const int *ihi_u_cur_gb,
+  const int *jlo_u_cur_gb,
+  const int *jhi_u_cur_gb,
+  const double *rhs,
+  const int *ilo_rhs_gb,
+  const int *ihi_rhs_gb,
+  const int *jlo_rhs_gb,
+  const int *jhi_rhs_gb,
+  const double *dt,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
 
 /* 2D form: TVD RK3 stage 2: 0.75*u + 0.25*(u1 + dt*L).
  * Replaces src/toolbox/lsm_tvd_runge_kutta2d.f:296; C declaration src/toolbox/lsm_tvd_runge_kutta2d.h:222.
@@ -1359,6 +1925,42 @@ void lsm2dtvdrk3stage2_(
   const int *jhi_fb,
   const double *dt);
 
+/* 2D form: TVD RK3 stage 2 on band cells.
+ * Replaces src/toolbox/lsm_tvd_runge_kutta2d_local.f:396; C declaration src/toolbox/lsm_tvd_runge_kutta2d_local.h:156.
+ */
+void lsm2dtvdrk3stage2local_(
+  double *u_stage2,
+  const int *ilo_u_stage2_gb,
+  const int *ihi_u_stage2_gb,
+  const int *jlo_u_stage2_gb,
+  const int *jhi_u_stage2_gb,
+  const double *u_stage1,
+  const int *ilo_u_stage1_gb,
+  const int *ihi_u_stage1_gb,
+  const int *jlo_u_stage1_gb,
+  const int *jhi_u_stage1_gb,
+  const double *u_cur,
+  const int *ilo_u_cur_gb,
+  const int *ihi_u_cur_gb,
+  const int *jlo_u_cur_gb,
+  const int *jhi_u_cur_gb,
+  const double *rhs,
+  const int *ilo_rhs_gb,
+  const int *ihi_rhs_gb,
+  const int *jlo_rhs_gb,
+  const int *jhi_rhs_gb,
+  const double *dt,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
 /* 2D form: TVD RK3 stage 3: u/3 + 2/3*(u2 + dt*L).
  * Replaces src/toolbox/lsm_tvd_runge_kutta2d.f:366; C declaration src/toolbox/lsm_tvd_runge_kutta2d.h:265.
  */
@@ -1388,6 +1990,42 @@ void lsm2dtvdrk3stage3_(
   const int *jlo_fb,
   const int *jhi_fb,
   const double *dt);
+
+/* 2D form: TVD RK3 stage 3 on band cells.
+ * Replaces src/toolbox/lsm_tvd_runge_kutta2d_local.f:491; C declaration src/toolbox/lsm_tvd_runge_kutta2d_local.h:189.
+ */
+void lsm2dtvdrk3stage3local_(
+  double *u_next,
+  const int *ilo_u_next_gb,
+  const int *ihi_u_next_gb,
+  const int *jlo_u_next_gb,
+  const int *jhi_u_next_gb,
+  const double *u_stage2,
+  const int *ilo_u_stage2_gb,
+  const int *ihi_u_stage2_gb,
+  const int *jlo_u_stage2_gb,
+  const int *jhi_u_stage2_gb,
+  const double *u_cur,
+  const int *ilo_u_cur_gb,
+  const int *ihi_u_cur_gb,
+  const int *jlo_u_cur_gb,
+  const int *jhi_u_cur_gb,
+  const double *rhs,
+  const int *ilo_rhs_gb,
+  const int *ihi_rhs_gb,
+  const int *jlo_rhs_gb,
+  const int *jhi_rhs_gb,
+  const double *dt,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
 
 /* 2D form: first-order upwind HJ ENO gradient for a velocity field.
  * Replaces src/toolbox/lsm_spatial_derivatives2d.f.in:1069; C declaration src/toolbox/lsm_spatial_derivatives2d.h:337.
@@ -1721,6 +2359,20 @@ void lsm2dzerooutlevelseteqnrhs_(
   const int *ihi_lse_rhs_gb,
   const int *jlo_lse_rhs_gb,
   const int *jhi_lse_rhs_gb);
+
+/* 2D form: zero the RHS on listed cells.
+ * Replaces src/toolbox/lsm_level_set_evolution2d_local.f.in:16; C declaration src/toolbox/lsm_level_set_evolution2d_local.h:70.
+ */
+void lsm2dzerooutlevelseteqnrhslocal_(
+  double *lse_rhs,
+  const int *ilo_lse_rhs_gb,
+  const int *ihi_lse_rhs_gb,
+  const int *jlo_lse_rhs_gb,
+  const int *jhi_lse_rhs_gb,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index);
 
 #ifdef __cplusplus
 }

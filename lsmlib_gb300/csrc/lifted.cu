@@ -451,6 +451,18 @@ void lsm2daddadvectiontermtolserhs_(double *lse_rhs, const int *ilo_lse_rhs_gb, 
   lsm3daddadvectiontermtolserhs_(lse_rhs, ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb, &L_.k0, &L_.k0, phi_x, phi_y, L_.zero(), ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb, &L_.k0, &L_.k0, vel_x, vel_y, L_.zero(), ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0);
 }
 
+// src/toolbox/lsm_level_set_evolution2d_local.f.in:55
+void lsm2daddadvectiontermtolserhslocal_(double *lse_rhs, const int *ilo_lse_rhs_gb, const int *ihi_lse_rhs_gb, const int *jlo_lse_rhs_gb, const int *jhi_lse_rhs_gb, const double *phi_x, const double *phi_y, const int *ilo_grad_phi_gb, const int *ihi_grad_phi_gb, const int *jlo_grad_phi_gb, const int *jhi_grad_phi_gb, const double *vel_x, const double *vel_y, const int *ilo_vel_gb, const int *ihi_vel_gb, const int *jlo_vel_gb, const int *jhi_vel_gb, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2daddadvectiontermtolserhslocal_");
+  L_.box(ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb);
+  L_.box(ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb);
+  L_.box(ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3daddadvectiontermtolserhslocal_(lse_rhs, ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb, &L_.k0, &L_.k0, phi_x, phi_y, L_.zero(), ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb, &L_.k0, &L_.k0, vel_x, vel_y, L_.zero(), ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb, &L_.k0, &L_.k0, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
 // src/toolbox/lsm_level_set_evolution2d.f.in:273
 void lsm2daddconstcurvtermtolserhs_(double *lse_rhs, const int *ilo_lse_rhs_gb, const int *ihi_lse_rhs_gb, const int *jlo_lse_rhs_gb, const int *jhi_lse_rhs_gb, const double *phi_x, const double *phi_y, const int *ilo_grad_phi_gb, const int *ihi_grad_phi_gb, const int *jlo_grad_phi_gb, const int *jhi_grad_phi_gb, const double *phi_xx, const double *phi_xy, const double *phi_yy, const int *ilo_grad2_phi_gb, const int *ihi_grad2_phi_gb, const int *jlo_grad2_phi_gb, const int *jhi_grad2_phi_gb, const double *b, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb) {
   Lift L_(2, "lsm2daddconstcurvtermtolserhs_");
@@ -462,6 +474,18 @@ void lsm2daddconstcurvtermtolserhs_(double *lse_rhs, const int *ilo_lse_rhs_gb, 
   lsm3daddconstcurvtermtolserhs_(lse_rhs, ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb, &L_.k0, &L_.k0, phi_x, phi_y, L_.zero(), ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb, &L_.k0, &L_.k0, phi_xx, phi_xy, L_.zero(), phi_yy, L_.zero(), L_.zero(), ilo_grad2_phi_gb, ihi_grad2_phi_gb, jlo_grad2_phi_gb, jhi_grad2_phi_gb, &L_.k0, &L_.k0, b, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0);
 }
 
+// src/toolbox/lsm_level_set_evolution2d_local.f.in:320
+void lsm2daddconstcurvtermtolserhslocal_(double *lse_rhs, const int *ilo_lse_rhs_gb, const int *ihi_lse_rhs_gb, const int *jlo_lse_rhs_gb, const int *jhi_lse_rhs_gb, const double *phi_x, const double *phi_y, const int *ilo_grad_phi_gb, const int *ihi_grad_phi_gb, const int *jlo_grad_phi_gb, const int *jhi_grad_phi_gb, const double *phi_xx, const double *phi_xy, const double *phi_yy, const int *ilo_grad2_phi_gb, const int *ihi_grad2_phi_gb, const int *jlo_grad2_phi_gb, const int *jhi_grad2_phi_gb, const double *b, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2daddconstcurvtermtolserhslocal_");
+  L_.box(ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb);
+  L_.box(ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb);
+  L_.box(ilo_grad2_phi_gb, ihi_grad2_phi_gb, jlo_grad2_phi_gb, jhi_grad2_phi_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3daddconstcurvtermtolserhslocal_(lse_rhs, ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb, &L_.k0, &L_.k0, phi_x, phi_y, L_.zero(), ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb, &L_.k0, &L_.k0, phi_xx, phi_xy, L_.zero(), phi_yy, L_.zero(), L_.zero(), ilo_grad2_phi_gb, ihi_grad2_phi_gb, jlo_grad2_phi_gb, jhi_grad2_phi_gb, &L_.k0, &L_.k0, b, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
 // src/toolbox/lsm_level_set_evolution2d.f.in:189
 void lsm2daddconstnormalveltermtolserhs_(double *lse_rhs, const int *ilo_lse_rhs_gb, const int *ihi_lse_rhs_gb, const int *jlo_lse_rhs_gb, const int *jhi_lse_rhs_gb, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const double *vel_n, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb) {
   Lift L_(2, "lsm2daddconstnormalveltermtolserhs_");
@@ -471,6 +495,18 @@ void lsm2daddconstnormalveltermtolserhs_(double *lse_rhs, const int *ilo_lse_rhs
   L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
   if (!L_.ready()) return;
   lsm3daddconstnormalveltermtolserhs_(lse_rhs, ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb, &L_.k0, &L_.k0, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, vel_n, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0);
+}
+
+// src/toolbox/lsm_level_set_evolution2d_local.f.in:227
+void lsm2daddconstnormalveltermtolserhslocal_(double *lse_rhs, const int *ilo_lse_rhs_gb, const int *ihi_lse_rhs_gb, const int *jlo_lse_rhs_gb, const int *jhi_lse_rhs_gb, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const double *vel_n, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2daddconstnormalveltermtolserhslocal_");
+  L_.box(ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb);
+  L_.box(ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb);
+  L_.box(ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3daddconstnormalveltermtolserhslocal_(lse_rhs, ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb, &L_.k0, &L_.k0, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, vel_n, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
 }
 
 // src/toolbox/lsm_level_set_evolution2d.f.in:345
@@ -494,6 +530,19 @@ void lsm2daddnormalveltermtolserhs_(double *lse_rhs, const int *ilo_lse_rhs_gb, 
   L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
   if (!L_.ready()) return;
   lsm3daddnormalveltermtolserhs_(lse_rhs, ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb, &L_.k0, &L_.k0, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, vel_n, ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0);
+}
+
+// src/toolbox/lsm_level_set_evolution2d_local.f.in:126
+void lsm2daddnormalveltermtolserhslocal_(double *lse_rhs, const int *ilo_lse_rhs_gb, const int *ihi_lse_rhs_gb, const int *jlo_lse_rhs_gb, const int *jhi_lse_rhs_gb, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const double *vel_n, const int *ilo_vel_gb, const int *ihi_vel_gb, const int *jlo_vel_gb, const int *jhi_vel_gb, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2daddnormalveltermtolserhslocal_");
+  L_.box(ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb);
+  L_.box(ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb);
+  L_.box(ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb);
+  L_.box(ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3daddnormalveltermtolserhslocal_(lse_rhs, ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb, &L_.k0, &L_.k0, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, vel_n, ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb, &L_.k0, &L_.k0, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
 }
 
 // src/toolbox/lsm_math_utils2d.f.in:69
@@ -569,6 +618,16 @@ void lsm2dcentralhessian_(double *phi_xx, double *phi_xy, double *phi_yy, const 
   lsm3dcentralhessian_(phi_xx, phi_xy, L_.junk(), phi_yy, L_.junk(), L_.junk(), ilo_hessian_gb, ihi_hessian_gb, jlo_hessian_gb, jhi_hessian_gb, &L_.k0, &L_.k0, phi, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dx, dy, dx);
 }
 
+// src/toolbox/lsm_localization2d.f:693
+void lsm2dcheckouternarrowbandlayer_(int *change_sign, const double *phi, const int *ilo_gb, const int *ihi_gb, const int *jlo_gb, const int *jhi_gb, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const int *index_outer, const int *nlo_index_outer, const int *nhi_index_outer, const int *nlo_outer_plus, const int *nhi_outer_plus, const int *nlo_outer_minus, const int *nhi_outer_minus) {
+  Lift L_(2, "lsm2dcheckouternarrowbandlayer_");
+  L_.box(ilo_gb, ihi_gb, jlo_gb, jhi_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.list(nlo_index_outer, nhi_index_outer);
+  if (!L_.ready()) return;
+  lsm3dcheckouternarrowbandlayer_(change_sign, phi, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, index_outer, nlo_index_outer, nhi_index_outer, nlo_outer_plus, nhi_outer_plus, nlo_outer_minus, nhi_outer_minus);
+}
+
 // src/toolbox/lsm_spatial_derivatives2d_local.f.in:1616
 void lsm2dcomputeavegradphilocal_(double *grad_phi_ave, const double *phi, const int *ilo_phi_gb, const int *ihi_phi_gb, const int *jlo_phi_gb, const int *jhi_phi_gb, const double *dx, const double *dy, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
   Lift L_(2, "lsm2dcomputeavegradphilocal_");
@@ -601,6 +660,18 @@ void lsm2dcomputemeancurvatureorder2_(double *kappa, const int *ilo_kappa_gb, co
   lsm3dcomputemeancurvatureorder2_(kappa, ilo_kappa_gb, ihi_kappa_gb, jlo_kappa_gb, jhi_kappa_gb, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, phi_x, phi_y, L_.zero(), grad_phi_mag, ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dx, dy, dx);
 }
 
+// src/geometry/lsm_curvature2d_local.f.in:15
+void lsm2dcomputemeancurvatureorder2local_(double *kappa, const int *ilo_kappa_gb, const int *ihi_kappa_gb, const int *jlo_kappa_gb, const int *jhi_kappa_gb, const double *phi, const int *ilo_phi_gb, const int *ihi_phi_gb, const int *jlo_phi_gb, const int *jhi_phi_gb, const double *phi_x, const double *phi_y, const double *grad_phi_mag, const int *ilo_grad_phi_gb, const int *ihi_grad_phi_gb, const int *jlo_grad_phi_gb, const int *jhi_grad_phi_gb, const double *dx, const double *dy, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2dcomputemeancurvatureorder2local_");
+  L_.box(ilo_kappa_gb, ihi_kappa_gb, jlo_kappa_gb, jhi_kappa_gb);
+  L_.box(ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb);
+  L_.box(ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3dcomputemeancurvatureorder2local_(kappa, ilo_kappa_gb, ihi_kappa_gb, jlo_kappa_gb, jhi_kappa_gb, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, phi_x, phi_y, L_.zero(), grad_phi_mag, ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb, &L_.k0, &L_.k0, dx, dy, dx, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
 // src/reinitialization/lsm_reinitialization2d.f.in:48
 void lsm2dcomputereinitializationeqnrhs_(double *reinit_rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *phi, const int *ilo_phi_gb, const int *ihi_phi_gb, const int *jlo_phi_gb, const int *jhi_phi_gb, const double *phi0, const int *ilo_phi0_gb, const int *ihi_phi0_gb, const int *jlo_phi0_gb, const int *jhi_phi0_gb, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const double *dx, const double *dy, const int *use_phi0_for_sgn) {
   Lift L_(2, "lsm2dcomputereinitializationeqnrhs_");
@@ -612,6 +683,20 @@ void lsm2dcomputereinitializationeqnrhs_(double *reinit_rhs, const int *ilo_rhs_
   L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
   if (!L_.ready()) return;
   lsm3dcomputereinitializationeqnrhs_(reinit_rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, phi0, ilo_phi0_gb, ihi_phi0_gb, jlo_phi0_gb, jhi_phi0_gb, &L_.k0, &L_.k0, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dx, dy, dx, use_phi0_for_sgn);
+}
+
+// src/reinitialization/lsm_reinitialization2d_local.f.in:49
+void lsm2dcomputereinitializationeqnrhslocal_(double *reinit_rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *phi, const int *ilo_phi_gb, const int *ihi_phi_gb, const int *jlo_phi_gb, const int *jhi_phi_gb, const double *phi0, const int *ilo_phi0_gb, const int *ihi_phi0_gb, const int *jlo_phi0_gb, const int *jhi_phi0_gb, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const double *dx, const double *dy, const int *use_phi0_for_sgn, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2dcomputereinitializationeqnrhslocal_");
+  L_.box(ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb);
+  L_.box(ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb);
+  L_.box(ilo_phi0_gb, ihi_phi0_gb, jlo_phi0_gb, jhi_phi0_gb);
+  L_.box(ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb);
+  L_.box(ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3dcomputereinitializationeqnrhslocal_(reinit_rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, phi0, ilo_phi0_gb, ihi_phi0_gb, jlo_phi0_gb, jhi_phi0_gb, &L_.k0, &L_.k0, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, dx, dy, dx, use_phi0_for_sgn, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
 }
 
 // src/toolbox/lsm_math_utils2d.f.in:218
@@ -631,6 +716,16 @@ void lsm2dcomputestableadvectiondtcontrolvolume_(double *dt, const double *vel_x
   L_.box(ilo_ib, ihi_ib, jlo_ib, jhi_ib);
   if (!L_.ready()) return;
   lsm3dcomputestableadvectiondtcontrolvolume_(dt, vel_x, vel_y, L_.zero(), ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb, &L_.k0, &L_.k0, control_vol, ilo_control_vol_gb, ihi_control_vol_gb, jlo_control_vol_gb, jhi_control_vol_gb, &L_.k0, &L_.k0, control_vol_sgn, ilo_ib, ihi_ib, jlo_ib, jhi_ib, &L_.k0, &L_.k0, dx, dy, dx, cfl_number);
+}
+
+// src/toolbox/lsm_math_utils2d_local.f.in:165
+void lsm2dcomputestableadvectiondtlocal_(double *dt, const double *vel_x, const double *vel_y, const int *ilo_vel_gb, const int *ihi_vel_gb, const int *jlo_vel_gb, const int *jhi_vel_gb, const double *dx, const double *dy, const double *cfl_number, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2dcomputestableadvectiondtlocal_");
+  L_.box(ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3dcomputestableadvectiondtlocal_(dt, vel_x, vel_y, L_.zero(), ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb, &L_.k0, &L_.k0, dx, dy, dx, cfl_number, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
 }
 
 // src/toolbox/lsm_math_utils2d.f.in:382
@@ -654,6 +749,17 @@ void lsm2dcomputestableconstnormalveldtcontrolvolume_(double *dt, const double *
   lsm3dcomputestableconstnormalveldtcontrolvolume_(dt, vel_n, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, control_vol, ilo_control_vol_gb, ihi_control_vol_gb, jlo_control_vol_gb, jhi_control_vol_gb, &L_.k0, &L_.k0, control_vol_sgn, ilo_ib, ihi_ib, jlo_ib, jhi_ib, &L_.k0, &L_.k0, dx, dy, dx, cfl_number);
 }
 
+// src/toolbox/lsm_math_utils2d_local.f.in:360
+void lsm2dcomputestableconstnormalveldtlocal_(double *dt, const double *vel_n, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const double *dx, const double *dy, const double *cfl_number, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2dcomputestableconstnormalveldtlocal_");
+  L_.box(ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb);
+  L_.box(ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3dcomputestableconstnormalveldtlocal_(dt, vel_n, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, dx, dy, dx, cfl_number, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
 // src/toolbox/lsm_math_utils2d.f.in:285
 void lsm2dcomputestablenormalveldt_(double *dt, const double *vel_n, const int *ilo_vel_gb, const int *ihi_vel_gb, const int *jlo_vel_gb, const int *jhi_vel_gb, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const int *ilo_ib, const int *ihi_ib, const int *jlo_ib, const int *jhi_ib, const double *dx, const double *dy, const double *cfl_number) {
   Lift L_(2, "lsm2dcomputestablenormalveldt_");
@@ -675,6 +781,28 @@ void lsm2dcomputestablenormalveldtcontrolvolume_(double *dt, const double *vel_n
   L_.box(ilo_ib, ihi_ib, jlo_ib, jhi_ib);
   if (!L_.ready()) return;
   lsm3dcomputestablenormalveldtcontrolvolume_(dt, vel_n, ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb, &L_.k0, &L_.k0, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, control_vol, ilo_control_vol_gb, ihi_control_vol_gb, jlo_control_vol_gb, jhi_control_vol_gb, &L_.k0, &L_.k0, control_vol_sgn, ilo_ib, ihi_ib, jlo_ib, jhi_ib, &L_.k0, &L_.k0, dx, dy, dx, cfl_number);
+}
+
+// src/toolbox/lsm_math_utils2d_local.f.in:246
+void lsm2dcomputestablenormalveldtlocal_(double *dt, const double *vel_n, const int *ilo_vel_gb, const int *ihi_vel_gb, const int *jlo_vel_gb, const int *jhi_vel_gb, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const double *dx, const double *dy, const double *cfl_number, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2dcomputestablenormalveldtlocal_");
+  L_.box(ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb);
+  L_.box(ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb);
+  L_.box(ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3dcomputestablenormalveldtlocal_(dt, vel_n, ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb, &L_.k0, &L_.k0, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, dx, dy, dx, cfl_number, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
+// src/toolbox/lsm_localization2d.f:833
+void lsm2dcopydatalocal_(double *dest, const int *ilo_dest_gb, const int *ihi_dest_gb, const int *jlo_dest_gb, const int *jhi_dest_gb, const double *src, const int *ilo_src_gb, const int *ihi_src_gb, const int *jlo_src_gb, const int *jhi_src_gb, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index) {
+  Lift L_(2, "lsm2dcopydatalocal_");
+  L_.box(ilo_dest_gb, ihi_dest_gb, jlo_dest_gb, jhi_dest_gb);
+  L_.box(ilo_src_gb, ihi_src_gb, jlo_src_gb, jhi_src_gb);
+  L_.list(nlo_index, nhi_index);
+  if (!L_.ready()) return;
+  lsm3dcopydatalocal_(dest, ilo_dest_gb, ihi_dest_gb, jlo_dest_gb, jhi_dest_gb, &L_.k0, &L_.k0, src, ilo_src_gb, ihi_src_gb, jlo_src_gb, jhi_src_gb, &L_.k0, &L_.k0, index_x, index_y, L_.zero_int(), nlo_index, nhi_index);
 }
 
 // src/boundary_conditions/lsm_boundary_conditions2d.f:264
@@ -838,6 +966,17 @@ void lsm2dhomogeneousneumannweno5_(double *phi, const int *ilo_gb, const int *ih
   lsm3dhomogeneousneumannweno5_(phi, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, bdry_location_idx);
 }
 
+// src/toolbox/lsm_localization2d.f:778
+void lsm2dimposemasklocal_(double *dest, const int *ilo_dest_gb, const int *ihi_dest_gb, const int *jlo_dest_gb, const int *jhi_dest_gb, const double *src, const int *ilo_src_gb, const int *ihi_src_gb, const int *jlo_src_gb, const int *jhi_src_gb, const double *mask, const int *ilo_mask_gb, const int *ihi_mask_gb, const int *jlo_mask_gb, const int *jhi_mask_gb, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index) {
+  Lift L_(2, "lsm2dimposemasklocal_");
+  L_.box(ilo_dest_gb, ihi_dest_gb, jlo_dest_gb, jhi_dest_gb);
+  L_.box(ilo_src_gb, ihi_src_gb, jlo_src_gb, jhi_src_gb);
+  L_.box(ilo_mask_gb, ihi_mask_gb, jlo_mask_gb, jhi_mask_gb);
+  L_.list(nlo_index, nhi_index);
+  if (!L_.ready()) return;
+  lsm3dimposemasklocal_(dest, ilo_dest_gb, ihi_dest_gb, jlo_dest_gb, jhi_dest_gb, &L_.k0, &L_.k0, src, ilo_src_gb, ihi_src_gb, jlo_src_gb, jhi_src_gb, &L_.k0, &L_.k0, mask, ilo_mask_gb, ihi_mask_gb, jlo_mask_gb, jhi_mask_gb, &L_.k0, &L_.k0, index_x, index_y, L_.zero_int(), nlo_index, nhi_index);
+}
+
 // src/toolbox/lsm_spatial_derivatives2d.f.in:2091
 void lsm2dlaplacianorder2_(double *laplacian_phi, const int *ilo_laplacian_phi_gb, const int *ihi_laplacian_phi_gb, const int *jlo_laplacian_phi_gb, const int *jhi_laplacian_phi_gb, const double *phi, const int *ilo_phi_gb, const int *ihi_phi_gb, const int *jlo_phi_gb, const int *jhi_phi_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const double *dx, const double *dy) {
   Lift L_(2, "lsm2dlaplacianorder2_");
@@ -868,6 +1007,15 @@ void lsm2dlinearextrapolation_(double *phi, const int *ilo_gb, const int *ihi_gb
   lsm3dlinearextrapolation_(phi, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, bdry_location_idx);
 }
 
+// src/toolbox/lsm_localization2d.f:486
+void lsm2dmarknarrowbandboundarylayer_(unsigned char *narrow_band, const int *ilo_gb, const int *ihi_gb, const int *jlo_gb, const int *jhi_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const unsigned char *mark_boundary_layer) {
+  Lift L_(2, "lsm2dmarknarrowbandboundarylayer_");
+  L_.box(ilo_gb, ihi_gb, jlo_gb, jhi_gb);
+  L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
+  if (!L_.ready()) return;
+  lsm3dmarknarrowbandboundarylayer_(narrow_band, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, mark_boundary_layer);
+}
+
 // src/toolbox/lsm_math_utils2d.f.in:15
 void lsm2dmaxnormdiff_(double *max_norm_diff, const double *field1, const int *ilo_field1_gb, const int *ihi_field1_gb, const int *jlo_field1_gb, const int *jhi_field1_gb, const double *field2, const int *ilo_field2_gb, const int *ihi_field2_gb, const int *jlo_field2_gb, const int *jhi_field2_gb, const int *ilo_ib, const int *ihi_ib, const int *jlo_ib, const int *jhi_ib) {
   Lift L_(2, "lsm2dmaxnormdiff_");
@@ -887,6 +1035,27 @@ void lsm2dmaxnormdiffcontrolvolume_(double *max_norm_diff, const double *field1,
   L_.box(ilo_ib, ihi_ib, jlo_ib, jhi_ib);
   if (!L_.ready()) return;
   lsm3dmaxnormdiffcontrolvolume_(max_norm_diff, field1, ilo_field1_gb, ihi_field1_gb, jlo_field1_gb, jhi_field1_gb, &L_.k0, &L_.k0, field2, ilo_field2_gb, ihi_field2_gb, jlo_field2_gb, jhi_field2_gb, &L_.k0, &L_.k0, control_vol, ilo_control_vol_gb, ihi_control_vol_gb, jlo_control_vol_gb, jhi_control_vol_gb, &L_.k0, &L_.k0, control_vol_sgn, ilo_ib, ihi_ib, jlo_ib, jhi_ib, &L_.k0, &L_.k0);
+}
+
+// src/toolbox/lsm_math_utils2d_local.f.in:16
+void lsm2dmaxnormdifflocal_(double *max_norm_diff, const double *field1, const int *ilo_field1_gb, const int *ihi_field1_gb, const int *jlo_field1_gb, const int *jhi_field1_gb, const double *field2, const int *ilo_field2_gb, const int *ihi_field2_gb, const int *jlo_field2_gb, const int *jhi_field2_gb, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2dmaxnormdifflocal_");
+  L_.box(ilo_field1_gb, ihi_field1_gb, jlo_field1_gb, jhi_field1_gb);
+  L_.box(ilo_field2_gb, ihi_field2_gb, jlo_field2_gb, jhi_field2_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3dmaxnormdifflocal_(max_norm_diff, field1, ilo_field1_gb, ihi_field1_gb, jlo_field1_gb, jhi_field1_gb, &L_.k0, &L_.k0, field2, ilo_field2_gb, ihi_field2_gb, jlo_field2_gb, jhi_field2_gb, &L_.k0, &L_.k0, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
+// src/toolbox/lsm_localization2d.f:621
+void lsm2dmultiplycutofflserhslocal_(const double *phi, double *lse_rhs, const int *ilo_gb, const int *ihi_gb, const int *jlo_gb, const int *jhi_gb, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb, const double *beta, const double *gamma) {
+  Lift L_(2, "lsm2dmultiplycutofflserhslocal_");
+  L_.box(ilo_gb, ihi_gb, jlo_gb, jhi_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3dmultiplycutofflserhslocal_(phi, lse_rhs, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb, beta, gamma);
 }
 
 // src/toolbox/lsm_spatial_derivatives2d.f.in:2166
@@ -910,6 +1079,18 @@ void lsm2drk1step_(double *u_next, const int *ilo_u_next_gb, const int *ihi_u_ne
   L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
   if (!L_.ready()) return;
   lsm3drk1step_(u_next, ilo_u_next_gb, ihi_u_next_gb, jlo_u_next_gb, jhi_u_next_gb, &L_.k0, &L_.k0, u_cur, ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb, &L_.k0, &L_.k0, rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dt);
+}
+
+// src/toolbox/lsm_tvd_runge_kutta2d_local.f:33
+void lsm2drk1steplocal_(double *u_next, const int *ilo_u_next_gb, const int *ihi_u_next_gb, const int *jlo_u_next_gb, const int *jhi_u_next_gb, const double *u_cur, const int *ilo_u_cur_gb, const int *ihi_u_cur_gb, const int *jlo_u_cur_gb, const int *jhi_u_cur_gb, const double *rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *dt, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2drk1steplocal_");
+  L_.box(ilo_u_next_gb, ihi_u_next_gb, jlo_u_next_gb, jhi_u_next_gb);
+  L_.box(ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb);
+  L_.box(ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3drk1steplocal_(u_next, ilo_u_next_gb, ihi_u_next_gb, jlo_u_next_gb, jhi_u_next_gb, &L_.k0, &L_.k0, u_cur, ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb, &L_.k0, &L_.k0, rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, dt, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
 }
 
 // src/boundary_conditions/lsm_boundary_conditions2d.f:149
@@ -955,6 +1136,18 @@ void lsm2dtvdrk2stage1_(double *u_stage1, const int *ilo_u_stage1_gb, const int 
   lsm3dtvdrk2stage1_(u_stage1, ilo_u_stage1_gb, ihi_u_stage1_gb, jlo_u_stage1_gb, jhi_u_stage1_gb, &L_.k0, &L_.k0, u_cur, ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb, &L_.k0, &L_.k0, rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dt);
 }
 
+// src/toolbox/lsm_tvd_runge_kutta2d_local.f:123
+void lsm2dtvdrk2stage1local_(double *u_stage1, const int *ilo_u_stage1_gb, const int *ihi_u_stage1_gb, const int *jlo_u_stage1_gb, const int *jhi_u_stage1_gb, const double *u_cur, const int *ilo_u_cur_gb, const int *ihi_u_cur_gb, const int *jlo_u_cur_gb, const int *jhi_u_cur_gb, const double *rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *dt, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2dtvdrk2stage1local_");
+  L_.box(ilo_u_stage1_gb, ihi_u_stage1_gb, jlo_u_stage1_gb, jhi_u_stage1_gb);
+  L_.box(ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb);
+  L_.box(ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3dtvdrk2stage1local_(u_stage1, ilo_u_stage1_gb, ihi_u_stage1_gb, jlo_u_stage1_gb, jhi_u_stage1_gb, &L_.k0, &L_.k0, u_cur, ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb, &L_.k0, &L_.k0, rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, dt, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
 // src/toolbox/lsm_tvd_runge_kutta2d.f:160
 void lsm2dtvdrk2stage2_(double *u_next, const int *ilo_u_next_gb, const int *ihi_u_next_gb, const int *jlo_u_next_gb, const int *jhi_u_next_gb, const double *u_stage1, const int *ilo_u_stage1_gb, const int *ihi_u_stage1_gb, const int *jlo_u_stage1_gb, const int *jhi_u_stage1_gb, const double *u_cur, const int *ilo_u_cur_gb, const int *ihi_u_cur_gb, const int *jlo_u_cur_gb, const int *jhi_u_cur_gb, const double *rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const double *dt) {
   Lift L_(2, "lsm2dtvdrk2stage2_");
@@ -967,6 +1160,19 @@ void lsm2dtvdrk2stage2_(double *u_next, const int *ilo_u_next_gb, const int *ihi
   lsm3dtvdrk2stage2_(u_next, ilo_u_next_gb, ihi_u_next_gb, jlo_u_next_gb, jhi_u_next_gb, &L_.k0, &L_.k0, u_stage1, ilo_u_stage1_gb, ihi_u_stage1_gb, jlo_u_stage1_gb, jhi_u_stage1_gb, &L_.k0, &L_.k0, u_cur, ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb, &L_.k0, &L_.k0, rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dt);
 }
 
+// src/toolbox/lsm_tvd_runge_kutta2d_local.f:212
+void lsm2dtvdrk2stage2local_(double *u_next, const int *ilo_u_next_gb, const int *ihi_u_next_gb, const int *jlo_u_next_gb, const int *jhi_u_next_gb, const double *u_stage1, const int *ilo_u_stage1_gb, const int *ihi_u_stage1_gb, const int *jlo_u_stage1_gb, const int *jhi_u_stage1_gb, const double *u_cur, const int *ilo_u_cur_gb, const int *ihi_u_cur_gb, const int *jlo_u_cur_gb, const int *jhi_u_cur_gb, const double *rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *dt, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2dtvdrk2stage2local_");
+  L_.box(ilo_u_next_gb, ihi_u_next_gb, jlo_u_next_gb, jhi_u_next_gb);
+  L_.box(ilo_u_stage1_gb, ihi_u_stage1_gb, jlo_u_stage1_gb, jhi_u_stage1_gb);
+  L_.box(ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb);
+  L_.box(ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3dtvdrk2stage2local_(u_next, ilo_u_next_gb, ihi_u_next_gb, jlo_u_next_gb, jhi_u_next_gb, &L_.k0, &L_.k0, u_stage1, ilo_u_stage1_gb, ihi_u_stage1_gb, jlo_u_stage1_gb, jhi_u_stage1_gb, &L_.k0, &L_.k0, u_cur, ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb, &L_.k0, &L_.k0, rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, dt, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
 // src/toolbox/lsm_tvd_runge_kutta2d.f:232
 void lsm2dtvdrk3stage1_(double *u_stage1, const int *ilo_u_stage1_gb, const int *ihi_u_stage1_gb, const int *jlo_u_stage1_gb, const int *jhi_u_stage1_gb, const double *u_cur, const int *ilo_u_cur_gb, const int *ihi_u_cur_gb, const int *jlo_u_cur_gb, const int *jhi_u_cur_gb, const double *rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const double *dt) {
   Lift L_(2, "lsm2dtvdrk3stage1_");
@@ -976,6 +1182,18 @@ void lsm2dtvdrk3stage1_(double *u_stage1, const int *ilo_u_stage1_gb, const int 
   L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
   if (!L_.ready()) return;
   lsm3dtvdrk3stage1_(u_stage1, ilo_u_stage1_gb, ihi_u_stage1_gb, jlo_u_stage1_gb, jhi_u_stage1_gb, &L_.k0, &L_.k0, u_cur, ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb, &L_.k0, &L_.k0, rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dt);
+}
+
+// src/toolbox/lsm_tvd_runge_kutta2d_local.f:308
+void lsm2dtvdrk3stage1local_(double *u_stage1, const int *ilo_u_stage1_gb, const int *ihi_u_stage1_gb, const int *jlo_u_stage1_gb, const int *jhi_u_stage1_gb, const double *u_cur, const int *ilo_u_cur_gb, const int *ihi_u_cur_gb, const int *jlo_u_cur_gb, const int *jhi_u_cur_gb, const double *rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *dt, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2dtvdrk3stage1local_");
+  L_.box(ilo_u_stage1_gb, ihi_u_stage1_gb, jlo_u_stage1_gb, jhi_u_stage1_gb);
+  L_.box(ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb);
+  L_.box(ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3dtvdrk3stage1local_(u_stage1, ilo_u_stage1_gb, ihi_u_stage1_gb, jlo_u_stage1_gb, jhi_u_stage1_gb, &L_.k0, &L_.k0, u_cur, ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb, &L_.k0, &L_.k0, rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, dt, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
 }
 
 // src/toolbox/lsm_tvd_runge_kutta2d.f:296
@@ -990,6 +1208,19 @@ void lsm2dtvdrk3stage2_(double *u_stage2, const int *ilo_u_stage2_gb, const int 
   lsm3dtvdrk3stage2_(u_stage2, ilo_u_stage2_gb, ihi_u_stage2_gb, jlo_u_stage2_gb, jhi_u_stage2_gb, &L_.k0, &L_.k0, u_stage1, ilo_u_stage1_gb, ihi_u_stage1_gb, jlo_u_stage1_gb, jhi_u_stage1_gb, &L_.k0, &L_.k0, u_cur, ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb, &L_.k0, &L_.k0, rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dt);
 }
 
+// src/toolbox/lsm_tvd_runge_kutta2d_local.f:396
+void lsm2dtvdrk3stage2local_(double *u_stage2, const int *ilo_u_stage2_gb, const int *ihi_u_stage2_gb, const int *jlo_u_stage2_gb, const int *jhi_u_stage2_gb, const double *u_stage1, const int *ilo_u_stage1_gb, const int *ihi_u_stage1_gb, const int *jlo_u_stage1_gb, const int *jhi_u_stage1_gb, const double *u_cur, const int *ilo_u_cur_gb, const int *ihi_u_cur_gb, const int *jlo_u_cur_gb, const int *jhi_u_cur_gb, const double *rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *dt, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2dtvdrk3stage2local_");
+  L_.box(ilo_u_stage2_gb, ihi_u_stage2_gb, jlo_u_stage2_gb, jhi_u_stage2_gb);
+  L_.box(ilo_u_stage1_gb, ihi_u_stage1_gb, jlo_u_stage1_gb, jhi_u_stage1_gb);
+  L_.box(ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb);
+  L_.box(ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3dtvdrk3stage2local_(u_stage2, ilo_u_stage2_gb, ihi_u_stage2_gb, jlo_u_stage2_gb, jhi_u_stage2_gb, &L_.k0, &L_.k0, u_stage1, ilo_u_stage1_gb, ihi_u_stage1_gb, jlo_u_stage1_gb, jhi_u_stage1_gb, &L_.k0, &L_.k0, u_cur, ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb, &L_.k0, &L_.k0, rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, dt, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
 // src/toolbox/lsm_tvd_runge_kutta2d.f:366
 void lsm2dtvdrk3stage3_(double *u_next, const int *ilo_u_next_gb, const int *ihi_u_next_gb, const int *jlo_u_next_gb, const int *jhi_u_next_gb, const double *u_stage2, const int *ilo_u_stage2_gb, const int *ihi_u_stage2_gb, const int *jlo_u_stage2_gb, const int *jhi_u_stage2_gb, const double *u_cur, const int *ilo_u_cur_gb, const int *ihi_u_cur_gb, const int *jlo_u_cur_gb, const int *jhi_u_cur_gb, const double *rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const double *dt) {
   Lift L_(2, "lsm2dtvdrk3stage3_");
@@ -1000,6 +1231,19 @@ void lsm2dtvdrk3stage3_(double *u_next, const int *ilo_u_next_gb, const int *ihi
   L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
   if (!L_.ready()) return;
   lsm3dtvdrk3stage3_(u_next, ilo_u_next_gb, ihi_u_next_gb, jlo_u_next_gb, jhi_u_next_gb, &L_.k0, &L_.k0, u_stage2, ilo_u_stage2_gb, ihi_u_stage2_gb, jlo_u_stage2_gb, jhi_u_stage2_gb, &L_.k0, &L_.k0, u_cur, ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb, &L_.k0, &L_.k0, rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dt);
+}
+
+// src/toolbox/lsm_tvd_runge_kutta2d_local.f:491
+void lsm2dtvdrk3stage3local_(double *u_next, const int *ilo_u_next_gb, const int *ihi_u_next_gb, const int *jlo_u_next_gb, const int *jhi_u_next_gb, const double *u_stage2, const int *ilo_u_stage2_gb, const int *ihi_u_stage2_gb, const int *jlo_u_stage2_gb, const int *jhi_u_stage2_gb, const double *u_cur, const int *ilo_u_cur_gb, const int *ihi_u_cur_gb, const int *jlo_u_cur_gb, const int *jhi_u_cur_gb, const double *rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *dt, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2dtvdrk3stage3local_");
+  L_.box(ilo_u_next_gb, ihi_u_next_gb, jlo_u_next_gb, jhi_u_next_gb);
+  L_.box(ilo_u_stage2_gb, ihi_u_stage2_gb, jlo_u_stage2_gb, jhi_u_stage2_gb);
+  L_.box(ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb);
+  L_.box(ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3dtvdrk3stage3local_(u_next, ilo_u_next_gb, ihi_u_next_gb, jlo_u_next_gb, jhi_u_next_gb, &L_.k0, &L_.k0, u_stage2, ilo_u_stage2_gb, ihi_u_stage2_gb, jlo_u_stage2_gb, jhi_u_stage2_gb, &L_.k0, &L_.k0, u_cur, ilo_u_cur_gb, ihi_u_cur_gb, jlo_u_cur_gb, jhi_u_cur_gb, &L_.k0, &L_.k0, rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, dt, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
 }
 
 // src/toolbox/lsm_spatial_derivatives2d.f.in:1069
@@ -1139,6 +1383,15 @@ void lsm2dzerooutlevelseteqnrhs_(double *lse_rhs, const int *ilo_lse_rhs_gb, con
   L_.box(ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb);
   if (!L_.ready()) return;
   lsm3dzerooutlevelseteqnrhs_(lse_rhs, ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb, &L_.k0, &L_.k0);
+}
+
+// src/toolbox/lsm_level_set_evolution2d_local.f.in:16
+void lsm2dzerooutlevelseteqnrhslocal_(double *lse_rhs, const int *ilo_lse_rhs_gb, const int *ihi_lse_rhs_gb, const int *jlo_lse_rhs_gb, const int *jhi_lse_rhs_gb, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index) {
+  Lift L_(2, "lsm2dzerooutlevelseteqnrhslocal_");
+  L_.box(ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb);
+  L_.list(nlo_index, nhi_index);
+  if (!L_.ready()) return;
+  lsm3dzerooutlevelseteqnrhslocal_(lse_rhs, ilo_lse_rhs_gb, ihi_lse_rhs_gb, jlo_lse_rhs_gb, jhi_lse_rhs_gb, &L_.k0, &L_.k0, index_x, index_y, L_.zero_int(), nlo_index, nhi_index);
 }
 
 }  // extern "C"

@@ -55,6 +55,12 @@ REF_SOURCES = [
     "reinitialization/lsm_reinitialization1d.f.in",
     "toolbox/lsm_math_utils1d.f.in",
     "boundary_conditions/lsm_boundary_conditions1d.f",
+    "toolbox/lsm_tvd_runge_kutta2d_local.f",
+    "toolbox/lsm_level_set_evolution2d_local.f.in",
+    "reinitialization/lsm_reinitialization2d_local.f.in",
+    "geometry/lsm_curvature2d_local.f.in",
+    "toolbox/lsm_math_utils2d_local.f.in",
+    "toolbox/lsm_localization2d.f",
 ]
 
 CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-std=gnu99",

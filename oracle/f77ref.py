@@ -61,8 +61,10 @@ def logical_lines(text, fname):
             continue
         if raw[0] in "cC*!":
             continue
-        if raw.startswith("\t"):
-            rest = raw[1:]
+        lead = len(raw) - len(raw.lstrip(" "))
+        if lead < 6 and raw[lead:lead + 1] == "\t":
+            # tab format: a tab in columns 1-6 starts the statement field
+            rest = raw[lead + 1:]
             if rest[:1] in "123456789":
                 cont, body = True, rest[1:]
             else:

@@ -80,7 +80,8 @@ def case(sym, seed, face=0):
     args = L.ABI[sym]["args"]
     sc = dict(H.DEFAULT_SCALARS)
     sc.update({"bdry_location_idx": face, "n": 2, "dir": 1 + seed % d, "beta": 0.15, "gamma": 0.3,
-               "grad_phi_ave": -1.0, "dt": 0.01, "mark_fb": 2, "mark_d1": 4, "mark_d2": 4, "mark_d3": 4})
+               "grad_phi_ave": -1.0, "dt": 0.01, "mark_fb": 2, "mark_d1": 4, "mark_d2": 4, "mark_d3": 4,
+               "change_sign": -1, "mark_boundary_layer": 7})
     vals = {}
     phi = field(rng, d)
     if is_local(sym):
@@ -91,6 +92,12 @@ def case(sym, seed, face=0):
             sc["nlo_index%d" % lev], sc["nhi_index%d" % lev] = bounds[lev]
         if any(a[0] == "nlo_index0" for a in args):
             sc.update({"mark_fb": 1, "mark_d1": 4, "mark_d2": 3, "mark_d3": 2})
+        # outer layer: the deepest level's entries, first half "plus", second half "minus"
+        outer = np.arange(bounds[3][0], bounds[3][1] + 1, dtype=np.int32)
+        half = len(outer) // 2
+        vals["index_outer"] = outer
+        sc.update({"nlo_index_outer": 0, "nhi_index_outer": len(outer) - 1, "nlo_outer_plus": 0,
+                   "nhi_outer_plus": half - 1, "nlo_outer_minus": half, "nhi_outer_minus": len(outer) - 1})
     for name, kind, is_arr, written in args:
         m = BOUND.match(name)
         if m:
