@@ -20,7 +20,11 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblsmgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Host code computes some per-call constants (e.g. the cut-off's (gamma -
+# 3 beta)); -ffp-contract=off keeps the host compiler from fusing them into
+# FMAs on hosts that have them (Arm), so they round as LSMLIB's do.
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+          "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr", "--extended-lambda", "-I", os.path.join(HERE, "..", "include")]
 
 # FP64 parity units: no contraction of a*b+c into FMA

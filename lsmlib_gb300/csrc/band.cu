@@ -168,8 +168,9 @@ void lsm3dmarknarrowbandboundarylayer_(unsigned char *narrow_band, BOXARG(g), co
   if (!call.ok()) return;
   View<U8> nb = view(call.inout(narrow_band, gb.size()), gb);
   if (!call.ok()) return;
-  // the six faces in the reference's order (localization3d.f:328-374)
-  for (int face = 0; face < 6; face++) {
+  // the six faces in the reference's order (localization3d.f:328-374); a 2D
+  // call (lifted) has the four x and y faces only (localization2d.f)
+  for (int face = 0; face < 2 * g_lift_dims; face++) {
     Box b = gb;
     b.lo[face / 2] = b.hi[face / 2] = f[face];
     Grid3 g3 = cover(b);
