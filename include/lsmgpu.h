@@ -168,8 +168,12 @@ int lsmgpu_advect_batch_weno5_tvdrk3_f32(float *phi, const long long *offsets, c
  * with grad_phi): *J; grad_phi = dJ/dphi over gb; grad_vel_* = dJ/dvel_*
  * over vel_gb.  Ghost entries of the gradients are set to zero.  Forward
  * states are kept every checkpoint_every steps and the steps between are
- * recomputed in the reverse sweep (device memory: about
+ * recomputed in the reverse sweep, except the last checkpoint_every steps,
+ * whose stage states the forward sweep keeps (device memory: about
  * 3 * checkpoint_every + n_steps / checkpoint_every + 16 padded fields).
+ * checkpoint_every >= n_steps keeps the whole trajectory and recomputes
+ * nothing; checkpoint_every = 0 picks the largest spacing whose fields fit in
+ * half of the free device memory.
  * Arrays may be host or device memory (host arrays are staged).
  * Returns an LSMGPU_* status. */
 int lsmgpu_advect_adjoint_weno5_tvdrk3_f64(const double *phi, const int *gb, const int *fb,

@@ -82,6 +82,25 @@ void launch_adj_stage(const AdjStageArgs<R> &a) {
   note_launch();
 }
 
+// checkpoint_every = 0: the largest spacing K <= n_steps whose stored fields
+// (3K segment stages, n_steps / K checkpoints, ~16 work fields) fit in half
+// of the free device memory; K = n_steps keeps the whole trajectory and
+// recomputes nothing.
+inline int auto_checkpoint(int n_steps, long long field_bytes, bool want_grad) {
+  if (n_steps <= 1 || !want_grad) return n_steps > 1 ? n_steps : 1;
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+    cudaGetLastError();
+    return 8 < n_steps ? 8 : n_steps;
+  }
+  const double budget = 0.5 * (double)free_b;
+  for (int k = n_steps; k > 1; k--) {
+    const long long fields = 3LL * k + (n_steps + k - 1) / k + 16;
+    if ((double)fields * (double)field_bytes <= budget) return k;
+  }
+  return 1;
+}
+
 template <class R, bool EXACT>
 int run(const char *name, const Box &gb, const Box &fb, const Box &vb, const AdjSpec &sp, const AdjIO<R> &io) {
   using fused::StageArgs;
@@ -94,10 +113,10 @@ int run(const char *name, const Box &gb, const Box &fb, const Box &vb, const Adj
   if (!call.ok()) return LSMGPU_ERR_BOUNDS;
   const int ngv = advect ? (io.gvel[0] != nullptr) + (io.gvel[1] != nullptr) + (io.gvel[2] != nullptr) : 0;
   const bool objective = io.tgt != nullptr;
-  if (sp.n_steps < 0 || sp.ckpt < 1 || (objective && !(sp.eps > 0.0)) || (ngv != 0 && ngv != 3) ||
+  if (sp.n_steps < 0 || sp.ckpt < 0 || (objective && !(sp.eps > 0.0)) || (ngv != 0 && ngv != 3) ||
       (ngv == 3 && !io.gphi) || (io.gphi && !objective && !io.grad_out)) {
     set_error(LSMGPU_ERR_ARGUMENT,
-              "%s: need n_steps >= 0, checkpoint_every >= 1, heaviside_eps > 0, a gradient source, and "
+              "%s: need n_steps >= 0, checkpoint_every >= 0, heaviside_eps > 0, a gradient source, and "
               "velocity gradients either all three (with grad_phi) or none",
               name);
     return LSMGPU_ERR_ARGUMENT;
@@ -119,7 +138,7 @@ int run(const char *name, const Box &gb, const Box &fb, const Box &vb, const Adj
 
   const Layout L = fused::make_layout(nx, ny, nz);
   const long long ne = L.elems();
-  const int K = sp.ckpt;
+  const int K = sp.ckpt > 0 ? sp.ckpt : auto_checkpoint(sp.n_steps, ne * (long long)sizeof(R), want_grad);
   const int nck = sp.n_steps > 0 ? (sp.n_steps + K - 1) / K : 1;
   R *X = call.temp<R>(ne), *T1 = call.temp<R>(ne), *T2 = call.temp<R>(ne);
   R *TG = objective ? call.temp<R>(ne) : nullptr;
@@ -210,11 +229,35 @@ int run(const char *name, const Box &gb, const Box &fb, const Box &vb, const Adj
     if (dst) stage(t_o2, dst, 3);
   };
 
+  // stage states of a segment: U[3m] = state at step m, U[3m+1], U[3m+2] its
+  // two intermediate stages (U[0] is the segment's checkpoint)
+  std::vector<CUtensorMap> tU(want_grad ? 3 * K : 0);
+  auto map_segment = [&](int seg) {
+    U[0] = ck[seg];
+    for (int m = 0; m < 3 * K; m++)
+      if ((m == 0 || seg == nck - 1) && !tmap(U[m], &tU[m])) return false;
+    return true;
+  };
+  if (want_grad && sp.n_steps > 0 && !map_segment(nck - 1)) {
+    call.fail("tensor map encoding failed");
+    return LSMGPU_ERR_CUDA;
+  }
+
   // ---- forward sweep with checkpoints ----------------------------------------
+  // The last segment's stage states are written straight into U, so the
+  // reverse sweep does not recompute it (with checkpoint_every >= n_steps
+  // nothing is recomputed).
+  const int last0 = want_grad ? (nck - 1) * K : sp.n_steps;
   for (int n = 0; n < sp.n_steps; n++) {
-    fwd_step(tX, X, tT1, T1, tT2, T2, X);
-    if ((n + 1) % K == 0 && (n + 1) < sp.n_steps)
-      cudaMemcpyAsync(ck[(n + 1) / K], X, (size_t)ne * sizeof(R), cudaMemcpyDeviceToDevice, s);
+    if (n < last0) {
+      fwd_step(tX, X, tT1, T1, tT2, T2, X);
+      if ((n + 1) % K == 0 && (n + 1) < sp.n_steps)
+        cudaMemcpyAsync(ck[(n + 1) / K], X, (size_t)ne * sizeof(R), cudaMemcpyDeviceToDevice, s);
+    } else {
+      const int m = n - last0;
+      R *dst = (n + 1 < sp.n_steps) ? U[3 * m + 3] : X;
+      fwd_step(tU[3 * m], U[3 * m], tU[3 * m + 1], U[3 * m + 1], tU[3 * m + 2], U[3 * m + 2], dst);
+    }
   }
   if (phi_out_d) {
     dim3 blk(32, 4, 2);
@@ -236,12 +279,6 @@ int run(const char *name, const Box &gb, const Box &fb, const Box &vb, const Adj
     if (want_gvel)
       for (int d = 0; d < 3; d++) cudaMemsetAsync(GV[d], 0, (size_t)ne * sizeof(R), s);
     if (GP0) cudaMemsetAsync(GP0, 0, (size_t)ne * sizeof(R), s);
-    std::vector<CUtensorMap> tU(3 * K);
-    for (int m = 1; m < 3 * K; m++)
-      if (!tmap(U[m], &tU[m])) {
-        call.fail("tensor map encoding failed");
-        return LSMGPU_ERR_CUDA;
-      }
     AdjStageArgs<R> aa{};
     aa.L = L;
     for (int d = 0; d < 3; d++) {
@@ -270,14 +307,15 @@ int run(const char *name, const Box &gb, const Box &fb, const Box &vb, const Adj
     };
     for (int seg = nck - 1; seg >= 0 && sp.n_steps > 0; seg--) {
       const int s0 = seg * K, s1 = (s0 + K < sp.n_steps) ? s0 + K : sp.n_steps, ns = s1 - s0;
-      U[0] = ck[seg];
-      if (!tmap(U[0], &tU[0])) {
-        call.fail("tensor map encoding failed");
-        return LSMGPU_ERR_CUDA;
+      if (seg != nck - 1) {  // the last segment is still in U from the forward sweep
+        if (!map_segment(seg)) {
+          call.fail("tensor map encoding failed");
+          return LSMGPU_ERR_CUDA;
+        }
+        for (int m = 0; m < ns; m++)
+          fwd_step(tU[3 * m], U[3 * m], tU[3 * m + 1], U[3 * m + 1], tU[3 * m + 2], U[3 * m + 2],
+                   m + 1 < ns ? U[3 * m + 3] : nullptr);
       }
-      for (int m = 0; m < ns; m++)
-        fwd_step(tU[3 * m], U[3 * m], tU[3 * m + 1], U[3 * m + 1], tU[3 * m + 2], U[3 * m + 2],
-                 m + 1 < ns ? U[3 * m + 3] : nullptr);
       for (int m = ns - 1; m >= 0; m--) {
         aa.s = U[3 * m + 2]; aa.M = LA; aa.mscale = R(2.0 / 3.0);
         aa.P = nullptr; aa.Q = nullptr; aa.out = LB;

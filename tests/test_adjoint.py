@@ -191,7 +191,7 @@ def test_adjoint_checkpoint_spacing_changes_nothing(precision, gpu_lib):
     phi, vel, tgt, sp, dt = adjoint_case((24, 20, 18))
     eps = 1.5 * sp[0]
     base = gpu_adjoint(phi, vel, tgt, sp, dt, 9, eps, precision, ckpt=9)
-    for ckpt in (1, 2, 4, 100):
+    for ckpt in (1, 2, 4, 100, 0):   # 0: the library picks the spacing
         J, gp, gv = gpu_adjoint(phi, vel, tgt, sp, dt, 9, eps, precision, ckpt=ckpt)
         assert J == base[0]
         assert np.array_equal(gp, base[1])
@@ -317,7 +317,7 @@ def test_adjoint_argument_errors(gpu_lib):
     gb, fb = boxes(phi.shape)
     P, V, T = ghosted(phi), [ghosted(v) for v in vel], ghosted(tgt)
     with pytest.raises(RuntimeError, match="checkpoint_every"):
-        L.advect_adjoint_weno5_tvdrk3(P, gb, fb, V, gb, T, sp[0], dt, 3, 0.1, checkpoint_every=0)
+        L.advect_adjoint_weno5_tvdrk3(P, gb, fb, V, gb, T, sp[0], dt, 3, 0.1, checkpoint_every=-1)
     with pytest.raises(RuntimeError, match="6 cells"):
         L.advect_adjoint_weno5_tvdrk3(P, gb, (0, 4, 0, 11, 0, 11), V, gb, T, sp[0], dt, 3, 0.1)
     with pytest.raises(RuntimeError, match="3 ghost cells"):
@@ -461,7 +461,7 @@ def test_reinit_vjp_checkpoint_spacing_changes_nothing(precision, gpu_lib):
     phi, sp, dtau = reinit_case(dims)
     gout = np.asfortranarray(np.random.default_rng(23).standard_normal(dims))
     base = gpu_reinit_vjp(phi, gout, sp, dtau, 7, precision, 7)
-    for ckpt in (1, 3, 50):
+    for ckpt in (1, 3, 50, 0):
         fin, gp = gpu_reinit_vjp(phi, gout, sp, dtau, 7, precision, ckpt)
         assert np.array_equal(fin, base[0]) and np.array_equal(gp, base[1])
 
