@@ -970,6 +970,60 @@ void lsm2dcopyextrapolation_(
   const int *jhi_fb,
   const int *bdry_location_idx);
 
+/* 2D form: build the narrow band: level-0 list in sweep order, outer lists, BFS levels.
+ * Replaces src/toolbox/lsm_localization2d.f:139; C declaration src/toolbox/lsm_localization2d.h:94.
+ */
+void lsm2ddeterminenarrowband_(
+  const double *phi,
+  const int *ilo_gb,
+  const int *ihi_gb,
+  const int *jlo_gb,
+  const int *jhi_gb,
+  unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  int *index_x,
+  int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  int *n_lo,
+  int *n_hi,
+  int *index_outer,
+  const int *nlo_index_outer,
+  const int *nhi_index_outer,
+  int *nlo_outer_plus,
+  int *nhi_outer_plus,
+  int *nlo_outer_minus,
+  int *nhi_outer_minus,
+  const double *width,
+  const double *width_inner,
+  const int *level);
+
+/* 2D form: build a narrow band from the sign of a mask.
+ * Replaces src/toolbox/lsm_localization2d.f:539; C declaration src/toolbox/lsm_localization2d.h:328.
+ */
+void lsm2ddeterminenarrowbandfrommask_(
+  const double *mask,
+  const int *ilo_mask_gb,
+  const int *ihi_mask_gb,
+  const int *jlo_mask_gb,
+  const int *jhi_mask_gb,
+  unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  int *index_x,
+  int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  int *n_lo,
+  int *n_hi,
+  const int *level,
+  const int *use_mask_sign);
+
 /* 2D form: |grad phi| with the reference's 1e-8 clamps.
  * Replaces src/toolbox/lsm_spatial_derivatives2d.f.in:2395; C declaration src/toolbox/lsm_spatial_derivatives2d.h:774.
  */
@@ -1454,6 +1508,23 @@ void lsm2dmarknarrowbandboundarylayer_(
   const int *jlo_fb,
   const int *jhi_fb,
   const unsigned char *mark_boundary_layer);
+
+/* 2D form: breadth-first neighbour levels of a narrow band.
+ * Replaces src/toolbox/lsm_localization2d.f:48.
+ */
+void lsm2dmarknarrowbandneighbors_(
+  unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  int *index_x,
+  int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  int *n_lo,
+  int *n_hi,
+  const int *level);
 
 /* 2D form: max |field1 - field2| over an index box.
  * Replaces src/toolbox/lsm_math_utils2d.f.in:15; C declaration src/toolbox/lsm_math_utils2d.h:90.

@@ -814,6 +814,27 @@ void lsm2dcopyextrapolation_(double *phi, const int *ilo_gb, const int *ihi_gb, 
   lsm3dcopyextrapolation_(phi, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, bdry_location_idx);
 }
 
+// src/toolbox/lsm_localization2d.f:139
+void lsm2ddeterminenarrowband_(const double *phi, const int *ilo_gb, const int *ihi_gb, const int *jlo_gb, const int *jhi_gb, unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, int *index_x, int *index_y, const int *nlo_index, const int *nhi_index, int *n_lo, int *n_hi, int *index_outer, const int *nlo_index_outer, const int *nhi_index_outer, int *nlo_outer_plus, int *nhi_outer_plus, int *nlo_outer_minus, int *nhi_outer_minus, const double *width, const double *width_inner, const int *level) {
+  Lift L_(2, "lsm2ddeterminenarrowband_");
+  L_.box(ilo_gb, ihi_gb, jlo_gb, jhi_gb);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.list(nlo_index_outer, nhi_index_outer);
+  if (!L_.ready()) return;
+  lsm3ddeterminenarrowband_(phi, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, index_x, index_y, (int *)L_.junk(), nlo_index, nhi_index, n_lo, n_hi, index_outer, nlo_index_outer, nhi_index_outer, nlo_outer_plus, nhi_outer_plus, nlo_outer_minus, nhi_outer_minus, width, width_inner, level);
+}
+
+// src/toolbox/lsm_localization2d.f:539
+void lsm2ddeterminenarrowbandfrommask_(const double *mask, const int *ilo_mask_gb, const int *ihi_mask_gb, const int *jlo_mask_gb, const int *jhi_mask_gb, unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, int *index_x, int *index_y, const int *nlo_index, const int *nhi_index, int *n_lo, int *n_hi, const int *level, const int *use_mask_sign) {
+  Lift L_(2, "lsm2ddeterminenarrowbandfrommask_");
+  L_.box(ilo_mask_gb, ihi_mask_gb, jlo_mask_gb, jhi_mask_gb);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  L_.list(nlo_index, nhi_index);
+  if (!L_.ready()) return;
+  lsm3ddeterminenarrowbandfrommask_(mask, ilo_mask_gb, ihi_mask_gb, jlo_mask_gb, jhi_mask_gb, &L_.k0, &L_.k0, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, index_x, index_y, (int *)L_.junk(), nlo_index, nhi_index, n_lo, n_hi, level, use_mask_sign);
+}
+
 // src/toolbox/lsm_spatial_derivatives2d.f.in:2395
 void lsm2dgradientmagnitude_(const double *phi_x, const double *phi_y, double *grad_phi_mag, const int *ilo_grad_phi_gb, const int *ihi_grad_phi_gb, const int *jlo_grad_phi_gb, const int *jhi_grad_phi_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb) {
   Lift L_(2, "lsm2dgradientmagnitude_");
@@ -1014,6 +1035,15 @@ void lsm2dmarknarrowbandboundarylayer_(unsigned char *narrow_band, const int *il
   L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
   if (!L_.ready()) return;
   lsm3dmarknarrowbandboundarylayer_(narrow_band, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, mark_boundary_layer);
+}
+
+// src/toolbox/lsm_localization2d.f:48
+void lsm2dmarknarrowbandneighbors_(unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, int *index_x, int *index_y, const int *nlo_index, const int *nhi_index, int *n_lo, int *n_hi, const int *level) {
+  Lift L_(2, "lsm2dmarknarrowbandneighbors_");
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  L_.list(nlo_index, nhi_index);
+  if (!L_.ready()) return;
+  lsm3dmarknarrowbandneighbors_(narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, index_x, index_y, (int *)L_.junk(), nlo_index, nhi_index, n_lo, n_hi, level);
 }
 
 // src/toolbox/lsm_math_utils2d.f.in:15

@@ -261,9 +261,12 @@ def lift_map(sym2, dims, abi3, sigs):
             elif not missing_component(name, dims):
                 return None
             elif written:
-                if kind not in ("real", "double"):
+                if kind in ("real", "double"):
+                    out.append("L_.junk()")
+                elif kind == "int":
+                    out.append("(int *)L_.junk()")   # e.g. the index_z list a 2D band build writes
+                else:
                     return None
-                out.append("L_.junk()")
             else:
                 out.append({"real": "L_.zero()", "double": "L_.zero()", "int": "L_.zero_int()"}.get(kind))
                 if out[-1] is None:
