@@ -93,6 +93,20 @@ void lsm1dcentralgradorder4_(
   const int *ihi_fb,
   const double *dx);
 
+/* 1D form: n-th undivided difference along dir (1e10 outside the fill range).
+ * Replaces src/toolbox/lsm_spatial_derivatives1d.f.in:49.
+ */
+void lsm1dcomputedn_(
+  double *dn,
+  const int *ilo_dn_gb,
+  const int *ihi_dn_gb,
+  const double *dn_minus_one,
+  const int *ilo_dn_minus_one_gb,
+  const int *ihi_dn_minus_one_gb,
+  const int *ilo_fb,
+  const int *ihi_fb,
+  const int *n);
+
 /* 1D form: reinitialization RHS sgn(phi)(1 - |grad phi|), Godunov.
  * Replaces src/reinitialization/lsm_reinitialization1d.f.in:48; C declaration src/reinitialization/lsm_reinitialization1d.h:71.
  */

@@ -502,6 +502,27 @@ void lsm2dcomputeavegradphilocal_(
   const int *jhi_nb_gb,
   const unsigned char *mark_fb);
 
+/* 2D form: n-th undivided difference along dir (1e10 outside the fill range).
+ * Replaces src/toolbox/lsm_spatial_derivatives2d.f.in:49.
+ */
+void lsm2dcomputedn_(
+  double *dn,
+  const int *ilo_dn_gb,
+  const int *ihi_dn_gb,
+  const int *jlo_dn_gb,
+  const int *jhi_dn_gb,
+  const double *dn_minus_one,
+  const int *ilo_dn_minus_one_gb,
+  const int *ihi_dn_minus_one_gb,
+  const int *jlo_dn_minus_one_gb,
+  const int *jhi_dn_minus_one_gb,
+  const int *ilo_fb,
+  const int *ihi_fb,
+  const int *jlo_fb,
+  const int *jhi_fb,
+  const int *n,
+  const int *dir);
+
 /* 2D form: n-th undivided differences over an index list.
  * Replaces src/toolbox/lsm_spatial_derivatives2d_local.f.in:43.
  */

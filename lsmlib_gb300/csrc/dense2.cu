@@ -242,4 +242,39 @@ void lsm3dhomogeneousneumannweno5_(BCARGS) {
   face_extrapolate("lsm3dhomogeneousneumannweno5_", phi, BOXOF(g), BOXOF(fb), *bdry_location_idx, BC_COPY);
 }
 
+// n-th undivided difference along dir (spatial_derivatives3d.f.in:49-176):
+// odd n face-centred, Dn(c) = Dm(c) - Dm(c - 1) over the fill box grown by one
+// cell along dir; even n, Dn(c) = -(Dm(c) - Dm(c + 1)) over the fill box;
+// every other cell of Dn's ghost box holds 1e10.  The dense derivative
+// routines form these differences in registers; this is the routine itself.
+void lsm3dcomputedn_(R *Dn, BOXARG(d), const R *Dn_minus_one, BOXARG(m), const int *ilo_fb, const int *ihi_fb,
+                     const int *jlo_fb, const int *jhi_fb, const int *klo_fb, const int *khi_fb, const int *n,
+                     const int *dir) {
+  Call call("lsm3dcomputedn_");
+  if (*dir < 1 || *dir > 3) call.fail("dir must be 1, 2 or 3");
+  if (!call.ok()) return;
+  const Box db = BOXOF(d), mb = BOXOF(m);
+  const int ax = *dir - 1;
+  const bool odd = (*n % 2) != 0;
+  Box cb = mkbox(ilo_fb, ihi_fb, jlo_fb, jhi_fb, klo_fb, khi_fb);  // cells with a difference
+  if (odd) cb.hi[ax] += 1;
+  // Dm(c) and Dm(c - 1) (odd) or Dm(c + 1) (even) along dir
+  Box need = cb;
+  if (odd) need.lo[ax] -= 1; else need.hi[ax] += 1;
+  if (!db.contains(cb, 0, 0, 0) || !mb.contains(need, 0, 0, 0)) call.fail("ghost box does not cover the stencil");
+  if (!call.ok() || db.empty()) return;
+  View<R> D = view(call.inout(Dn, db.size()), db);
+  View<const R> Mv = vin(call, Dn_minus_one, mb);
+  if (!call.ok()) return;
+  const int o0 = ax == 0 ? (odd ? 1 : -1) : 0, o1 = ax == 1 ? (odd ? 1 : -1) : 0, o2 = ax == 2 ? (odd ? 1 : -1) : 0;
+  const R sgn = odd ? R(1) : R(-1);
+  for_box(db, [=] __device__(int i, int j, int k) {
+    if (inbox(cb, i, j, k))
+      D(i, j, k) = sgn * (Mv(i, j, k) - Mv(i - o0, j - o1, k - o2));
+    else
+      D(i, j, k) = R(1.0e10);
+  });
+  call.finish();
+}
+
 }  // extern "C"

@@ -37,6 +37,7 @@ class Lift {
   int *zero_int() const { return (int *)zero_; }
   const int k0 = 0;        // the k (and, in 1D, j) bounds of every lifted box
   const double one = 1.0;  // dz (dy) where the 3D routine multiplies a cell volume
+  const int x_axis = 1;    // the direction argument of a 1D routine
 
  private:
   int saved_;

@@ -67,6 +67,16 @@ void lsm1dcentralgradorder4_(double *phi_x, const int *ilo_grad_phi_gb, const in
   lsm3dcentralgradorder4_(phi_x, L_.junk(), L_.junk(), ilo_grad_phi_gb, ihi_grad_phi_gb, &L_.k0, &L_.k0, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, &L_.k0, &L_.k0, &L_.k0, &L_.k0, ilo_fb, ihi_fb, &L_.k0, &L_.k0, &L_.k0, &L_.k0, dx, dx, dx);
 }
 
+// src/toolbox/lsm_spatial_derivatives1d.f.in:49
+void lsm1dcomputedn_(double *dn, const int *ilo_dn_gb, const int *ihi_dn_gb, const double *dn_minus_one, const int *ilo_dn_minus_one_gb, const int *ihi_dn_minus_one_gb, const int *ilo_fb, const int *ihi_fb, const int *n) {
+  Lift L_(1, "lsm1dcomputedn_");
+  L_.box(ilo_dn_gb, ihi_dn_gb);
+  L_.box(ilo_dn_minus_one_gb, ihi_dn_minus_one_gb);
+  L_.box(ilo_fb, ihi_fb);
+  if (!L_.ready()) return;
+  lsm3dcomputedn_(dn, ilo_dn_gb, ihi_dn_gb, &L_.k0, &L_.k0, &L_.k0, &L_.k0, dn_minus_one, ilo_dn_minus_one_gb, ihi_dn_minus_one_gb, &L_.k0, &L_.k0, &L_.k0, &L_.k0, ilo_fb, ihi_fb, &L_.k0, &L_.k0, &L_.k0, &L_.k0, n, &L_.x_axis);
+}
+
 // src/reinitialization/lsm_reinitialization1d.f.in:48
 void lsm1dcomputereinitializationeqnrhs_(double *reinit_rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const double *phi, const int *ilo_phi_gb, const int *ihi_phi_gb, const double *phi0, const int *ilo_phi0_gb, const int *ihi_phi0_gb, const double *phi_x_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const double *phi_x_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *ilo_fb, const int *ihi_fb, const double *dx, const int *use_phi0_for_sgn) {
   Lift L_(1, "lsm1dcomputereinitializationeqnrhs_");
@@ -636,6 +646,16 @@ void lsm2dcomputeavegradphilocal_(double *grad_phi_ave, const double *phi, const
   L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
   if (!L_.ready()) return;
   lsm3dcomputeavegradphilocal_(grad_phi_ave, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, dx, dy, dx, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
+// src/toolbox/lsm_spatial_derivatives2d.f.in:49
+void lsm2dcomputedn_(double *dn, const int *ilo_dn_gb, const int *ihi_dn_gb, const int *jlo_dn_gb, const int *jhi_dn_gb, const double *dn_minus_one, const int *ilo_dn_minus_one_gb, const int *ihi_dn_minus_one_gb, const int *jlo_dn_minus_one_gb, const int *jhi_dn_minus_one_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const int *n, const int *dir) {
+  Lift L_(2, "lsm2dcomputedn_");
+  L_.box(ilo_dn_gb, ihi_dn_gb, jlo_dn_gb, jhi_dn_gb);
+  L_.box(ilo_dn_minus_one_gb, ihi_dn_minus_one_gb, jlo_dn_minus_one_gb, jhi_dn_minus_one_gb);
+  L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
+  if (!L_.ready()) return;
+  lsm3dcomputedn_(dn, ilo_dn_gb, ihi_dn_gb, jlo_dn_gb, jhi_dn_gb, &L_.k0, &L_.k0, dn_minus_one, ilo_dn_minus_one_gb, ihi_dn_minus_one_gb, jlo_dn_minus_one_gb, jhi_dn_minus_one_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, n, dir);
 }
 
 // src/toolbox/lsm_spatial_derivatives2d_local.f.in:43

@@ -43,6 +43,7 @@ DESC = {
     "lsm3dcentralgradorder4_": ("deriv", "fourth-order central gradient"),
     "lsm3dlaplacianorder2_": ("deriv", "second-order Laplacian"),
     "lsm3dgradientmagnitude_": ("deriv", "|grad phi| with the reference's 1e-8 clamps"),
+    "lsm3dcomputedn_": ("deriv", "n-th undivided difference along dir (1e10 outside the fill range)"),
     # RK
     "lsm3drk1step_": ("rk", "forward Euler step u_next = u + dt*L"),
     "lsm3dtvdrk2stage1_": ("rk", "TVD RK2 stage 1 (an Euler step)"),
@@ -286,6 +287,8 @@ def lift_map(sym2, dims, abi3, sigs):
                 j += 1
             elif (name == "dz" and dims <= 2) or (name == "dy" and dims == 1):
                 out.append(spacing)
+            elif name == "dir" and dims == 1:
+                out.append("&L_.x_axis")   # a 1D routine differences along x
             else:
                 return None
     if j != len(a2):

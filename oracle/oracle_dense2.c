@@ -122,3 +122,28 @@ void lsm3daddexternalandnormalveltermtolserhs_(real_t *rhs, A3(r), const real_t 
       rhs[o] = rhs[o] - ux * gx - uy * gy - uz * gz;
   }
 }
+
+/* lsm3dComputeDn (spatial_derivatives3d.f.in:49-176) */
+void lsm3dcomputedn_(real_t *dn, A3(d), const real_t *dm, A3(m), const int *ilo_fb, const int *ihi_fb,
+                     const int *jlo_fb, const int *jhi_fb, const int *klo_fb, const int *khi_fb, const int *n,
+                     const int *dir) {
+  gbox D = B3(d), M = B3(m);
+  int off[3] = {0, 0, 0}, shift[3] = {0, 0, 0};
+  real_t sgn;
+  if (*n % 2 == 1) {
+    off[*dir - 1] = 1;
+    sgn = 1.0;
+    shift[*dir - 1] = 1;
+  } else {
+    off[*dir - 1] = -1;
+    sgn = -1.0;
+  }
+  FOR_BOX(*ilo_fb, *ihi_fb + shift[0], *jlo_fb, *jhi_fb + shift[1], *klo_fb, *khi_fb + shift[2])
+    dn[at(&D, i, j, k)] = sgn * (dm[at(&M, i, j, k)] - dm[at(&M, i - off[0], j - off[1], k - off[2])]);
+  /* cells outside that range hold big (:138-172) */
+  FOR_BOX(D.lo[0], D.hi[0], D.lo[1], D.hi[1], D.lo[2], D.hi[2]) {
+    int in = i >= *ilo_fb && i <= *ihi_fb + shift[0] && j >= *jlo_fb && j <= *jhi_fb + shift[1] &&
+             k >= *klo_fb && k <= *khi_fb + shift[2];
+    if (!in) dn[at(&D, i, j, k)] = 1.e10;
+  }
+}

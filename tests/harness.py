@@ -176,7 +176,8 @@ def rough_field(rng, gb, scale=1.0):
 DEFAULT_SCALARS = {"dx": 0.1, "dy": 0.12, "dz": 0.09, "dt": 0.013, "cfl_number": 0.5,
                    "b": 0.3, "vel_n": 0.7, "use_phi0_for_sgn": 0,
                    "max_norm_diff": -7.0, "epsilon": 0.45, "control_vol_sgn": 1,
-                   "ave_abs_diff": -7.0, "count": -7, "int_f": -7.0, "volume": -7.0, "area": -7.0}
+                   "ave_abs_diff": -7.0, "count": -7, "int_f": -7.0, "volume": -7.0, "area": -7.0,
+                   "n": 3, "dir": 2}
 
 GB = (-3, 12, -3, 10, -3, 8)     # ghost box with negative lower bounds
 FB = (0, 9, 0, 7, 0, 5)          # fill box three cells inside it
