@@ -185,8 +185,12 @@ def lifted_3d_call(sym, vals, copies=7):
             for _ in range(3 - d):
                 a = np.repeat(a[..., None], copies, axis=-1)
             out[name] = np.asfortranarray(a)
+        elif name in vals:
+            out[name] = vals[name]
+        elif name == "dir":
+            out[name] = 1   # a 1D routine differences along x
         else:
-            out[name] = vals[name] if name in vals else (1.0 if VOLUME.search(sym3) else vals["dx"])
+            out[name] = 1.0 if VOLUME.search(sym3) else vals["dx"]
     return sym3, out
 
 
