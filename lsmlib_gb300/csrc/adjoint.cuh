@@ -50,6 +50,17 @@ using fused::Layout;
 
 constexpr int kSeg = 26;     // cells of a row segment written by one warp
 constexpr int kRows = 8;     // warps (rows) per CTA of k_adj_xz, columns per CTA row of k_adj_y
+// resident CTAs per SM the FP32 reverse kernels are compiled for (register
+// caps).  Measured at 192^3 (reverse step, same box): k_adj_y capped for 4
+// CTAs of 256 threads (61 registers, no spills) 0.858 ms against 0.904 ms
+// uncapped (79 registers); 5 CTAs (48 registers) 0.861 ms; k_adj_xz_row for 4
+// CTAs spills (64 registers) and ran 0.920 ms.
+#ifndef LSMGPU_ADJ_ROW_CTAS
+#define LSMGPU_ADJ_ROW_CTAS 3
+#endif
+#ifndef LSMGPU_ADJ_Y_CTAS
+#define LSMGPU_ADJ_Y_CTAS 4
+#endif
 constexpr int kRowMax = 256; // longest x row k_adj_xz_row takes (one CTA per row)
 
 // periodic image of index a in [0, n): one add or subtract for a in
@@ -434,7 +445,7 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? 3 : 1) k_adj_xz(A
 // shared memory (two buffers, one barrier per plane) and sums its two x faces
 // from its neighbours' slots with periodic wrap.
 template <class R, bool EXACT, int MODE>
-__global__ void __launch_bounds__(kRowMax, sizeof(R) == 4 ? 3 : 1) k_adj_xz_row(AdjStageArgs<R> a) {
+__global__ void __launch_bounds__(kRowMax, sizeof(R) == 4 ? LSMGPU_ADJ_ROW_CTAS : 1) k_adj_xz_row(AdjStageArgs<R> a) {
   extern __shared__ __align__(16) unsigned char xr_smem[];
   const Layout &L = a.L;
   const int nx = L.nx, nz = L.nz;
@@ -540,7 +551,7 @@ __global__ void __launch_bounds__(kRowMax, sizeof(R) == 4 ? 3 : 1) k_adj_xz_row(
 }
 
 template <class R, bool EXACT, int MODE>
-__global__ void __launch_bounds__(32 * kRows) k_adj_y(AdjStageArgs<R> a) {
+__global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? LSMGPU_ADJ_Y_CTAS : 1) k_adj_y(AdjStageArgs<R> a) {
   const Layout &L = a.L;
   const int i = blockIdx.x * 32 + threadIdx.x;
   const int k = blockIdx.y * kRows + threadIdx.y;
