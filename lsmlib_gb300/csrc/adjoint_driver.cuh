@@ -39,6 +39,15 @@ struct AdjIO {
   R *gvel[3];            // dJ/dvel over vb
 };
 
+// march threads per SM the chunk lengths aim at (z march of k_adj_xz_row,
+// y march of k_adj_y)
+#ifndef LSMGPU_ADJ_Z_THREADS
+#define LSMGPU_ADJ_Z_THREADS 2048
+#endif
+#ifndef LSMGPU_ADJ_Y_THREADS
+#define LSMGPU_ADJ_Y_THREADS 4096
+#endif
+
 // march length per thread: enough chunks for `per_sm` threads per SM (each
 // march also computes 6 cells before its first output), at least 16 cells
 inline int pick_chunk(int n_march, long long threads_per_chunk, int per_sm) {
@@ -292,8 +301,8 @@ int run(const char *name, const Box &gb, const Box &fb, const Box &vb, const Adj
     // thread targets per SM measured best at 192^3 (more chunks than resident
     // threads: latency hiding outweighs the extra warm-up cells)
     aa.zchunk = pick_chunk(nz, nx <= kRowMax ? 32LL * ((nx + 31) / 32) * ny : 32LL * ((nx + kSeg - 1) / kSeg) * ny,
-                           2048);
-    aa.ychunk = pick_chunk(ny, (long long)nx * nz, 4096);
+                           LSMGPU_ADJ_Z_THREADS);
+    aa.ychunk = pick_chunk(ny, (long long)nx * nz, LSMGPU_ADJ_Y_THREADS);
     const dim3 cgrid((unsigned)((nx + 31) / 32), (unsigned)((ny + 7) / 8), (unsigned)nz), cblk(32, 8);
     // one reverse stage at forward state `st`
     auto rstage = [&]() {
