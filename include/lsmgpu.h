@@ -245,6 +245,25 @@ int lsmgpu_compute_stable_advection_dt_noalloc(
 /* Library version string. */
 const char *lsmgpu_version(void);
 
+/* ---------------------------------------------------------------------------
+ * Diagnostics.  No counterpart in LSMLIB's library; the first is the GPU
+ * form of its EXAMINE_ARRAY macro (lsm_macros.h), which prints the
+ * positions of NaN / inf values.
+ * ------------------------------------------------------------------------- */
+
+/* Counts the NaN and infinite values of `field` (column-major over gb[6])
+ * inside box[6] and, when first is not NULL, stores the first one a serial
+ * (k, j, i) sweep of the box meets (box.lo - 1 on each axis when there is
+ * none).  Host or device arrays.  Returns an LSMGPU_* status. */
+int lsmgpu_count_nonfinite_f64(const double *field, const int *gb, const int *box, long long *count, int *first);
+int lsmgpu_count_nonfinite_f32(const float *field, const int *gb, const int *box, long long *count, int *first);
+
+/* Exercises the bounded device wait of the TMA-staged kernels: one block
+ * waits on a barrier that is never released, gives up after `polls` polls
+ * (at most 1048576), records LSMGPU_ERR_TIMEOUT and returns; the context
+ * stays usable.  Returns LSMGPU_ERR_TIMEOUT (the expected outcome). */
+int lsmgpu_selftest_bounded_wait(unsigned int polls);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,7 +28,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr", "--extended-lambda", "-I", os.path.join(HERE, "..", "include")]
 
 # FP64 parity units: no contraction of a*b+c into FMA
-NO_FMA = {"dense.cu", "dense2.cu", "local.cu", "band.cu", "fused_f64.cu", "batched_f64.cu", "adjoint_f64.cu",
+NO_FMA = {"dense.cu", "dense2.cu", "local.cu", "band.cu", "fused_f64.cu", "batched_f64.cu", "adjoint_f64.cu", "diag.cu",
           "noalloc.cu", "bandflow_f64.cu", "geometry.cu"}
 
 
@@ -76,7 +76,7 @@ def build(verbose=False, extra=None):
     newest = max(os.path.getmtime(o) for o in objs)
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
         tmp = LIB + ".tmp"
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-ldl"]
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), p.stdout + p.stderr))

@@ -9,6 +9,8 @@
 #include <mutex>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "lsmgpu_common.cuh"
 
 namespace lsmgpu {
@@ -59,7 +61,10 @@ bool cuda_ok(cudaError_t e, const char *what) {
   return false;
 }
 
+// Every entry point is one NVTX range named after it (visible in Nsight
+// timelines; without a tool attached a push / pop is a cheap no-op).
 Call::Call(const char *name) : name_(name) {
+  nvtxRangePushA(name);
   clear_error();
   g_lock.lock();
   locked_ = true;
@@ -73,6 +78,7 @@ Call::Call(const char *name) : name_(name) {
 Call::~Call() {
   if (!finished_) finish();
   if (locked_) g_lock.unlock();
+  nvtxRangePop();
 }
 
 void Call::fail(const char *msg) {
