@@ -47,11 +47,12 @@ def test_nonfinite_scan_matches_numpy(precision, gpu_lib):
     arr = np.asfortranarray(rng.standard_normal(H.shape_of(GB)).astype(dt))
     rc, n, first = _scan(gpu_lib, arr, precision)
     assert rc == 0 and (n, first) == _expected(arr)
-    # plant NaN and inf, one of them in the ghost cells outside the box
+    # plant NaN and inf (array indices; cells (2, 5, 2) and (8, 1, 5) lie in
+    # the box, the other two in the ghost cells outside it)
     for idx, v in (((5, 7, 3), np.nan), ((2, 9, 8), np.inf), ((11, 3, 6), -np.inf), ((0, 0, 0), np.nan)):
         arr[idx] = v
     rc, n, first = _scan(gpu_lib, arr, precision)
-    assert rc == 0 and (n, first) == _expected(arr) and n == 3
+    assert rc == 0 and (n, first) == _expected(arr) == (2, (2, 5, 2))
 
 
 @pytest.mark.gpu
