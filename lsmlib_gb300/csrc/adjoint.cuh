@@ -159,13 +159,11 @@ __device__ __forceinline__ R weno5_adj(const R v[5], R dv[5]) {
 // multiplies the weights and the beta_k once, so the five face adjoints come
 // out of the derivative formulas directly.  kap = dL/dW for the WENO5 value W
 // on side `minus`; returns W.
-static __device__ __forceinline__ float lin_slots_f32(const float a[7], float kap, bool minus, float mu, float dt,
+// D[0..5] = (s(c-2+f) - s(c-3+f)) / dx, the scaled differences of the cell
+static __device__ __forceinline__ float lin_slots_f32(const float D[6], float kap, bool minus, float mu, float dt,
                                                       float inv, float G[6]) {
   const float c13 = 1.f / 3.f, c76 = 7.f / 6.f, c116 = 11.f / 6.f, c16 = 1.f / 6.f, c56 = 5.f / 6.f;
   const float c136 = 13.f / 6.f;
-  float D[6];
-#pragma unroll
-  for (int f = 0; f < 6; f++) D[f] = (a[f + 1] - a[f]) * inv;
   float v[5];
 #pragma unroll
   for (int q = 0; q < 5; q++) v[q] = minus ? D[q] : D[5 - q];
@@ -228,16 +226,14 @@ static __device__ __forceinline__ float lin_slots_f32(const float a[7], float ka
 
 // Face adjoints G[m] (faces c-2+m, scaled by dt) of one cell along one axis
 // for the linearisation coefficient kap = dL/dW of the WENO5 value W on side
-// `minus` (faces c-2..c+2) or plus (faces c-1..c+3); a[0..6] = s(c-3 .. c+3)
-// along the axis, mu the adjoint weight of the cell, inv = 1/dx_d.  Returns W.
+// `minus` (faces c-2..c+2) or plus (faces c-1..c+3); D[0..5] = the scaled
+// differences (s(c-2+f) - s(c-3+f)) * inv along the axis, mu the adjoint
+// weight of the cell, inv = 1/dx_d.  Returns W.
 template <class R, bool EXACT>
-__device__ __forceinline__ R lin_slots(const R a[7], R kap, bool minus, R mu, R dt, R inv, R G[6]) {
+__device__ __forceinline__ R lin_slots(const R D[6], R kap, bool minus, R mu, R dt, R inv, R G[6]) {
   if constexpr (!EXACT && sizeof(R) == 4) {
-    return lin_slots_f32(a, kap, minus, mu, dt, inv, G);
+    return lin_slots_f32(D, kap, minus, mu, dt, inv, G);
   } else {
-    R D[6];  // D(c+f) for f = -2..3
-#pragma unroll
-    for (int f = 0; f < 6; f++) D[f] = (a[f + 1] - a[f]) * inv;
     R v[5], dv[5];
 #pragma unroll
     for (int q = 0; q < 5; q++) v[q] = minus ? D[q] : D[5 - q];
@@ -268,18 +264,28 @@ struct Coef {
   unsigned char side;
 };
 
+// D[0..5]: the cell's scaled differences along axis d (see lin_slots)
 template <class R, bool EXACT, int MODE>
-__device__ __forceinline__ R coef_slots(const R a[7], Coef<R> cf, int d, R mu, R dt, R inv, R G[6]) {
+__device__ __forceinline__ R coef_slots_d(const R D[6], Coef<R> cf, int d, R mu, R dt, R inv, R G[6]) {
   if constexpr (MODE == ADJ_ADV) {
     const R u = cf.k;
     const bool on = !(fabs(u) < R(Consts<double>::zero_tol));
-    const R W = lin_slots<R, EXACT>(a, on ? -u : R(0), u > R(0), mu, dt, inv, G);
+    const R W = lin_slots<R, EXACT>(D, on ? -u : R(0), u > R(0), mu, dt, inv, G);
     return on ? dt * mu * (-W) : R(0);
   } else {
     const int sb = (cf.side >> (2 * d)) & 3;
-    lin_slots<R, EXACT>(a, sb ? cf.k : R(0), sb == 2, mu, dt, inv, G);
+    lin_slots<R, EXACT>(D, sb ? cf.k : R(0), sb == 2, mu, dt, inv, G);
     return R(0);
   }
+}
+
+// the same from the values a[0..6] = s(c-3 .. c+3) along the axis
+template <class R, bool EXACT, int MODE>
+__device__ __forceinline__ R coef_slots(const R a[7], Coef<R> cf, int d, R mu, R dt, R inv, R G[6]) {
+  R D[6];
+#pragma unroll
+  for (int f = 0; f < 6; f++) D[f] = (a[f + 1] - a[f]) * inv;
+  return coef_slots_d<R, EXACT, MODE>(D, cf, d, mu, dt, inv, G);
 }
 
 template <class R>
@@ -366,12 +372,21 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? 3 : 1) k_adj_xz(A
   int zk = wrapi(z0 - 3, nz);
   long long ok = pz * (long long)(zk + fused::GZ);
 
-  R win[7], mring[4], F[6];
+  // dw: the scaled differences along the march of the cell being linearised
+  // (slid one face per step), last: the newest value they reach
+  R dw[6], mring[4], F[6], last;
   R prevV = R(0);
+  {
+    R w[6];
 #pragma unroll
-  for (int q = 0; q < 6; q++) {
-    win[q + 1] = s[plane_add(ok, zk, q - 3, nz, pz)];
-    F[q] = R(0);
+    for (int q = 0; q < 6; q++) {
+      w[q] = s[plane_add(ok, zk, q - 3, nz, pz)];
+      F[q] = R(0);
+    }
+    dw[0] = R(0);
+#pragma unroll
+    for (int f = 0; f < 5; f++) dw[f + 1] = (w[f + 1] - w[f]) * iz;
+    last = w[5];
   }
 #pragma unroll
   for (int q = 0; q < 4; q++) mring[q] = R(0);
@@ -388,8 +403,9 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? 3 : 1) k_adj_xz(A
 
   for (int kk = z0 - 3; kk < zend + 3; kk++) {
 #pragma unroll
-    for (int q = 0; q < 6; q++) win[q] = win[q + 1];
-    win[6] = cs;
+    for (int f = 0; f < 5; f++) dw[f] = dw[f + 1];
+    dw[5] = (cs - last) * iz;
+    last = cs;
 #pragma unroll
     for (int q = 0; q < 3; q++) mring[q] = mring[q + 1];
     mring[3] = msc * cm;
@@ -405,7 +421,7 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? 3 : 1) k_adj_xz(A
       cv = load_coef<R, MODE>(a, 2, col + ok);
     }
     R G[6];
-    const R gz = coef_slots<R, EXACT, MODE>(win, uz, 2, mring[3], dt, iz, G);
+    const R gz = coef_slots_d<R, EXACT, MODE>(dw, uz, 2, mring[3], dt, iz, G);
     if (MODE == ADJ_ADV && a.gvel[2] && own && kk >= z0 && kk < zend) a.gvel[2][col + okk] += gz;
     const R Az = ring_step<R>(F, prevV, G);
     const int k = kk - 3;
@@ -473,12 +489,21 @@ __global__ void __launch_bounds__(kRowMax, sizeof(R) == 4 ? LSMGPU_ADJ_ROW_CTAS 
   int zk = wrapi(z0 - 3, nz);
   long long ok = pz * (long long)(zk + fused::GZ);
 
-  R win[7], mring[4], F[6];
+  // dw: the scaled differences along the march of the cell being linearised
+  // (slid one face per step), last: the newest value they reach
+  R dw[6], mring[4], F[6], last;
   R prevV = R(0);
+  {
+    R w[6];
 #pragma unroll
-  for (int q = 0; q < 6; q++) {
-    win[q + 1] = s[plane_add(ok, zk, q - 3, nz, pz)];
-    F[q] = R(0);
+    for (int q = 0; q < 6; q++) {
+      w[q] = s[plane_add(ok, zk, q - 3, nz, pz)];
+      F[q] = R(0);
+    }
+    dw[0] = R(0);
+#pragma unroll
+    for (int f = 0; f < 5; f++) dw[f + 1] = (w[f + 1] - w[f]) * iz;
+    last = w[5];
   }
 #pragma unroll
   for (int q = 0; q < 4; q++) mring[q] = R(0);
@@ -495,8 +520,9 @@ __global__ void __launch_bounds__(kRowMax, sizeof(R) == 4 ? LSMGPU_ADJ_ROW_CTAS 
   int b = 0;
   for (int kk = z0 - 3; kk < zend + 3; kk++) {
 #pragma unroll
-    for (int q = 0; q < 6; q++) win[q] = win[q + 1];
-    win[6] = cs;
+    for (int f = 0; f < 5; f++) dw[f] = dw[f + 1];
+    dw[5] = (cs - last) * iz;
+    last = cs;
 #pragma unroll
     for (int q = 0; q < 3; q++) mring[q] = mring[q + 1];
     mring[3] = msc * cm;
@@ -511,7 +537,7 @@ __global__ void __launch_bounds__(kRowMax, sizeof(R) == 4 ? LSMGPU_ADJ_ROW_CTAS 
       cv = load_coef<R, MODE>(a, 2, col + ok);
     }
     R G[6];
-    const R gz = coef_slots<R, EXACT, MODE>(win, uz, 2, mring[3], dt, iz, G);
+    const R gz = coef_slots_d<R, EXACT, MODE>(dw, uz, 2, mring[3], dt, iz, G);
     if (MODE == ADJ_ADV && a.gvel[2] && own && kk >= z0 && kk < zend) a.gvel[2][col + okk] += gz;
     const R Az = ring_step<R>(F, prevV, G);
     const int k = kk - 3;
@@ -566,12 +592,21 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? LSMGPU_ADJ_Y_CTAS
   int yk = wrapi(y0 - 3, ny);
   long long ok = py * (long long)(yk + fused::GY);
 
-  R win[7], mring[4], F[6];
+  // dw: the scaled differences along the march of the cell being linearised
+  // (slid one face per step), last: the newest value they reach
+  R dw[6], mring[4], F[6], last;
   R prevV = R(0);
+  {
+    R w[6];
 #pragma unroll
-  for (int q = 0; q < 6; q++) {
-    win[q + 1] = s[plane_add(ok, yk, q - 3, ny, py)];
-    F[q] = R(0);
+    for (int q = 0; q < 6; q++) {
+      w[q] = s[plane_add(ok, yk, q - 3, ny, py)];
+      F[q] = R(0);
+    }
+    dw[0] = R(0);
+#pragma unroll
+    for (int f = 0; f < 5; f++) dw[f + 1] = (w[f + 1] - w[f]) * iy;
+    last = w[5];
   }
 #pragma unroll
   for (int q = 0; q < 4; q++) mring[q] = R(0);
@@ -579,8 +614,9 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? LSMGPU_ADJ_Y_CTAS
   Coef<R> cv = load_coef<R, MODE>(a, 1, base + ok);
   for (int jj = y0 - 3; jj < yend + 3; jj++) {
 #pragma unroll
-    for (int q = 0; q < 6; q++) win[q] = win[q + 1];
-    win[6] = cs;
+    for (int f = 0; f < 5; f++) dw[f] = dw[f + 1];
+    dw[5] = (cs - last) * iy;
+    last = cs;
 #pragma unroll
     for (int q = 0; q < 3; q++) mring[q] = mring[q + 1];
     mring[3] = msc * cm;
@@ -595,7 +631,7 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? LSMGPU_ADJ_Y_CTAS
       cv = load_coef<R, MODE>(a, 1, base + ok);
     }
     R G[6];
-    const R gy = coef_slots<R, EXACT, MODE>(win, uy, 1, mring[3], dt, iy, G);
+    const R gy = coef_slots_d<R, EXACT, MODE>(dw, uy, 1, mring[3], dt, iy, G);
     if (MODE == ADJ_ADV && a.gvel[1] && jj >= y0 && jj < yend) a.gvel[1][base + ojj] += gy;
     const R Ay = ring_step<R>(F, prevV, G);
     if (jj - 3 < y0) continue;
