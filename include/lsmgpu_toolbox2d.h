@@ -991,6 +991,29 @@ void lsm2dcopyextrapolation_(
   const int *jhi_fb,
   const int *bdry_location_idx);
 
+/* 2D form: first-order delta function from sign changes (z terms use norm_phi_x and 1/dx, as the reference does).
+ * Replaces src/toolbox/lsm_calculus_toolbox2d.f.in:16; C declaration src/toolbox/lsm_calculus_toolbox2d.h:45.
+ */
+void lsm2ddeltafunctionorder1_(
+  const double *phi,
+  double *delta,
+  const int *ilo_gb,
+  const int *ihi_gb,
+  const int *jlo_gb,
+  const int *jhi_gb,
+  const double *norm_phi_x,
+  const double *norm_phi_y,
+  const int *ilo_grad_phi_gb,
+  const int *ihi_grad_phi_gb,
+  const int *jlo_grad_phi_gb,
+  const int *jhi_grad_phi_gb,
+  const int *ilo_fb,
+  const int *ihi_fb,
+  const int *jlo_fb,
+  const int *jhi_fb,
+  const double *dx,
+  const double *dy);
+
 /* 2D form: build the narrow band: level-0 list in sweep order, outer lists, BFS levels.
  * Replaces src/toolbox/lsm_localization2d.f:139; C declaration src/toolbox/lsm_localization2d.h:94.
  */

@@ -277,4 +277,36 @@ void lsm3dcomputedn_(R *Dn, BOXARG(d), const R *Dn_minus_one, BOXARG(m), const i
   call.finish();
 }
 
+// First-order delta function from sign changes along each axis
+// (calculus_toolbox3d.f.in:15-130).  The reference's z terms use norm_phi_x
+// and 1/dx (:103-115); kept, so the results are the reference's.
+void lsm3ddeltafunctionorder1_(const R *phi, R *delta, BOXARG(g), const R *norm_phi_x, const R *norm_phi_y,
+                               const R *norm_phi_z, BOXARG(n), const int *ilo_fb, const int *ihi_fb,
+                               const int *jlo_fb, const int *jhi_fb, const int *klo_fb, const int *khi_fb,
+                               const R *dx, const R *dy, const R *dz) {
+  Call call("lsm3ddeltafunctionorder1_");
+  const Box gb = BOXOF(g), nb = BOXOF(n), fb = mkbox(ilo_fb, ihi_fb, jlo_fb, jhi_fb, klo_fb, khi_fb);
+  if (!gb.contains(fb, 1, 1, 1) || !nb.contains(fb, 0, 0, 0)) call.fail("ghost box does not cover the stencil");
+  if (!call.ok() || fb.empty()) return;
+  View<const R> P = vin(call, phi, gb);
+  View<R> D = vio(call, delta, gb);
+  View<const R> NX = vin(call, norm_phi_x, nb), NY = vin(call, norm_phi_y, nb);
+  (void)norm_phi_z;
+  if (!call.ok()) return;
+  const R ox = R(1.0) / *dx, oy = R(1.0) / *dy;
+  for_box(fb, [=] __device__(int i, int j, int k) {
+    const R c = P(i, j, k);
+    auto side = [&](R nbr, R n, R o) {
+      if (nbr * c <= R(0)) return nbr * n * o / (nbr - c);
+      return R(0);
+    };
+    const R nx = NX(i, j, k), ny = NY(i, j, k);
+    const R xp = side(P(i + 1, j, k), nx, ox), xm = side(P(i - 1, j, k), nx, ox);
+    const R yp = side(P(i, j + 1, k), ny, oy), ym = side(P(i, j - 1, k), ny, oy);
+    const R zp = side(P(i, j, k + 1), nx, ox), zm = side(P(i, j, k - 1), nx, ox);
+    D(i, j, k) = fabs(xp) + fabs(xm) + fabs(yp) + fabs(ym) + fabs(zp) + fabs(zm);
+  });
+  call.finish();
+}
+
 }  // extern "C"

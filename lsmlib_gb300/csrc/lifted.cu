@@ -834,6 +834,16 @@ void lsm2dcopyextrapolation_(double *phi, const int *ilo_gb, const int *ihi_gb, 
   lsm3dcopyextrapolation_(phi, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, bdry_location_idx);
 }
 
+// src/toolbox/lsm_calculus_toolbox2d.f.in:16
+void lsm2ddeltafunctionorder1_(const double *phi, double *delta, const int *ilo_gb, const int *ihi_gb, const int *jlo_gb, const int *jhi_gb, const double *norm_phi_x, const double *norm_phi_y, const int *ilo_grad_phi_gb, const int *ihi_grad_phi_gb, const int *jlo_grad_phi_gb, const int *jhi_grad_phi_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const double *dx, const double *dy) {
+  Lift L_(2, "lsm2ddeltafunctionorder1_");
+  L_.box(ilo_gb, ihi_gb, jlo_gb, jhi_gb);
+  L_.box(ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb);
+  L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
+  if (!L_.ready()) return;
+  lsm3ddeltafunctionorder1_(phi, delta, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, norm_phi_x, norm_phi_y, L_.zero(), ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dx, dy, dx);
+}
+
 // src/toolbox/lsm_localization2d.f:139
 void lsm2ddeterminenarrowband_(const double *phi, const int *ilo_gb, const int *ihi_gb, const int *jlo_gb, const int *jhi_gb, unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, int *index_x, int *index_y, const int *nlo_index, const int *nhi_index, int *n_lo, int *n_hi, int *index_outer, const int *nlo_index_outer, const int *nhi_index_outer, int *nlo_outer_plus, int *nhi_outer_plus, int *nlo_outer_minus, int *nhi_outer_minus, const double *width, const double *width_inner, const int *level) {
   Lift L_(2, "lsm2ddeterminenarrowband_");

@@ -44,6 +44,7 @@ DESC = {
     "lsm3dlaplacianorder2_": ("deriv", "second-order Laplacian"),
     "lsm3dgradientmagnitude_": ("deriv", "|grad phi| with the reference's 1e-8 clamps"),
     "lsm3dcomputedn_": ("deriv", "n-th undivided difference along dir (1e10 outside the fill range)"),
+    "lsm3ddeltafunctionorder1_": ("deriv", "first-order delta function from sign changes (z terms use norm_phi_x and 1/dx, as the reference does)"),
     # RK
     "lsm3drk1step_": ("rk", "forward Euler step u_next = u + dt*L"),
     "lsm3dtvdrk2stage1_": ("rk", "TVD RK2 stage 1 (an Euler step)"),

@@ -61,6 +61,7 @@ REF_SOURCES = [
     "geometry/lsm_curvature2d_local.f.in",
     "toolbox/lsm_math_utils2d_local.f.in",
     "toolbox/lsm_localization2d.f",
+    "toolbox/lsm_calculus_toolbox2d.f.in",
 ]
 
 CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-std=gnu99",

@@ -147,3 +147,33 @@ void lsm3dcomputedn_(real_t *dn, A3(d), const real_t *dm, A3(m), const int *ilo_
     if (!in) dn[at(&D, i, j, k)] = 1.e10;
   }
 }
+
+/* lsm3dDeltaFunctionOrder1 (calculus_toolbox3d.f.in:15-130; its z terms use
+ * norm_phi_x and 1/dx, :103-115) */
+static real_t delta_side(real_t nbr, real_t c, real_t n, real_t o) {
+  if (nbr * c <= 0.0) {
+    real_t v = nbr * n * o;
+    return v / (nbr - c);
+  }
+  return 0.0;
+}
+void lsm3ddeltafunctionorder1_(const real_t *phi, real_t *delta, A3(g), const real_t *nx, const real_t *ny,
+                               const real_t *nz, A3(n), const int *ilo_fb, const int *ihi_fb, const int *jlo_fb,
+                               const int *jhi_fb, const int *klo_fb, const int *khi_fb, const real_t *dx,
+                               const real_t *dy, const real_t *dz) {
+  gbox G = B3(g), N = B3(n);
+  real_t ox = 1.0 / *dx, oy = 1.0 / *dy;
+  (void)nz;
+  (void)dz;
+  FOR_BOX(*ilo_fb, *ihi_fb, *jlo_fb, *jhi_fb, *klo_fb, *khi_fb) {
+    real_t c = phi[at(&G, i, j, k)];
+    long q = at(&N, i, j, k);
+    real_t xp = delta_side(phi[at(&G, i + 1, j, k)], c, nx[q], ox);
+    real_t xm = delta_side(phi[at(&G, i - 1, j, k)], c, nx[q], ox);
+    real_t yp = delta_side(phi[at(&G, i, j + 1, k)], c, ny[q], oy);
+    real_t ym = delta_side(phi[at(&G, i, j - 1, k)], c, ny[q], oy);
+    real_t zp = delta_side(phi[at(&G, i, j, k + 1)], c, nx[q], ox);
+    real_t zm = delta_side(phi[at(&G, i, j, k - 1)], c, nx[q], ox);
+    delta[at(&G, i, j, k)] = fabs(xp) + fabs(xm) + fabs(yp) + fabs(ym) + fabs(zp) + fabs(zm);
+  }
+}
