@@ -242,6 +242,27 @@ int lsmgpu_compute_stable_advection_dt_noalloc(
     const int *klo_ib, const int *khi_ib, const double *dx, const double *dy, const double *dz,
     const double *cfl_number);
 
+/* Fourth-order mean curvature over an index list, with the argument list of
+ * lsm3dComputeMeanCurvatureOrder4Local (src/geometry/lsm_curvature3d_local.f.in:285).
+ * That reference routine evaluates the Gaussian-curvature formula (numerator
+ * and |grad phi|^4 denominator, lsm_curvature3d_local.f.in:385-410), and its
+ * drop-in entry point lsm3dcomputemeancurvatureorder4local_ keeps that; this
+ * one evaluates the mean curvature of lsm3dComputeMeanCurvatureOrder4
+ * (lsm_curvature3d.f.in:253) on the listed cells.  The 2D drop-in
+ * lsm2dcomputemeancurvatureorder4local_ runs on it. */
+void lsmgpu_mean_curvature_order4_local(
+    double *kappa, const int *ilo_kappa_gb, const int *ihi_kappa_gb, const int *jlo_kappa_gb,
+    const int *jhi_kappa_gb, const int *klo_kappa_gb, const int *khi_kappa_gb, const double *phi,
+    const int *ilo_phi_gb, const int *ihi_phi_gb, const int *jlo_phi_gb, const int *jhi_phi_gb,
+    const int *klo_phi_gb, const int *khi_phi_gb, const double *phi_x, const double *phi_y,
+    const double *phi_z, const double *grad_phi_mag, const int *ilo_grad_phi_gb,
+    const int *ihi_grad_phi_gb, const int *jlo_grad_phi_gb, const int *jhi_grad_phi_gb,
+    const int *klo_grad_phi_gb, const int *khi_grad_phi_gb, const double *dx, const double *dy,
+    const double *dz, const int *index_x, const int *index_y, const int *index_z, const int *nlo_index,
+    const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb,
+    const int *jlo_nb_gb, const int *jhi_nb_gb, const int *klo_nb_gb, const int *khi_nb_gb,
+    const unsigned char *mark_fb);
+
 /* Library version string. */
 const char *lsmgpu_version(void);
 

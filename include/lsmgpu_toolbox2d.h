@@ -219,6 +219,76 @@ void lsm2daddconstprecomputedcurvtermtolserhs_(
   const int *jlo_rhs_fb,
   const int *jhi_rhs_fb);
 
+/* 2D form: rhs += b * kappa * |grad phi| on band cells.
+ * Replaces src/toolbox/lsm_level_set_evolution2d_local.f.in:408; C declaration src/toolbox/lsm_level_set_evolution2d_local.h:47.
+ */
+void lsm2daddconstprecomputedcurvtermtolserhslocal_(
+  double *lse_rhs,
+  const int *ilo_rhs_gb,
+  const int *ihi_rhs_gb,
+  const int *jlo_rhs_gb,
+  const int *jhi_rhs_gb,
+  const double *kappa,
+  const int *ilo_kappa_gb,
+  const int *ihi_kappa_gb,
+  const int *jlo_kappa_gb,
+  const int *jhi_kappa_gb,
+  const double *grad_phi_mag,
+  const int *ilo_phi_gb,
+  const int *ihi_phi_gb,
+  const int *jlo_phi_gb,
+  const int *jhi_phi_gb,
+  const double *b,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
+/* 2D form: external plus normal velocity term with the combined Godunov upwinding on band cells.
+ * Replaces src/toolbox/lsm_level_set_evolution2d_local.f.in:474; C declaration src/toolbox/lsm_level_set_evolution2d_local.h:414.
+ */
+void lsm2daddexternalandnormalveltermtolserhslocal_(
+  double *lse_rhs,
+  const int *ilo_rhs_gb,
+  const int *ihi_rhs_gb,
+  const int *jlo_rhs_gb,
+  const int *jhi_rhs_gb,
+  const double *phi_x_plus,
+  const double *phi_y_plus,
+  const int *ilo_grad_phi_plus_gb,
+  const int *ihi_grad_phi_plus_gb,
+  const int *jlo_grad_phi_plus_gb,
+  const int *jhi_grad_phi_plus_gb,
+  const double *phi_x_minus,
+  const double *phi_y_minus,
+  const int *ilo_grad_phi_minus_gb,
+  const int *ihi_grad_phi_minus_gb,
+  const int *jlo_grad_phi_minus_gb,
+  const int *jhi_grad_phi_minus_gb,
+  const double *vel_n,
+  const double *vel_x,
+  const double *vel_y,
+  const int *ilo_vel_gb,
+  const int *ihi_vel_gb,
+  const int *jlo_vel_gb,
+  const int *jhi_vel_gb,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
 /* 2D form: rhs -= Vn |grad phi| (Godunov), Vn a field.
  * Replaces src/toolbox/lsm_level_set_evolution2d.f.in:101; C declaration src/toolbox/lsm_level_set_evolution2d.h:139.
  */
@@ -582,6 +652,68 @@ void lsm2dcomputemeancurvatureorder2_(
  * Replaces src/geometry/lsm_curvature2d_local.f.in:15; C declaration src/geometry/lsm_curvature2d_local.h:64.
  */
 void lsm2dcomputemeancurvatureorder2local_(
+  double *kappa,
+  const int *ilo_kappa_gb,
+  const int *ihi_kappa_gb,
+  const int *jlo_kappa_gb,
+  const int *jhi_kappa_gb,
+  const double *phi,
+  const int *ilo_phi_gb,
+  const int *ihi_phi_gb,
+  const int *jlo_phi_gb,
+  const int *jhi_phi_gb,
+  const double *phi_x,
+  const double *phi_y,
+  const double *grad_phi_mag,
+  const int *ilo_grad_phi_gb,
+  const int *ihi_grad_phi_gb,
+  const int *jlo_grad_phi_gb,
+  const int *jhi_grad_phi_gb,
+  const double *dx,
+  const double *dy,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
+/* 2D form: fourth-order mean curvature (cross derivatives from the first derivatives).
+ * Replaces src/geometry/lsm_curvature2d.f.in:252; C declaration src/geometry/lsm_curvature2d.h:175.
+ */
+void lsm2dcomputemeancurvatureorder4_(
+  double *kappa,
+  const int *ilo_kappa_gb,
+  const int *ihi_kappa_gb,
+  const int *jlo_kappa_gb,
+  const int *jhi_kappa_gb,
+  const double *phi,
+  const int *ilo_phi_gb,
+  const int *ihi_phi_gb,
+  const int *jlo_phi_gb,
+  const int *jhi_phi_gb,
+  const double *phi_x,
+  const double *phi_y,
+  const double *grad_phi_mag,
+  const int *ilo_grad_phi_gb,
+  const int *ihi_grad_phi_gb,
+  const int *jlo_grad_phi_gb,
+  const int *jhi_grad_phi_gb,
+  const int *ilo_fb,
+  const int *ihi_fb,
+  const int *jlo_fb,
+  const int *jhi_fb,
+  const double *dx,
+  const double *dy);
+
+/* 2D form: fourth-order mean curvature on band cells.
+ * Replaces src/geometry/lsm_curvature2d_local.f.in:299; C declaration src/geometry/lsm_curvature2d_local.h:207.
+ */
+void lsm2dcomputemeancurvatureorder4local_(
   double *kappa,
   const int *ilo_kappa_gb,
   const int *ihi_kappa_gb,

@@ -66,8 +66,9 @@ int run(const char *name, R *kappa, const Box &kb, const R *phi, const Box &pb, 
   if (fb.empty()) return LSMGPU_OK;
   CurvArgs<R> a{};
   a.phi = view((const R *)call.in(phi, pb.size()), pb);
-  a.kappa = view(call.inout(kappa, kb.size()), kb);
-  a.mag = mag ? view(call.inout(mag, kb.size()), kb) : View<R>{};
+  // kappa and |grad phi| are written on every fill-box cell and nowhere else
+  a.kappa = view(call.out_region(kappa, kb, fb), kb);
+  a.mag = mag ? view(call.out_region(mag, kb, fb), kb) : View<R>{};
   if (!call.ok()) return lsmgpu_get_last_error(nullptr, 0);
   a.fb = fb;
   a.gx = R(0.5) / dx; a.gy = R(0.5) / dy; a.gz = R(0.5) / dz;

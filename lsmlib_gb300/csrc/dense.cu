@@ -295,6 +295,18 @@ __global__ void k_mean_curv2(View<R> kappa, View<const R> phi, View<const R> px,
   kappa(i, j, k) = out;
 }
 
+// Gaussian curvature (order 2, 4) and mean curvature (order 4): the order-2
+// form differences phi, the order-4 forms take phi_xy, phi_yz, phi_zx from the
+// first derivatives (curvature3d.f.in:136-508)
+template <int K>
+__global__ void k_curv_variant(View<R> kappa, View<const R> phi, View<const R> px, View<const R> py,
+                               View<const R> pz, View<const R> mag, Box fb, CurvFactors<R> F) {
+  LSMGPU_CELL_INDEX(fb, i, j, k);
+  const long long o = px.off(i, j, k);
+  kappa(i, j, k) = curvature_variant<R, K>(phi.p + phi.off(i, j, k), phi.s1, phi.s2, px.p + o, py.p + o, pz.p + o,
+                                           px.s1, px.s2, mag(i, j, k), F);
+}
+
 // ---- max reductions ---------------------------------------------------------------
 // An order-preserving map of doubles onto unsigned 64-bit keys, so a max over
 // cells becomes atomicMax on keys.  Max is exact and order independent, so the
@@ -401,6 +413,27 @@ using namespace lsmgpu;
 // ============================================================================
 // C entry points
 // ============================================================================
+template <int K>
+void curv_variant(const char *name, R *kappa, const Box &kb, const R *phi, const Box &phb, const R *phi_x,
+                  const R *phi_y, const R *phi_z, const R *grad_phi_mag, const Box &gb, const Box &fb, R dxv, R dyv,
+                  R dzv) {
+  Call call(name);
+  const int rp = (K == CURV_GAUSS2) ? 1 : 2, rg = (K == CURV_GAUSS2) ? 0 : 2;
+  if (!kb.contains(fb, 0, 0, 0) || !gb.contains(fb, rg, rg, rg) || !phb.contains(fb, rp, rp, rp))
+    call.fail("ghost box does not cover the stencil");
+  if (!call.ok() || fb.empty()) return;
+  View<R> KA = view(call.inout(kappa, kb.size()), kb);
+  View<const R> PH = view((const R *)call.in(phi, phb.size()), phb);
+  const long long ng = gb.size();
+  View<const R> X = view((const R *)call.in(phi_x, ng), gb), Y = view((const R *)call.in(phi_y, ng), gb),
+                Z = view((const R *)call.in(phi_z, ng), gb), G = view((const R *)call.in(grad_phi_mag, ng), gb);
+  if (!call.ok()) return;
+  Grid3 g3 = cover(fb);
+  LSMGPU_LAUNCH(k_curv_variant<K>, g3.grid, g3.block, 0, KA, PH, X, Y, Z, G, fb,
+                curvature_factors<R, K>(dxv, dyv, dzv));
+  call.finish();
+}
+
 extern "C" {
 
 #define PM_PARAMS                                                                        \
@@ -677,6 +710,21 @@ void lsm3dcomputemeancurvatureorder2_(R *kappa, BOXARG(k), const R *phi, BOXARG(
                 R(1.0) / dyv / dyv, R(1.0) / dzv / dzv, R(0.25) / dxv / dyv, R(0.25) / dxv / dzv,
                 R(0.25) / dyv / dzv);
   call.finish();
+}
+
+#define CURV_ARGS                                                                                         \
+  R *kappa, BOXARG(k), const R *phi, BOXARG(f), const R *phi_x, const R *phi_y, const R *phi_z,         \
+      const R *grad_phi_mag, BOXARG(g), BOXARG(kf), DXP
+#define CURV_PASS kappa, BOXOF(k), phi, BOXOF(f), phi_x, phi_y, phi_z, grad_phi_mag, BOXOF(g), BOXOF(kf), *dx, *dy, *dz
+
+void lsm3dcomputegaussiancurvatureorder2_(CURV_ARGS) {
+  curv_variant<CURV_GAUSS2>("lsm3dcomputegaussiancurvatureorder2_", CURV_PASS);
+}
+void lsm3dcomputemeancurvatureorder4_(CURV_ARGS) {
+  curv_variant<CURV_MEAN4>("lsm3dcomputemeancurvatureorder4_", CURV_PASS);
+}
+void lsm3dcomputegaussiancurvatureorder4_(CURV_ARGS) {
+  curv_variant<CURV_GAUSS4>("lsm3dcomputegaussiancurvatureorder4_", CURV_PASS);
 }
 
 // reductions ---------------------------------------------------------------------------

@@ -29,14 +29,6 @@ void for_box(const Box &b, F f) {
 View<const R> vin(Call &c, const R *p, const Box &b) { return view((const R *)c.in(p, b.size()), b); }
 View<R> vio(Call &c, R *p, const Box &b) { return view(c.inout(p, b.size()), b); }
 
-// one axis of the combined Godunov selection (level_set_evolution3d.f.in:630-649)
-__device__ __forceinline__ R ext_pick(R v, R vn, R p, R m) {
-  const R hp = v + vn * p, hm = v + vn * m;
-  if (hp > R(0)) return (hm > R(0)) ? m : -v / vn;
-  if (hm < R(0)) return p;
-  return (fabs(hp) > fabs(hm)) ? p : m;
-}
-
 // boundary conditions (boundary_conditions3d.f:46-639)
 enum { BC_LINEAR, BC_SIGNED, BC_COPY };
 
@@ -207,9 +199,9 @@ void lsm3daddexternalandnormalveltermtolserhs_(R *lse_rhs, BOXARG(r), const R *p
   if (!call.ok()) return;
   for_box(loop, [=] __device__(int i, int j, int k) {
     const R w = VN(i, j, k), ux = VX(i, j, k), uy = VY(i, j, k), uz = VZ(i, j, k);
-    const R gx = ext_pick(ux, w, XP(i, j, k), XM(i, j, k));
-    const R gy = ext_pick(uy, w, YP(i, j, k), YM(i, j, k));
-    const R gz = ext_pick(uz, w, ZP(i, j, k), ZM(i, j, k));
+    const R gx = ext_pick<R>(ux, w, XP(i, j, k), XM(i, j, k));
+    const R gy = ext_pick<R>(uy, w, YP(i, j, k), YM(i, j, k));
+    const R gz = ext_pick<R>(uz, w, ZP(i, j, k), ZM(i, j, k));
     const R n2 = gx * gx + gy * gy + gz * gz;
     if (fabs(w) >= Consts<R>::zero_tol && n2 >= Consts<R>::zero_tol)
       O(i, j, k) = O(i, j, k) - ux * gx - uy * gy - uz * gz - w * sqrt(n2);

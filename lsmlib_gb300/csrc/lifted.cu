@@ -530,6 +530,31 @@ void lsm2daddconstprecomputedcurvtermtolserhs_(double *lse_rhs, const int *ilo_r
   lsm3daddconstprecomputedcurvtermtolserhs_(lse_rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, kappa, ilo_kappa_gb, ihi_kappa_gb, jlo_kappa_gb, jhi_kappa_gb, &L_.k0, &L_.k0, grad_phi_mag, ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb, &L_.k0, &L_.k0, b, ilo_rhs_fb, ihi_rhs_fb, jlo_rhs_fb, jhi_rhs_fb, &L_.k0, &L_.k0);
 }
 
+// src/toolbox/lsm_level_set_evolution2d_local.f.in:408
+void lsm2daddconstprecomputedcurvtermtolserhslocal_(double *lse_rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *kappa, const int *ilo_kappa_gb, const int *ihi_kappa_gb, const int *jlo_kappa_gb, const int *jhi_kappa_gb, const double *grad_phi_mag, const int *ilo_phi_gb, const int *ihi_phi_gb, const int *jlo_phi_gb, const int *jhi_phi_gb, const double *b, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2daddconstprecomputedcurvtermtolserhslocal_");
+  L_.box(ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb);
+  L_.box(ilo_kappa_gb, ihi_kappa_gb, jlo_kappa_gb, jhi_kappa_gb);
+  L_.box(ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3daddconstprecomputedcurvtermtolserhslocal_(lse_rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, kappa, ilo_kappa_gb, ihi_kappa_gb, jlo_kappa_gb, jhi_kappa_gb, &L_.k0, &L_.k0, grad_phi_mag, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, b, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
+// src/toolbox/lsm_level_set_evolution2d_local.f.in:474
+void lsm2daddexternalandnormalveltermtolserhslocal_(double *lse_rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const double *vel_n, const double *vel_x, const double *vel_y, const int *ilo_vel_gb, const int *ihi_vel_gb, const int *jlo_vel_gb, const int *jhi_vel_gb, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2daddexternalandnormalveltermtolserhslocal_");
+  L_.box(ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb);
+  L_.box(ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb);
+  L_.box(ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb);
+  L_.box(ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3daddexternalandnormalveltermtolserhslocal_(lse_rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, vel_n, vel_x, vel_y, L_.zero(), ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb, &L_.k0, &L_.k0, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
 // src/toolbox/lsm_level_set_evolution2d.f.in:101
 void lsm2daddnormalveltermtolserhs_(double *lse_rhs, const int *ilo_lse_rhs_gb, const int *ihi_lse_rhs_gb, const int *jlo_lse_rhs_gb, const int *jhi_lse_rhs_gb, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const double *vel_n, const int *ilo_vel_gb, const int *ihi_vel_gb, const int *jlo_vel_gb, const int *jhi_vel_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb) {
   Lift L_(2, "lsm2daddnormalveltermtolserhs_");
@@ -690,6 +715,29 @@ void lsm2dcomputemeancurvatureorder2local_(double *kappa, const int *ilo_kappa_g
   L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
   if (!L_.ready()) return;
   lsm3dcomputemeancurvatureorder2local_(kappa, ilo_kappa_gb, ihi_kappa_gb, jlo_kappa_gb, jhi_kappa_gb, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, phi_x, phi_y, L_.zero(), grad_phi_mag, ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb, &L_.k0, &L_.k0, dx, dy, dx, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
+// src/geometry/lsm_curvature2d.f.in:252
+void lsm2dcomputemeancurvatureorder4_(double *kappa, const int *ilo_kappa_gb, const int *ihi_kappa_gb, const int *jlo_kappa_gb, const int *jhi_kappa_gb, const double *phi, const int *ilo_phi_gb, const int *ihi_phi_gb, const int *jlo_phi_gb, const int *jhi_phi_gb, const double *phi_x, const double *phi_y, const double *grad_phi_mag, const int *ilo_grad_phi_gb, const int *ihi_grad_phi_gb, const int *jlo_grad_phi_gb, const int *jhi_grad_phi_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const double *dx, const double *dy) {
+  Lift L_(2, "lsm2dcomputemeancurvatureorder4_");
+  L_.box(ilo_kappa_gb, ihi_kappa_gb, jlo_kappa_gb, jhi_kappa_gb);
+  L_.box(ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb);
+  L_.box(ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb);
+  L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
+  if (!L_.ready()) return;
+  lsm3dcomputemeancurvatureorder4_(kappa, ilo_kappa_gb, ihi_kappa_gb, jlo_kappa_gb, jhi_kappa_gb, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, phi_x, phi_y, L_.zero(), grad_phi_mag, ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dx, dy, dx);
+}
+
+// src/geometry/lsm_curvature2d_local.f.in:299
+void lsm2dcomputemeancurvatureorder4local_(double *kappa, const int *ilo_kappa_gb, const int *ihi_kappa_gb, const int *jlo_kappa_gb, const int *jhi_kappa_gb, const double *phi, const int *ilo_phi_gb, const int *ihi_phi_gb, const int *jlo_phi_gb, const int *jhi_phi_gb, const double *phi_x, const double *phi_y, const double *grad_phi_mag, const int *ilo_grad_phi_gb, const int *ihi_grad_phi_gb, const int *jlo_grad_phi_gb, const int *jhi_grad_phi_gb, const double *dx, const double *dy, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2dcomputemeancurvatureorder4local_");
+  L_.box(ilo_kappa_gb, ihi_kappa_gb, jlo_kappa_gb, jhi_kappa_gb);
+  L_.box(ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb);
+  L_.box(ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsmgpu_mean_curvature_order4_local(kappa, ilo_kappa_gb, ihi_kappa_gb, jlo_kappa_gb, jhi_kappa_gb, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, phi_x, phi_y, L_.zero(), grad_phi_mag, ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb, &L_.k0, &L_.k0, dx, dy, dx, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
 }
 
 // src/reinitialization/lsm_reinitialization2d.f.in:48

@@ -177,6 +177,37 @@ using namespace lsmgpu;
 #define NBARG const unsigned char *narrow_band, BOXARG(nb)
 #define DXP const R *dx, const R *dy, const R *dz
 
+// Gaussian curvature (order 2, 4) and curvature order 4 over lists
+// (curvature3d_local.f.in:151-574).  The reference's 3D MeanCurvatureOrder4
+// local routine evaluates the Gaussian-curvature formula (numerator and
+// |grad phi|^4 denominator, curvature3d_local.f.in:385-410); its entry point
+// keeps that, and lsmgpu_mean_curvature_order4_local evaluates the mean
+// curvature the dense routine and the 2D local routine compute.
+template <int K>
+void curv_variant_local(const char *name, R *kappa, const Box &kb, const R *phi, const Box &fb, const R *phi_x,
+                        const R *phi_y, const R *phi_z, const R *grad_phi_mag, const Box &gb, R dxv, R dyv, R dzv,
+                        const int *index_x, const int *index_y, const int *index_z, const int *nlo,
+                        const int *nhi, const unsigned char *narrow_band, const Box &nbb,
+                        const unsigned char *mark_fb) {
+  LocalCall lc(name);
+  List L = lc.list(index_x, index_y, index_z, *nlo, *nhi);
+  Gate g = lc.gate(narrow_band, nbb, *mark_fb);
+  View<R> KA = lc.inout(kappa, kb);
+  View<const R> F = lc.in(phi, fb);
+  View<const R> X = lc.in(phi_x, gb), Y = lc.in(phi_y, gb), Z = lc.in(phi_z, gb), G = lc.in(grad_phi_mag, gb);
+  const int rp = (K == CURV_GAUSS2) ? 1 : 2, rg = (K == CURV_GAUSS2) ? 0 : 2;
+  g.safe = isect(isect(kb, inner(gb, rg, rg, rg, rg, rg, rg)), inner(fb, rp, rp, rp, rp, rp, rp));
+  if (!lc.c.ok()) return;
+  const CurvFactors<R> cf = curvature_factors<R, K>(dxv, dyv, dzv);
+  for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) {
+    if (!g(i, j, k)) return;
+    const long long o = X.off(i, j, k);
+    KA(i, j, k) = curvature_variant<R, K>(F.p + F.off(i, j, k), F.s1, F.s2, X.p + o, Y.p + o, Z.p + o, X.s1, X.s2,
+                                          G(i, j, k), cf);
+  });
+  lc.c.finish();
+}
+
 extern "C" {
 
 void lsm3dcomputednlocal_(R *dn, BOXARG(d), const R *dm, BOXARG(m), const int *n, const int *dir, IDX3,
@@ -704,6 +735,74 @@ void lsm3dcomputemeancurvatureorder2local_(R *kappa, BOXARG(k), const R *phi, BO
     K(i, j, k) = (den < Consts<R>::zero_tol)
                      ? R(0)
                      : curv_numerator(xx, yy, zz, xy, xz, yz, X(i, j, k), Y(i, j, k), Z(i, j, k)) / den;
+  });
+  lc.c.finish();
+}
+
+#define CURVL_ARGS                                                                                        \
+  R *kappa, BOXARG(k), const R *phi, BOXARG(f), const R *phi_x, const R *phi_y, const R *phi_z,         \
+      const R *grad_phi_mag, BOXARG(g), DXP, LTAIL
+#define CURVL_PASS                                                                                        \
+  kappa, BOXOF(k), phi, BOXOF(f), phi_x, phi_y, phi_z, grad_phi_mag, BOXOF(g), *dx, *dy, *dz, index_x, index_y, \
+      index_z, nlo, nhi, narrow_band, BOXOF(nb), mark_fb
+
+void lsm3dcomputegaussiancurvatureorder2local_(CURVL_ARGS) {
+  curv_variant_local<CURV_GAUSS2>("lsm3dcomputegaussiancurvatureorder2local_", CURVL_PASS);
+}
+void lsm3dcomputemeancurvatureorder4local_(CURVL_ARGS) {
+  curv_variant_local<CURV_GAUSS4>("lsm3dcomputemeancurvatureorder4local_", CURVL_PASS);
+}
+void lsm3dcomputegaussiancurvatureorder4local_(CURVL_ARGS) {
+  curv_variant_local<CURV_GAUSS4>("lsm3dcomputegaussiancurvatureorder4local_", CURVL_PASS);
+}
+void lsmgpu_mean_curvature_order4_local(CURVL_ARGS) {
+  curv_variant_local<CURV_MEAN4>("lsmgpu_mean_curvature_order4_local", CURVL_PASS);
+}
+
+// rhs += b * kappa * |grad phi| on listed cells
+// (level_set_evolution3d_local.f.in:530-607)
+void lsm3daddconstprecomputedcurvtermtolserhslocal_(R *lse_rhs, BOXARG(r), const R *kappa, BOXARG(k),
+                                                    const R *grad_phi_mag, BOXARG(g), const R *b, LTAIL) {
+  LSETUP("lsm3daddconstprecomputedcurvtermtolserhslocal_")
+  View<R> O = lc.inout(lse_rhs, BOXOF(r));
+  View<const R> KA = lc.in(kappa, BOXOF(k)), G = lc.in(grad_phi_mag, BOXOF(g));
+  g.safe = isect(BOXOF(r), isect(BOXOF(k), BOXOF(g)));
+  if (!lc.c.ok()) return;
+  const R bb = *b;
+  for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) {
+    if (!g(i, j, k)) return;
+    O(i, j, k) = O(i, j, k) + bb * KA(i, j, k) * G(i, j, k);
+  });
+  lc.c.finish();
+}
+
+// rhs -= u . grad(phi) + Vn |grad phi| with the combined Godunov selection on
+// listed cells (level_set_evolution3d_local.f.in:612-812)
+void lsm3daddexternalandnormalveltermtolserhslocal_(R *lse_rhs, BOXARG(r), const R *phi_x_plus,
+                                                    const R *phi_y_plus, const R *phi_z_plus, BOXARG(p),
+                                                    const R *phi_x_minus, const R *phi_y_minus,
+                                                    const R *phi_z_minus, BOXARG(m), const R *vel_n,
+                                                    const R *vel_x, const R *vel_y, const R *vel_z, BOXARG(v),
+                                                    LTAIL) {
+  LSETUP("lsm3daddexternalandnormalveltermtolserhslocal_")
+  Box pb = BOXOF(p), mb = BOXOF(m), vb = BOXOF(v);
+  View<R> O = lc.inout(lse_rhs, BOXOF(r));
+  View<const R> XP = lc.in(phi_x_plus, pb), YP = lc.in(phi_y_plus, pb), ZP = lc.in(phi_z_plus, pb);
+  View<const R> XM = lc.in(phi_x_minus, mb), YM = lc.in(phi_y_minus, mb), ZM = lc.in(phi_z_minus, mb);
+  View<const R> VN = lc.in(vel_n, vb), VX = lc.in(vel_x, vb), VY = lc.in(vel_y, vb), VZ = lc.in(vel_z, vb);
+  g.safe = isect(isect(BOXOF(r), vb), isect(pb, mb));
+  if (!lc.c.ok()) return;
+  for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) {
+    if (!g(i, j, k)) return;
+    const R w = VN(i, j, k), ux = VX(i, j, k), uy = VY(i, j, k), uz = VZ(i, j, k);
+    const R gx = ext_pick<R>(ux, w, XP(i, j, k), XM(i, j, k));
+    const R gy = ext_pick<R>(uy, w, YP(i, j, k), YM(i, j, k));
+    const R gz = ext_pick<R>(uz, w, ZP(i, j, k), ZM(i, j, k));
+    const R n2 = gx * gx + gy * gy + gz * gz;
+    if (fabs(w) >= Consts<R>::zero_tol && n2 >= Consts<R>::zero_tol)
+      O(i, j, k) = O(i, j, k) - ux * gx - uy * gy - uz * gz - w * sqrt(n2);
+    else
+      O(i, j, k) = O(i, j, k) - ux * gx - uy * gy - uz * gz;
   });
   lc.c.finish();
 }

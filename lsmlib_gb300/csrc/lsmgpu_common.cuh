@@ -149,6 +149,12 @@ class Call {
   template <class T> T *in(const T *p, long long n) { return (T *)stage(p, n * (long long)sizeof(T), true, false); }
   template <class T> T *inout(T *p, long long n) { return (T *)stage(p, n * (long long)sizeof(T), true, true); }
   template <class T> T *out(T *p, long long n) { return (T *)stage(p, n * (long long)sizeof(T), false, true); }
+  // out_region(): written by the kernel over `region` only (a sub-box of the
+  // array's ghost box gb); a host-resident array is neither copied in nor
+  // copied back outside `region`, so its other cells keep their values
+  template <class T> T *out_region(T *p, const Box &gb, const Box &region) {
+    return (T *)stage_region(p, (long long)sizeof(T), gb, region);
+  }
   // Device-only temporary memory for this call.
   template <class T> T *temp(long long n) { return (T *)arena_alloc(n * (long long)sizeof(T)); }
   // Scalar output written by a kernel into device memory and copied to *dst
@@ -162,11 +168,14 @@ class Call {
 
  private:
   void *stage(const void *p, long long bytes, bool copy_in, bool copy_out);
+  void *stage_region(void *p, long long elem, const Box &gb, const Box &region);
   void *scalar(void *dst, size_t bytes);
   void *arena_alloc(long long bytes);
   const char *name_;
   bool ok_ = true, host_staged_ = false, finished_ = false, need_sync_ = false;
-  struct Back { void *host; void *dev; long long bytes; };
+  // bytes > 0: one linear copy; region.size() > 0 with bytes == 0: a 3D copy
+  // of `region` out of arrays laid out over `gb` with `elem`-byte elements
+  struct Back { void *host; void *dev; long long bytes; long long elem; Box gb, region; };
   Back backs_[64];
   int nback_ = 0;
   long long arena_mark_ = 0;

@@ -147,8 +147,36 @@ void *Call::stage(const void *p, long long bytes, bool copy_in, bool copy_out) {
       ok_ = false;
       return nullptr;
     }
-    backs_[nback_++] = {(void *)p, d, bytes};
+    backs_[nback_++] = {(void *)p, d, bytes, 0, Box{}, Box{}};
   }
+  return d;
+}
+
+void *Call::stage_region(void *p, long long elem, const Box &gb, const Box &region) {
+  if (!ok_) return nullptr;
+  if (p == nullptr) {
+    set_error(LSMGPU_ERR_ARGUMENT, "%s: null array pointer", name_);
+    ok_ = false;
+    return nullptr;
+  }
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    attr.type = cudaMemoryTypeUnregistered;
+  }
+  if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) return p;
+  host_staged_ = true;
+  need_sync_ = true;
+  void *d = arena_alloc(gb.size() * elem);
+  if (!d) return nullptr;
+  const Box r = isect(gb, region);
+  if (r.empty()) return d;
+  if (nback_ >= 64) {
+    set_error(LSMGPU_ERR_ARGUMENT, "%s: too many staged outputs", name_);
+    ok_ = false;
+    return nullptr;
+  }
+  backs_[nback_++] = {p, d, 0, elem, gb, r};
   return d;
 }
 
@@ -168,7 +196,7 @@ void *Call::scalar(void *dst, size_t bytes) {
     attr.type = cudaMemoryTypeUnregistered;
   }
   if (!(attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged)) need_sync_ = true;
-  backs_[nback_++] = {dst, d, (long long)bytes};
+  backs_[nback_++] = {dst, d, (long long)bytes, 0, Box{}, Box{}};
   return d;
 }
 
@@ -184,9 +212,26 @@ void Call::finish() {
   }
   if (ok_) {
     for (int b = 0; b < nback_; b++) {
-      if (backs_[b].bytes <= 0) continue;
-      if (!cuda_ok(cudaMemcpyAsync(backs_[b].host, backs_[b].dev, (size_t)backs_[b].bytes,
-                                   cudaMemcpyDefault, stream()),
+      const Back &k = backs_[b];
+      if (k.bytes <= 0 && k.elem > 0) {
+        // the region's rows, one 3D copy (x extent in bytes, y rows, z planes)
+        cudaMemcpy3DParms m = {};
+        const size_t pitch = (size_t)(k.gb.n(0) * k.elem);
+        m.srcPtr = make_cudaPitchedPtr(k.dev, pitch, pitch, (size_t)k.gb.n(1));
+        m.dstPtr = make_cudaPitchedPtr(k.host, pitch, pitch, (size_t)k.gb.n(1));
+        m.srcPos = m.dstPos = make_cudaPos((size_t)((k.region.lo[0] - k.gb.lo[0]) * k.elem),
+                                           (size_t)(k.region.lo[1] - k.gb.lo[1]),
+                                           (size_t)(k.region.lo[2] - k.gb.lo[2]));
+        m.extent = make_cudaExtent((size_t)(k.region.n(0) * k.elem), (size_t)k.region.n(1), (size_t)k.region.n(2));
+        m.kind = cudaMemcpyDefault;
+        if (!cuda_ok(cudaMemcpy3DAsync(&m, stream()), "cudaMemcpy3DAsync(D2H region)")) {
+          ok_ = false;
+          break;
+        }
+        continue;
+      }
+      if (k.bytes <= 0) continue;
+      if (!cuda_ok(cudaMemcpyAsync(k.host, k.dev, (size_t)k.bytes, cudaMemcpyDefault, stream()),
                    "cudaMemcpyAsync(D2H)")) {
         ok_ = false;
         break;

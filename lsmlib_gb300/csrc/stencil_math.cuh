@@ -208,4 +208,78 @@ __device__ __forceinline__ R curv_numerator(R xx, R yy, R zz, R xy, R xz, R yz, 
          yy * z * z + zz * y * y - R(2) * yz * y * z;
 }
 
+// one axis of the combined external + normal velocity Godunov selection
+// (level_set_evolution3d.f.in:630-649, level_set_evolution3d_local.f.in:714-787)
+template <class R>
+__device__ __forceinline__ R ext_pick(R v, R vn, R p, R m) {
+  const R hp = v + vn * p, hm = v + vn * m;
+  if (hp > R(0)) return (hm > R(0)) ? m : -v / vn;
+  if (hm < R(0)) return p;
+  return (fabs(hp) > fabs(hm)) ? p : m;
+}
+
+// ---- curvature variants (curvature3d.f.in:136-508, curvature3d_local.f.in:151-574)
+enum CurvKind { CURV_GAUSS2 = 1, CURV_MEAN4 = 2, CURV_GAUSS4 = 3 };
+
+// order 2: f = {1/dx^2, 1/dy^2, 1/dz^2, 1/(4 dx dy), 1/(4 dx dz), 1/(4 dy dz)};
+// order 4: f = {1/(12 dx^2), 1/(12 dy^2), 1/(12 dz^2), 1/(12 dx), 1/(12 dy), 1/(12 dz)}
+template <class R>
+struct CurvFactors {
+  R f[6];
+};
+
+// kappa at cell (i, j, k): c points at phi there (strides sy, sz), x, y, z
+// and gm the first derivatives and |grad phi| there; for order 4 the cross
+// derivatives come from the first derivatives (phi_x along y, phi_y along z,
+// phi_z along x) through px, py, pz at the cell with strides pys, pzs.
+template <class R, int K>
+__device__ __forceinline__ R curvature_variant(const R *c, long long sy, long long sz, const R *px, const R *py,
+                                               const R *pz, long long pys, long long pzs, R gm,
+                                               const CurvFactors<R> &F) {
+  R xx, yy, zz, xy, xz, yz;
+  const R x = px[0], y = py[0], z = pz[0];
+  if (K == CURV_GAUSS2) {
+    xx = (c[1] - R(2.0) * c[0] + c[-1]) * F.f[0];
+    yy = (c[sy] - R(2.0) * c[0] + c[-sy]) * F.f[1];
+    zz = (c[sz] - R(2.0) * c[0] + c[-sz]) * F.f[2];
+    xy = (c[1 + sy] - c[1 - sy] - c[-1 + sy] + c[-1 - sy]) * F.f[3];
+    xz = (c[1 + sz] - c[1 - sz] - c[-1 + sz] + c[-1 - sz]) * F.f[4];
+    yz = (c[sy + sz] - c[sy - sz] - c[-sy + sz] + c[-sy - sz]) * F.f[5];
+  } else {
+    const R sixteen = R(16), thirty = R(30), eight = R(8);
+    xx = (-c[2] + sixteen * c[1] - thirty * c[0] - c[-2] + sixteen * c[-1]) * F.f[0];
+    yy = (-c[2 * sy] + sixteen * c[sy] - thirty * c[0] - c[-2 * sy] + sixteen * c[-sy]) * F.f[1];
+    zz = (-c[2 * sz] + sixteen * c[sz] - thirty * c[0] - c[-2 * sz] + sixteen * c[-sz]) * F.f[2];
+    xy = (-px[2 * pys] + eight * px[pys] + px[-2 * pys] - eight * px[-pys]) * F.f[4];  // phi_x along y
+    yz = (-py[2 * pzs] + eight * py[pzs] + py[-2 * pzs] - eight * py[-pzs]) * F.f[5];  // phi_y along z
+    xz = (-pz[2] + eight * pz[1] + pz[-2] - eight * pz[-1]) * F.f[3];                  // phi_z along x
+  }
+  if (K == CURV_MEAN4) {
+    const R den = gm * gm * gm;
+    if (den < Consts<R>::zero_tol) return R(0);
+    const R t = xx * y * y + yy * x * x - R(2) * xy * x * y + xx * z * z + zz * x * x - R(2) * xz * x * z +
+                yy * z * z + zz * y * y - R(2) * yz * y * z;
+    return t / den;
+  }
+  const R den = gm * gm * gm * gm;
+  if (den < Consts<R>::zero_tol) return R(0);
+  const R t = x * x * (yy * zz - yz * yz) + y * y * (xx * zz - xz * xz) + z * z * (xx * yy - xy * xy) +
+              R(2) * (x * y * (xz * yz - xy * zz) + y * z * (xy * xz - yz * xx) + x * z * (xy * yz - xz * yy));
+  return t / den;
+}
+
+template <class R, int K>
+inline CurvFactors<R> curvature_factors(R dx, R dy, R dz) {
+  CurvFactors<R> F;
+  if (K == CURV_GAUSS2) {
+    F.f[0] = R(1.0) / dx / dx; F.f[1] = R(1.0) / dy / dy; F.f[2] = R(1.0) / dz / dz;
+    F.f[3] = R(0.25) / dx / dy; F.f[4] = R(0.25) / dx / dz; F.f[5] = R(0.25) / dy / dz;
+  } else {
+    const R c = R(0.0833333333333333333333);
+    F.f[0] = c / dx / dx; F.f[1] = c / dy / dy; F.f[2] = c / dz / dz;
+    F.f[3] = c / dx; F.f[4] = c / dy; F.f[5] = c / dz;
+  }
+  return F;
+}
+
 }  // namespace lsmgpu

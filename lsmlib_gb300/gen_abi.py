@@ -61,6 +61,9 @@ DESC = {
     # reinit / curvature
     "lsm3dcomputereinitializationeqnrhs_": ("reinit", "reinitialization RHS sgn(phi)(1 - |grad phi|), Godunov"),
     "lsm3dcomputemeancurvatureorder2_": ("geom", "second-order mean curvature"),
+    "lsm3dcomputegaussiancurvatureorder2_": ("geom", "second-order Gaussian curvature"),
+    "lsm3dcomputemeancurvatureorder4_": ("geom", "fourth-order mean curvature (cross derivatives from the first derivatives)"),
+    "lsm3dcomputegaussiancurvatureorder4_": ("geom", "fourth-order Gaussian curvature (cross derivatives from the first derivatives)"),
     # reductions
     "lsm3dmaxnormdiff_": ("red", "max |field1 - field2| over an index box"),
     "lsm3dcomputestableadvectiondt_": ("red", "CFL-stable dt for advection"),
@@ -133,6 +136,11 @@ DESC = {
     "lsm3daddconstcurvtermtolserhslocal_": ("local", "curvature term on band cells"),
     "lsm3dcomputereinitializationeqnrhslocal_": ("local", "reinitialization RHS on band cells"),
     "lsm3dcomputemeancurvatureorder2local_": ("local", "second-order mean curvature on band cells"),
+    "lsm3dcomputegaussiancurvatureorder2local_": ("local", "second-order Gaussian curvature on band cells"),
+    "lsm3dcomputemeancurvatureorder4local_": ("local", "fourth-order curvature on band cells: the Gaussian-curvature formula, as the reference routine evaluates it (lsmgpu_mean_curvature_order4_local gives the mean curvature)"),
+    "lsm3dcomputegaussiancurvatureorder4local_": ("local", "fourth-order Gaussian curvature on band cells"),
+    "lsm3daddconstprecomputedcurvtermtolserhslocal_": ("local", "rhs += b * kappa * |grad phi| on band cells"),
+    "lsm3daddexternalandnormalveltermtolserhslocal_": ("local", "external plus normal velocity term with the combined Godunov upwinding on band cells"),
     "lsm3dmaxnormdifflocal_": ("local", "max |field1 - field2| over band cells (starts at 0)"),
     "lsm3dcomputestableadvectiondtlocal_": ("local", "CFL-stable advection dt over band cells"),
     "lsm3dcomputestablenormalveldtlocal_": ("local", "CFL-stable normal-velocity dt over band cells"),
@@ -231,6 +239,13 @@ BOUND = re.compile(r"^(ilo|ihi|jlo|jhi|klo|khi)_")
 NOT_LIFTED = {"lsm1dcomputestablenormalveldt_", "lsm1dcomputestablenormalveldtcontrolvolume_",
               "lsm2daddexternalandnormalveltermtolserhs_", "lsm1dsignedlinearextrapolation_"}
 
+# 2D / 1D routines lifted onto a library entry point other than the 3D
+# routine of the same name, which has the same argument list: the 3D
+# MeanCurvatureOrder4 local routine evaluates the Gaussian-curvature formula
+# (curvature3d_local.f.in:385-410), the 2D one the mean curvature
+LIFT_VIA = {"lsm2dcomputemeancurvatureorder4local_": ("lsmgpu_mean_curvature_order4_local",
+                                                      "fourth-order mean curvature on band cells")}
+
 # 3D routines whose dz (and dy) multiply a cell volume: lifted with 1 there
 VOLUME_FACTOR = re.compile(r"volumeintegral|volumeregion|surfaceintegral|surfacearea")
 
@@ -303,7 +318,7 @@ def lift_map(sym2, dims, abi3, sigs):
                 regs.append("L_.box(%s, %s);" % (a2[q][0], a2[q + 1][0]))
         if name.startswith("nlo_index") and q + 1 < len(a2) and a2[q + 1][0].startswith("nhi_index"):
             regs.append("L_.list(%s, %s);" % (name, a2[q + 1][0]))
-    return {"sym3": sym3, "args": out, "regs": regs}
+    return {"sym3": sym3, "call": LIFT_VIA.get(sym2, (sym3,))[0], "args": out, "regs": regs}
 
 
 def write_lifted(abi, lifted):
@@ -332,7 +347,7 @@ def write_lifted(abi, lifted):
         for r in mp["regs"]:
             lines.append("  " + r)
         lines.append("  if (!L_.ready()) return;")
-        lines.append("  %s(%s);" % (mp["sym3"], ", ".join(mp["args"])))
+        lines.append("  %s(%s);" % (mp["call"], ", ".join(mp["args"])))
         lines.append("}")
         lines.append("")
     lines += ['}  // extern "C"', ""]
@@ -388,6 +403,12 @@ def main():
             abi[s] = {"ref": f"{os.path.relpath(src, REF)}:{line}",
                       "header": f"{hpath}:{hline}" if hpath else None, "args": sg["args"]}
         groups.setdefault(DESC[s][0], []).append(s)
+    # library entry points with a 3D routine's argument list (declared in
+    # include/lsmgpu.h, not in the toolbox header)
+    for target, _ in LIFT_VIA.values():
+        sym3 = next(s3 for s2, (t, _) in LIFT_VIA.items() if t == target for s3 in ["lsm3d" + s2[5:]])
+        abi[target] = {"ref": abi[sym3]["ref"], "header": "include/lsmgpu.h", "args": abi[sym3]["args"],
+                       "extension": "lsmgpu entry point with the argument list of the routine in ref"}
     # 2D and 1D routines lifted onto the 3D ones
     lifted, desc2 = {}, {}
     for s in sorted(sigs):
@@ -401,9 +422,9 @@ def main():
         src, line = sg["src"].split(":")
         hpath, hline = header_line(s)
         abi[s] = {"ref": f"{os.path.relpath(src, REF)}:{line}",
-                  "header": f"{hpath}:{hline}" if hpath else None, "args": sg["args"], "lifted_from": mp["sym3"]}
+                  "header": f"{hpath}:{hline}" if hpath else None, "args": sg["args"], "lifted_from": mp["call"]}
         lifted[s] = (dims, mp)
-        desc2[s] = "%dD form: %s" % (dims, DESC[mp["sym3"]][1])
+        desc2[s] = "%dD form: %s" % (dims, LIFT_VIA[s][1] if s in LIFT_VIA else DESC[mp["sym3"]][1])
     write_lifted(abi, lifted)
     for dims in (2, 1):
         syms = [s for s in lifted if lifted[s][0] == dims]
