@@ -263,6 +263,67 @@ void lsmgpu_mean_curvature_order4_local(
     const int *jlo_nb_gb, const int *jhi_nb_gb, const int *klo_nb_gb, const int *khi_nb_gb,
     const unsigned char *mark_fb);
 
+/* The 2D reference routines' formulas on 3D arrays, with the argument lists
+ * of the 3D routines named; the 2D drop-in entry points run on them.
+ *
+ * lsmgpu_orthogonalization_rhs_unit_sgn_smoothing(_local): the
+ * orthogonalization RHS of lsm3dComputeOrthogonalizationEqnRHS(LOCAL)
+ * (src/reinitialization/lsm_reinitialization3d.f.in:296,
+ * lsm_reinitialization3d_local.f.in:326) with sgn(psi) = psi /
+ * sqrt(psi^2 + max(dx)^2), as lsm2dComputeOrthogonalizationEqnRHS smooths it
+ * (lsm_reinitialization2d.f.in:360); the 3D routines use
+ * max(dx)^2 |grad psi|^2.
+ *
+ * lsmgpu_distance_for_subcell_fix_full_central: the subcell-fix distance of
+ * lsm3dComputeDistanceForSubcellFix (lsm_reinitialization3d.f.in:477) in
+ * the form of lsm2dComputeDistanceForSubcellFix (lsm_reinitialization2d.f.in:392):
+ * sign changes by negative products phi0(neighbour) phi0(cell), the full
+ * central difference in delta, and 2 phi0 / delta. */
+void lsmgpu_orthogonalization_rhs_unit_sgn_smoothing(
+    double *ortho_rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb,
+    const int *jhi_rhs_gb, const int *klo_rhs_gb, const int *khi_rhs_gb, const double *phi_x_plus,
+    const double *phi_y_plus, const double *phi_z_plus, const int *ilo_grad_phi_plus_gb,
+    const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb,
+    const int *klo_grad_phi_plus_gb, const int *khi_grad_phi_plus_gb, const double *phi_x_minus,
+    const double *phi_y_minus, const double *phi_z_minus, const int *ilo_grad_phi_minus_gb,
+    const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb,
+    const int *klo_grad_phi_minus_gb, const int *khi_grad_phi_minus_gb, const double *psi,
+    const int *ilo_psi_gb, const int *ihi_psi_gb, const int *jlo_psi_gb, const int *jhi_psi_gb,
+    const int *klo_psi_gb, const int *khi_psi_gb, const double *psi_x_plus, const double *psi_y_plus,
+    const double *psi_z_plus, const int *ilo_grad_psi_plus_gb, const int *ihi_grad_psi_plus_gb,
+    const int *jlo_grad_psi_plus_gb, const int *jhi_grad_psi_plus_gb, const int *klo_grad_psi_plus_gb,
+    const int *khi_grad_psi_plus_gb, const double *psi_x_minus, const double *psi_y_minus,
+    const double *psi_z_minus, const int *ilo_grad_psi_minus_gb, const int *ihi_grad_psi_minus_gb,
+    const int *jlo_grad_psi_minus_gb, const int *jhi_grad_psi_minus_gb, const int *klo_grad_psi_minus_gb,
+    const int *khi_grad_psi_minus_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb,
+    const int *jhi_fb, const int *klo_fb, const int *khi_fb, const double *dx, const double *dy,
+    const double *dz);
+void lsmgpu_orthogonalization_rhs_unit_sgn_smoothing_local(
+    double *ortho_rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb,
+    const int *jhi_rhs_gb, const int *klo_rhs_gb, const int *khi_rhs_gb, const double *phi_x_plus,
+    const double *phi_y_plus, const double *phi_z_plus, const int *ilo_grad_phi_plus_gb,
+    const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb,
+    const int *klo_grad_phi_plus_gb, const int *khi_grad_phi_plus_gb, const double *phi_x_minus,
+    const double *phi_y_minus, const double *phi_z_minus, const int *ilo_grad_phi_minus_gb,
+    const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb,
+    const int *klo_grad_phi_minus_gb, const int *khi_grad_phi_minus_gb, const double *psi,
+    const int *ilo_psi_gb, const int *ihi_psi_gb, const int *jlo_psi_gb, const int *jhi_psi_gb,
+    const int *klo_psi_gb, const int *khi_psi_gb, const double *psi_x_plus, const double *psi_y_plus,
+    const double *psi_z_plus, const int *ilo_grad_psi_plus_gb, const int *ihi_grad_psi_plus_gb,
+    const int *jlo_grad_psi_plus_gb, const int *jhi_grad_psi_plus_gb, const int *klo_grad_psi_plus_gb,
+    const int *khi_grad_psi_plus_gb, const double *psi_x_minus, const double *psi_y_minus,
+    const double *psi_z_minus, const int *ilo_grad_psi_minus_gb, const int *ihi_grad_psi_minus_gb,
+    const int *jlo_grad_psi_minus_gb, const int *jhi_grad_psi_minus_gb, const int *klo_grad_psi_minus_gb,
+    const int *khi_grad_psi_minus_gb, const double *dx, const double *dy, const double *dz,
+    const int *index_x, const int *index_y, const int *index_z, const int *nlo_index, const int *nhi_index,
+    const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb,
+    const int *jhi_nb_gb, const int *klo_nb_gb, const int *khi_nb_gb, const unsigned char *mark_fb);
+void lsmgpu_distance_for_subcell_fix_full_central(
+    double *distance0, const double *phi0, const int *ilo_phi0_gb, const int *ihi_phi0_gb,
+    const int *jlo_phi0_gb, const int *jhi_phi0_gb, const int *klo_phi0_gb, const int *khi_phi0_gb,
+    const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const int *klo_fb,
+    const int *khi_fb, const double *dx, const double *dy, const double *dz);
+
 /* Library version string. */
 const char *lsmgpu_version(void);
 

@@ -572,6 +572,23 @@ void lsm2dcomputeavegradphilocal_(
   const int *jhi_nb_gb,
   const unsigned char *mark_fb);
 
+/* 2D form: distance estimate for the subcell fix (2 phi0 / delta).
+ * Replaces src/reinitialization/lsm_reinitialization2d.f.in:392; C declaration src/reinitialization/lsm_reinitialization2d.h:216.
+ */
+void lsm2dcomputedistanceforsubcellfix_(
+  double *distance0,
+  const double *phi0,
+  const int *ilo_phi0_gb,
+  const int *ihi_phi0_gb,
+  const int *jlo_phi0_gb,
+  const int *jhi_phi0_gb,
+  const int *ilo_fb,
+  const int *ihi_fb,
+  const int *jlo_fb,
+  const int *jhi_fb,
+  const double *dx,
+  const double *dy);
+
 /* 2D form: n-th undivided difference along dir (1e10 outside the fill range).
  * Replaces src/toolbox/lsm_spatial_derivatives2d.f.in:49.
  */
@@ -744,6 +761,102 @@ void lsm2dcomputemeancurvatureorder4local_(
   const int *jhi_nb_gb,
   const unsigned char *mark_fb);
 
+/* 2D form: orthogonalization RHS (sgn(psi) smoothed with max(dx)^2).
+ * Replaces src/reinitialization/lsm_reinitialization2d.f.in:255; C declaration src/reinitialization/lsm_reinitialization2d.h:149.
+ */
+void lsm2dcomputeorthogonalizationeqnrhs_(
+  double *ortho_rhs,
+  const int *ilo_rhs_gb,
+  const int *ihi_rhs_gb,
+  const int *jlo_rhs_gb,
+  const int *jhi_rhs_gb,
+  const double *phi_x_plus,
+  const double *phi_y_plus,
+  const int *ilo_grad_phi_plus_gb,
+  const int *ihi_grad_phi_plus_gb,
+  const int *jlo_grad_phi_plus_gb,
+  const int *jhi_grad_phi_plus_gb,
+  const double *phi_x_minus,
+  const double *phi_y_minus,
+  const int *ilo_grad_phi_minus_gb,
+  const int *ihi_grad_phi_minus_gb,
+  const int *jlo_grad_phi_minus_gb,
+  const int *jhi_grad_phi_minus_gb,
+  const double *psi,
+  const int *ilo_psi_gb,
+  const int *ihi_psi_gb,
+  const int *jlo_psi_gb,
+  const int *jhi_psi_gb,
+  const double *psi_x_plus,
+  const double *psi_y_plus,
+  const int *ilo_grad_psi_plus_gb,
+  const int *ihi_grad_psi_plus_gb,
+  const int *jlo_grad_psi_plus_gb,
+  const int *jhi_grad_psi_plus_gb,
+  const double *psi_x_minus,
+  const double *psi_y_minus,
+  const int *ilo_grad_psi_minus_gb,
+  const int *ihi_grad_psi_minus_gb,
+  const int *jlo_grad_psi_minus_gb,
+  const int *jhi_grad_psi_minus_gb,
+  const int *ilo_fb,
+  const int *ihi_fb,
+  const int *jlo_fb,
+  const int *jhi_fb,
+  const double *dx,
+  const double *dy);
+
+/* 2D form: orthogonalization RHS on band cells (sgn(psi) smoothed with max(dx)^2).
+ * Replaces src/reinitialization/lsm_reinitialization2d_local.f.in:284; C declaration src/reinitialization/lsm_reinitialization2d_local.h:84.
+ */
+void lsm2dcomputeorthogonalizationeqnrhslocal_(
+  double *ortho_rhs,
+  const int *ilo_rhs_gb,
+  const int *ihi_rhs_gb,
+  const int *jlo_rhs_gb,
+  const int *jhi_rhs_gb,
+  const double *phi_x_plus,
+  const double *phi_y_plus,
+  const int *ilo_grad_phi_plus_gb,
+  const int *ihi_grad_phi_plus_gb,
+  const int *jlo_grad_phi_plus_gb,
+  const int *jhi_grad_phi_plus_gb,
+  const double *phi_x_minus,
+  const double *phi_y_minus,
+  const int *ilo_grad_phi_minus_gb,
+  const int *ihi_grad_phi_minus_gb,
+  const int *jlo_grad_phi_minus_gb,
+  const int *jhi_grad_phi_minus_gb,
+  const double *psi,
+  const int *ilo_psi_gb,
+  const int *ihi_psi_gb,
+  const int *jlo_psi_gb,
+  const int *jhi_psi_gb,
+  const double *psi_x_plus,
+  const double *psi_y_plus,
+  const int *ilo_grad_psi_plus_gb,
+  const int *ihi_grad_psi_plus_gb,
+  const int *jlo_grad_psi_plus_gb,
+  const int *jhi_grad_psi_plus_gb,
+  const double *psi_x_minus,
+  const double *psi_y_minus,
+  const int *ilo_grad_psi_minus_gb,
+  const int *ihi_grad_psi_minus_gb,
+  const int *jlo_grad_psi_minus_gb,
+  const int *jhi_grad_psi_minus_gb,
+  const double *dx,
+  const double *dy,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
 /* 2D form: reinitialization RHS sgn(phi)(1 - |grad phi|), Godunov.
  * Replaces src/reinitialization/lsm_reinitialization2d.f.in:48; C declaration src/reinitialization/lsm_reinitialization2d.h:78.
  */
@@ -827,6 +940,45 @@ void lsm2dcomputereinitializationeqnrhslocal_(
   const int *jlo_nb_gb,
   const int *jhi_nb_gb,
   const unsigned char *mark_fb);
+
+/* 2D form: first-order reinitialization RHS with the Russo-Smereka subcell fix.
+ * Replaces src/reinitialization/lsm_reinitialization2d.f.in:468; C declaration src/reinitialization/lsm_reinitialization2d.h:259.
+ */
+void lsm2dcomputereinitializationeqnrhssubcellfixorder1_(
+  double *reinit_rhs,
+  const int *ilo_rhs_gb,
+  const int *ihi_rhs_gb,
+  const int *jlo_rhs_gb,
+  const int *jhi_rhs_gb,
+  const double *phi,
+  const int *ilo_phi_gb,
+  const int *ihi_phi_gb,
+  const int *jlo_phi_gb,
+  const int *jhi_phi_gb,
+  const double *phi0,
+  const double *distance0,
+  const int *ilo_phi0_gb,
+  const int *ihi_phi0_gb,
+  const int *jlo_phi0_gb,
+  const int *jhi_phi0_gb,
+  const double *phi_x_plus,
+  const double *phi_y_plus,
+  const int *ilo_grad_phi_plus_gb,
+  const int *ihi_grad_phi_plus_gb,
+  const int *jlo_grad_phi_plus_gb,
+  const int *jhi_grad_phi_plus_gb,
+  const double *phi_x_minus,
+  const double *phi_y_minus,
+  const int *ilo_grad_phi_minus_gb,
+  const int *ihi_grad_phi_minus_gb,
+  const int *jlo_grad_phi_minus_gb,
+  const int *jhi_grad_phi_minus_gb,
+  const int *ilo_fb,
+  const int *ihi_fb,
+  const int *jlo_fb,
+  const int *jhi_fb,
+  const double *dx,
+  const double *dy);
 
 /* 2D form: CFL-stable dt for advection.
  * Replaces src/toolbox/lsm_math_utils2d.f.in:218; C declaration src/toolbox/lsm_math_utils2d.h:204.

@@ -74,6 +74,57 @@ void face_extrapolate(const char *name, R *phi, const Box &gb, const Box &fb, in
 
 using namespace lsmgpu;
 
+// orthogonalization equation RHS (reinitialization3d.f.in:296-470); SGN3 =
+// false gives the 2D routine's smoothing of sgn(psi) (see ortho_rhs)
+template <bool SGN3>
+void ortho_dense(const char *name, R *ortho_rhs, const Box &rb, const R *phi_x_plus, const R *phi_y_plus,
+                 const R *phi_z_plus, const Box &pb, const R *phi_x_minus, const R *phi_y_minus,
+                 const R *phi_z_minus, const Box &mb, const R *psi, const Box &sb, const R *psi_x_plus,
+                 const R *psi_y_plus, const R *psi_z_plus, const Box &spb, const R *psi_x_minus,
+                 const R *psi_y_minus, const R *psi_z_minus, const Box &smb, const Box &fb, R dx, R dy, R dz) {
+  Call call(name);
+  if (!rb.contains(fb, 0, 0, 0) || !pb.contains(fb, 0, 0, 0) || !mb.contains(fb, 0, 0, 0) ||
+      !sb.contains(fb, 0, 0, 0) || !spb.contains(fb, 0, 0, 0) || !smb.contains(fb, 0, 0, 0))
+    call.fail("ghost box does not cover the fill box");
+  if (!call.ok() || fb.empty()) return;
+  View<R> O = view(call.out_region(ortho_rhs, rb, fb), rb);
+  View<const R> XP = vin(call, phi_x_plus, pb), YP = vin(call, phi_y_plus, pb), ZP = vin(call, phi_z_plus, pb);
+  View<const R> XM = vin(call, phi_x_minus, mb), YM = vin(call, phi_y_minus, mb), ZM = vin(call, phi_z_minus, mb);
+  View<const R> S = vin(call, psi, sb);
+  View<const R> SXP = vin(call, psi_x_plus, spb), SYP = vin(call, psi_y_plus, spb), SZP = vin(call, psi_z_plus, spb);
+  View<const R> SXM = vin(call, psi_x_minus, smb), SYM = vin(call, psi_y_minus, smb),
+                SZM = vin(call, psi_z_minus, smb);
+  if (!call.ok()) return;
+  R dx_sq = rmax(rmax(dx, dy), dz);
+  dx_sq = dx_sq * dx_sq;
+  for_box(fb, [=] __device__(int i, int j, int k) {
+    const R psp[3] = {SXP(i, j, k), SYP(i, j, k), SZP(i, j, k)}, psm[3] = {SXM(i, j, k), SYM(i, j, k), SZM(i, j, k)};
+    const R pp[3] = {XP(i, j, k), YP(i, j, k), ZP(i, j, k)}, pm[3] = {XM(i, j, k), YM(i, j, k), ZM(i, j, k)};
+    O(i, j, k) = lsmgpu::ortho_rhs<R, SGN3>(S(i, j, k), psp, psm, pp, pm, dx_sq);
+  });
+  call.finish();
+}
+
+// distance estimate for the subcell fix (reinitialization3d.f.in:477-575;
+// HALF = false: the 2D routine's form, see subcell_distance); distance0 and
+// phi0 share phi0's ghost box
+template <bool HALF>
+void subcell_distance_dense(const char *name, R *distance0, const R *phi0, const Box &zb, const Box &fb, R dx,
+                            R dy, R dz) {
+  Call call(name);
+  if (!zb.contains(fb, 1, 1, 1)) call.fail("phi0 ghost box must hold 1 ghost cell around the fill box");
+  if (!call.ok() || fb.empty()) return;
+  View<R> D = view(call.out_region(distance0, zb, fb), zb);
+  View<const R> P0 = vin(call, phi0, zb);
+  if (!call.ok()) return;
+  const R flag = R(-1000.0) * rmax(rmax(dx, dy), dz);
+  for_box(fb, [=] __device__(int i, int j, int k) {
+    const long long st[3] = {1, P0.s1, P0.s2};
+    D(i, j, k) = subcell_distance<R, HALF>(P0.p + P0.off(i, j, k), st, flag);
+  });
+  call.finish();
+}
+
 extern "C" {
 
 void lsm3dcentralhessian_(R *phi_xx, R *phi_xy, R *phi_xz, R *phi_yy, R *phi_yz, R *phi_zz, BOXARG(h),
@@ -297,6 +348,63 @@ void lsm3ddeltafunctionorder1_(const R *phi, R *delta, BOXARG(g), const R *norm_
     const R yp = side(P(i, j + 1, k), ny, oy), ym = side(P(i, j - 1, k), ny, oy);
     const R zp = side(P(i, j, k + 1), nx, ox), zm = side(P(i, j, k - 1), nx, ox);
     D(i, j, k) = fabs(xp) + fabs(xm) + fabs(yp) + fabs(ym) + fabs(zp) + fabs(zm);
+  });
+  call.finish();
+}
+
+#define ORTHO_ARGS                                                                                       \
+  R *ortho_rhs, BOXARG(r), const R *phi_x_plus, const R *phi_y_plus, const R *phi_z_plus, BOXARG(p),     \
+      const R *phi_x_minus, const R *phi_y_minus, const R *phi_z_minus, BOXARG(m), const R *psi, BOXARG(s), \
+      const R *psi_x_plus, const R *psi_y_plus, const R *psi_z_plus, BOXARG(sp), const R *psi_x_minus,    \
+      const R *psi_y_minus, const R *psi_z_minus, BOXARG(sm), BOXARG(fb), const R *dx, const R *dy,       \
+      const R *dz
+#define ORTHO_PASS                                                                                       \
+  ortho_rhs, BOXOF(r), phi_x_plus, phi_y_plus, phi_z_plus, BOXOF(p), phi_x_minus, phi_y_minus, phi_z_minus, \
+      BOXOF(m), psi, BOXOF(s), psi_x_plus, psi_y_plus, psi_z_plus, BOXOF(sp), psi_x_minus, psi_y_minus,    \
+      psi_z_minus, BOXOF(sm), BOXOF(fb), *dx, *dy, *dz
+
+void lsm3dcomputeorthogonalizationeqnrhs_(ORTHO_ARGS) {
+  ortho_dense<true>("lsm3dcomputeorthogonalizationeqnrhs_", ORTHO_PASS);
+}
+void lsmgpu_orthogonalization_rhs_unit_sgn_smoothing(ORTHO_ARGS) {
+  ortho_dense<false>("lsmgpu_orthogonalization_rhs_unit_sgn_smoothing", ORTHO_PASS);
+}
+
+void lsm3dcomputedistanceforsubcellfix_(R *distance0, const R *phi0, BOXARG(z), BOXARG(fb), const R *dx,
+                                        const R *dy, const R *dz) {
+  subcell_distance_dense<true>("lsm3dcomputedistanceforsubcellfix_", distance0, phi0, BOXOF(z), BOXOF(fb), *dx,
+                               *dy, *dz);
+}
+void lsmgpu_distance_for_subcell_fix_full_central(R *distance0, const R *phi0, BOXARG(z), BOXARG(fb),
+                                                  const R *dx, const R *dy, const R *dz) {
+  subcell_distance_dense<false>("lsmgpu_distance_for_subcell_fix_full_central", distance0, phi0, BOXOF(z),
+                                BOXOF(fb), *dx, *dy, *dz);
+}
+
+// first-order reinitialization RHS with the subcell fix
+// (reinitialization3d.f.in:586-757)
+void lsm3dcomputereinitializationeqnrhssubcellfixorder1_(R *reinit_rhs, BOXARG(r), const R *phi, BOXARG(f),
+                                                         const R *phi0, const R *distance0, BOXARG(z),
+                                                         const R *phi_x_plus, const R *phi_y_plus,
+                                                         const R *phi_z_plus, BOXARG(p), const R *phi_x_minus,
+                                                         const R *phi_y_minus, const R *phi_z_minus, BOXARG(m),
+                                                         BOXARG(fb), const R *dx, const R *dy, const R *dz) {
+  Call call("lsm3dcomputereinitializationeqnrhssubcellfixorder1_");
+  const Box rb = BOXOF(r), phb = BOXOF(f), zb = BOXOF(z), pb = BOXOF(p), mb = BOXOF(m), fb = BOXOF(fb);
+  if (!rb.contains(fb, 0, 0, 0) || !phb.contains(fb, 0, 0, 0) || !zb.contains(fb, 0, 0, 0) ||
+      !pb.contains(fb, 0, 0, 0) || !mb.contains(fb, 0, 0, 0))
+    call.fail("ghost box does not cover the fill box");
+  if (!call.ok() || fb.empty()) return;
+  View<R> O = view(call.out_region(reinit_rhs, rb, fb), rb);
+  View<const R> PH = vin(call, phi, phb), P0 = vin(call, phi0, zb), D0 = vin(call, distance0, zb);
+  View<const R> XP = vin(call, phi_x_plus, pb), YP = vin(call, phi_y_plus, pb), ZP = vin(call, phi_z_plus, pb);
+  View<const R> XM = vin(call, phi_x_minus, mb), YM = vin(call, phi_y_minus, mb), ZM = vin(call, phi_z_minus, mb);
+  if (!call.ok()) return;
+  const R max_dx = rmax(rmax(*dx, *dy), *dz);
+  const R flag = R(-1000.0) * max_dx;
+  for_box(fb, [=] __device__(int i, int j, int k) {
+    const R gp[3] = {XP(i, j, k), YP(i, j, k), ZP(i, j, k)}, gm[3] = {XM(i, j, k), YM(i, j, k), ZM(i, j, k)};
+    O(i, j, k) = subcell_rhs<R>(PH(i, j, k), P0(i, j, k), D0(i, j, k), gp, gm, flag, max_dx);
   });
   call.finish();
 }

@@ -673,6 +673,15 @@ void lsm2dcomputeavegradphilocal_(double *grad_phi_ave, const double *phi, const
   lsm3dcomputeavegradphilocal_(grad_phi_ave, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, dx, dy, dx, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
 }
 
+// src/reinitialization/lsm_reinitialization2d.f.in:392
+void lsm2dcomputedistanceforsubcellfix_(double *distance0, const double *phi0, const int *ilo_phi0_gb, const int *ihi_phi0_gb, const int *jlo_phi0_gb, const int *jhi_phi0_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const double *dx, const double *dy) {
+  Lift L_(2, "lsm2dcomputedistanceforsubcellfix_");
+  L_.box(ilo_phi0_gb, ihi_phi0_gb, jlo_phi0_gb, jhi_phi0_gb);
+  L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
+  if (!L_.ready()) return;
+  lsmgpu_distance_for_subcell_fix_full_central(distance0, phi0, ilo_phi0_gb, ihi_phi0_gb, jlo_phi0_gb, jhi_phi0_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dx, dy, dx);
+}
+
 // src/toolbox/lsm_spatial_derivatives2d.f.in:49
 void lsm2dcomputedn_(double *dn, const int *ilo_dn_gb, const int *ihi_dn_gb, const int *jlo_dn_gb, const int *jhi_dn_gb, const double *dn_minus_one, const int *ilo_dn_minus_one_gb, const int *ihi_dn_minus_one_gb, const int *jlo_dn_minus_one_gb, const int *jhi_dn_minus_one_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const int *n, const int *dir) {
   Lift L_(2, "lsm2dcomputedn_");
@@ -740,6 +749,35 @@ void lsm2dcomputemeancurvatureorder4local_(double *kappa, const int *ilo_kappa_g
   lsmgpu_mean_curvature_order4_local(kappa, ilo_kappa_gb, ihi_kappa_gb, jlo_kappa_gb, jhi_kappa_gb, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, phi_x, phi_y, L_.zero(), grad_phi_mag, ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb, &L_.k0, &L_.k0, dx, dy, dx, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
 }
 
+// src/reinitialization/lsm_reinitialization2d.f.in:255
+void lsm2dcomputeorthogonalizationeqnrhs_(double *ortho_rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const double *psi, const int *ilo_psi_gb, const int *ihi_psi_gb, const int *jlo_psi_gb, const int *jhi_psi_gb, const double *psi_x_plus, const double *psi_y_plus, const int *ilo_grad_psi_plus_gb, const int *ihi_grad_psi_plus_gb, const int *jlo_grad_psi_plus_gb, const int *jhi_grad_psi_plus_gb, const double *psi_x_minus, const double *psi_y_minus, const int *ilo_grad_psi_minus_gb, const int *ihi_grad_psi_minus_gb, const int *jlo_grad_psi_minus_gb, const int *jhi_grad_psi_minus_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const double *dx, const double *dy) {
+  Lift L_(2, "lsm2dcomputeorthogonalizationeqnrhs_");
+  L_.box(ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb);
+  L_.box(ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb);
+  L_.box(ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb);
+  L_.box(ilo_psi_gb, ihi_psi_gb, jlo_psi_gb, jhi_psi_gb);
+  L_.box(ilo_grad_psi_plus_gb, ihi_grad_psi_plus_gb, jlo_grad_psi_plus_gb, jhi_grad_psi_plus_gb);
+  L_.box(ilo_grad_psi_minus_gb, ihi_grad_psi_minus_gb, jlo_grad_psi_minus_gb, jhi_grad_psi_minus_gb);
+  L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
+  if (!L_.ready()) return;
+  lsmgpu_orthogonalization_rhs_unit_sgn_smoothing(ortho_rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, psi, ilo_psi_gb, ihi_psi_gb, jlo_psi_gb, jhi_psi_gb, &L_.k0, &L_.k0, psi_x_plus, psi_y_plus, L_.zero(), ilo_grad_psi_plus_gb, ihi_grad_psi_plus_gb, jlo_grad_psi_plus_gb, jhi_grad_psi_plus_gb, &L_.k0, &L_.k0, psi_x_minus, psi_y_minus, L_.zero(), ilo_grad_psi_minus_gb, ihi_grad_psi_minus_gb, jlo_grad_psi_minus_gb, jhi_grad_psi_minus_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dx, dy, dx);
+}
+
+// src/reinitialization/lsm_reinitialization2d_local.f.in:284
+void lsm2dcomputeorthogonalizationeqnrhslocal_(double *ortho_rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const double *psi, const int *ilo_psi_gb, const int *ihi_psi_gb, const int *jlo_psi_gb, const int *jhi_psi_gb, const double *psi_x_plus, const double *psi_y_plus, const int *ilo_grad_psi_plus_gb, const int *ihi_grad_psi_plus_gb, const int *jlo_grad_psi_plus_gb, const int *jhi_grad_psi_plus_gb, const double *psi_x_minus, const double *psi_y_minus, const int *ilo_grad_psi_minus_gb, const int *ihi_grad_psi_minus_gb, const int *jlo_grad_psi_minus_gb, const int *jhi_grad_psi_minus_gb, const double *dx, const double *dy, const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb) {
+  Lift L_(2, "lsm2dcomputeorthogonalizationeqnrhslocal_");
+  L_.box(ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb);
+  L_.box(ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb);
+  L_.box(ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb);
+  L_.box(ilo_psi_gb, ihi_psi_gb, jlo_psi_gb, jhi_psi_gb);
+  L_.box(ilo_grad_psi_plus_gb, ihi_grad_psi_plus_gb, jlo_grad_psi_plus_gb, jhi_grad_psi_plus_gb);
+  L_.box(ilo_grad_psi_minus_gb, ihi_grad_psi_minus_gb, jlo_grad_psi_minus_gb, jhi_grad_psi_minus_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsmgpu_orthogonalization_rhs_unit_sgn_smoothing_local(ortho_rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, psi, ilo_psi_gb, ihi_psi_gb, jlo_psi_gb, jhi_psi_gb, &L_.k0, &L_.k0, psi_x_plus, psi_y_plus, L_.zero(), ilo_grad_psi_plus_gb, ihi_grad_psi_plus_gb, jlo_grad_psi_plus_gb, jhi_grad_psi_plus_gb, &L_.k0, &L_.k0, psi_x_minus, psi_y_minus, L_.zero(), ilo_grad_psi_minus_gb, ihi_grad_psi_minus_gb, jlo_grad_psi_minus_gb, jhi_grad_psi_minus_gb, &L_.k0, &L_.k0, dx, dy, dx, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
 // src/reinitialization/lsm_reinitialization2d.f.in:48
 void lsm2dcomputereinitializationeqnrhs_(double *reinit_rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *phi, const int *ilo_phi_gb, const int *ihi_phi_gb, const int *jlo_phi_gb, const int *jhi_phi_gb, const double *phi0, const int *ilo_phi0_gb, const int *ihi_phi0_gb, const int *jlo_phi0_gb, const int *jhi_phi0_gb, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const double *dx, const double *dy, const int *use_phi0_for_sgn) {
   Lift L_(2, "lsm2dcomputereinitializationeqnrhs_");
@@ -765,6 +803,19 @@ void lsm2dcomputereinitializationeqnrhslocal_(double *reinit_rhs, const int *ilo
   L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
   if (!L_.ready()) return;
   lsm3dcomputereinitializationeqnrhslocal_(reinit_rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, phi0, ilo_phi0_gb, ihi_phi0_gb, jlo_phi0_gb, jhi_phi0_gb, &L_.k0, &L_.k0, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, dx, dy, dx, use_phi0_for_sgn, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
+// src/reinitialization/lsm_reinitialization2d.f.in:468
+void lsm2dcomputereinitializationeqnrhssubcellfixorder1_(double *reinit_rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *phi, const int *ilo_phi_gb, const int *ihi_phi_gb, const int *jlo_phi_gb, const int *jhi_phi_gb, const double *phi0, const double *distance0, const int *ilo_phi0_gb, const int *ihi_phi0_gb, const int *jlo_phi0_gb, const int *jhi_phi0_gb, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const double *dx, const double *dy) {
+  Lift L_(2, "lsm2dcomputereinitializationeqnrhssubcellfixorder1_");
+  L_.box(ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb);
+  L_.box(ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb);
+  L_.box(ilo_phi0_gb, ihi_phi0_gb, jlo_phi0_gb, jhi_phi0_gb);
+  L_.box(ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb);
+  L_.box(ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb);
+  L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
+  if (!L_.ready()) return;
+  lsm3dcomputereinitializationeqnrhssubcellfixorder1_(reinit_rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, phi0, distance0, ilo_phi0_gb, ihi_phi0_gb, jlo_phi0_gb, jhi_phi0_gb, &L_.k0, &L_.k0, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dx, dy, dx);
 }
 
 // src/toolbox/lsm_math_utils2d.f.in:218

@@ -208,6 +208,39 @@ void curv_variant_local(const char *name, R *kappa, const Box &kb, const R *phi,
   lc.c.finish();
 }
 
+// orthogonalization equation RHS on listed cells
+// (reinitialization3d_local.f.in:326-480); SGN3 = false gives the 2D
+// routine's smoothing of sgn(psi) (reinitialization2d_local.f.in:406)
+template <bool SGN3>
+void ortho_local(const char *name, R *ortho_rhs, const Box &rb, const R *phi_x_plus, const R *phi_y_plus,
+                 const R *phi_z_plus, const Box &pb, const R *phi_x_minus, const R *phi_y_minus,
+                 const R *phi_z_minus, const Box &mb, const R *psi, const Box &sb, const R *psi_x_plus,
+                 const R *psi_y_plus, const R *psi_z_plus, const Box &spb, const R *psi_x_minus,
+                 const R *psi_y_minus, const R *psi_z_minus, const Box &smb, R dx, R dy, R dz,
+                 const int *index_x, const int *index_y, const int *index_z, const int *nlo, const int *nhi,
+                 const unsigned char *narrow_band, const Box &nbb, const unsigned char *mark_fb) {
+  LocalCall lc(name);
+  List L = lc.list(index_x, index_y, index_z, *nlo, *nhi);
+  Gate g = lc.gate(narrow_band, nbb, *mark_fb);
+  View<R> O = lc.inout(ortho_rhs, rb);
+  View<const R> XP = lc.in(phi_x_plus, pb), YP = lc.in(phi_y_plus, pb), ZP = lc.in(phi_z_plus, pb);
+  View<const R> XM = lc.in(phi_x_minus, mb), YM = lc.in(phi_y_minus, mb), ZM = lc.in(phi_z_minus, mb);
+  View<const R> S = lc.in(psi, sb);
+  View<const R> SXP = lc.in(psi_x_plus, spb), SYP = lc.in(psi_y_plus, spb), SZP = lc.in(psi_z_plus, spb);
+  View<const R> SXM = lc.in(psi_x_minus, smb), SYM = lc.in(psi_y_minus, smb), SZM = lc.in(psi_z_minus, smb);
+  g.safe = isect(isect(isect(rb, sb), isect(pb, mb)), isect(spb, smb));
+  if (!lc.c.ok()) return;
+  R dx_sq = rmax(rmax(dx, dy), dz);
+  dx_sq = dx_sq * dx_sq;
+  for_list(L, *nlo, *nhi, [=] __device__(int i, int j, int k) {
+    if (!g(i, j, k)) return;
+    const R psp[3] = {SXP(i, j, k), SYP(i, j, k), SZP(i, j, k)}, psm[3] = {SXM(i, j, k), SYM(i, j, k), SZM(i, j, k)};
+    const R pp[3] = {XP(i, j, k), YP(i, j, k), ZP(i, j, k)}, pm[3] = {XM(i, j, k), YM(i, j, k), ZM(i, j, k)};
+    O(i, j, k) = lsmgpu::ortho_rhs<R, SGN3>(S(i, j, k), psp, psm, pp, pm, dx_sq);
+  });
+  lc.c.finish();
+}
+
 extern "C" {
 
 void lsm3dcomputednlocal_(R *dn, BOXARG(d), const R *dm, BOXARG(m), const int *n, const int *dir, IDX3,
@@ -805,6 +838,24 @@ void lsm3daddexternalandnormalveltermtolserhslocal_(R *lse_rhs, BOXARG(r), const
       O(i, j, k) = O(i, j, k) - ux * gx - uy * gy - uz * gz;
   });
   lc.c.finish();
+}
+
+#define ORTHOL_ARGS                                                                                      \
+  R *ortho_rhs, BOXARG(r), const R *phi_x_plus, const R *phi_y_plus, const R *phi_z_plus, BOXARG(p),     \
+      const R *phi_x_minus, const R *phi_y_minus, const R *phi_z_minus, BOXARG(m), const R *psi, BOXARG(s), \
+      const R *psi_x_plus, const R *psi_y_plus, const R *psi_z_plus, BOXARG(sp), const R *psi_x_minus,    \
+      const R *psi_y_minus, const R *psi_z_minus, BOXARG(sm), DXP, LTAIL
+#define ORTHOL_PASS                                                                                      \
+  ortho_rhs, BOXOF(r), phi_x_plus, phi_y_plus, phi_z_plus, BOXOF(p), phi_x_minus, phi_y_minus, phi_z_minus, \
+      BOXOF(m), psi, BOXOF(s), psi_x_plus, psi_y_plus, psi_z_plus, BOXOF(sp), psi_x_minus, psi_y_minus,    \
+      psi_z_minus, BOXOF(sm), *dx, *dy, *dz, index_x, index_y, index_z, nlo, nhi, narrow_band, BOXOF(nb),  \
+      mark_fb
+
+void lsm3dcomputeorthogonalizationeqnrhslocal_(ORTHOL_ARGS) {
+  ortho_local<true>("lsm3dcomputeorthogonalizationeqnrhslocal_", ORTHOL_PASS);
+}
+void lsmgpu_orthogonalization_rhs_unit_sgn_smoothing_local(ORTHOL_ARGS) {
+  ortho_local<false>("lsmgpu_orthogonalization_rhs_unit_sgn_smoothing_local", ORTHOL_PASS);
 }
 
 }  // extern "C"

@@ -218,6 +218,83 @@ __device__ __forceinline__ R ext_pick(R v, R vn, R p, R m) {
   return (fabs(hp) > fabs(hm)) ? p : m;
 }
 
+// ---- orthogonalization and subcell fix (reinitialization3d.f.in:296-757) --------
+// orthogonalization RHS at one cell: upwinding of grad(phi) along
+// sgn(psi) grad(psi*), grad(psi*) the average of the plus and minus
+// derivatives of psi (reinitialization3d.f.in:380-425)
+// GRAD_SMOOTH: sgn(psi) = psi / sqrt(psi^2 + dx_sq |grad psi*|^2) as the 3D
+// routine smooths it (reinitialization3d.f.in:439); otherwise
+// psi / sqrt(psi^2 + dx_sq), the 2D routine's form (reinitialization2d.f.in:360)
+template <class R, bool GRAD_SMOOTH = true>
+__device__ __forceinline__ R ortho_rhs(R psi, const R psp[3], const R psm[3], const R pp[3], const R pm[3],
+                                       R dx_sq) {
+  R g[3];
+  for (int d = 0; d < 3; d++) g[d] = R(0.5) * (psp[d] + psm[d]);
+  R n = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+  n = sqrt(n);
+  if (!(fabs(psi) > Consts<R>::zero_tol && n > Consts<R>::zero_tol)) return R(0);
+  const R s = GRAD_SMOOTH ? psi / sqrt(psi * psi + dx_sq * (n * n)) : psi / sqrt(psi * psi + dx_sq);
+  R t = rmax(s * g[0], R(0)) * pm[0];
+  t = t + rmin(s * g[0], R(0)) * pp[0];
+  t = t + rmax(s * g[1], R(0)) * pm[1];
+  t = t + rmin(s * g[1], R(0)) * pp[1];
+  t = t + rmax(s * g[2], R(0)) * pm[2];
+  t = t + rmin(s * g[2], R(0)) * pp[2];
+  return -(R(1.0) / n * t);
+}
+
+// signed distance estimate near the interface for the subcell fix
+// (Russo-Smereka): `flag` away from sign changes, else phi0 over the largest
+// one-sided or central difference.  HALF_CENTRAL is the 3D routine's form
+// (reinitialization3d.f.in:520-569: sign changes by comparisons, half the
+// central difference, phi0 / delta); otherwise the 2D routine's
+// (reinitialization2d.f.in:425-460: sign changes by negative products, the
+// full central difference, 2 phi0 / delta)
+template <class R, bool HALF_CENTRAL = true>
+__device__ __forceinline__ R subcell_distance(const R *c, const long long s[3], R flag) {
+  const R p = c[0], z = R(0);
+  bool near = false;
+  for (int d = 0; d < 3; d++) {
+    const R a = c[s[d]], b = c[-s[d]];
+    if (HALF_CENTRAL)
+      near = near || (a > z && p <= z) || (a <= z && p > z) || (b > z && p <= z) || (b <= z && p > z);
+    else
+      near = near || (a * p < z) || (b * p < z);
+  }
+  if (!near) return flag;
+  R delta = Consts<R>::zero_tol;
+  for (int d = 0; d < 3; d++) {
+    const R a = c[s[d]], b = c[-s[d]];
+    const R central = HALF_CENTRAL ? fabs(a - b) / R(2.0) : fabs(a - b);
+    const R m = rmax(rmax(central, fabs(a - p)), fabs(p - b));
+    delta = rmax(m, delta);
+  }
+  return HALF_CENTRAL ? p / delta : R(2.0) * p / delta;
+}
+
+// first-order reinitialization RHS with the subcell fix
+// (reinitialization3d.f.in:660-745)
+template <class R>
+__device__ __forceinline__ R subcell_rhs(R pc, R p0, R dist, const R gp[3], const R gm[3], R flag, R max_dx) {
+  const R sgn0 = (fabs(p0) > Consts<R>::zero_tol) ? copysign(R(1.0), p0) : R(0);
+  if (!(dist == flag)) return dist - sgn0 * fabs(pc) / max_dx;
+  R st[3];
+  for (int d = 0; d < 3; d++) {
+    R u, w;
+    if (pc > R(0)) {
+      u = rmax(-gp[d], R(0));
+      w = rmax(gm[d], R(0));
+    } else {
+      u = rmax(gp[d], R(0));
+      w = rmax(-gm[d], R(0));
+    }
+    st[d] = rmax(u, w);
+  }
+  if (!(fabs(pc) > Consts<R>::zero_tol)) return R(0);
+  const R n2 = st[0] * st[0] + st[1] * st[1] + st[2] * st[2];
+  return sgn0 - sgn0 * sqrt(n2);
+}
+
 // ---- curvature variants (curvature3d.f.in:136-508, curvature3d_local.f.in:151-574)
 enum CurvKind { CURV_GAUSS2 = 1, CURV_MEAN4 = 2, CURV_GAUSS4 = 3 };
 

@@ -60,6 +60,9 @@ DESC = {
     "lsm3daddconstcurvtermtolserhs_": ("lse", "rhs += b * kappa |grad phi| from first and second derivatives"),
     # reinit / curvature
     "lsm3dcomputereinitializationeqnrhs_": ("reinit", "reinitialization RHS sgn(phi)(1 - |grad phi|), Godunov"),
+    "lsm3dcomputeorthogonalizationeqnrhs_": ("reinit", "orthogonalization RHS: grad(phi) upwinded along sgn(psi) grad(psi)"),
+    "lsm3dcomputedistanceforsubcellfix_": ("reinit", "distance estimate next to sign changes of phi0 for the subcell fix (-1000 max(dx) elsewhere)"),
+    "lsm3dcomputereinitializationeqnrhssubcellfixorder1_": ("reinit", "first-order reinitialization RHS with the Russo-Smereka subcell fix"),
     "lsm3dcomputemeancurvatureorder2_": ("geom", "second-order mean curvature"),
     "lsm3dcomputegaussiancurvatureorder2_": ("geom", "second-order Gaussian curvature"),
     "lsm3dcomputemeancurvatureorder4_": ("geom", "fourth-order mean curvature (cross derivatives from the first derivatives)"),
@@ -135,6 +138,7 @@ DESC = {
     "lsm3daddconstnormalveltermtolserhslocal_": ("local", "normal velocity term (constant) on band cells"),
     "lsm3daddconstcurvtermtolserhslocal_": ("local", "curvature term on band cells"),
     "lsm3dcomputereinitializationeqnrhslocal_": ("local", "reinitialization RHS on band cells"),
+    "lsm3dcomputeorthogonalizationeqnrhslocal_": ("local", "orthogonalization RHS on band cells"),
     "lsm3dcomputemeancurvatureorder2local_": ("local", "second-order mean curvature on band cells"),
     "lsm3dcomputegaussiancurvatureorder2local_": ("local", "second-order Gaussian curvature on band cells"),
     "lsm3dcomputemeancurvatureorder4local_": ("local", "fourth-order curvature on band cells: the Gaussian-curvature formula, as the reference routine evaluates it (lsmgpu_mean_curvature_order4_local gives the mean curvature)"),
@@ -243,8 +247,20 @@ NOT_LIFTED = {"lsm1dcomputestablenormalveldt_", "lsm1dcomputestablenormalveldtco
 # routine of the same name, which has the same argument list: the 3D
 # MeanCurvatureOrder4 local routine evaluates the Gaussian-curvature formula
 # (curvature3d_local.f.in:385-410), the 2D one the mean curvature
+# the 2D orthogonalization RHS smooths sgn(psi) with max(dx)^2 alone, the 3D
+# one with max(dx)^2 |grad psi|^2 (reinitialization2d.f.in:360,
+# reinitialization3d.f.in:439); the 2D subcell-fix distance tests sign
+# changes by negative products, takes the full central difference and returns
+# 2 phi0 / delta (reinitialization2d.f.in:392)
 LIFT_VIA = {"lsm2dcomputemeancurvatureorder4local_": ("lsmgpu_mean_curvature_order4_local",
-                                                      "fourth-order mean curvature on band cells")}
+                                                      "fourth-order mean curvature on band cells"),
+            "lsm2dcomputeorthogonalizationeqnrhs_": ("lsmgpu_orthogonalization_rhs_unit_sgn_smoothing",
+                                                     "orthogonalization RHS (sgn(psi) smoothed with max(dx)^2)"),
+            "lsm2dcomputeorthogonalizationeqnrhslocal_": (
+                "lsmgpu_orthogonalization_rhs_unit_sgn_smoothing_local",
+                "orthogonalization RHS on band cells (sgn(psi) smoothed with max(dx)^2)"),
+            "lsm2dcomputedistanceforsubcellfix_": ("lsmgpu_distance_for_subcell_fix_full_central",
+                                                   "distance estimate for the subcell fix (2 phi0 / delta)")}
 
 # 3D routines whose dz (and dy) multiply a cell volume: lifted with 1 there
 VOLUME_FACTOR = re.compile(r"volumeintegral|volumeregion|surfaceintegral|surfacearea")
