@@ -1596,6 +1596,64 @@ void lsm2dhjeno3_(
   const double *dx,
   const double *dy);
 
+/* 2D form: HJ ENO3 plus/minus gradients on level-0 band cells.
+ * Replaces src/toolbox/lsm_spatial_derivatives2d_local.f.in:498; C declaration src/toolbox/lsm_spatial_derivatives2d_local.h:220.
+ */
+void lsm2dhjeno3local_(
+  double *phi_x_plus,
+  double *phi_y_plus,
+  const int *ilo_grad_phi_plus_gb,
+  const int *ihi_grad_phi_plus_gb,
+  const int *jlo_grad_phi_plus_gb,
+  const int *jhi_grad_phi_plus_gb,
+  double *phi_x_minus,
+  double *phi_y_minus,
+  const int *ilo_grad_phi_minus_gb,
+  const int *ihi_grad_phi_minus_gb,
+  const int *jlo_grad_phi_minus_gb,
+  const int *jhi_grad_phi_minus_gb,
+  const double *phi,
+  const int *ilo_phi_gb,
+  const int *ihi_phi_gb,
+  const int *jlo_phi_gb,
+  const int *jhi_phi_gb,
+  double *d1,
+  const int *ilo_d1_gb,
+  const int *ihi_d1_gb,
+  const int *jlo_d1_gb,
+  const int *jhi_d1_gb,
+  double *d2,
+  const int *ilo_d2_gb,
+  const int *ihi_d2_gb,
+  const int *jlo_d2_gb,
+  const int *jhi_d2_gb,
+  double *d3,
+  const int *ilo_d3_gb,
+  const int *ihi_d3_gb,
+  const int *jlo_d3_gb,
+  const int *jhi_d3_gb,
+  const double *dx,
+  const double *dy,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index0,
+  const int *nhi_index0,
+  const int *nlo_index1,
+  const int *nhi_index1,
+  const int *nlo_index2,
+  const int *nhi_index2,
+  const int *nlo_index3,
+  const int *nhi_index3,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb,
+  const unsigned char *mark_d1,
+  const unsigned char *mark_d2,
+  const unsigned char *mark_d3);
+
 /* 2D form: fifth-order HJ WENO plus/minus gradients.
  * Replaces src/toolbox/lsm_spatial_derivatives2d.f.in:756; C declaration src/toolbox/lsm_spatial_derivatives2d.h:287.
  */
@@ -2496,6 +2554,56 @@ void lsm2dupwindhjeno2_(
   const int *jhi_fb,
   const double *dx,
   const double *dy);
+
+/* 2D form: upwind HJ ENO2 gradient for a velocity field on level-0 band cells.
+ * Replaces src/toolbox/lsm_spatial_derivatives2d_local.f.in:1160; C declaration src/toolbox/lsm_spatial_derivatives2d_local.h:361.
+ */
+void lsm2dupwindhjeno2local_(
+  double *phi_x,
+  double *phi_y,
+  const int *ilo_grad_phi_gb,
+  const int *ihi_grad_phi_gb,
+  const int *jlo_grad_phi_gb,
+  const int *jhi_grad_phi_gb,
+  const double *phi,
+  const int *ilo_phi_gb,
+  const int *ihi_phi_gb,
+  const int *jlo_phi_gb,
+  const int *jhi_phi_gb,
+  const double *vel_x,
+  const double *vel_y,
+  const int *ilo_vel_gb,
+  const int *ihi_vel_gb,
+  const int *jlo_vel_gb,
+  const int *jhi_vel_gb,
+  double *d1,
+  const int *ilo_d1_gb,
+  const int *ihi_d1_gb,
+  const int *jlo_d1_gb,
+  const int *jhi_d1_gb,
+  double *d2,
+  const int *ilo_d2_gb,
+  const int *ihi_d2_gb,
+  const int *jlo_d2_gb,
+  const int *jhi_d2_gb,
+  const double *dx,
+  const double *dy,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index0,
+  const int *nhi_index0,
+  const int *nlo_index1,
+  const int *nhi_index1,
+  const int *nlo_index2,
+  const int *nhi_index2,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb,
+  const unsigned char *mark_d1,
+  const unsigned char *mark_d2);
 
 /* 2D form: third-order upwind HJ ENO gradient.
  * Replaces src/toolbox/lsm_spatial_derivatives2d.f.in:1416; C declaration src/toolbox/lsm_spatial_derivatives2d.h:445.

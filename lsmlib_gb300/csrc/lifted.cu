@@ -1052,6 +1052,24 @@ void lsm2dhjeno3_(double *phi_x_plus, double *phi_y_plus, const int *ilo_grad_ph
   lsm3dhjeno3_(phi_x_plus, phi_y_plus, L_.junk(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.junk(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, d1, ilo_d1_gb, ihi_d1_gb, jlo_d1_gb, jhi_d1_gb, &L_.k0, &L_.k0, d2, ilo_d2_gb, ihi_d2_gb, jlo_d2_gb, jhi_d2_gb, &L_.k0, &L_.k0, d3, ilo_d3_gb, ihi_d3_gb, jlo_d3_gb, jhi_d3_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dx, dy, dx);
 }
 
+// src/toolbox/lsm_spatial_derivatives2d_local.f.in:498
+void lsm2dhjeno3local_(double *phi_x_plus, double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, double *phi_x_minus, double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const double *phi, const int *ilo_phi_gb, const int *ihi_phi_gb, const int *jlo_phi_gb, const int *jhi_phi_gb, double *d1, const int *ilo_d1_gb, const int *ihi_d1_gb, const int *jlo_d1_gb, const int *jhi_d1_gb, double *d2, const int *ilo_d2_gb, const int *ihi_d2_gb, const int *jlo_d2_gb, const int *jhi_d2_gb, double *d3, const int *ilo_d3_gb, const int *ihi_d3_gb, const int *jlo_d3_gb, const int *jhi_d3_gb, const double *dx, const double *dy, const int *index_x, const int *index_y, const int *nlo_index0, const int *nhi_index0, const int *nlo_index1, const int *nhi_index1, const int *nlo_index2, const int *nhi_index2, const int *nlo_index3, const int *nhi_index3, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb, const unsigned char *mark_d1, const unsigned char *mark_d2, const unsigned char *mark_d3) {
+  Lift L_(2, "lsm2dhjeno3local_");
+  L_.box(ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb);
+  L_.box(ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb);
+  L_.box(ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb);
+  L_.box(ilo_d1_gb, ihi_d1_gb, jlo_d1_gb, jhi_d1_gb);
+  L_.box(ilo_d2_gb, ihi_d2_gb, jlo_d2_gb, jhi_d2_gb);
+  L_.box(ilo_d3_gb, ihi_d3_gb, jlo_d3_gb, jhi_d3_gb);
+  L_.list(nlo_index0, nhi_index0);
+  L_.list(nlo_index1, nhi_index1);
+  L_.list(nlo_index2, nhi_index2);
+  L_.list(nlo_index3, nhi_index3);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3dhjeno3local_(phi_x_plus, phi_y_plus, L_.junk(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.junk(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, d1, ilo_d1_gb, ihi_d1_gb, jlo_d1_gb, jhi_d1_gb, &L_.k0, &L_.k0, d2, ilo_d2_gb, ihi_d2_gb, jlo_d2_gb, jhi_d2_gb, &L_.k0, &L_.k0, d3, ilo_d3_gb, ihi_d3_gb, jlo_d3_gb, jhi_d3_gb, &L_.k0, &L_.k0, dx, dy, dx, index_x, index_y, L_.zero_int(), nlo_index0, nhi_index0, nlo_index1, nhi_index1, nlo_index2, nhi_index2, nlo_index3, nhi_index3, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb, mark_d1, mark_d2, mark_d3);
+}
+
 // src/toolbox/lsm_spatial_derivatives2d.f.in:756
 void lsm2dhjweno5_(double *phi_x_plus, double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, double *phi_x_minus, double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const double *phi, const int *ilo_phi_gb, const int *ihi_phi_gb, const int *jlo_phi_gb, const int *jhi_phi_gb, double *d1, const int *ilo_d1_gb, const int *ihi_d1_gb, const int *jlo_d1_gb, const int *jhi_d1_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const double *dx, const double *dy) {
   Lift L_(2, "lsm2dhjweno5_");
@@ -1428,6 +1446,22 @@ void lsm2dupwindhjeno2_(double *phi_x, double *phi_y, const int *ilo_grad_phi_gb
   L_.box(ilo_fb, ihi_fb, jlo_fb, jhi_fb);
   if (!L_.ready()) return;
   lsm3dupwindhjeno2_(phi_x, phi_y, L_.junk(), ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, vel_x, vel_y, L_.zero(), ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb, &L_.k0, &L_.k0, d1, ilo_d1_gb, ihi_d1_gb, jlo_d1_gb, jhi_d1_gb, &L_.k0, &L_.k0, d2, ilo_d2_gb, ihi_d2_gb, jlo_d2_gb, jhi_d2_gb, &L_.k0, &L_.k0, ilo_fb, ihi_fb, jlo_fb, jhi_fb, &L_.k0, &L_.k0, dx, dy, dx);
+}
+
+// src/toolbox/lsm_spatial_derivatives2d_local.f.in:1160
+void lsm2dupwindhjeno2local_(double *phi_x, double *phi_y, const int *ilo_grad_phi_gb, const int *ihi_grad_phi_gb, const int *jlo_grad_phi_gb, const int *jhi_grad_phi_gb, const double *phi, const int *ilo_phi_gb, const int *ihi_phi_gb, const int *jlo_phi_gb, const int *jhi_phi_gb, const double *vel_x, const double *vel_y, const int *ilo_vel_gb, const int *ihi_vel_gb, const int *jlo_vel_gb, const int *jhi_vel_gb, double *d1, const int *ilo_d1_gb, const int *ihi_d1_gb, const int *jlo_d1_gb, const int *jhi_d1_gb, double *d2, const int *ilo_d2_gb, const int *ihi_d2_gb, const int *jlo_d2_gb, const int *jhi_d2_gb, const double *dx, const double *dy, const int *index_x, const int *index_y, const int *nlo_index0, const int *nhi_index0, const int *nlo_index1, const int *nhi_index1, const int *nlo_index2, const int *nhi_index2, const unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const unsigned char *mark_fb, const unsigned char *mark_d1, const unsigned char *mark_d2) {
+  Lift L_(2, "lsm2dupwindhjeno2local_");
+  L_.box(ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb);
+  L_.box(ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb);
+  L_.box(ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb);
+  L_.box(ilo_d1_gb, ihi_d1_gb, jlo_d1_gb, jhi_d1_gb);
+  L_.box(ilo_d2_gb, ihi_d2_gb, jlo_d2_gb, jhi_d2_gb);
+  L_.list(nlo_index0, nhi_index0);
+  L_.list(nlo_index1, nhi_index1);
+  L_.list(nlo_index2, nhi_index2);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  if (!L_.ready()) return;
+  lsm3dupwindhjeno2local_(phi_x, phi_y, L_.junk(), ilo_grad_phi_gb, ihi_grad_phi_gb, jlo_grad_phi_gb, jhi_grad_phi_gb, &L_.k0, &L_.k0, phi, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, vel_x, vel_y, L_.zero(), ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb, &L_.k0, &L_.k0, d1, ilo_d1_gb, ihi_d1_gb, jlo_d1_gb, jhi_d1_gb, &L_.k0, &L_.k0, d2, ilo_d2_gb, ihi_d2_gb, jlo_d2_gb, jhi_d2_gb, &L_.k0, &L_.k0, dx, dy, dx, index_x, index_y, L_.zero_int(), nlo_index0, nhi_index0, nlo_index1, nhi_index1, nlo_index2, nhi_index2, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb, mark_d1, mark_d2);
 }
 
 // src/toolbox/lsm_spatial_derivatives2d.f.in:1416

@@ -326,6 +326,61 @@ void lsm3dhjeno2local_(PMARGS, R *d1, BOXARG(d1), R *d2, BOXARG(d2), DXP, IDX3, 
   lc.c.finish();
 }
 
+// 3D upwind HJ ENO2 over lists: no 3D original in LSMLIB; follows the 2D
+// lsm2dUpwindHJENO2LOCAL (spatial_derivatives2d_local.f.in:1160-1390): D1
+// over levels 0-2, D2 over 0-1, then on level-0 cells 0 where |vel| <
+// zero_tol, the minus-side ENO2 value where vel > 0, the plus side otherwise
+void lsm3dupwindhjeno2local_(R *phi_x, R *phi_y, R *phi_z, BOXARG(g), const R *phi, BOXARG(f), const R *vel_x,
+                             const R *vel_y, const R *vel_z, BOXARG(v), R *d1, BOXARG(d1), R *d2, BOXARG(d2),
+                             DXP, IDX3, const int *nlo0, const int *nhi0, const int *nlo1, const int *nhi1,
+                             const int *nlo2, const int *nhi2, NBARG, const unsigned char *mark_fb,
+                             const unsigned char *mark_d1, const unsigned char *mark_d2) {
+  LocalCall lc("lsm3dupwindhjeno2local_");
+  (void)nlo1;
+  (void)nlo2;
+  Box gb = BOXOF(g), vb = BOXOF(v);
+  List L = lc.list(index_x, index_y, index_z, *nlo0, *nhi2);
+  Gate gfb = lc.gate(narrow_band, BOXOF(nb), *mark_fb);
+  Gate g1 = gfb, g2 = gfb;
+  g1.mark = (signed char)*mark_d1;
+  g2.mark = (signed char)*mark_d2;
+  PM3 G{lc.inout(phi_x, gb), lc.inout(phi_y, gb), lc.inout(phi_z, gb)};
+  View<const R> F = lc.in(phi, BOXOF(f));
+  const View<const R> V[3] = {lc.in(vel_x, vb), lc.in(vel_y, vb), lc.in(vel_z, vb)};
+  View<R> D1 = lc.inout(d1, BOXOF(d1)), D2 = lc.inout(d2, BOXOF(d2));
+  if (!lc.c.ok()) return;
+  const R inv[3] = {R(1.0) / *dx, R(1.0) / *dy, R(1.0) / *dz};
+  const Box d1b = BOXOF(d1), d2b = BOXOF(d2), fbx = BOXOF(f), outb = isect(gb, vb);
+  for (int d = 0; d < 3; d++) {
+    dn_local(D1, d1b, F, fbx, 1, d, L, *nlo0, *nhi2, g1);
+    View<const R> D1c{D1.p, D1.lo0, D1.lo1, D1.lo2, D1.s1, D1.s2};
+    dn_local(D2, d2b, D1c, d1b, 2, d, L, *nlo0, *nhi1, g2);
+    const R w = inv[d];
+    const View<const R> U = V[d];
+    const View<R> O = d == 0 ? G.x : (d == 1 ? G.y : G.z);
+    const Gate gd = gfb.with(isect(outb, isect(inner_axis(d1b, d, 0, 1), inner_axis(d2b, d, 1, 1))), *mark_fb);
+    for_list(L, *nlo0, *nhi0, [=] __device__(int i, int j, int k) {
+      if (!gd(i, j, k)) return;
+      const R u = U(i, j, k);
+      const long long a = D1.off(i, j, k), b = D2.off(i, j, k);
+      const long long s1 = dstride(D1, d), s2 = dstride(D2, d);
+      const R *q = D2.p;
+      R r;
+      if (fabs(u) < Consts<R>::zero_tol) {
+        r = R(0);
+      } else if (u > R(0)) {
+        const R c = (fabs(q[b - s2]) < fabs(q[b])) ? q[b - s2] : q[b];
+        r = (D1.p[a] + R(0.5) * c) * w;
+      } else {
+        const R c = (fabs(q[b]) < fabs(q[b + s2])) ? q[b] : q[b + s2];
+        r = (D1.p[a + s1] - R(0.5) * c) * w;
+      }
+      O(i, j, k) = r;
+    });
+  }
+  lc.c.finish();
+}
+
 void lsm3dhjeno3local_(PMARGS, R *d1, BOXARG(d1), R *d2, BOXARG(d2), R *d3, BOXARG(d3), DXP, IDX3,
                        const int *nlo0, const int *nhi0, const int *nlo1, const int *nhi1,
                        const int *nlo2, const int *nhi2, const int *nlo3, const int *nhi3, NBARG,

@@ -119,6 +119,7 @@ DESC = {
     "lsm3dhjeno2local_": ("local", "HJ ENO2 plus/minus gradients on level-0 band cells"),
     "lsm3dhjeno3local_": ("local", "HJ ENO3 plus/minus gradients on level-0 band cells"),
     "lsm3dhjweno5local_": ("local", "HJ WENO5 plus/minus gradients on level-0 band cells"),
+    "lsm3dupwindhjeno2local_": ("local", "upwind HJ ENO2 gradient for a velocity field on level-0 band cells"),
     "lsm3dcentralgradorder2local_": ("local", "second-order central gradient on band cells"),
     "lsm3dcentralgradorder4local_": ("local", "fourth-order central gradient on band cells"),
     "lsm3dlaplacianorder2local_": ("local", "second-order Laplacian on band cells"),
@@ -151,6 +152,9 @@ DESC = {
     "lsm3dmaxnormdiffcontrolvolumelocal_": ("local", "max |field1 - field2| over band cells with a negative control volume (starts at 0)"),
     "lsm3dcomputestablenormalveldtcontrolvolumelocal_": ("local", "CFL-stable normal-velocity dt over band cells of one control-volume sign"),
     "lsm3dcomputestableconstnormalveldtlocal_": ("local", "CFL-stable constant normal-velocity dt over band cells (the reference routine reads two unassigned variables; this computes the dense routine's formula)"),
+    # scalar functions
+    "lsmheaviside_": ("calc", "smoothed Heaviside function of one value (evaluated on the calling thread)"),
+    "lsmdeltafunction_": ("calc", "smoothed delta function of one value (evaluated on the calling thread)"),
     # band construction
     "lsm3ddeterminenarrowband_": ("band", "build the narrow band: level-0 list in sweep order, outer lists, BFS levels"),
     "lsm3dmarknarrowbandneighbors_": ("band", "breadth-first neighbour levels of a narrow band"),
@@ -177,7 +181,18 @@ _TAIL_IDX = ([["dx", "real", False, False], ["dy", "real", False, False], ["dz",
               ["index_x", "int", True, False], ["index_y", "int", True, False], ["index_z", "int", True, False]]
              + [[f"{a}_index{l}", "int", False, False] for l in range(4) for a in ("nlo", "nhi")]
              + [["narrow_band", "int1", True, False]] + _box("nb") + [["mark_fb", "int1", False, False]])
+_UP2 = ([["phi_x", "real", True, True], ["phi_y", "real", True, True], ["phi_z", "real", True, True]]
+        + _box("grad_phi") + [["phi", "real", True, False]] + _box("phi")
+        + [["vel_x", "real", True, False], ["vel_y", "real", True, False], ["vel_z", "real", True, False]]
+        + _box("vel") + [["d1", "real", True, True]] + _box("d1") + [["d2", "real", True, True]] + _box("d2")
+        + [["dx", "real", False, False], ["dy", "real", False, False], ["dz", "real", False, False],
+           ["index_x", "int", True, False], ["index_y", "int", True, False], ["index_z", "int", True, False]]
+        + [[f"{a}_index{l}", "int", False, False] for l in range(3) for a in ("nlo", "nhi")]
+        + [["narrow_band", "int1", True, False]] + _box("nb")
+        + [["mark_fb", "int1", False, False], ["mark_d1", "int1", False, False], ["mark_d2", "int1", False, False]])
 NEW_SIGS = {
+    "lsm3dupwindhjeno2local_": {"src": "NEW (pattern: src/toolbox/lsm_spatial_derivatives2d_local.f.in:1160)",
+                                "args": _UP2},
     "lsm3dhjweno5local_": {"src": "NEW (pattern: src/toolbox/lsm_spatial_derivatives2d_local.f.in:816)",
                            "args": _PM + [["d1", "real", True, True]] + _box("d1") + _TAIL_IDX +
                                    [["mark_d1", "int1", False, False]]},
@@ -199,6 +214,7 @@ GROUP_TITLE = {
     "local": "Narrow-band (index-list) variants (*_local)",
     "band": "Narrow-band construction and utilities (src/toolbox/lsm_localization3d)",
     "bc": "Boundary conditions (src/boundary_conditions/lsm_boundary_conditions3d)",
+    "calc": "Smoothed Heaviside and delta functions (src/toolbox/lsm_calculus_toolbox)",
 }
 
 
@@ -406,8 +422,26 @@ def write_header(path, guard, title, syms, abi, desc):
         f.write("\n".join(lines))
 
 
+# LSMLIB's lsm2dHJENO3LOCAL reads index_x / index_y (spatial_derivatives2d_local.f.in:578,
+# :642) but leaves them out of its Fortran argument list (:498-523); its C
+# declaration (spatial_derivatives2d_local.h) passes them after dy, so callers
+# pass them there and the drop-in takes them there.  The Fortran routine cannot
+# be called correctly, so it is no parity target ("ref_unusable").
+SIG_FROM_C_HEADER = {"lsm2dhjeno3local_": ("dy", [["index_x", "int", True, False], ["index_y", "int", True, False]])}
+
+
+def fix_sigs(sigs):
+    for sym, (after, extra) in SIG_FROM_C_HEADER.items():
+        args = sigs[sym]["args"]
+        if not any(a[0] == extra[0][0] for a in args):
+            q = [a[0] for a in args].index(after) + 1
+            sigs[sym]["args"] = args[:q] + extra + args[q:]
+        sigs[sym]["ref_unusable"] = True
+    return sigs
+
+
 def main():
-    sigs = json.load(open(os.path.join(REPO, "oracle", "_ref", "sigs.json")))
+    sigs = fix_sigs(json.load(open(os.path.join(REPO, "oracle", "_ref", "sigs.json"))))
     abi, groups = {}, {}
     for s in DESC:
         if s in NEW_SIGS:
@@ -439,6 +473,8 @@ def main():
         hpath, hline = header_line(s)
         abi[s] = {"ref": f"{os.path.relpath(src, REF)}:{line}",
                   "header": f"{hpath}:{hline}" if hpath else None, "args": sg["args"], "lifted_from": mp["call"]}
+        if sg.get("ref_unusable"):
+            abi[s]["ref_unusable"] = True
         lifted[s] = (dims, mp)
         desc2[s] = "%dD form: %s" % (dims, LIFT_VIA[s][1] if s in LIFT_VIA else DESC[mp["sym3"]][1])
     write_lifted(abi, lifted)

@@ -144,6 +144,48 @@ void lsm3dhjeno2local_(PM_ARGS, real_t *d1, A3(d1), real_t *d2, A3(d2), DX_ARGS,
   }
 }
 
+/* 3D upwind HJ ENO2 on a band.  LSMLIB has no 3D version; this follows the
+ * 2D lsm2dUpwindHJENO2LOCAL (spatial_derivatives2d_local.f.in:1160-1390):
+ * D1 over levels 0-2, D2 over 0-1, then on level-0 cells 0 where
+ * |vel| < zero_tol, the minus-side ENO2 value where vel > 0, the plus side
+ * otherwise. */
+void lsm3dupwindhjeno2local_(real_t *gx, real_t *gy, real_t *gz, A3(g), const real_t *phi, A3(f),
+                             const real_t *vx, const real_t *vy, const real_t *vz, A3(v), real_t *d1,
+                             A3(d1), real_t *d2, A3(d2), DX_ARGS, LIST_ARGS, const int *nlo0,
+                             const int *nhi0, const int *nlo1, const int *nhi1, const int *nlo2,
+                             const int *nhi2, NB_ARGS, const mark_t *mark_fb, const mark_t *mark_d1,
+                             const mark_t *mark_d2) {
+  gbox G = B3(g), F = B3(f), V = B3(v), NB = NBBOX, D1 = B3(d1), D2 = B3(d2);
+  real_t *out[3] = {gx, gy, gz};
+  const real_t *vel[3] = {vx, vy, vz};
+  const real_t inv[3] = {1.0 / *dx, 1.0 / *dy, 1.0 / *dz};
+  (void)nlo1;
+  for (int d = 0; d < 3; d++) {
+    dn_local(d1, &D1, phi, &F, 1, d, ix, iy, iz, *nlo0, *nlo0, *nhi2, nb, &NB, *mark_d1);
+    dn_local(d2, &D2, d1, &D1, 2, d, ix, iy, iz, *nlo0, *nlo0, *nhi1, nb, &NB, *mark_d2);
+    FOR_LIST(*nlo0, *nlo0, *nhi0) {
+      if (!inb(&G, i, j, k) || !inb(&V, i, j, k) || !inb(&NB, i, j, k) ||
+          !inb_axis(&D1, d, 0, 1, i, j, k) || !inb_axis(&D2, d, 1, 1, i, j, k))
+        continue;
+      if (nb[at(&NB, i, j, k)] > *mark_fb) continue;
+      real_t u = vel[d][at(&V, i, j, k)];
+      long a = at(&D1, i, j, k), b = at(&D2, i, j, k);
+      long s1 = sh(&D1, d, 1), s2 = sh(&D2, d, 1);
+      real_t r;
+      if (fabs(u) < ORACLE_ZERO_TOL) {
+        r = 0.0;
+      } else if (u > 0.0) {
+        real_t c = (fabs(d2[b - s2]) < fabs(d2[b])) ? d2[b - s2] : d2[b];
+        r = (d1[a] + 0.5 * c) * inv[d];
+      } else {
+        real_t c = (fabs(d2[b]) < fabs(d2[b + s2])) ? d2[b] : d2[b + s2];
+        r = (d1[a + s1] - 0.5 * c) * inv[d];
+      }
+      out[d][at(&G, i, j, k)] = r;
+    }
+  }
+}
+
 /* 3D HJ ENO3 on a band.  LSMLIB has no 3D version; this follows the 2D
  * lsm2dHJENO3LOCAL (spatial_derivatives2d_local.f.in:498-813): D1 over levels
  * 0-3, D2 over 0-2, D3 over 0-1, then the dense ENO3 selection

@@ -28,7 +28,7 @@ LOCAL = [s for s in L.ABI if s.startswith("lsm3d") and any(a[0] == "index_x" for
 # the oracle implements the dense formula and is pinned against it below
 REF_UNDEFINED = {"lsm3dcomputestableconstnormalveldtlocal_"}
 BC = [s for s in L.ABI if s.startswith("lsm3d") and ("extrapolation" in s or "neumann" in s)]
-NEW_3D = {"lsm3dhjeno3local_", "lsm3dhjweno5local_"}
+NEW_3D = {"lsm3dhjeno3local_", "lsm3dhjweno5local_", "lsm3dupwindhjeno2local_"}
 
 
 def band_phi(seed, gb=GB):
@@ -179,6 +179,58 @@ def test_new_3d_local_weno5_matches_dense_on_band():
             assert abs(a[nm][c] - b[nm][c]) <= 1e-12 * max(1.0, abs(b[nm][c]))
         checked += 1
     assert checked > 50
+
+
+# (list routine, dense routine, outputs, [(offsets along each axis, largest
+# narrow_band value they may hold)]): where every such neighbour holds a
+# computed difference, the list routine's result is the dense one's, bit for
+# bit.  ENO3 reads D3 (levels 0-1) at c-1..c+2, which reads D2 (levels 0-2)
+# at c-2..c+2, which reads D1 (levels 0-3) at c-2..c+3; upwind ENO2 reads D2
+# (levels 0-1) at c-1..c+1 and D1 (levels 0-2) at c-1..c+2.
+NEW_VS_DENSE = [
+    ("lsm3dhjeno3local_", "lsm3dhjeno3_",
+     ("phi_x_plus", "phi_y_minus", "phi_z_plus", "phi_x_minus", "phi_y_plus", "phi_z_minus"),
+     [(range(-2, 4), 4), (range(-2, 3), 3), (range(-1, 3), 2)]),
+    ("lsm3dupwindhjeno2local_", "lsm3dupwindhjeno2_", ("phi_x", "phi_y", "phi_z"),
+     [(range(-1, 3), 3), (range(-1, 2), 2)]),
+]
+
+
+@pytest.mark.parametrize("sym,dense_sym,outs,reach", NEW_VS_DENSE)
+def test_new_3d_local_matches_dense_on_band(sym, dense_sym, outs, reach):
+    """3D list routines LSMLIB lacks (they follow its 2D list routines) equal
+    LSMLIB's dense 3D routine on level-0 cells whose differences are all
+    computed from phi."""
+    vals = local_case(sym, 0)
+    a, _ = H.run(H.oracle(), sym, vals)
+    dense = H.dense_case(dense_sym, seed=0, gb=GB, fb=FB)
+    for k in ("phi", "vel_x", "vel_y", "vel_z", "dx", "dy", "dz"):
+        if k in dense and k in vals:
+            dense[k] = vals[k]
+    b, _ = H.run(H.oracle(), dense_sym, dense)
+    ix, iy, iz, nb = vals["index_x"], vals["index_y"], vals["index_z"], vals["narrow_band"]
+    checked = 0
+    for l in range(vals["nlo_index0"], vals["nhi_index0"] + 1):
+        i, j, k = ix[l], iy[l], iz[l]
+        if not (FB[0] <= i <= FB[1] and FB[2] <= j <= FB[3] and FB[4] <= k <= FB[5]):
+            continue
+        c = (i - GB[0], j - GB[2], k - GB[4])
+        if nb[c] > 1:
+            continue
+        ok = True
+        for offs, top in reach:
+            for d in range(3):
+                for o in offs:
+                    q = list(c)
+                    q[d] += o
+                    if not (0 <= q[d] < nb.shape[d]) or not (1 <= nb[tuple(q)] <= top):
+                        ok = False
+        if not ok:
+            continue
+        for nm in outs:
+            assert H.same(a[nm][c], b[nm][c]), (sym, nm, c, a[nm][c], b[nm][c])
+        checked += 1
+    assert checked > 30, checked
 
 
 @pytest.mark.parametrize("seed", [0, 1, 2])
