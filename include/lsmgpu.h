@@ -324,6 +324,36 @@ void lsmgpu_distance_for_subcell_fix_full_central(
     const int *ilo_fb, const int *ihi_fb, const int *jlo_fb, const int *jhi_fb, const int *klo_fb,
     const int *khi_fb, const double *dx, const double *dy, const double *dz);
 
+/* lsmgpu_external_normal_vel_term_fill_box: the combined external and normal
+ * velocity term of lsm3dAddExternalAndNormalVelTermToLSERHS
+ * (src/toolbox/lsm_level_set_evolution3d.f.in:532), same arguments, in the
+ * form of lsm2dAddExternalAndNormalVelTermToLSERHS
+ * (lsm_level_set_evolution2d.f.in:399): over the fill box only, and nothing
+ * added where |Vn| < zero_tol (the 3D routine loops from the fill box to the
+ * ghost box end and adds the advection part there).
+ *
+ * lsmgpu_signed_linear_extrapolation_inner_sign: lsm3dSignedLinearExtrapolation
+ * (src/boundary_conditions/lsm_boundary_conditions3d.f) with the slope's
+ * sign taken from the cell next to the edge, as
+ * lsm1dSignedLinearExtrapolation does (lsm_boundary_conditions1d.f:103). */
+void lsmgpu_external_normal_vel_term_fill_box(
+    double *lse_rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb,
+    const int *jhi_rhs_gb, const int *klo_rhs_gb, const int *khi_rhs_gb, const double *phi_x_plus,
+    const double *phi_y_plus, const double *phi_z_plus, const int *ilo_grad_phi_plus_gb,
+    const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb,
+    const int *klo_grad_phi_plus_gb, const int *khi_grad_phi_plus_gb, const double *phi_x_minus,
+    const double *phi_y_minus, const double *phi_z_minus, const int *ilo_grad_phi_minus_gb,
+    const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb,
+    const int *klo_grad_phi_minus_gb, const int *khi_grad_phi_minus_gb, const double *vel_n,
+    const double *vel_x, const double *vel_y, const double *vel_z, const int *ilo_vel_gb,
+    const int *ihi_vel_gb, const int *jlo_vel_gb, const int *jhi_vel_gb, const int *klo_vel_gb,
+    const int *khi_vel_gb, const int *ilo_rhs_fb, const int *ihi_rhs_fb, const int *jlo_rhs_fb,
+    const int *jhi_rhs_fb, const int *klo_rhs_fb, const int *khi_rhs_fb);
+void lsmgpu_signed_linear_extrapolation_inner_sign(
+    double *phi, const int *ilo_gb, const int *ihi_gb, const int *jlo_gb, const int *jhi_gb,
+    const int *klo_gb, const int *khi_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb,
+    const int *jhi_fb, const int *klo_fb, const int *khi_fb, const int *bdry_location_idx);
+
 /* Library version string. */
 const char *lsmgpu_version(void);
 

@@ -161,6 +161,48 @@ void lsm1dcomputestableadvectiondtcontrolvolume_(
   const double *dx,
   const double *cfl_number);
 
+/* 1D form: CFL-stable dt for a normal velocity: max |vel_n| / dx.
+ * Replaces src/toolbox/lsm_math_utils1d.f.in:157; C declaration src/toolbox/lsm_math_utils1d.h:136.
+ */
+void lsm1dcomputestablenormalveldt_(
+  double *dt,
+  const double *vel_n,
+  const int *ilo_vel_gb,
+  const int *ihi_vel_gb,
+  const double *phi_x_plus,
+  const int *ilo_grad_phi_plus_gb,
+  const int *ihi_grad_phi_plus_gb,
+  const double *phi_x_minus,
+  const int *ilo_grad_phi_minus_gb,
+  const int *ihi_grad_phi_minus_gb,
+  const int *ilo_ib,
+  const int *ihi_ib,
+  const double *dx,
+  const double *cfl_number);
+
+/* 1D form: CFL-stable dt for a normal velocity over cells of one control-volume sign.
+ * Replaces src/toolbox/lsm_math_utils1d.f.in:633; C declaration src/toolbox/lsm_math_utils1d.h:355.
+ */
+void lsm1dcomputestablenormalveldtcontrolvolume_(
+  double *dt,
+  const double *vel_n,
+  const int *ilo_vel_gb,
+  const int *ihi_vel_gb,
+  const double *phi_x_plus,
+  const int *ilo_grad_phi_plus_gb,
+  const int *ihi_grad_phi_plus_gb,
+  const double *phi_x_minus,
+  const int *ilo_grad_phi_minus_gb,
+  const int *ihi_grad_phi_minus_gb,
+  const double *control_vol,
+  const int *ilo_control_vol_gb,
+  const int *ihi_control_vol_gb,
+  const int *control_vol_sgn,
+  const int *ilo_ib,
+  const int *ihi_ib,
+  const double *dx,
+  const double *cfl_number);
+
 /* 1D form: copy extrapolation into the ghost cells of one face.
  * Replaces src/boundary_conditions/lsm_boundary_conditions1d.f:169; C declaration src/boundary_conditions/lsm_boundary_conditions1d.h:123.
  */
@@ -397,6 +439,17 @@ void lsm1drk1step_(
   const int *ilo_fb,
   const int *ihi_fb,
   const double *dt);
+
+/* 1D form: signed linear extrapolation, sign from the cell next to the edge.
+ * Replaces src/boundary_conditions/lsm_boundary_conditions1d.f:103; C declaration src/boundary_conditions/lsm_boundary_conditions1d.h:103.
+ */
+void lsm1dsignedlinearextrapolation_(
+  double *phi,
+  const int *ilo_gb,
+  const int *ihi_gb,
+  const int *ilo_fb,
+  const int *ihi_fb,
+  const int *bdry_location_idx);
 
 /* 1D form: integral of F over {phi = 0} with a smoothed delta.
  * Replaces src/toolbox/lsm_math_utils1d.f.in:390; C declaration src/toolbox/lsm_math_utils1d.h:238.

@@ -250,6 +250,39 @@ void lsm2daddconstprecomputedcurvtermtolserhslocal_(
   const int *jhi_nb_gb,
   const unsigned char *mark_fb);
 
+/* 2D form: rhs -= u . grad(phi) + Vn |grad phi| over the fill box, combined Godunov upwinding.
+ * Replaces src/toolbox/lsm_level_set_evolution2d.f.in:399; C declaration src/toolbox/lsm_level_set_evolution2d.h:341.
+ */
+void lsm2daddexternalandnormalveltermtolserhs_(
+  double *lse_rhs,
+  const int *ilo_rhs_gb,
+  const int *ihi_rhs_gb,
+  const int *jlo_rhs_gb,
+  const int *jhi_rhs_gb,
+  const double *phi_x_plus,
+  const double *phi_y_plus,
+  const int *ilo_grad_phi_plus_gb,
+  const int *ihi_grad_phi_plus_gb,
+  const int *jlo_grad_phi_plus_gb,
+  const int *jhi_grad_phi_plus_gb,
+  const double *phi_x_minus,
+  const double *phi_y_minus,
+  const int *ilo_grad_phi_minus_gb,
+  const int *ihi_grad_phi_minus_gb,
+  const int *jlo_grad_phi_minus_gb,
+  const int *jhi_grad_phi_minus_gb,
+  const double *vel_n,
+  const double *vel_x,
+  const double *vel_y,
+  const int *ilo_vel_gb,
+  const int *ihi_vel_gb,
+  const int *jlo_vel_gb,
+  const int *jhi_vel_gb,
+  const int *ilo_rhs_fb,
+  const int *ihi_rhs_fb,
+  const int *jlo_rhs_fb,
+  const int *jhi_rhs_fb);
+
 /* 2D form: external plus normal velocity term with the combined Godunov upwinding on band cells.
  * Replaces src/toolbox/lsm_level_set_evolution2d_local.f.in:474; C declaration src/toolbox/lsm_level_set_evolution2d_local.h:414.
  */

@@ -30,7 +30,9 @@ View<const R> vin(Call &c, const R *p, const Box &b) { return view((const R *)c.
 View<R> vio(Call &c, R *p, const Box &b) { return view(c.inout(p, b.size()), b); }
 
 // boundary conditions (boundary_conditions3d.f:46-639)
-enum { BC_LINEAR, BC_SIGNED, BC_COPY };
+// BC_SIGNED_INNER: the 1D routine's form, the sign taken from the cell next
+// to the edge (boundary_conditions1d.f:103-140) instead of the edge cell
+enum { BC_LINEAR, BC_SIGNED, BC_COPY, BC_SIGNED_INNER };
 
 void face_extrapolate(const char *name, R *phi, const Box &gb, const Box &fb, int face, int kind) {
   Call call(name);
@@ -56,7 +58,7 @@ void face_extrapolate(const char *name, R *phi, const Box &gb, const Box &fb, in
     if (kind != BC_COPY) {
       c[axis] = inner;
       const R nx = P(c[0], c[1], c[2]);
-      slope = (kind == BC_LINEAR) ? e - nx : copysign(R(1.0), e) * fabs(e - nx);
+      slope = (kind == BC_LINEAR) ? e - nx : copysign(R(1.0), kind == BC_SIGNED_INNER ? nx : e) * fabs(e - nx);
     }
     for (int m = first; m <= last; m++) {
       c[axis] = m;
@@ -121,6 +123,51 @@ void subcell_distance_dense(const char *name, R *distance0, const R *phi0, const
   for_box(fb, [=] __device__(int i, int j, int k) {
     const long long st[3] = {1, P0.s1, P0.s2};
     D(i, j, k) = subcell_distance<R, HALF>(P0.p + P0.off(i, j, k), st, flag);
+  });
+  call.finish();
+}
+
+// rhs -= u . grad(phi) + Vn |grad phi| with the combined Godunov selection
+// (level_set_evolution3d.f.in:532-718).  FILL_BOX = false: the 3D routine's
+// loop (k, j from the fill box to the ghost box end, i over the ghost box,
+// :620) and its branches (the advection part alone where |Vn| or |grad phi|^2
+// is below zero_tol); FILL_BOX = true: the 2D routine's form
+// (level_set_evolution2d.f.in:399-520): the fill box, and nothing added where
+// |Vn| < zero_tol
+template <bool FILL_BOX>
+void external_normal(const char *name, R *lse_rhs, const Box &rb, const R *phi_x_plus, const R *phi_y_plus,
+                     const R *phi_z_plus, const Box &pb, const R *phi_x_minus, const R *phi_y_minus,
+                     const R *phi_z_minus, const Box &mb, const R *vel_n, const R *vel_x, const R *vel_y,
+                     const R *vel_z, const Box &vb, const Box &fb) {
+  Call call(name);
+  Box loop = fb;
+  if (!FILL_BOX) {
+    loop = rb;
+    loop.lo[1] = fb.lo[1];
+    loop.lo[2] = fb.lo[2];
+  }
+  if (!rb.contains(loop, 0, 0, 0) || !pb.contains(loop, 0, 0, 0) || !mb.contains(loop, 0, 0, 0) ||
+      !vb.contains(loop, 0, 0, 0))
+    call.fail("ghost box does not cover the loop range");
+  if (!call.ok() || loop.empty()) return;
+  View<R> O = vio(call, lse_rhs, rb);
+  View<const R> XP = vin(call, phi_x_plus, pb), YP = vin(call, phi_y_plus, pb), ZP = vin(call, phi_z_plus, pb);
+  View<const R> XM = vin(call, phi_x_minus, mb), YM = vin(call, phi_y_minus, mb), ZM = vin(call, phi_z_minus, mb);
+  View<const R> VN = vin(call, vel_n, vb), VX = vin(call, vel_x, vb), VY = vin(call, vel_y, vb), VZ = vin(call, vel_z, vb);
+  if (!call.ok()) return;
+  for_box(loop, [=] __device__(int i, int j, int k) {
+    const R w = VN(i, j, k), ux = VX(i, j, k), uy = VY(i, j, k), uz = VZ(i, j, k);
+    const R gx = ext_pick<R>(ux, w, XP(i, j, k), XM(i, j, k));
+    const R gy = ext_pick<R>(uy, w, YP(i, j, k), YM(i, j, k));
+    const R gz = ext_pick<R>(uz, w, ZP(i, j, k), ZM(i, j, k));
+    const R n2 = gx * gx + gy * gy + gz * gz;
+    if (FILL_BOX) {
+      if (fabs(w) >= Consts<R>::zero_tol) O(i, j, k) = O(i, j, k) - ux * gx - uy * gy - uz * gz - w * sqrt(n2);
+    } else if (fabs(w) >= Consts<R>::zero_tol && n2 >= Consts<R>::zero_tol) {
+      O(i, j, k) = O(i, j, k) - ux * gx - uy * gy - uz * gz - w * sqrt(n2);
+    } else {
+      O(i, j, k) = O(i, j, k) - ux * gx - uy * gy - uz * gz;
+    }
   });
   call.finish();
 }
@@ -230,36 +277,19 @@ void lsm3daddconstprecomputedcurvtermtolserhs_(R *lse_rhs, BOXARG(r), const R *k
   call.finish();
 }
 
-void lsm3daddexternalandnormalveltermtolserhs_(R *lse_rhs, BOXARG(r), const R *phi_x_plus, const R *phi_y_plus,
-                                               const R *phi_z_plus, BOXARG(p), const R *phi_x_minus,
-                                               const R *phi_y_minus, const R *phi_z_minus, BOXARG(m),
-                                               const R *vel_n, const R *vel_x, const R *vel_y, const R *vel_z,
-                                               BOXARG(v), BOXARG(fb)) {
-  Call call("lsm3daddexternalandnormalveltermtolserhs_");
-  Box rb = BOXOF(r), pb = BOXOF(p), mb = BOXOF(m), vb = BOXOF(v), fb = BOXOF(fb);
-  Box loop = rb;
-  loop.lo[1] = fb.lo[1];
-  loop.lo[2] = fb.lo[2];
-  if (!pb.contains(loop, 0, 0, 0) || !mb.contains(loop, 0, 0, 0) || !vb.contains(loop, 0, 0, 0))
-    call.fail("ghost box does not cover the loop range");
-  if (!call.ok() || loop.empty()) return;
-  View<R> O = vio(call, lse_rhs, rb);
-  View<const R> XP = vin(call, phi_x_plus, pb), YP = vin(call, phi_y_plus, pb), ZP = vin(call, phi_z_plus, pb);
-  View<const R> XM = vin(call, phi_x_minus, mb), YM = vin(call, phi_y_minus, mb), ZM = vin(call, phi_z_minus, mb);
-  View<const R> VN = vin(call, vel_n, vb), VX = vin(call, vel_x, vb), VY = vin(call, vel_y, vb), VZ = vin(call, vel_z, vb);
-  if (!call.ok()) return;
-  for_box(loop, [=] __device__(int i, int j, int k) {
-    const R w = VN(i, j, k), ux = VX(i, j, k), uy = VY(i, j, k), uz = VZ(i, j, k);
-    const R gx = ext_pick<R>(ux, w, XP(i, j, k), XM(i, j, k));
-    const R gy = ext_pick<R>(uy, w, YP(i, j, k), YM(i, j, k));
-    const R gz = ext_pick<R>(uz, w, ZP(i, j, k), ZM(i, j, k));
-    const R n2 = gx * gx + gy * gy + gz * gz;
-    if (fabs(w) >= Consts<R>::zero_tol && n2 >= Consts<R>::zero_tol)
-      O(i, j, k) = O(i, j, k) - ux * gx - uy * gy - uz * gz - w * sqrt(n2);
-    else
-      O(i, j, k) = O(i, j, k) - ux * gx - uy * gy - uz * gz;
-  });
-  call.finish();
+#define EXT_ARGS                                                                                          \
+  R *lse_rhs, BOXARG(r), const R *phi_x_plus, const R *phi_y_plus, const R *phi_z_plus, BOXARG(p),        \
+      const R *phi_x_minus, const R *phi_y_minus, const R *phi_z_minus, BOXARG(m), const R *vel_n,         \
+      const R *vel_x, const R *vel_y, const R *vel_z, BOXARG(v), BOXARG(fb)
+#define EXT_PASS                                                                                          \
+  lse_rhs, BOXOF(r), phi_x_plus, phi_y_plus, phi_z_plus, BOXOF(p), phi_x_minus, phi_y_minus, phi_z_minus, \
+      BOXOF(m), vel_n, vel_x, vel_y, vel_z, BOXOF(v), BOXOF(fb)
+
+void lsm3daddexternalandnormalveltermtolserhs_(EXT_ARGS) {
+  external_normal<false>("lsm3daddexternalandnormalveltermtolserhs_", EXT_PASS);
+}
+void lsmgpu_external_normal_vel_term_fill_box(EXT_ARGS) {
+  external_normal<true>("lsmgpu_external_normal_vel_term_fill_box", EXT_PASS);
 }
 
 #define BCARGS R *phi, BOXARG(g), BOXARG(fb), const int *bdry_location_idx
@@ -268,6 +298,10 @@ void lsm3dlinearextrapolation_(BCARGS) {
 }
 void lsm3dsignedlinearextrapolation_(BCARGS) {
   face_extrapolate("lsm3dsignedlinearextrapolation_", phi, BOXOF(g), BOXOF(fb), *bdry_location_idx, BC_SIGNED);
+}
+void lsmgpu_signed_linear_extrapolation_inner_sign(BCARGS) {
+  face_extrapolate("lsmgpu_signed_linear_extrapolation_inner_sign", phi, BOXOF(g), BOXOF(fb), *bdry_location_idx,
+                   BC_SIGNED_INNER);
 }
 void lsm3dcopyextrapolation_(BCARGS) {
   face_extrapolate("lsm3dcopyextrapolation_", phi, BOXOF(g), BOXOF(fb), *bdry_location_idx, BC_COPY);

@@ -268,6 +268,15 @@ void lsm1drk1step_(double *u_next, const int *ilo_u_next_gb, const int *ihi_u_ne
   lsm3drk1step_(u_next, ilo_u_next_gb, ihi_u_next_gb, &L_.k0, &L_.k0, &L_.k0, &L_.k0, u_cur, ilo_u_cur_gb, ihi_u_cur_gb, &L_.k0, &L_.k0, &L_.k0, &L_.k0, rhs, ilo_rhs_gb, ihi_rhs_gb, &L_.k0, &L_.k0, &L_.k0, &L_.k0, ilo_fb, ihi_fb, &L_.k0, &L_.k0, &L_.k0, &L_.k0, dt);
 }
 
+// src/boundary_conditions/lsm_boundary_conditions1d.f:103
+void lsm1dsignedlinearextrapolation_(double *phi, const int *ilo_gb, const int *ihi_gb, const int *ilo_fb, const int *ihi_fb, const int *bdry_location_idx) {
+  Lift L_(1, "lsm1dsignedlinearextrapolation_");
+  L_.box(ilo_gb, ihi_gb);
+  L_.box(ilo_fb, ihi_fb);
+  if (!L_.ready()) return;
+  lsmgpu_signed_linear_extrapolation_inner_sign(phi, ilo_gb, ihi_gb, &L_.k0, &L_.k0, &L_.k0, &L_.k0, ilo_fb, ihi_fb, &L_.k0, &L_.k0, &L_.k0, &L_.k0, bdry_location_idx);
+}
+
 // src/toolbox/lsm_math_utils1d.f.in:390
 void lsm1dsurfaceintegral_(double *int_f, const double *f, const int *ilo_f_gb, const int *ihi_f_gb, const double *phi, const int *ilo_phi_gb, const int *ihi_phi_gb, const double *phi_x, const int *ilo_grad_phi_gb, const int *ihi_grad_phi_gb, const int *ilo_ib, const int *ihi_ib, const double *dx, const double *epsilon) {
   Lift L_(1, "lsm1dsurfaceintegral_");
@@ -540,6 +549,18 @@ void lsm2daddconstprecomputedcurvtermtolserhslocal_(double *lse_rhs, const int *
   L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
   if (!L_.ready()) return;
   lsm3daddconstprecomputedcurvtermtolserhslocal_(lse_rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, kappa, ilo_kappa_gb, ihi_kappa_gb, jlo_kappa_gb, jhi_kappa_gb, &L_.k0, &L_.k0, grad_phi_mag, ilo_phi_gb, ihi_phi_gb, jlo_phi_gb, jhi_phi_gb, &L_.k0, &L_.k0, b, index_x, index_y, L_.zero_int(), nlo_index, nhi_index, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, mark_fb);
+}
+
+// src/toolbox/lsm_level_set_evolution2d.f.in:399
+void lsm2daddexternalandnormalveltermtolserhs_(double *lse_rhs, const int *ilo_rhs_gb, const int *ihi_rhs_gb, const int *jlo_rhs_gb, const int *jhi_rhs_gb, const double *phi_x_plus, const double *phi_y_plus, const int *ilo_grad_phi_plus_gb, const int *ihi_grad_phi_plus_gb, const int *jlo_grad_phi_plus_gb, const int *jhi_grad_phi_plus_gb, const double *phi_x_minus, const double *phi_y_minus, const int *ilo_grad_phi_minus_gb, const int *ihi_grad_phi_minus_gb, const int *jlo_grad_phi_minus_gb, const int *jhi_grad_phi_minus_gb, const double *vel_n, const double *vel_x, const double *vel_y, const int *ilo_vel_gb, const int *ihi_vel_gb, const int *jlo_vel_gb, const int *jhi_vel_gb, const int *ilo_rhs_fb, const int *ihi_rhs_fb, const int *jlo_rhs_fb, const int *jhi_rhs_fb) {
+  Lift L_(2, "lsm2daddexternalandnormalveltermtolserhs_");
+  L_.box(ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb);
+  L_.box(ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb);
+  L_.box(ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb);
+  L_.box(ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb);
+  L_.box(ilo_rhs_fb, ihi_rhs_fb, jlo_rhs_fb, jhi_rhs_fb);
+  if (!L_.ready()) return;
+  lsmgpu_external_normal_vel_term_fill_box(lse_rhs, ilo_rhs_gb, ihi_rhs_gb, jlo_rhs_gb, jhi_rhs_gb, &L_.k0, &L_.k0, phi_x_plus, phi_y_plus, L_.zero(), ilo_grad_phi_plus_gb, ihi_grad_phi_plus_gb, jlo_grad_phi_plus_gb, jhi_grad_phi_plus_gb, &L_.k0, &L_.k0, phi_x_minus, phi_y_minus, L_.zero(), ilo_grad_phi_minus_gb, ihi_grad_phi_minus_gb, jlo_grad_phi_minus_gb, jhi_grad_phi_minus_gb, &L_.k0, &L_.k0, vel_n, vel_x, vel_y, L_.zero(), ilo_vel_gb, ihi_vel_gb, jlo_vel_gb, jhi_vel_gb, &L_.k0, &L_.k0, ilo_rhs_fb, ihi_rhs_fb, jlo_rhs_fb, jhi_rhs_fb, &L_.k0, &L_.k0);
 }
 
 // src/toolbox/lsm_level_set_evolution2d_local.f.in:474

@@ -250,14 +250,9 @@ def ctype(kind, is_arr, written):
 BOUND = re.compile(r"^(ilo|ihi|jlo|jhi|klo|khi)_")
 
 # 2D / 1D routines whose arithmetic or loop bounds are not the 3D routine's
-# with the missing terms removed: the 1D normal-velocity dt is |vn| / dx
-# (math_utils1d.f.in); the 2D external-plus-normal velocity term loops over
-# the fill box where the 3D routine loops from the fill box to the ghost box
-# end (level_set_evolution3d.f.in:620); the 1D signed extrapolation takes the
-# sign from the second fill-box cell (boundary_conditions1d.f), the 3D one
-# from the first.
-NOT_LIFTED = {"lsm1dcomputestablenormalveldt_", "lsm1dcomputestablenormalveldtcontrolvolume_",
-              "lsm2daddexternalandnormalveltermtolserhs_", "lsm1dsignedlinearextrapolation_"}
+# with the missing terms removed and that no other routine covers (none at
+# present; see LIFT_VIA and HAND_LIFTED).
+NOT_LIFTED = set()
 
 # 2D / 1D routines lifted onto a library entry point other than the 3D
 # routine of the same name, which has the same argument list: the 3D
@@ -276,7 +271,28 @@ LIFT_VIA = {"lsm2dcomputemeancurvatureorder4local_": ("lsmgpu_mean_curvature_ord
                 "lsmgpu_orthogonalization_rhs_unit_sgn_smoothing_local",
                 "orthogonalization RHS on band cells (sgn(psi) smoothed with max(dx)^2)"),
             "lsm2dcomputedistanceforsubcellfix_": ("lsmgpu_distance_for_subcell_fix_full_central",
-                                                   "distance estimate for the subcell fix (2 phi0 / delta)")}
+                                                   "distance estimate for the subcell fix (2 phi0 / delta)"),
+            # the 2D external + normal velocity term loops over the fill box
+            # and adds nothing where |Vn| < zero_tol (level_set_evolution2d.f.in:399);
+            # the 3D one loops from the fill box to the ghost box end
+            # (level_set_evolution3d.f.in:620) and adds the advection part there
+            "lsm2daddexternalandnormalveltermtolserhs_": (
+                "lsmgpu_external_normal_vel_term_fill_box",
+                "rhs -= u . grad(phi) + Vn |grad phi| over the fill box, combined Godunov upwinding"),
+            # the 1D signed extrapolation takes the sign from the cell next to
+            # the edge (boundary_conditions1d.f:103), the 3D one from the edge
+            "lsm1dsignedlinearextrapolation_": ("lsmgpu_signed_linear_extrapolation_inner_sign",
+                                                "signed linear extrapolation, sign from the cell next to the edge")}
+
+# 1D routines written by hand in csrc/lifted_by_hand.cu: their arguments do
+# not map by name onto the 3D routine they run on (the 1D normal-velocity dt
+# reads only |vel_n| / dx, math_utils1d.f.in:157, :633: the 3D advection dt
+# with vel_x = vel_n)
+HAND_LIFTED = {"lsm1dcomputestablenormalveldt_": ("lsm3dcomputestableadvectiondt_",
+                                                  "CFL-stable dt for a normal velocity: max |vel_n| / dx"),
+               "lsm1dcomputestablenormalveldtcontrolvolume_": (
+                   "lsm3dcomputestableadvectiondtcontrolvolume_",
+                   "CFL-stable dt for a normal velocity over cells of one control-volume sign")}
 
 # 3D routines whose dz (and dy) multiply a cell volume: lifted with 1 there
 VOLUME_FACTOR = re.compile(r"volumeintegral|volumeregion|surfaceintegral|surfacearea")
@@ -477,7 +493,15 @@ def main():
             abi[s]["ref_unusable"] = True
         lifted[s] = (dims, mp)
         desc2[s] = "%dD form: %s" % (dims, LIFT_VIA[s][1] if s in LIFT_VIA else DESC[mp["sym3"]][1])
-    write_lifted(abi, lifted)
+    for s, (sym3, text) in HAND_LIFTED.items():
+        sg = sigs[s]
+        src, line = sg["src"].split(":")
+        hpath, hline = header_line(s)
+        abi[s] = {"ref": f"{os.path.relpath(src, REF)}:{line}", "header": f"{hpath}:{hline}" if hpath else None,
+                  "args": sg["args"], "lifted_from": sym3, "by_hand": True}
+        lifted[s] = (1 if s.startswith("lsm1d") else 2, None)
+        desc2[s] = "%dD form: %s" % (lifted[s][0], text)
+    write_lifted(abi, {s: v for s, v in lifted.items() if v[1] is not None})
     for dims in (2, 1):
         syms = [s for s in lifted if lifted[s][0] == dims]
         write_header(os.path.join(REPO, "include", "lsmgpu_toolbox%dd.h" % dims), "LSMGPU_TOOLBOX%dD_H" % dims,

@@ -7,7 +7,11 @@
  *    index-list forms (curvature3d_local.f.in:151-574);
  *  - lsm3dAddConstPrecomputedCurvTermToLSERHSLOCAL and
  *    lsm3dAddExternalAndNormalVelTermToLSERHSLOCAL
- *    (level_set_evolution3d_local.f.in:530-812).
+ *    (level_set_evolution3d_local.f.in:530-812);
+ *  - the external + normal velocity term in the form of the 2D routine
+ *    (level_set_evolution2d.f.in:399-520: fill box only, nothing added where
+ *    |Vn| < zero_tol) on 3D arrays, the library's
+ *    lsmgpu_external_normal_vel_term_fill_box.
  * The reference's MeanCurvatureOrder4 list routine evaluates the Gaussian
  * formula (curvature3d_local.f.in:385-410); so does this restatement.
  */
@@ -176,5 +180,21 @@ void lsm3daddexternalandnormalveltermtolserhslocal_(real_t *rhs, A3(r), const re
       rhs[r] = rhs[r] - ux * gx - uy * gy - uz * gz - w * sqrt(n2);
     else
       rhs[r] = rhs[r] - ux * gx - uy * gy - uz * gz;
+  }
+}
+
+void lsmgpu_external_normal_vel_term_fill_box(real_t *rhs, A3(r), const real_t *pxp, const real_t *pyp,
+                                              const real_t *pzp, A3(p), const real_t *pxm, const real_t *pym,
+                                              const real_t *pzm, A3(m), const real_t *vn, const real_t *vx,
+                                              const real_t *vy, const real_t *vz, A3(v), A3(fb)) {
+  gbox R = B3(r), P = B3(p), M = B3(m), V = B3(v);
+  FOR_BOX(*fb_ilo, *fb_ihi, *fb_jlo, *fb_jhi, *fb_klo, *fb_khi) {
+    long a = at(&P, i, j, k), b = at(&M, i, j, k), c = at(&V, i, j, k), r = at(&R, i, j, k);
+    real_t w = vn[c];
+    if (!(fabs(w) >= ORACLE_ZERO_TOL)) continue;
+    real_t gx = godunov_ext(vx[c], w, pxp[a], pxm[b]);
+    real_t gy = godunov_ext(vy[c], w, pyp[a], pym[b]);
+    real_t gz = godunov_ext(vz[c], w, pzp[a], pzm[b]);
+    rhs[r] = rhs[r] - vx[c] * gx - vy[c] * gy - vz[c] * gz - w * sqrt(gx * gx + gy * gy + gz * gz);
   }
 }

@@ -157,7 +157,37 @@ def test_every_lifted_routine_has_a_reference_routine(ref):
 
 # ---- CPU: the 3D oracle on data copied along the missing axes ---------------------------
 
-DENSE = [s for s in LIFTED if not is_local(s) and not is_bc(s)]
+DENSE = [s for s in LIFTED if not is_local(s) and not is_bc(s) and not L.ABI[s].get("by_hand")]
+BY_HAND = [s for s in LIFTED if L.ABI[s].get("by_hand")]
+
+
+@pytest.mark.parametrize("sym", BY_HAND)
+@pytest.mark.parametrize("sgn", [1, -1])
+def test_by_hand_1d_dt_is_the_advection_dt_of_vel_n(sym, sgn, ref):
+    """lsm1dComputeStableNormalVelDt (and its control-volume form) reads only
+    |vel_n| / dx: the reference's own routine equals the oracle's 3D advection
+    dt with vel_x = vel_n and zero y, z velocities, bit for bit."""
+    vals = case(sym, 5)
+    vals["control_vol_sgn"] = sgn
+    _, s_ref = H.run(ref, sym, vals)
+    sym3 = L.ABI[sym]["lifted_from"]
+    v3 = {}
+    for name, kind, is_arr, written in L.ABI[sym3]["args"]:
+        m = re.match(r"^(ilo|ihi|jlo|jhi|klo|khi)_(.*)$", name)
+        if m:
+            v3[name] = vals[name] if m.group(1)[0] == "i" else 0
+        elif name == "vel_x":
+            v3[name] = np.asfortranarray(vals["vel_n"].reshape(-1, 1, 1))
+        elif is_arr and name in vals:
+            v3[name] = np.asfortranarray(np.asarray(vals[name]).reshape(-1, 1, 1))
+        elif is_arr:
+            v3[name] = np.zeros((len(vals["vel_n"]), 1, 1), order="F")
+        elif name in vals:
+            v3[name] = vals[name]
+        else:
+            v3[name] = vals["dx"]
+    _, s3 = H.run(H.oracle(), sym3, v3)
+    assert H.same(s_ref["dt"], s3["dt"]), (s_ref["dt"], s3["dt"])
 
 
 def lifted_3d_call(sym, vals, copies=7):
