@@ -2914,6 +2914,175 @@ void lsm2dzerooutlevelseteqnrhslocal_(
   const int *nlo_index,
   const int *nhi_index);
 
+/* 2D: mean curvature from a 9-point stencil (face gradients).
+ * Replaces src/geometry/lsm_curvature2d.f.in:98; C declaration src/geometry/lsm_curvature2d.h:102.
+ */
+void lsm2dcomputemeancurvature9stencil_(
+  double *kappa,
+  const int *ilo_kappa_gb,
+  const int *ihi_kappa_gb,
+  const int *jlo_kappa_gb,
+  const int *jhi_kappa_gb,
+  const double *phi,
+  const int *ilo_phi_gb,
+  const int *ihi_phi_gb,
+  const int *jlo_phi_gb,
+  const int *jhi_phi_gb,
+  const int *ilo_fb,
+  const int *ihi_fb,
+  const int *jlo_fb,
+  const int *jhi_fb,
+  const double *dx,
+  const double *dy);
+
+/* 2D: mean curvature from a 9-point stencil on band cells.
+ * Replaces src/geometry/lsm_curvature2d_local.f.in:115; C declaration src/geometry/lsm_curvature2d_local.h:116.
+ */
+void lsm2dcomputemeancurvature9stencillocal_(
+  double *kappa,
+  const int *ilo_kappa_gb,
+  const int *ihi_kappa_gb,
+  const int *jlo_kappa_gb,
+  const int *jhi_kappa_gb,
+  const double *phi,
+  const int *ilo_phi_gb,
+  const int *ihi_phi_gb,
+  const int *jlo_phi_gb,
+  const int *jhi_phi_gb,
+  const double *dx,
+  const double *dy,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
+/* 2D: mean curvature of a signed distance function, Laplacian / (1 - phi Laplacian).
+ * Replaces src/geometry/lsm_curvature2d.f.in:178; C declaration src/geometry/lsm_curvature2d.h:140.
+ */
+void lsm2dcomputemeancurvaturesgndist_(
+  double *kappa,
+  const int *ilo_kappa_gb,
+  const int *ihi_kappa_gb,
+  const int *jlo_kappa_gb,
+  const int *jhi_kappa_gb,
+  const double *phi,
+  const int *ilo_phi_gb,
+  const int *ihi_phi_gb,
+  const int *jlo_phi_gb,
+  const int *jhi_phi_gb,
+  const int *ilo_fb,
+  const int *ihi_fb,
+  const int *jlo_fb,
+  const int *jhi_fb,
+  const double *dx,
+  const double *dy);
+
+/* 2D: signed-distance mean curvature on band cells (dx where the denominator vanishes, as the reference).
+ * Replaces src/geometry/lsm_curvature2d_local.f.in:211; C declaration src/geometry/lsm_curvature2d_local.h:162.
+ */
+void lsm2dcomputemeancurvaturesgndistlocal_(
+  double *kappa,
+  const int *ilo_kappa_gb,
+  const int *ihi_kappa_gb,
+  const int *jlo_kappa_gb,
+  const int *jhi_kappa_gb,
+  const double *phi,
+  const int *ilo_phi_gb,
+  const int *ihi_phi_gb,
+  const int *jlo_phi_gb,
+  const int *jhi_phi_gb,
+  const double *dx,
+  const double *dy,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
+/* 2D: second-order central divergence of (fx, fy).
+ * Replaces src/toolbox/lsm_spatial_derivatives2d.f.in:2452; C declaration src/toolbox/lsm_spatial_derivatives2d.h:799.
+ */
+void lsm2ddivergencecentral_(
+  double *divf,
+  const int *ilo_divf_gb,
+  const int *ihi_divf_gb,
+  const int *jlo_divf_gb,
+  const int *jhi_divf_gb,
+  const double *fx,
+  const double *fy,
+  const int *ilo_gb,
+  const int *ihi_gb,
+  const int *jlo_gb,
+  const int *jhi_gb,
+  const int *ilo_fb,
+  const int *ihi_fb,
+  const int *jlo_fb,
+  const int *jhi_fb,
+  const double *dx,
+  const double *dy);
+
+/* 2D: second-order central divergence on band cells.
+ * Replaces src/toolbox/lsm_spatial_derivatives2d_local.f.in:1769; C declaration src/toolbox/lsm_spatial_derivatives2d_local.h:628.
+ */
+void lsm2ddivergencecentrallocal_(
+  double *divf,
+  const int *ilo_divf_gb,
+  const int *ihi_divf_gb,
+  const int *jlo_divf_gb,
+  const int *jhi_divf_gb,
+  const double *fx,
+  const double *fy,
+  const int *ilo_gb,
+  const int *ihi_gb,
+  const int *jlo_gb,
+  const int *jhi_gb,
+  const double *dx,
+  const double *dy,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
+/* 2D: second-order delta function (Smereka) from phi and the unit normal.
+ * Replaces src/toolbox/lsm_calculus_toolbox2d.f.in:100; C declaration src/toolbox/lsm_calculus_toolbox2d.h:83.
+ */
+void lsm2ddeltafunctionorder2_(
+  const double *phi,
+  double *delta,
+  const int *ilo_gb,
+  const int *ihi_gb,
+  const int *jlo_gb,
+  const int *jhi_gb,
+  const double *norm_phi_x,
+  const double *norm_phi_y,
+  const int *ilo_grad_phi_gb,
+  const int *ihi_grad_phi_gb,
+  const int *jlo_grad_phi_gb,
+  const int *jhi_grad_phi_gb,
+  const int *ilo_fb,
+  const int *ihi_fb,
+  const int *jlo_fb,
+  const int *jhi_fb,
+  const double *dx,
+  const double *dy);
+
 #ifdef __cplusplus
 }
 #endif

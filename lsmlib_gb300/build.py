@@ -29,7 +29,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 
 # FP64 parity units: no contraction of a*b+c into FMA
 NO_FMA = {"dense.cu", "dense2.cu", "local.cu", "band.cu", "fused_f64.cu", "batched_f64.cu", "adjoint_f64.cu", "diag.cu",
-          "noalloc.cu", "bandflow_f64.cu", "geometry.cu"}
+          "noalloc.cu", "bandflow_f64.cu", "geometry.cu", "plane2d.cu", "lifted_by_hand.cu"}
 
 
 def nvcc():

@@ -446,6 +446,18 @@ def write_header(path, guard, title, syms, abi, desc):
 SIG_FROM_C_HEADER = {"lsm2dhjeno3local_": ("dy", [["index_x", "int", True, False], ["index_y", "int", True, False]])}
 
 
+# 2D routines with no 3D counterpart, written as 2D kernels (csrc/plane2d.cu)
+PLANE2D = {
+    "lsm2dcomputemeancurvature9stencil_": "mean curvature from a 9-point stencil (face gradients)",
+    "lsm2dcomputemeancurvature9stencillocal_": "mean curvature from a 9-point stencil on band cells",
+    "lsm2dcomputemeancurvaturesgndist_": "mean curvature of a signed distance function, Laplacian / (1 - phi Laplacian)",
+    "lsm2dcomputemeancurvaturesgndistlocal_": "signed-distance mean curvature on band cells (dx where the denominator vanishes, as the reference)",
+    "lsm2ddivergencecentral_": "second-order central divergence of (fx, fy)",
+    "lsm2ddivergencecentrallocal_": "second-order central divergence on band cells",
+    "lsm2ddeltafunctionorder2_": "second-order delta function (Smereka) from phi and the unit normal",
+}
+
+
 def fix_sigs(sigs):
     for sym, (after, extra) in SIG_FROM_C_HEADER.items():
         args = sigs[sym]["args"]
@@ -501,6 +513,14 @@ def main():
                   "args": sg["args"], "lifted_from": sym3, "by_hand": True}
         lifted[s] = (1 if s.startswith("lsm1d") else 2, None)
         desc2[s] = "%dD form: %s" % (lifted[s][0], text)
+    for s, text in PLANE2D.items():
+        sg = sigs[s]
+        src, line = sg["src"].split(":")
+        hpath, hline = header_line(s)
+        abi[s] = {"ref": f"{os.path.relpath(src, REF)}:{line}", "header": f"{hpath}:{hline}" if hpath else None,
+                  "args": sg["args"], "plane2d": True}
+        lifted[s] = (2, None)
+        desc2[s] = "2D: " + text
     write_lifted(abi, {s: v for s, v in lifted.items() if v[1] is not None})
     for dims in (2, 1):
         syms = [s for s in lifted if lifted[s][0] == dims]
