@@ -3083,6 +3083,92 @@ void lsm2ddeltafunctionorder2_(
   const double *dx,
   const double *dy);
 
+/* 2D: integral of F delta |grad phi| dV over an index box (index box from the C declaration).
+ * Replaces src/toolbox/lsm_math_utils2d.f.in:713; C declaration src/toolbox/lsm_math_utils2d.h:462.
+ */
+void lsm2dsurfaceintegralprecomputeddelta_(
+  double *int_f,
+  const double *f,
+  const int *ilo_f_gb,
+  const int *ihi_f_gb,
+  const int *jlo_f_gb,
+  const int *jhi_f_gb,
+  const double *delta_phi,
+  const int *ilo_phi_gb,
+  const int *ihi_phi_gb,
+  const int *jlo_phi_gb,
+  const int *jhi_phi_gb,
+  const double *grad_phi_mag,
+  const int *ilo_grad_phi_gb,
+  const int *ihi_grad_phi_gb,
+  const int *jlo_grad_phi_gb,
+  const int *jhi_grad_phi_gb,
+  const int *ilo_ib,
+  const int *ihi_ib,
+  const int *jlo_ib,
+  const int *jhi_ib,
+  const double *dx,
+  const double *dy);
+
+/* 2D: integral of F delta |grad phi| dV over cells of one control-volume sign.
+ * Replaces src/toolbox/lsm_math_utils2d.f.in:1744; C declaration src/toolbox/lsm_math_utils2d.h:938.
+ */
+void lsm2dsurfaceintegralprecomputeddeltacontrolvolume_(
+  double *int_f,
+  const double *f,
+  const int *ilo_f_gb,
+  const int *ihi_f_gb,
+  const int *jlo_f_gb,
+  const int *jhi_f_gb,
+  const double *delta_phi,
+  const int *ilo_phi_gb,
+  const int *ihi_phi_gb,
+  const int *jlo_phi_gb,
+  const int *jhi_phi_gb,
+  const double *grad_phi_mag,
+  const int *ilo_grad_phi_gb,
+  const int *ihi_grad_phi_gb,
+  const int *jlo_grad_phi_gb,
+  const int *jhi_grad_phi_gb,
+  const double *control_vol,
+  const int *ilo_control_vol_gb,
+  const int *ihi_control_vol_gb,
+  const int *jlo_control_vol_gb,
+  const int *jhi_control_vol_gb,
+  const int *control_vol_sgn,
+  const int *ilo_ib,
+  const int *ihi_ib,
+  const int *jlo_ib,
+  const int *jhi_ib,
+  const double *dx,
+  const double *dy);
+
+/* 2D: mean |field1 - field2| over band cells (0 when none).
+ * Replaces src/toolbox/lsm_math_utils2d_local.f.in:86; C declaration src/toolbox/lsm_math_utils2d_local.h:106.
+ */
+void lsm2daveabsdifflocal_(
+  double *ave_abs_diff,
+  const double *field1,
+  const int *ilo_field1_gb,
+  const int *ihi_field1_gb,
+  const int *jlo_field1_gb,
+  const int *jhi_field1_gb,
+  const double *field2,
+  const int *ilo_field2_gb,
+  const int *ihi_field2_gb,
+  const int *jlo_field2_gb,
+  const int *jhi_field2_gb,
+  const int *index_x,
+  const int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  const unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  const unsigned char *mark_fb);
+
 #ifdef __cplusplus
 }
 #endif

@@ -2,7 +2,9 @@
 // signed-distance mean curvatures (curvature2d.f.in:98, :178 and their list
 // forms, curvature2d_local.f.in:115, :211), the central divergence
 // (spatial_derivatives2d.f.in:2452, spatial_derivatives2d_local.f.in:1769)
-// and Smereka's second-order delta function (calculus_toolbox2d.f.in:100).
+// Smereka's second-order delta function (calculus_toolbox2d.f.in:100), the
+// surface integrals with a precomputed delta function (math_utils2d.f.in:713,
+// :1744) and the list mean absolute difference (math_utils2d_local.f.in:86).
 // LSMLIB's symbol names and argument lists (include/lsmgpu_toolbox2d.h); a
 // 2D array phi(ilo:ihi, jlo:jhi) is the 3D array phi(ilo:ihi, jlo:jhi, 0:0).
 // One thread per fill-box cell or list entry, the reference's operation
@@ -168,6 +170,139 @@ __device__ R delta2(const View<const R> &P, const View<const R> &NX, const View<
   return (dxp + dxm) * K.odxsq + (dyp + dym) * K.odysq;
 }
 
+// ---- deterministic sums ------------------------------------------------------
+// LSMLIB adds its terms serially.  Here the n terms (cells of an index box in
+// memory order, or list entries) are split into kSumBlocks fixed contiguous
+// chunks; a block adds its chunk lane-strided and in a fixed tree, one block
+// adds the chunk sums in a fixed tree.  The result depends on the data only,
+// within (n + 16) 2^-53 sum|term| of the serial sum.  Counts are exact.
+constexpr int kSumBlocks = 304;  // two per SM
+constexpr int kSumThreads = 256;
+
+template <class F>
+__global__ void __launch_bounds__(kSumThreads) k_plane_sum(F term, long long n, R *part_sum,
+                                                           unsigned long long *part_cnt) {
+  __shared__ R ss[kSumThreads];
+  __shared__ unsigned long long sc[kSumThreads];
+  const int t = threadIdx.x;
+  const long long chunk = (n + gridDim.x - 1) / gridDim.x;
+  const long long b0 = (long long)blockIdx.x * chunk;
+  const long long b1 = b0 + chunk < n ? b0 + chunk : n;
+  R sum = R(0);
+  unsigned long long cnt = 0;
+  for (long long q = b0 + t; q < b1; q += kSumThreads) {
+    R v;
+    if (term(q, v)) {
+      sum = sum + v;
+      cnt++;
+    }
+  }
+  ss[t] = sum;
+  sc[t] = cnt;
+  __syncthreads();
+  for (int w = kSumThreads / 2; w > 0; w >>= 1) {
+    if (t < w) {
+      ss[t] = ss[t] + ss[t + w];
+      sc[t] += sc[t + w];
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    part_sum[blockIdx.x] = ss[0];
+    part_cnt[blockIdx.x] = sc[0];
+  }
+}
+
+// AVERAGE: sum / count (0 when nothing was counted), else the sum
+template <bool AVERAGE>
+__global__ void __launch_bounds__(kSumThreads) k_plane_sum_final(const R *part_sum,
+                                                                 const unsigned long long *part_cnt, int np,
+                                                                 R *out) {
+  __shared__ R ss[kSumThreads];
+  __shared__ unsigned long long sc[kSumThreads];
+  const int t = threadIdx.x;
+  R sum = R(0);
+  unsigned long long cnt = 0;
+  for (int q = t; q < np; q += kSumThreads) {
+    sum = sum + part_sum[q];
+    cnt += part_cnt[q];
+  }
+  ss[t] = sum;
+  sc[t] = cnt;
+  __syncthreads();
+  for (int w = kSumThreads / 2; w > 0; w >>= 1) {
+    if (t < w) {
+      ss[t] = ss[t] + ss[t + w];
+      sc[t] += sc[t + w];
+    }
+    __syncthreads();
+  }
+  if (t == 0) *out = AVERAGE ? (sc[0] > 0 ? ss[0] / (R)sc[0] : R(0)) : ss[0];
+}
+
+template <bool AVERAGE, class F>
+void plane_sum(Call &call, F term, long long n, R *out) {
+  R *dout = call.scalar_out(out);
+  R *ps = call.temp<R>(kSumBlocks);
+  unsigned long long *pc = call.temp<unsigned long long>(kSumBlocks);
+  if (!call.ok()) return;
+  LSMGPU_LAUNCH(k_plane_sum<F>, kSumBlocks, kSumThreads, 0, term, n, ps, pc);
+  LSMGPU_LAUNCH(k_plane_sum_final<AVERAGE>, 1, kSumThreads, 0, ps, pc, kSumBlocks, dout);
+  call.finish();
+}
+
+// integral of F delta |grad phi| dV over an index box, optionally over the
+// cells of one control-volume sign (math_utils2d.f.in:713-770, :1744-1830)
+struct DeltaIntegral {
+  View<const R> f, dl, gm, cv;
+  int cv_sgn;  // 0: every cell; > 0: control_vol > 0; < 0: control_vol < 0
+  Box ib;
+  R dv;
+  __device__ __forceinline__ bool operator()(long long q, R &v) const {
+    const long long nx = ib.n(0);
+    const int i = ib.lo[0] + (int)(q % nx), j = ib.lo[1] + (int)(q / nx);
+    if (cv_sgn > 0 && !(cv(i, j, 0) > R(0))) return false;
+    if (cv_sgn < 0 && !(cv(i, j, 0) < R(0))) return false;
+    v = dl(i, j, 0) * gm(i, j, 0) * f(i, j, 0) * dv;
+    return true;
+  }
+};
+
+// |field1 - field2| on the gated entries of a list (math_utils2d_local.f.in:86-150)
+struct ListAbsDiff {
+  const int *ix, *iy;
+  View<const R> a, b;
+  View<const U8> nb;
+  Box nbb, safe;
+  signed char mark;
+  __device__ __forceinline__ bool operator()(long long q, R &v) const {
+    const int i = ix[q], j = iy[q];
+    if (!(inbox(safe, i, j, 0) && inbox(nbb, i, j, 0) && (signed char)nb(i, j, 0) <= mark)) return false;
+    v = fabs(a(i, j, 0) - b(i, j, 0));
+    return true;
+  }
+};
+
+void delta_integral(const char *name, R *int_f, const R *f, const Box &fbx, const R *delta_phi, const Box &pb,
+                    const R *grad_phi_mag, const Box &gb, const R *control_vol, const Box &cb, int cv_sgn,
+                    const Box &ib, R dx, R dy) {
+  Call call(name);
+  if (!fbx.contains(ib, 0, 0, 0) || !pb.contains(ib, 0, 0, 0) || !gb.contains(ib, 0, 0, 0) ||
+      (control_vol && !cb.contains(ib, 0, 0, 0)))
+    call.fail("ghost box does not cover the index box");
+  if (!call.ok()) return;
+  DeltaIntegral T{};
+  T.f = vin(call, f, fbx);
+  T.dl = vin(call, delta_phi, pb);
+  T.gm = vin(call, grad_phi_mag, gb);
+  if (control_vol) T.cv = vin(call, control_vol, cb);
+  T.cv_sgn = control_vol ? (cv_sgn > 0 ? 1 : -1) : 0;
+  T.ib = ib;
+  T.dv = dx * dy;
+  if (!call.ok()) return;
+  plane_sum<false>(call, T, ib.empty() ? 0 : ib.size(), int_f);
+}
+
 }  // namespace
 }  // namespace lsmgpu
 
@@ -297,6 +432,41 @@ void lsm2ddeltafunctionorder2_(const R *phi, R *delta, B2ARG(g), const R *norm_p
   K.o2dxsq = R(0.5) / dxv / dxv; K.o2dysq = R(0.5) / dyv / dyv;
   for_plane(fb, [=] __device__(int i, int j) { D(i, j, 0) = delta2(P, NX, NY, i, j, K); });
   call.finish();
+}
+
+void lsm2dsurfaceintegralprecomputeddelta_(R *int_f, const R *f, B2ARG(f), const R *delta_phi, B2ARG(p),
+                                           const R *grad_phi_mag, B2ARG(g), B2ARG(ib), const R *dx, const R *dy) {
+  delta_integral("lsm2dsurfaceintegralprecomputeddelta_", int_f, f, B2OF(f), delta_phi, B2OF(p), grad_phi_mag,
+                 B2OF(g), nullptr, Box{}, 0, B2OF(ib), *dx, *dy);
+}
+
+void lsm2dsurfaceintegralprecomputeddeltacontrolvolume_(R *int_f, const R *f, B2ARG(f), const R *delta_phi,
+                                                        B2ARG(p), const R *grad_phi_mag, B2ARG(g),
+                                                        const R *control_vol, B2ARG(c), const int *control_vol_sgn,
+                                                        B2ARG(ib), const R *dx, const R *dy) {
+  delta_integral("lsm2dsurfaceintegralprecomputeddeltacontrolvolume_", int_f, f, B2OF(f), delta_phi, B2OF(p),
+                 grad_phi_mag, B2OF(g), control_vol, B2OF(c), *control_vol_sgn, B2OF(ib), *dx, *dy);
+}
+
+void lsm2daveabsdifflocal_(R *ave_abs_diff, const R *field1, B2ARG(a), const R *field2, B2ARG(b),
+                           const int *index_x, const int *index_y, const int *nlo_index, const int *nhi_index,
+                           const U8 *narrow_band, B2ARG(nb), const U8 *mark_fb) {
+  Call call("lsm2daveabsdifflocal_");
+  const Box ab = B2OF(a), bb = B2OF(b), nbb = B2OF(nb);
+  ListAbsDiff T{};
+  const long long n = (long long)*nhi_index - *nlo_index + 1;
+  if (n > 0) {
+    T.ix = call.in(index_x, n);
+    T.iy = call.in(index_y, n);
+  }
+  T.a = vin(call, field1, ab);
+  T.b = vin(call, field2, bb);
+  T.nb = view((const U8 *)call.in(narrow_band, nbb.size()), nbb);
+  T.nbb = nbb;
+  T.safe = isect(ab, bb);
+  T.mark = (signed char)*mark_fb;
+  if (!call.ok()) return;
+  plane_sum<true>(call, T, n > 0 ? n : 0, ave_abs_diff);
 }
 
 }  // extern "C"

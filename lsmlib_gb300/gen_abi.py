@@ -438,12 +438,18 @@ def write_header(path, guard, title, syms, abi, desc):
         f.write("\n".join(lines))
 
 
-# LSMLIB's lsm2dHJENO3LOCAL reads index_x / index_y (spatial_derivatives2d_local.f.in:578,
+# LSMLIB's lsm2dHJENO3LOCAL (and lsm2dSurfaceIntegralPrecomputedDelta, below) reads index_x / index_y (spatial_derivatives2d_local.f.in:578,
 # :642) but leaves them out of its Fortran argument list (:498-523); its C
 # declaration (spatial_derivatives2d_local.h) passes them after dy, so callers
 # pass them there and the drop-in takes them there.  The Fortran routine cannot
 # be called correctly, so it is no parity target ("ref_unusable").
-SIG_FROM_C_HEADER = {"lsm2dhjeno3local_": ("dy", [["index_x", "int", True, False], ["index_y", "int", True, False]])}
+SIG_FROM_C_HEADER = {"lsm2dhjeno3local_": ("dy", [["index_x", "int", True, False], ["index_y", "int", True, False]]),
+                     # loops over ilo_ib..jhi_ib (math_utils2d.f.in:760) that its
+                     # Fortran argument list leaves out (:713-727); its C
+                     # declaration (math_utils2d.h:462) passes them before dx
+                     "lsm2dsurfaceintegralprecomputeddelta_": (
+                         "jhi_grad_phi_gb", [["ilo_ib", "int", False, False], ["ihi_ib", "int", False, False],
+                                             ["jlo_ib", "int", False, False], ["jhi_ib", "int", False, False]])}
 
 
 # 2D routines with no 3D counterpart, written as 2D kernels (csrc/plane2d.cu)
@@ -455,6 +461,9 @@ PLANE2D = {
     "lsm2ddivergencecentral_": "second-order central divergence of (fx, fy)",
     "lsm2ddivergencecentrallocal_": "second-order central divergence on band cells",
     "lsm2ddeltafunctionorder2_": "second-order delta function (Smereka) from phi and the unit normal",
+    "lsm2dsurfaceintegralprecomputeddelta_": "integral of F delta |grad phi| dV over an index box (index box from the C declaration)",
+    "lsm2dsurfaceintegralprecomputeddeltacontrolvolume_": "integral of F delta |grad phi| dV over cells of one control-volume sign",
+    "lsm2daveabsdifflocal_": "mean |field1 - field2| over band cells (0 when none)",
 }
 
 
@@ -519,6 +528,8 @@ def main():
         hpath, hline = header_line(s)
         abi[s] = {"ref": f"{os.path.relpath(src, REF)}:{line}", "header": f"{hpath}:{hline}" if hpath else None,
                   "args": sg["args"], "plane2d": True}
+        if sg.get("ref_unusable"):
+            abi[s]["ref_unusable"] = True
         lifted[s] = (2, None)
         desc2[s] = "2D: " + text
     write_lifted(abi, {s: v for s, v in lifted.items() if v[1] is not None})
