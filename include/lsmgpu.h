@@ -354,6 +354,21 @@ void lsmgpu_signed_linear_extrapolation_inner_sign(
     const int *klo_gb, const int *khi_gb, const int *ilo_fb, const int *ihi_fb, const int *jlo_fb,
     const int *jhi_fb, const int *klo_fb, const int *khi_fb, const int *bdry_location_idx);
 
+/* lsmgpu_determine_narrow_band_2d_bookkeeping: lsm3dDetermineNarrowBand
+ * (src/toolbox/lsm_localization3d.f:174), same arguments, with the list
+ * bookkeeping of lsm2dDetermineNarrowBand (lsm_localization2d.f:225-240):
+ * n_hi(0) = nlo_index + (level-0 cells) - 1 and the outer-list bounds
+ * likewise even for an empty band, neighbour levels only when level 0
+ * holds two or more cells. */
+void lsmgpu_determine_narrow_band_2d_bookkeeping(
+    const double *phi, const int *ilo_gb, const int *ihi_gb, const int *jlo_gb, const int *jhi_gb,
+    const int *klo_gb, const int *khi_gb, unsigned char *narrow_band, const int *ilo_nb_gb,
+    const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, const int *klo_nb_gb,
+    const int *khi_nb_gb, int *index_x, int *index_y, int *index_z, const int *nlo_index,
+    const int *nhi_index, int *n_lo, int *n_hi, int *index_outer, const int *nlo_index_outer,
+    const int *nhi_index_outer, int *nlo_outer_plus, int *nhi_outer_plus, int *nlo_outer_minus,
+    int *nhi_outer_minus, const double *width, const double *width_inner, const int *level);
+
 /* Library version string. */
 const char *lsmgpu_version(void);
 

@@ -1362,6 +1362,40 @@ void lsm2ddeterminenarrowband_(
   const double *width_inner,
   const int *level);
 
+/* 2D form: build a narrow band of cells near phi = 0 and away from a mask (|phi - mask| > max dx).
+ * Replaces src/toolbox/lsm_localization2d.f:365; C declaration src/toolbox/lsm_localization2d.h:237.
+ */
+void lsm2ddeterminenarrowbandawayfrommask_(
+  const double *phi,
+  const double *mask,
+  const int *ilo_gb,
+  const int *ihi_gb,
+  const int *jlo_gb,
+  const int *jhi_gb,
+  unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  int *index_x,
+  int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  int *n_lo,
+  int *n_hi,
+  int *index_outer,
+  const int *nlo_index_outer,
+  const int *nhi_index_outer,
+  int *nlo_outer_plus,
+  int *nhi_outer_plus,
+  int *nlo_outer_minus,
+  int *nhi_outer_minus,
+  const double *width,
+  const double *width_inner,
+  const int *level,
+  const double *dx,
+  const double *dy);
+
 /* 2D form: build a narrow band from the sign of a mask.
  * Replaces src/toolbox/lsm_localization2d.f:539; C declaration src/toolbox/lsm_localization2d.h:328.
  */
@@ -1384,6 +1418,38 @@ void lsm2ddeterminenarrowbandfrommask_(
   int *n_hi,
   const int *level,
   const int *use_mask_sign);
+
+/* 2D form: build a narrow band of cells near the zero sets of both phi and psi.
+ * Replaces src/toolbox/lsm_localization2d.f:248; C declaration src/toolbox/lsm_localization2d.h:165.
+ */
+void lsm2ddeterminenarrowbandfromtwolevelsets_(
+  const double *phi,
+  const double *psi,
+  const int *ilo_gb,
+  const int *ihi_gb,
+  const int *jlo_gb,
+  const int *jhi_gb,
+  unsigned char *narrow_band,
+  const int *ilo_nb_gb,
+  const int *ihi_nb_gb,
+  const int *jlo_nb_gb,
+  const int *jhi_nb_gb,
+  int *index_x,
+  int *index_y,
+  const int *nlo_index,
+  const int *nhi_index,
+  int *n_lo,
+  int *n_hi,
+  int *index_outer,
+  const int *nlo_index_outer,
+  const int *nhi_index_outer,
+  int *nlo_outer_plus,
+  int *nhi_outer_plus,
+  int *nlo_outer_minus,
+  int *nhi_outer_minus,
+  const double *width,
+  const double *width_inner,
+  const int *level);
 
 /* 2D form: |grad phi| with the reference's 1e-8 clamps.
  * Replaces src/toolbox/lsm_spatial_derivatives2d.f.in:2395; C declaration src/toolbox/lsm_spatial_derivatives2d.h:774.

@@ -22,37 +22,36 @@ namespace {
 }  // namespace
 }  // namespace lsmgpu
 
-using namespace lsmgpu;
+namespace lsmgpu {
+namespace {
 
-extern "C" {
-
-void lsm3ddeterminenarrowband_(const R *phi, BOXARG(g), unsigned char *narrow_band, BOXARG(nb), int *index_x,
-                               int *index_y, int *index_z, const int *nlo_index, const int *nhi_index,
-                               int *n_lo, int *n_hi, int *index_outer, const int *nlo_index_outer,
-                               const int *nhi_index_outer, int *nlo_outer_plus, int *nhi_outer_plus,
-                               int *nlo_outer_minus, int *nhi_outer_minus, const R *width,
-                               const R *width_inner, const int *level) {
-  Call call("lsm3ddeterminenarrowband_");
-  Box gb = BOXOF(g), nbb = BOXOF(nb);
+// lsm3dDetermineNarrowBand (localization3d.f:174-302) and the forms of its
+// 2D relatives (BandForm): level 0 in sweep order, outer lists, neighbour levels
+void determine_band(const char *name, const R *phi, const Box &gb, const R *second, unsigned char *narrow_band,
+                    const Box &nbb, int *index_x, int *index_y, int *index_z, const int *nlo_index,
+                    const int *nhi_index, int *n_lo, int *n_hi, int *index_outer, const int *nlo_index_outer,
+                    const int *nhi_index_outer, int *nlo_outer_plus, int *nhi_outer_plus, int *nlo_outer_minus,
+                    int *nhi_outer_minus, R width, R width_inner, int level, BandForm<R> form) {
+  Call call(name);
   if (!nbb.contains(gb, 0, 0, 0)) call.fail("narrow_band ghost box must cover phi's ghost box");
-  if (*level < 0) call.fail("level must be >= 0");
+  if (level < 0) call.fail("level must be >= 0");
   const long long cap = (long long)*nhi_index - *nlo_index + 1;
   const long long ocap = (long long)*nhi_index_outer - *nlo_index_outer + 1;
   if (cap <= 0 || ocap <= 0) call.fail("empty index arrays");
   if (!call.ok()) return;
   const R *phd = call.in(phi, gb.size());
+  if (second) form.second = call.in(second, gb.size());
   U8 *nbd = call.inout(narrow_band, nbb.size());
   int *ix = call.inout(index_x, cap), *iy = call.inout(index_y, cap), *iz = call.inout(index_z, cap);
   int *outer = call.inout(index_outer, ocap);
   if (!call.ok()) return;
   std::vector<int> lo, hi;
   int ob[4];
-  long long n0 = 0;
+  int nwrite = 1;
   if (!band_build<R>(call, phd, gb, nbd, nbb, ix, iy, iz, *nlo_index, *nhi_index, outer, *nlo_index_outer,
-                     *nhi_index_outer, *width, *width_inner, *level, lo, hi, ob, &n0, new_claims(call, nbb)))
+                     *nhi_index_outer, width, width_inner, level, lo, hi, ob, nullptr, new_claims(call, nbb), false,
+                     form, &nwrite))
     return;
-  // an empty band writes only level 0 (localization3d.f:289-292)
-  const int nwrite = n0 > 0 ? *level + 1 : 1;
   put_ints(n_lo, lo.data(), nwrite);
   put_ints(n_hi, hi.data(), nwrite);
   put_ints(nlo_outer_plus, &ob[0], 1);
@@ -60,6 +59,59 @@ void lsm3ddeterminenarrowband_(const R *phi, BOXARG(g), unsigned char *narrow_ba
   put_ints(nlo_outer_minus, &ob[2], 1);
   put_ints(nhi_outer_minus, &ob[3], 1);
   call.finish();
+}
+
+}  // namespace
+}  // namespace lsmgpu
+
+using namespace lsmgpu;
+
+extern "C" {
+
+#define BAND_TAIL                                                                                         \
+  unsigned char *narrow_band, BOXARG(nb), int *index_x, int *index_y, int *index_z, const int *nlo_index,   \
+      const int *nhi_index, int *n_lo, int *n_hi, int *index_outer, const int *nlo_index_outer,            \
+      const int *nhi_index_outer, int *nlo_outer_plus, int *nhi_outer_plus, int *nlo_outer_minus,         \
+      int *nhi_outer_minus, const R *width, const R *width_inner, const int *level
+#define BAND_PASS                                                                                         \
+  narrow_band, BOXOF(nb), index_x, index_y, index_z, nlo_index, nhi_index, n_lo, n_hi, index_outer,         \
+      nlo_index_outer, nhi_index_outer, nlo_outer_plus, nhi_outer_plus, nlo_outer_minus, nhi_outer_minus,   \
+      *width, *width_inner, *level
+
+void lsm3ddeterminenarrowband_(const R *phi, BOXARG(g), BAND_TAIL) {
+  determine_band("lsm3ddeterminenarrowband_", phi, BOXOF(g), nullptr, BAND_PASS, BandForm<R>());
+}
+
+// the bookkeeping of lsm2dDetermineNarrowBand (localization2d.f:225-240) on
+// 3D arrays: n_hi(0) = count - 1 even for an empty band, neighbour levels
+// only when level 0 holds two or more cells
+void lsmgpu_determine_narrow_band_2d_bookkeeping(const R *phi, BOXARG(g), BAND_TAIL) {
+  BandForm<R> f;
+  f.bookkeeping = 1;
+  determine_band("lsmgpu_determine_narrow_band_2d_bookkeeping", phi, BOXOF(g), nullptr, BAND_PASS, f);
+}
+
+// no 3D original; follows lsm2dDetermineNarrowBandFromTwoLevelSets
+// (localization2d.f:248-343): level 0 = cells with |phi| < width and
+// |psi| < width, outer lists by phi
+void lsm3ddeterminenarrowbandfromtwolevelsets_(const R *phi, const R *psi, BOXARG(g), BAND_TAIL) {
+  BandForm<R> f;
+  f.l0_mode = 3;
+  f.bookkeeping = 2;
+  determine_band("lsm3ddeterminenarrowbandfromtwolevelsets_", phi, BOXOF(g), psi, BAND_PASS, f);
+}
+
+// no 3D original; follows lsm2dDetermineNarrowBandAwayFromMask
+// (localization2d.f:365-464): level 0 = cells with |phi| < width and
+// |phi - mask| > max(dx, dy, dz)
+void lsm3ddeterminenarrowbandawayfrommask_(const R *phi, const R *mask, BOXARG(g), BAND_TAIL, const R *dx,
+                                           const R *dy, const R *dz) {
+  BandForm<R> f;
+  f.l0_mode = 4;
+  f.bookkeeping = 2;
+  const R m = *dx > *dy ? *dx : *dy;
+  f.max_dx = m > *dz ? m : *dz;
+  determine_band("lsm3ddeterminenarrowbandawayfrommask_", phi, BOXOF(g), mask, BAND_PASS, f);
 }
 
 void lsm3dmarknarrowbandneighbors_(unsigned char *narrow_band, BOXARG(nb), int *index_x, int *index_y,

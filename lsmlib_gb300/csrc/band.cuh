@@ -237,7 +237,11 @@ struct Level0T {
   int *ix, *iy, *iz;      // list arrays (element 0 = entry nlo_index)
   int *outer;             // index_outer (element 0 = entry nlo_outer)
   int nlo, nlo_outer, nhi_outer;
-  int mode;               // 0: |phi| < width, 1: mask >= 0, 2: mask <= 0
+  int mode;               // 0: |phi| < width, 1: mask >= 0, 2: mask <= 0,
+                          // 3: |phi| < width and |second| < width,
+                          // 4: |phi| < width and |phi - second| > max_dx
+  View<const T> second;   // over gb (modes 3, 4)
+  R max_dx;
   __device__ void cell(long long e, int &i, int &j, int &k) const {
     if (nxy * (gb.hi[2] - gb.lo[2] + 1) <= 0x7fffffffLL) {  // 32-bit division when the box allows
       const unsigned u = (unsigned)e, uxy = (unsigned)nxy, ux = (unsigned)nx;
@@ -265,7 +269,14 @@ struct Level0T {
   typedef T V;
   __device__ T load(long long e) const { return phi.p[e]; }
   __device__ int flags(long long e) const { return classify(phi.p[e], e); }
-  __device__ int classify(T raw, long long) const {
+  __device__ int classify(T raw, long long e) const {
+    if (mode >= 3) {  // the 2D two-level-set / away-from-mask selections (localization2d.f:248-460)
+      const R v = (R)raw, a = fabs(v), w = (R)second.p[e];
+      if (!(a < width)) return 0;
+      if (mode == 3 ? !(fabs(w) < width) : !(fabs(v - w) > max_dx)) return 0;
+      if (a >= width_inner) return v <= R(0) ? 3 : 5;
+      return 1;
+    }
     if constexpr (sizeof(T) == 4) {
       const float v = (float)raw;
       if (mode == 1) return v >= 0.f ? 1 : 0;
@@ -323,7 +334,7 @@ __global__ void k_mark0(Level0T<T> z) {
     if (k0 + q <= z.gb.hi[2]) v[q] = z.phi.p[z.phi.off(i, j, k0 + q)];
 #pragma unroll
   for (int q = 0; q < kMarkZ; q++)
-    if (k0 + q <= z.gb.hi[2]) z.nb(i, j, k0 + q) = (z.classify(v[q], 0) & 1) ? 1 : 0;
+    if (k0 + q <= z.gb.hi[2]) z.nb(i, j, k0 + q) = (z.classify(v[q], z.phi.off(i, j, k0 + q)) & 1) ? 1 : 0;
 }
 
 // claim value of an unclaimed cell (a byte pattern, so a memset sets it)
@@ -470,15 +481,35 @@ void put_ints(int *dst, const int *src, int n) {
 }
 
 
+// Level-0 selection and list bookkeeping of a band build.
+//  l0_mode: 0 |phi| < width; 3 also |second| < width; 4 also
+//           |phi - second| > max_dx (second over phi's ghost box)
+//  bookkeeping: 0 the 3D routines' (localization3d.f:274-292: an empty band
+//           sets n_hi(0) = nlo and the outer bounds to their starts, and
+//           writes level 0 only); 1 lsm2dDetermineNarrowBand's
+//           (localization2d.f:225-240: n_hi(0) = count - 1 always, neighbour
+//           levels only when level 0 holds two or more cells); 2 the 2D
+//           two-level-set and away-from-mask routines' (:327-340: as 1, with
+//           neighbour levels whenever level > 0)
+template <class T>
+struct BandForm {
+  int l0_mode = 0;
+  const T *second = nullptr;
+  double max_dx = 0;
+  int bookkeeping = 0;
+};
+
 // Builds the band of `phi` (device arrays) inside `call`: level-0 lists,
 // outer lists and `level` neighbour levels.  lo/hi receive n_lo/n_hi, ob the
-// outer-list bounds {plus lo, plus hi, minus lo, minus hi}.  Returns false
-// after recording an error (capacity or CUDA).
+// outer-list bounds {plus lo, plus hi, minus lo, minus hi}, *nwrite (when
+// set) the number of levels the reference writes.  Returns false after
+// recording an error (capacity or CUDA).
 template <class T>
 bool band_build(Call &call, const T *phi, const Box &gb, U8 *nbd, const Box &nbb, int *ix, int *iy, int *iz,
                 int nlo, int nhi, int *outer, int nlo_outer, int nhi_outer, double width, double width_inner,
                 int level, std::vector<int> &lo, std::vector<int> &hi, int ob[4], long long *level0_count,
-                int *claim, bool fuse_marks = false) {
+                int *claim, bool fuse_marks = false, const BandForm<T> &form = BandForm<T>(),
+                int *nwrite = nullptr) {
   const long long cap = (long long)nhi - nlo + 1;
   const long long ocap = (long long)nhi_outer - nlo_outer + 1;
   Level0T<T> z;
@@ -493,7 +524,9 @@ bool band_build(Call &call, const T *phi, const Box &gb, U8 *nbd, const Box &nbb
   z.nlo = nlo;
   z.nlo_outer = nlo_outer;
   z.nhi_outer = nhi_outer;
-  z.mode = 0;
+  z.mode = form.l0_mode;
+  if (form.second) z.second = view(form.second, gb);
+  z.max_dx = form.max_dx;
   const long long n = gb.size();
   long long tot[3];
   // fused marks: the count pass writes every cell's level-0 mark (the nb
@@ -521,6 +554,18 @@ bool band_build(Call &call, const T *phi, const Box &gb, U8 *nbd, const Box &nbb
   lo[0] = nlo;
   ob[0] = nhi_outer; ob[1] = nhi_outer; ob[2] = nlo_outer; ob[3] = nlo_outer;
   if (level0_count) *level0_count = tot[0];
+  if (form.bookkeeping != 0) {
+    hi[0] = (int)(nlo + tot[0] - 1);
+    ob[2] = nlo_outer;
+    ob[3] = (int)(nlo_outer + tot[1] - 1);
+    ob[0] = (int)(nhi_outer - tot[2] + 1);
+    ob[1] = nhi_outer;
+    const bool levels = level > 0 && (form.bookkeeping == 2 || hi[0] > lo[0]);
+    if (nwrite) *nwrite = levels ? level + 1 : 1;
+    if (levels && !bfs_levels(call, z.nb, nbb, ix, iy, iz, nlo, nhi, lo, hi, level, claim)) return false;
+    return true;
+  }
+  if (nwrite) *nwrite = tot[0] > 0 ? level + 1 : 1;
   if (tot[0] > 0) {
     hi[0] = (int)(nlo + tot[0] - 1);
     ob[2] = nlo_outer;

@@ -972,7 +972,18 @@ void lsm2ddeterminenarrowband_(const double *phi, const int *ilo_gb, const int *
   L_.list(nlo_index, nhi_index);
   L_.list(nlo_index_outer, nhi_index_outer);
   if (!L_.ready()) return;
-  lsm3ddeterminenarrowband_(phi, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, index_x, index_y, (int *)L_.junk(), nlo_index, nhi_index, n_lo, n_hi, index_outer, nlo_index_outer, nhi_index_outer, nlo_outer_plus, nhi_outer_plus, nlo_outer_minus, nhi_outer_minus, width, width_inner, level);
+  lsmgpu_determine_narrow_band_2d_bookkeeping(phi, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, index_x, index_y, (int *)L_.junk(), nlo_index, nhi_index, n_lo, n_hi, index_outer, nlo_index_outer, nhi_index_outer, nlo_outer_plus, nhi_outer_plus, nlo_outer_minus, nhi_outer_minus, width, width_inner, level);
+}
+
+// src/toolbox/lsm_localization2d.f:365
+void lsm2ddeterminenarrowbandawayfrommask_(const double *phi, const double *mask, const int *ilo_gb, const int *ihi_gb, const int *jlo_gb, const int *jhi_gb, unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, int *index_x, int *index_y, const int *nlo_index, const int *nhi_index, int *n_lo, int *n_hi, int *index_outer, const int *nlo_index_outer, const int *nhi_index_outer, int *nlo_outer_plus, int *nhi_outer_plus, int *nlo_outer_minus, int *nhi_outer_minus, const double *width, const double *width_inner, const int *level, const double *dx, const double *dy) {
+  Lift L_(2, "lsm2ddeterminenarrowbandawayfrommask_");
+  L_.box(ilo_gb, ihi_gb, jlo_gb, jhi_gb);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.list(nlo_index_outer, nhi_index_outer);
+  if (!L_.ready()) return;
+  lsm3ddeterminenarrowbandawayfrommask_(phi, mask, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, index_x, index_y, (int *)L_.junk(), nlo_index, nhi_index, n_lo, n_hi, index_outer, nlo_index_outer, nhi_index_outer, nlo_outer_plus, nhi_outer_plus, nlo_outer_minus, nhi_outer_minus, width, width_inner, level, dx, dy, dx);
 }
 
 // src/toolbox/lsm_localization2d.f:539
@@ -983,6 +994,17 @@ void lsm2ddeterminenarrowbandfrommask_(const double *mask, const int *ilo_mask_g
   L_.list(nlo_index, nhi_index);
   if (!L_.ready()) return;
   lsm3ddeterminenarrowbandfrommask_(mask, ilo_mask_gb, ihi_mask_gb, jlo_mask_gb, jhi_mask_gb, &L_.k0, &L_.k0, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, index_x, index_y, (int *)L_.junk(), nlo_index, nhi_index, n_lo, n_hi, level, use_mask_sign);
+}
+
+// src/toolbox/lsm_localization2d.f:248
+void lsm2ddeterminenarrowbandfromtwolevelsets_(const double *phi, const double *psi, const int *ilo_gb, const int *ihi_gb, const int *jlo_gb, const int *jhi_gb, unsigned char *narrow_band, const int *ilo_nb_gb, const int *ihi_nb_gb, const int *jlo_nb_gb, const int *jhi_nb_gb, int *index_x, int *index_y, const int *nlo_index, const int *nhi_index, int *n_lo, int *n_hi, int *index_outer, const int *nlo_index_outer, const int *nhi_index_outer, int *nlo_outer_plus, int *nhi_outer_plus, int *nlo_outer_minus, int *nhi_outer_minus, const double *width, const double *width_inner, const int *level) {
+  Lift L_(2, "lsm2ddeterminenarrowbandfromtwolevelsets_");
+  L_.box(ilo_gb, ihi_gb, jlo_gb, jhi_gb);
+  L_.box(ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb);
+  L_.list(nlo_index, nhi_index);
+  L_.list(nlo_index_outer, nhi_index_outer);
+  if (!L_.ready()) return;
+  lsm3ddeterminenarrowbandfromtwolevelsets_(phi, psi, ilo_gb, ihi_gb, jlo_gb, jhi_gb, &L_.k0, &L_.k0, narrow_band, ilo_nb_gb, ihi_nb_gb, jlo_nb_gb, jhi_nb_gb, &L_.k0, &L_.k0, index_x, index_y, (int *)L_.junk(), nlo_index, nhi_index, n_lo, n_hi, index_outer, nlo_index_outer, nhi_index_outer, nlo_outer_plus, nhi_outer_plus, nlo_outer_minus, nhi_outer_minus, width, width_inner, level);
 }
 
 // src/toolbox/lsm_spatial_derivatives2d.f.in:2395

@@ -160,6 +160,8 @@ DESC = {
     "lsm3dmarknarrowbandneighbors_": ("band", "breadth-first neighbour levels of a narrow band"),
     "lsm3dmarknarrowbandboundarylayer_": ("band", "mark the one-cell faces of a fill box"),
     "lsm3ddeterminenarrowbandfrommask_": ("band", "build a narrow band from the sign of a mask"),
+    "lsm3ddeterminenarrowbandfromtwolevelsets_": ("band", "build a narrow band of cells near the zero sets of both phi and psi"),
+    "lsm3ddeterminenarrowbandawayfrommask_": ("band", "build a narrow band of cells near phi = 0 and away from a mask (|phi - mask| > max dx)"),
     "lsm3dmultiplycutofflserhslocal_": ("band", "cubic cut-off of the RHS between beta and gamma"),
     "lsm3dcheckouternarrowbandlayer_": ("band", "1 when the outer band layer holds both signs of phi"),
     "lsm3dimposemasklocal_": ("band", "dest = max(mask, src) on listed cells"),
@@ -190,7 +192,23 @@ _UP2 = ([["phi_x", "real", True, True], ["phi_y", "real", True, True], ["phi_z",
         + [[f"{a}_index{l}", "int", False, False] for l in range(3) for a in ("nlo", "nhi")]
         + [["narrow_band", "int1", True, False]] + _box("nb")
         + [["mark_fb", "int1", False, False], ["mark_d1", "int1", False, False], ["mark_d2", "int1", False, False]])
+_BAND3 = ([[f"{a}_gb", "int", False, False] for a in ("ilo", "ihi", "jlo", "jhi", "klo", "khi")]
+          + [["narrow_band", "int1", True, True]] + _box("nb")
+          + [["index_x", "int", True, True], ["index_y", "int", True, True], ["index_z", "int", True, True],
+             ["nlo_index", "int", False, False], ["nhi_index", "int", False, False],
+             ["n_lo", "int", True, True], ["n_hi", "int", True, True], ["index_outer", "int", True, True],
+             ["nlo_index_outer", "int", False, False], ["nhi_index_outer", "int", False, False],
+             ["nlo_outer_plus", "int", False, True], ["nhi_outer_plus", "int", False, True],
+             ["nlo_outer_minus", "int", False, True], ["nhi_outer_minus", "int", False, True],
+             ["width", "real", False, False], ["width_inner", "real", False, False], ["level", "int", False, False]])
 NEW_SIGS = {
+    "lsm3ddeterminenarrowbandfromtwolevelsets_": {
+        "src": "NEW (pattern: src/toolbox/lsm_localization2d.f:248)",
+        "args": [["phi", "real", True, False], ["psi", "real", True, False]] + _BAND3},
+    "lsm3ddeterminenarrowbandawayfrommask_": {
+        "src": "NEW (pattern: src/toolbox/lsm_localization2d.f:365)",
+        "args": [["phi", "real", True, False], ["mask", "real", True, False]] + _BAND3
+                + [["dx", "real", False, False], ["dy", "real", False, False], ["dz", "real", False, False]]},
     "lsm3dupwindhjeno2local_": {"src": "NEW (pattern: src/toolbox/lsm_spatial_derivatives2d_local.f.in:1160)",
                                 "args": _UP2},
     "lsm3dhjweno5local_": {"src": "NEW (pattern: src/toolbox/lsm_spatial_derivatives2d_local.f.in:816)",
@@ -282,7 +300,13 @@ LIFT_VIA = {"lsm2dcomputemeancurvatureorder4local_": ("lsmgpu_mean_curvature_ord
             # the 1D signed extrapolation takes the sign from the cell next to
             # the edge (boundary_conditions1d.f:103), the 3D one from the edge
             "lsm1dsignedlinearextrapolation_": ("lsmgpu_signed_linear_extrapolation_inner_sign",
-                                                "signed linear extrapolation, sign from the cell next to the edge")}
+                                                "signed linear extrapolation, sign from the cell next to the edge"),
+            # the 2D band build sets n_hi(0) = count - 1 even for an empty band
+            # and adds neighbour levels only when level 0 holds two or more
+            # cells (localization2d.f:225-240); the 3D one (localization3d.f:274)
+            # sets n_hi(0) = nlo for an empty band and adds them for any
+            "lsm2ddeterminenarrowband_": ("lsmgpu_determine_narrow_band_2d_bookkeeping",
+                                          "build the narrow band: level-0 list in sweep order, outer lists, BFS levels")}
 
 # 1D routines written by hand in csrc/lifted_by_hand.cu: their arguments do
 # not map by name onto the 3D routine they run on (the 1D normal-velocity dt

@@ -771,6 +771,85 @@ void lsm3ddeterminenarrowband_(const real_t *phi, A3(g), mark_t *nb, A3(n), int 
   }
 }
 
+/* The 2D band builders' forms on 3D arrays (localization2d.f:174-464):
+ * mode 0 |phi| < width; 3 also |second| < width (FromTwoLevelSets, :248);
+ * 4 also |phi - second| > max_dx (AwayFromMask, :365).  bookkeeping 1
+ * (DetermineNarrowBand, :225-240): n_hi(0) = count - 1 always, neighbour
+ * levels when level > 0 and n_hi(0) > n_lo(0); 2 (:327-340): neighbour
+ * levels whenever level > 0. */
+static void determine_band_2dform(int mode, int bookkeeping, const real_t *phi, const real_t *second,
+                                  real_t max_dx, const gbox *G, mark_t *nb, const int *n_lo_box, int *ix_,
+                                  int *iy_, int *iz_, const int *nlo_index, const int *nhi_index, int *n_lo,
+                                  int *n_hi, int *index_outer, const int *nlo_outer_idx,
+                                  const int *nhi_outer_idx, int *nlo_outer_plus, int *nhi_outer_plus,
+                                  int *nlo_outer_minus, int *nhi_outer_minus, real_t width,
+                                  real_t width_inner, const int *level) {
+  gbox N = mk_box(n_lo_box, n_lo_box + 1, n_lo_box + 2, n_lo_box + 3, n_lo_box + 4, n_lo_box + 5);
+  const int base = *nlo_index, obase = *nlo_outer_idx;
+  int count = *nlo_index;
+  n_lo[0] = *nlo_index;
+  int cm = *nlo_outer_idx, cp = *nhi_outer_idx;
+  *nlo_outer_minus = *nlo_outer_idx;
+  *nhi_outer_plus = *nhi_outer_idx;
+  FOR_BOX(G->lo[0], G->hi[0], G->lo[1], G->hi[1], G->lo[2], G->hi[2]) {
+    long g = at(G, i, j, k);
+    real_t v = phi[g], a = fabs(v);
+    int take = a < width;
+    if (take && mode == 3) take = fabs(second[g]) < width;
+    if (take && mode == 4) take = fabs(v - second[g]) > max_dx;
+    long c = at(&N, i, j, k);
+    if (take) {
+      ix_[count - base] = i;
+      iy_[count - base] = j;
+      iz_[count - base] = k;
+      nb[c] = 1;
+      if (a >= width_inner) {
+        if (v <= 0.0)
+          index_outer[(cm++) - obase] = count;
+        else
+          index_outer[(cp--) - obase] = count;
+      }
+      count++;
+    } else {
+      nb[c] = 0;
+    }
+  }
+  n_hi[0] = count - 1;
+  *nhi_outer_minus = cm - 1;
+  *nlo_outer_plus = cp + 1;
+  if (*level > 0 && (bookkeeping == 2 || n_hi[0] > n_lo[0]))
+    lsm3dmarknarrowbandneighbors_(nb, N.lo, N.hi, N.lo + 1, N.hi + 1, N.lo + 2, N.hi + 2, ix_, iy_, iz_,
+                                  nlo_index, nhi_index, n_lo, n_hi, level);
+}
+
+#define BAND_ARGS                                                                                     \
+  mark_t *nb, A3(n), int *ix_, int *iy_, int *iz_, const int *nlo_index, const int *nhi_index,          \
+      int *n_lo, int *n_hi, int *index_outer, const int *nlo_outer_idx, const int *nhi_outer_idx,       \
+      int *nlo_outer_plus, int *nhi_outer_plus, int *nlo_outer_minus, int *nhi_outer_minus,             \
+      const real_t *width, const real_t *width_inner, const int *level
+#define BAND_PASS                                                                                     \
+  nb, nbox, ix_, iy_, iz_, nlo_index, nhi_index, n_lo, n_hi, index_outer, nlo_outer_idx, nhi_outer_idx, \
+      nlo_outer_plus, nhi_outer_plus, nlo_outer_minus, nhi_outer_minus, *width, *width_inner, level
+
+void lsmgpu_determine_narrow_band_2d_bookkeeping(const real_t *phi, A3(g), BAND_ARGS) {
+  gbox G = B3(g);
+  const int nbox[6] = {*n_ilo, *n_ihi, *n_jlo, *n_jhi, *n_klo, *n_khi};
+  determine_band_2dform(0, 1, phi, NULL, 0.0, &G, BAND_PASS);
+}
+
+void lsm3ddeterminenarrowbandfromtwolevelsets_(const real_t *phi, const real_t *psi, A3(g), BAND_ARGS) {
+  gbox G = B3(g);
+  const int nbox[6] = {*n_ilo, *n_ihi, *n_jlo, *n_jhi, *n_klo, *n_khi};
+  determine_band_2dform(3, 2, phi, psi, 0.0, &G, BAND_PASS);
+}
+
+void lsm3ddeterminenarrowbandawayfrommask_(const real_t *phi, const real_t *mask, A3(g), BAND_ARGS,
+                                           const real_t *dx, const real_t *dy, const real_t *dz) {
+  gbox G = B3(g);
+  const int nbox[6] = {*n_ilo, *n_ihi, *n_jlo, *n_jhi, *n_klo, *n_khi};
+  determine_band_2dform(4, 2, phi, mask, fmax2(fmax2(*dx, *dy), *dz), &G, BAND_PASS);
+}
+
 /* lsm3dMarkNarrowBandBoundaryLayer (:303-377): the six one-cell faces of the
  * fill box, over the ghost-box extent of the other axes */
 void lsm3dmarknarrowbandboundarylayer_(mark_t *nb, A3(g), const int *ilo_fb, const int *ihi_fb,

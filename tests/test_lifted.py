@@ -30,7 +30,11 @@ SCRATCH = ("d1", "d2", "d3")   # dense routines accept their scratch and leave i
 VOLUME = re.compile(r"volumeintegral|volumeregion|surfaceintegral|surfacearea")
 U = 2.0 ** -53
 # 2D narrow-band construction: its own cases below
-BAND2 = ("lsm2ddeterminenarrowband_", "lsm2dmarknarrowbandneighbors_", "lsm2ddeterminenarrowbandfrommask_")
+BAND2 = ("lsm2ddeterminenarrowband_", "lsm2dmarknarrowbandneighbors_", "lsm2ddeterminenarrowbandfrommask_",
+         "lsm2ddeterminenarrowbandfromtwolevelsets_", "lsm2ddeterminenarrowbandawayfrommask_")
+# builders whose level 0 is selected by |phi| < width
+WIDTH_BAND2 = ("lsm2ddeterminenarrowband_", "lsm2ddeterminenarrowbandfromtwolevelsets_",
+               "lsm2ddeterminenarrowbandawayfrommask_")
 
 
 def is_local(sym):
@@ -332,13 +336,20 @@ def band_phi2(seed):
     return np.asfortranarray(phi + 0.01 * rng.standard_normal(phi.shape))
 
 
-def band2_call(sym, seed, level=3):
+def band2_call(sym, seed, level=3, phi=None):
     """Every argument of a 2D band-construction call over GB_BAND, with list
-    capacity for every cell and stale contents in the outputs."""
+    capacity for every cell and stale contents in the outputs.  psi is a
+    second circle crossing phi's; the away-from-mask mask differs from phi by
+    more than max(dx, dy) on part of the band."""
     n = (GB_BAND[1] - GB_BAND[0] + 1, GB_BAND[3] - GB_BAND[2] + 1)
     cap = n[0] * n[1]
-    phi = band_phi2(seed)
-    v = {"phi": phi, "mask": phi, "narrow_band": np.zeros(n, dtype=np.uint8, order="F"),
+    phi = band_phi2(seed) if phi is None else phi
+    mask = phi
+    if sym == "lsm2ddeterminenarrowbandawayfrommask_":
+        i = np.arange(n[0]).reshape(-1, 1)
+        mask = np.asfortranarray(phi + 2.0 * DXB * (i % 3 == 0))
+    psi = np.asfortranarray(np.roll(band_phi2(seed + 7), 9, axis=0))
+    v = {"phi": phi, "mask": mask, "psi": psi, "dx": DXB, "dy": 1.1 * DXB, "narrow_band": np.zeros(n, dtype=np.uint8, order="F"),
          "index_x": np.full(cap, -99, np.int32), "index_y": np.full(cap, -99, np.int32),
          "nlo_index": 0, "nhi_index": cap - 1, "n_lo": np.full(level + 1, -7, np.int32),
          "n_hi": np.full(level + 1, -7, np.int32), "index_outer": np.full(cap, -99, np.int32),
@@ -392,10 +403,67 @@ def test_band2_principle_on_the_oracle(sym, seed, ref):
             v3[name] = np.zeros(cap, np.int32)
         elif name.startswith(("klo", "khi")):
             v3[name] = 0
+        elif name == "dz":
+            v3[name] = vals["dx"]
         else:
             raise KeyError(name)
     a3, s3 = H.run(H.oracle(), sym3, v3)
     band2_compare(sym, r_ref, (a3, s3))
+
+
+def degenerate_phi(kind):
+    """5 everywhere (no cell within the width), or one cell at 0"""
+    n = (GB_BAND[1] - GB_BAND[0] + 1, GB_BAND[3] - GB_BAND[2] + 1)
+    phi = np.full(n, 5.0, order="F")
+    if kind == "single":
+        phi[17, 11] = 0.0
+    return phi
+
+
+def degenerate_call(sym, kind):
+    # an empty level 0 with two or more neighbour levels makes the reference
+    # read list entry -1 (localization2d.f:120); one level keeps it defined
+    vals = band2_call(sym, 0, level=1 if kind == "empty" else 3, phi=degenerate_phi(kind))
+    if "psi" in vals:
+        vals["psi"] = np.zeros_like(vals["phi"], order="F")
+    if "mask" in vals:
+        vals["mask"] = np.asfortranarray(vals["phi"] + 1.0)
+    return vals
+
+
+@pytest.mark.parametrize("sym", WIDTH_BAND2)
+@pytest.mark.parametrize("kind", ["empty", "single"])
+def test_band2_degenerate_principle_on_the_oracle(sym, kind, ref):
+    """Empty and one-cell bands: the list bookkeeping of the 2D routines
+    (n_hi(0) = count - 1; neighbour levels only from two cells up in
+    lsm2dDetermineNarrowBand) through the 3D-array forms the 2D entry
+    points run on."""
+    vals = degenerate_call(sym, kind)
+    r_ref = H.run(ref, sym, vals)
+    sym3 = L.ABI[sym]["lifted_from"]
+    v3 = {}
+    for name, kind_, is_arr, written in L.ABI[sym3]["args"]:
+        if name in vals:
+            v3[name] = vals[name]
+        elif name == "index_z":
+            v3[name] = np.zeros(len(vals["index_x"]), np.int32)
+        elif name.startswith(("klo", "khi")):
+            v3[name] = 0
+        elif name == "dz":
+            v3[name] = vals["dx"]
+    r3 = H.run(H.oracle(), sym3, v3)
+    band2_compare(sym, r_ref, r3)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("sym", WIDTH_BAND2)
+@pytest.mark.parametrize("kind", ["empty", "single"])
+def test_band2_degenerate_gpu_matches_reference(sym, kind, ref, gpu_lib):
+    vals = degenerate_call(sym, kind)
+    r_ref = H.run(ref, sym, vals)
+    r_gpu = H.run(gpu_lib, sym, vals)
+    L.check(gpu_lib)
+    band2_compare(sym, r_ref, r_gpu)
 
 
 @pytest.mark.gpu

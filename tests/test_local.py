@@ -23,7 +23,9 @@ LEVEL = 3
 
 LOCAL = [s for s in L.ABI if s.startswith("lsm3d") and any(a[0] == "index_x" for a in L.ABI[s]["args"])
          and s not in ("lsm3ddeterminenarrowband_", "lsm3dmarknarrowbandneighbors_",
-                       "lsm3ddeterminenarrowbandfrommask_", "lsm3dcheckouternarrowbandlayer_")]
+                       "lsm3ddeterminenarrowbandfrommask_", "lsm3dcheckouternarrowbandlayer_",
+                       # no 3D original: checked through their 2D forms (test_lifted.py)
+                       "lsm3ddeterminenarrowbandfromtwolevelsets_", "lsm3ddeterminenarrowbandawayfrommask_")]
 # LSMLIB's lsm3dComputeStableConstNormalVelDtLOCAL reads unassigned locals;
 # the oracle implements the dense formula and is pinned against it below
 REF_UNDEFINED = {"lsm3dcomputestableconstnormalveldtlocal_"}
