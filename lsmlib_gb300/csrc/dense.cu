@@ -111,9 +111,12 @@ void hj_pm(const char *name, R *pxp, R *pyp, R *pzp, const Box &pb, R *pxm, R *p
   if (!phb.contains(fb, r, r, r)) call.fail("phi ghost box does not cover the fill box plus the stencil");
   if (!pb.contains(fb, 0, 0, 0) || !mb.contains(fb, 0, 0, 0)) call.fail("output ghost box does not cover the fill box");
   if (!call.ok() || fb.empty()) return;
-  const long long np = pb.size(), nm = mb.size();
-  Out3 P{view(call.inout(pxp, np), pb), view(call.inout(pyp, np), pb), view(call.inout(pzp, np), pb)};
-  Out3 M{view(call.inout(pxm, nm), mb), view(call.inout(pym, nm), mb), view(call.inout(pzm, nm), mb)};
+  // outputs written on every fill-box cell and nowhere else (host arrays:
+  // no copy in, the fill box copied back)
+  Out3 P{view(call.out_region(pxp, pb, fb), pb), view(call.out_region(pyp, pb, fb), pb),
+         view(call.out_region(pzp, pb, fb), pb)};
+  Out3 M{view(call.out_region(pxm, mb, fb), mb), view(call.out_region(pym, mb, fb), mb),
+         view(call.out_region(pzm, mb, fb), mb)};
   View<const R> ph = view((const R *)call.in(phi, phb.size()), phb);
   if (!call.ok()) return;
   Grid3 g = cover(fb);
@@ -129,8 +132,9 @@ void hj_upwind(const char *name, R *px, R *py, R *pz, const Box &gb, const R *ph
   if (!phb.contains(fb, r, r, r)) call.fail("phi ghost box does not cover the fill box plus the stencil");
   if (!gb.contains(fb, 0, 0, 0) || !vb.contains(fb, 0, 0, 0)) call.fail("ghost box does not cover the fill box");
   if (!call.ok() || fb.empty()) return;
-  const long long ng = gb.size(), nv = vb.size();
-  Out3 G{view(call.inout(px, ng), gb), view(call.inout(py, ng), gb), view(call.inout(pz, ng), gb)};
+  const long long nv = vb.size();
+  Out3 G{view(call.out_region(px, gb, fb), gb), view(call.out_region(py, gb, fb), gb),
+         view(call.out_region(pz, gb, fb), gb)};
   View<const R> ph = view((const R *)call.in(phi, phb.size()), phb);
   View<const R> VX = view((const R *)call.in(vx, nv), vb);
   View<const R> VY = view((const R *)call.in(vy, nv), vb);
@@ -209,7 +213,7 @@ void rk(const char *name, R *out, const Box &ob, const R *a, const Box &ab, cons
       (KIND != 0 && !ab.contains(fb, 0, 0, 0)))
     call.fail("ghost box does not cover the fill box");
   if (!call.ok() || fb.empty()) return;
-  View<R> O = view(call.inout(out, ob.size()), ob);
+  View<R> O = view(call.out_region(out, ob, fb), ob);
   View<const R> A = (KIND != 0) ? view((const R *)call.in(a, ab.size()), ab) : View<const R>{};
   View<const R> U = view((const R *)call.in(u, ub.size()), ub);
   View<const R> L = view((const R *)call.in(rhs, rb.size()), rb);
@@ -422,7 +426,7 @@ void curv_variant(const char *name, R *kappa, const Box &kb, const R *phi, const
   if (!kb.contains(fb, 0, 0, 0) || !gb.contains(fb, rg, rg, rg) || !phb.contains(fb, rp, rp, rp))
     call.fail("ghost box does not cover the stencil");
   if (!call.ok() || fb.empty()) return;
-  View<R> KA = view(call.inout(kappa, kb.size()), kb);
+  View<R> KA = view(call.out_region(kappa, kb, fb), kb);
   View<const R> PH = view((const R *)call.in(phi, phb.size()), phb);
   const long long ng = gb.size();
   View<const R> X = view((const R *)call.in(phi_x, ng), gb), Y = view((const R *)call.in(phi_y, ng), gb),
@@ -487,8 +491,8 @@ static void central(const char *name, int order, R *px, R *py, R *pz, const Box 
   if (!fb_phi.contains(fb, r, r, r)) call.fail("phi ghost box does not cover the fill box plus the stencil");
   if (!gb.contains(fb, 0, 0, 0)) call.fail("output ghost box does not cover the fill box");
   if (!call.ok() || fb.empty()) return;
-  const long long n = gb.size();
-  Out3 G{view(call.inout(px, n), gb), view(call.inout(py, n), gb), view(call.inout(pz, n), gb)};
+  Out3 G{view(call.out_region(px, gb, fb), gb), view(call.out_region(py, gb, fb), gb),
+         view(call.out_region(pz, gb, fb), gb)};
   View<const R> ph = view((const R *)call.in(phi, fb_phi.size()), fb_phi);
   if (!call.ok()) return;
   Grid3 g = cover(fb);
@@ -515,7 +519,7 @@ void lsm3dlaplacianorder2_(R *lap, BOXARG(l), const R *phi, BOXARG(f), FBARGS, D
   Box lb = BOXOF(l), phb = BOXOF(f), fb = FBOX;
   if (!phb.contains(fb, 1, 1, 1) || !lb.contains(fb, 0, 0, 0)) call.fail("ghost box does not cover the stencil");
   if (!call.ok() || fb.empty()) return;
-  View<R> L = view(call.inout(lap, lb.size()), lb);
+  View<R> L = view(call.out_region(lap, lb, fb), lb);
   View<const R> ph = view((const R *)call.in(phi, phb.size()), phb);
   if (!call.ok()) return;
   Grid3 g = cover(fb);
@@ -534,7 +538,7 @@ void lsm3dgradientmagnitude_(const R *phi_x, const R *phi_y, const R *phi_z, R *
   const long long n = gb.size();
   View<const R> X = view((const R *)call.in(phi_x, n), gb), Y = view((const R *)call.in(phi_y, n), gb),
                 Z = view((const R *)call.in(phi_z, n), gb);
-  View<R> M = view(call.inout(grad_phi_mag, n), gb);
+  View<R> M = view(call.out_region(grad_phi_mag, gb, fb), gb);
   if (!call.ok()) return;
   Grid3 g = cover(fb);
   LSMGPU_LAUNCH(k_gradmag, g.grid, g.block, 0, X, Y, Z, M, fb);
@@ -674,7 +678,7 @@ void lsm3dcomputereinitializationeqnrhs_(R *reinit_rhs, BOXARG(r), const R *phi,
       (use0 ? !zb.contains(fb, 0, 0, 0) : !phb.contains(fb, 0, 0, 0)))
     call.fail("ghost box does not cover the fill box");
   if (!call.ok() || fb.empty()) return;
-  View<R> O = view(call.inout(reinit_rhs, rb.size()), rb);
+  View<R> O = view(call.out_region(reinit_rhs, rb, fb), rb);
   View<const R> PH = use0 ? View<const R>{} : view((const R *)call.in(phi, phb.size()), phb);
   View<const R> P0 = use0 ? view((const R *)call.in(phi0, zb.size()), zb) : View<const R>{};
   const long long np = pb.size(), nm = mb.size();
@@ -698,7 +702,7 @@ void lsm3dcomputemeancurvatureorder2_(R *kappa, BOXARG(k), const R *phi, BOXARG(
   if (!kb.contains(fb, 0, 0, 0) || !gb.contains(fb, 0, 0, 0) || !phb.contains(fb, 1, 1, 1))
     call.fail("ghost box does not cover the stencil");
   if (!call.ok() || fb.empty()) return;
-  View<R> K = view(call.inout(kappa, kb.size()), kb);
+  View<R> K = view(call.out_region(kappa, kb, fb), kb);
   View<const R> PH = view((const R *)call.in(phi, phb.size()), phb);
   const long long ng = gb.size();
   View<const R> X = view((const R *)call.in(phi_x, ng), gb), Y = view((const R *)call.in(phi_y, ng), gb),

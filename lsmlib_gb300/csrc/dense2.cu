@@ -28,6 +28,8 @@ void for_box(const Box &b, F f) {
 
 View<const R> vin(Call &c, const R *p, const Box &b) { return view((const R *)c.in(p, b.size()), b); }
 View<R> vio(Call &c, R *p, const Box &b) { return view(c.inout(p, b.size()), b); }
+// an output written on every cell of `fb` and nowhere else
+View<R> vout(Call &c, R *p, const Box &b, const Box &fb) { return view(c.out_region(p, b, fb), b); }
 
 // boundary conditions (boundary_conditions3d.f:46-639)
 // BC_SIGNED_INNER: the 1D routine's form, the sign taken from the cell next
@@ -180,8 +182,8 @@ void lsm3dcentralhessian_(R *phi_xx, R *phi_xy, R *phi_xz, R *phi_yy, R *phi_yz,
   Box hb = BOXOF(h), gb = BOXOF(g), fb = BOXOF(fb);
   if (!gb.contains(fb, 1, 1, 1) || !hb.contains(fb, 0, 0, 0)) call.fail("ghost box does not cover the stencil");
   if (!call.ok() || fb.empty()) return;
-  View<R> XX = vio(call, phi_xx, hb), XY = vio(call, phi_xy, hb), XZ = vio(call, phi_xz, hb),
-          YY = vio(call, phi_yy, hb), YZ = vio(call, phi_yz, hb), ZZ = vio(call, phi_zz, hb);
+  View<R> XX = vout(call, phi_xx, hb, fb), XY = vout(call, phi_xy, hb, fb), XZ = vout(call, phi_xz, hb, fb),
+          YY = vout(call, phi_yy, hb, fb), YZ = vout(call, phi_yz, hb, fb), ZZ = vout(call, phi_zz, hb, fb);
   View<const R> F = vin(call, phi, gb);
   if (!call.ok()) return;
   const R ddx = *dx, ddy = *dy, ddz = *dz;
@@ -206,7 +208,7 @@ void lsm3daveragegradphi_(R *phi_x, R *phi_y, R *phi_z, BOXARG(g), const R *phi_
   if (!gb.contains(fb, 0, 0, 0) || !pb.contains(fb, 0, 0, 0) || !mb.contains(fb, 0, 0, 0))
     call.fail("ghost box does not cover the fill box");
   if (!call.ok() || fb.empty()) return;
-  View<R> X = vio(call, phi_x, gb), Y = vio(call, phi_y, gb), Z = vio(call, phi_z, gb);
+  View<R> X = vout(call, phi_x, gb, fb), Y = vout(call, phi_y, gb, fb), Z = vout(call, phi_z, gb, fb);
   View<const R> XP = vin(call, phi_x_plus, pb), YP = vin(call, phi_y_plus, pb), ZP = vin(call, phi_z_plus, pb);
   View<const R> XM = vin(call, phi_x_minus, mb), YM = vin(call, phi_y_minus, mb), ZM = vin(call, phi_z_minus, mb);
   if (!call.ok()) return;
