@@ -497,6 +497,7 @@ def gpu_arm(args, world, rank, local):
             "batched_4096": sub_batched(stream, dev),
             "adjoint_192": sub_adjoint(stream, dev),
             "geometry_512": sub_geometry(stream, dev),
+            "dropin_192": sub_dropin(stream, dev),
         }
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -684,6 +685,64 @@ def sub_adjoint(stream, dev, n=192, steps=40, ckpt=8):
     out["checkpoint_every_%d" % ckpt] = measure(ckpt)
     return out
 
+
+
+DROPIN_ROUTINES = ("lsm3dhjweno5_", "lsm3dupwindhjweno5_", "lsm3dtvdrk3stage2_",
+                   "lsm3dcomputereinitializationeqnrhs_")
+
+
+def dropin_values(sym, n, make):
+    """Arguments of a drop-in routine over the n^3 fill box with 3 ghost cells:
+    every array over the ghost box from `make(shape)`, LSMLIB's default
+    spacings and scalars."""
+    import lsmlib_gb300 as L
+    gb = (-GHOST, n - 1 + GHOST)
+    shape = (n + 2 * GHOST,) * 3
+    names = ("ilo", "ihi", "jlo", "jhi", "klo", "khi")
+    sc = {"dx": 2.0 / n, "dy": 2.0 / n, "dz": 2.0 / n, "dt": 0.4 / n, "use_phi0_for_sgn": 1}
+    vals = {}
+    for name, kind, is_arr, written in L.ABI[sym]["args"]:
+        pre = name[:3]
+        if is_arr:
+            vals[name] = make(shape)
+        elif pre in names and not is_arr:
+            fill = name.endswith("_fb") or name[4:] == "fb"
+            lo_hi = (0, n - 1) if fill else gb
+            vals[name] = lo_hi[pre[1:] == "hi"]
+        else:
+            vals[name] = sc[name]
+    return vals
+
+
+def sub_dropin(stream, dev, n=192, reps=5):
+    """LSMLIB's dense drop-in routines through the C ABI (FP64) on host
+    arrays (staged: inputs copied in, outputs' fill box copied back, the call
+    returns when done) and on device arrays (used in place), n^3 fill box."""
+    import torch
+    import lsmlib_gb300 as L
+    lib = L.lib()
+    rng = np.random.default_rng(5)
+    out = {"workload": "dropin-%d: %s, FP64, random fields over the ghost box" % (n, ", ".join(DROPIN_ROUTINES))}
+    for sym in DROPIN_ROUTINES:
+        host = dropin_values(sym, n, lambda sh: np.asfortranarray(rng.standard_normal(sh)))
+        L.invoke(lib, sym, host)
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            L.invoke(lib, sym, host)
+            ts.append(time.perf_counter() - t0)
+        devv = {k: (torch.from_numpy(np.ascontiguousarray(v.T)).to(dev) if isinstance(v, np.ndarray) else v)
+                for k, v in host.items()}
+        L.invoke(lib, sym, devv)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            L.invoke(lib, sym, devv)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[sym] = {"host_arrays_ms": 1e3 * sorted(ts)[reps // 2], "device_arrays_ms": e0.elapsed_time(e1) / reps}
+    return out
 
 
 def sub_geometry(stream, dev, n=512, reps=10):
