@@ -536,9 +536,13 @@ __global__ void __launch_bounds__(kRowMax, sizeof(R) == 4 ? LSMGPU_ADJ_ROW_CTAS 
       cm = M[ok];
       cv = load_coef<R, MODE>(a, 2, col + ok);
     }
+    // accumulators' old values and the P / Q terms are loaded ahead of the
+    // slot evaluations that precede their use (distinct arrays)
+    const bool gzw = MODE == ADJ_ADV && a.gvel[2] && own && kk >= z0 && kk < zend;
+    const R gz_old = gzw ? a.gvel[2][col + okk] : R(0);
     R G[6];
     const R gz = coef_slots_d<R, EXACT, MODE>(dw, uz, 2, mring[3], dt, iz, G);
-    if (MODE == ADJ_ADV && a.gvel[2] && own && kk >= z0 && kk < zend) a.gvel[2][col + okk] += gz;
+    if (gzw) a.gvel[2][col + okk] = gz_old + gz;
     const R Az = ring_step<R>(F, prevV, G);
     const int k = kk - 3;
     if (k < z0) continue;  // uniform over the CTA
@@ -554,9 +558,12 @@ __global__ void __launch_bounds__(kRowMax, sizeof(R) == 4 ? LSMGPU_ADJ_ROW_CTAS 
       for (int q = 0; q < 7; q++) xsn[q] = s[o + xo[q]];
       xvn = load_coef<R, MODE>(a, 0, col + o);
     }
-    const R gx = coef_slots<R, EXACT, MODE>(w7, ux, 0, mring[0], dt, ix, G);
     const long long c = col + ob;
-    if (MODE == ADJ_ADV && a.gvel[0] && own) a.gvel[0][c] += gx;
+    const bool gxw = MODE == ADJ_ADV && a.gvel[0] && own;
+    const R gx_old = gxw ? a.gvel[0][c] : R(0);
+    const R p_c = (a.P && own) ? a.P[c] : R(0), q_c = (a.Q && own) ? a.Q[c] : R(0);
+    const R gx = coef_slots<R, EXACT, MODE>(w7, ux, 0, mring[0], dt, ix, G);
+    if (gxw) a.gvel[0][c] = gx_old + gx;
     R *bb = buf + b * 6 * npad;
     if (own) {
 #pragma unroll
@@ -570,8 +577,8 @@ __global__ void __launch_bounds__(kRowMax, sizeof(R) == 4 ? LSMGPU_ADJ_ROW_CTAS 
     b ^= 1;
     if (!own) continue;
     R o = mring[0] + (Ax + Az);
-    if (a.P) o += a.pscale * a.P[c];
-    if (a.Q) o += a.qscale * a.Q[c];
+    if (a.P) o += a.pscale * p_c;
+    if (a.Q) o += a.qscale * q_c;
     a.out[c] = o;
   }
 }
@@ -630,12 +637,19 @@ __global__ void __launch_bounds__(32 * kRows, sizeof(R) == 4 ? LSMGPU_ADJ_Y_CTAS
       cm = M[ok];
       cv = load_coef<R, MODE>(a, 1, base + ok);
     }
+    // the accumulators' old values are loaded before the slot evaluation so
+    // their latency overlaps it (out, gvel and the state arrays are distinct)
+    const bool gw = MODE == ADJ_ADV && a.gvel[1] && jj >= y0 && jj < yend;
+    const bool ow = jj - 3 >= y0;
+    const long long tgt = base + plane_add(ojj, yjj, -3, ny, py);
+    const R g_old = gw ? a.gvel[1][base + ojj] : R(0);
+    const R o_old = ow ? a.out[tgt] : R(0);
     R G[6];
     const R gy = coef_slots_d<R, EXACT, MODE>(dw, uy, 1, mring[3], dt, iy, G);
-    if (MODE == ADJ_ADV && a.gvel[1] && jj >= y0 && jj < yend) a.gvel[1][base + ojj] += gy;
+    if (gw) a.gvel[1][base + ojj] = g_old + gy;
     const R Ay = ring_step<R>(F, prevV, G);
-    if (jj - 3 < y0) continue;
-    a.out[base + plane_add(ojj, yjj, -3, ny, py)] += Ay;
+    if (!ow) continue;
+    a.out[tgt] = o_old + Ay;
   }
 }
 

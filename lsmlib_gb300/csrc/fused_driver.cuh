@@ -99,27 +99,31 @@ void launch_bc(R *buf, const Layout &L, int bc) {
   }
 }
 
+// Launches one stage kernel; with prepare_only it only sets the kernel's
+// dynamic shared memory limit (done once, and before a launch is captured into
+// a graph).  The function has internal linkage: each translation unit that
+// launches a stage kernel has its own kernel instance, and its own copy of
+// this function and of the flag below, so the limit is set on the instance
+// the unit launches.
 template <class R, int MODE, bool EXACT>
-void launch_stage(const CUtensorMap &tm, const StageArgs<R> &a) {
+static void launch_stage(const CUtensorMap &tm, const StageArgs<R> &a, bool prepare_only = false) {
   const Layout &L = a.L;
   dim3 blk(TX, TY);
   dim3 grd((unsigned)((L.nx + TX - 1) / TX), (unsigned)((L.ny + TY - 1) / TY), (unsigned)((L.nz + TZ - 1) / TZ));
   const size_t smem = (size_t)SX * SY * SZ * sizeof(R);
   static bool attr_set = false;
-  if constexpr (!EXACT && sizeof(R) == 4) {
-    // FP32 form: the packed cell-pair kernel
-    if (!attr_set) {
+  if (!attr_set) {
+    if constexpr (!EXACT && sizeof(R) == 4)
       cudaFuncSetAttribute(k_stage_f32<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      attr_set = true;
-    }
-    k_stage_f32<MODE><<<grd, blk, smem, stream()>>>(tm, a);
-  } else {
-    if (!attr_set) {
+    else
       cudaFuncSetAttribute(k_stage<R, MODE, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      attr_set = true;
-    }
-    k_stage<R, MODE, EXACT><<<grd, blk, smem, stream()>>>(tm, a);
+    attr_set = true;
   }
+  if (prepare_only) return;
+  if constexpr (!EXACT && sizeof(R) == 4)
+    k_stage_f32<MODE><<<grd, blk, smem, stream()>>>(tm, a);  // FP32 form: the packed cell-pair kernel
+  else
+    k_stage<R, MODE, EXACT><<<grd, blk, smem, stream()>>>(tm, a);
   note_launch();
 }
 
@@ -203,23 +207,42 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, const R *vx
   a.periodic = rs.bc == LSMGPU_BC_PERIODIC;
   a.err = err;
 
-  for (int step = 0; step < rs.n_steps; step++) {
-    a.stage = 1; a.phi_n = A; a.out = B;
-    if (rs.mode == REINIT) launch_stage<R, REINIT, EXACT>(tA, a);
-    else if (rs.mode == ADV_CONST) launch_stage<R, ADV_CONST, EXACT>(tA, a);
-    else launch_stage<R, ADV_FIELD, EXACT>(tA, a);
-    launch_bc(B, L, rs.bc);
-    a.stage = 2; a.out = C;
-    if (rs.mode == REINIT) launch_stage<R, REINIT, EXACT>(tB, a);
-    else if (rs.mode == ADV_CONST) launch_stage<R, ADV_CONST, EXACT>(tB, a);
-    else launch_stage<R, ADV_FIELD, EXACT>(tB, a);
-    launch_bc(C, L, rs.bc);
-    a.stage = 3; a.out = A;
-    if (rs.mode == REINIT) launch_stage<R, REINIT, EXACT>(tC, a);
-    else if (rs.mode == ADV_CONST) launch_stage<R, ADV_CONST, EXACT>(tC, a);
-    else launch_stage<R, ADV_FIELD, EXACT>(tC, a);
-    launch_bc(A, L, rs.bc);
-  }
+  if (rs.mode == REINIT) launch_stage<R, REINIT, EXACT>(tA, a, true);
+  else if (rs.mode == ADV_CONST) launch_stage<R, ADV_CONST, EXACT>(tA, a, true);
+  else launch_stage<R, ADV_FIELD, EXACT>(tA, a, true);
+  // the n_steps x (3 stages + ghost fills) launches, replayed as one CUDA
+  // graph when the same buffers, sizes and parameters come again
+  auto steps = [&]() {
+    StageArgs<R> b = a;
+    for (int step = 0; step < rs.n_steps; step++) {
+      b.stage = 1; b.phi_n = A; b.out = B;
+      if (rs.mode == REINIT) launch_stage<R, REINIT, EXACT>(tA, b);
+      else if (rs.mode == ADV_CONST) launch_stage<R, ADV_CONST, EXACT>(tA, b);
+      else launch_stage<R, ADV_FIELD, EXACT>(tA, b);
+      launch_bc(B, L, rs.bc);
+      b.stage = 2; b.out = C;
+      if (rs.mode == REINIT) launch_stage<R, REINIT, EXACT>(tB, b);
+      else if (rs.mode == ADV_CONST) launch_stage<R, ADV_CONST, EXACT>(tB, b);
+      else launch_stage<R, ADV_FIELD, EXACT>(tB, b);
+      launch_bc(C, L, rs.bc);
+      b.stage = 3; b.out = A;
+      if (rs.mode == REINIT) launch_stage<R, REINIT, EXACT>(tC, b);
+      else if (rs.mode == ADV_CONST) launch_stage<R, ADV_CONST, EXACT>(tC, b);
+      else launch_stage<R, ADV_FIELD, EXACT>(tC, b);
+      launch_bc(A, L, rs.bc);
+    }
+  };
+  GraphKey key;
+  key.add((int)sizeof(R));
+  key.add((int)EXACT);
+  key.add(rs.mode);
+  key.add(rs.n_steps);
+  key.add(rs.bc);
+  key.add(A);
+  key.add(B);
+  key.add(C);
+  key.add(a);  // value-initialised, so its padding is zero
+  if (!graph_replay(key, steps)) steps();
   {
     dim3 blk(32, 4, 2);
     dim3 grd((unsigned)((nx + 6 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));

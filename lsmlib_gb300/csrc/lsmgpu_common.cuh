@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stddef.h>
+#include <string.h>
 
 #include "../../include/lsmgpu.h"
 
@@ -132,6 +133,32 @@ inline Grid3 cover(const Box &fb, int bx = 32, int by = 4, int bz = 2) {
 // ---------------------------------------------------------------------------
 cudaStream_t stream();                      // library stream (lsmgpu_set_stream)
 void note_launch();                         // counts kernels for lsmgpu_launch_count()
+
+// Replays `body`'s stream work as a CUDA graph on the library stream.  The
+// graph is captured (on a library-owned stream, thread-local capture mode)
+// the first time a key is seen and kept for later calls with the same key;
+// the key must hold every value the captured work depends on (buffers,
+// sizes, scalars).  Returns false when capturing or launching fails (nothing
+// was queued; the caller then runs `body` directly).
+struct GraphKey {
+  unsigned char bytes[512];
+  size_t n = 0;
+  template <class T>
+  void add(const T &v) {  // appends v's bytes (T without padding, or zero-initialised)
+    static_assert(sizeof(T) <= sizeof(bytes), "key part too large");
+    if (n + sizeof(T) > sizeof(bytes)) {
+      n = sizeof(bytes) + 1;  // marks the key unusable
+      return;
+    }
+    memcpy(bytes + n, &v, sizeof(T));
+    n += sizeof(T);
+  }
+};
+bool graph_replay(const GraphKey &key, void (*body)(void *), void *ctx);
+template <class F>
+bool graph_replay(const GraphKey &key, F &body) {
+  return graph_replay(key, [](void *c) { (*static_cast<F *>(c))(); }, &body);
+}
 void set_error(int code, const char *fmt, ...);
 void clear_error();
 bool cuda_ok(cudaError_t e, const char *what);  // records and returns false on error

@@ -40,7 +40,84 @@ Arena g_arena[64];
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
-cudaStream_t stream() { return g_stream.load(); }
+namespace {
+thread_local cudaStream_t t_capture_stream = nullptr;  // set while a graph is captured
+
+// cached executable graphs: key, graph, kernels per replay; per device
+struct GraphEntry {
+  int dev;
+  GraphKey key;
+  cudaGraphExec_t exec;
+  long long kernels;
+};
+std::vector<GraphEntry> g_graphs;
+constexpr size_t kMaxGraphs = 16;
+cudaStream_t g_capture[64] = {};
+}  // namespace
+
+cudaStream_t stream() { return t_capture_stream ? t_capture_stream : g_stream.load(); }
+
+// Called with the library lock held (inside a Call), so the cache and the
+// capture stream are not shared with another thread meanwhile.
+bool graph_replay(const GraphKey &key, void (*body)(void *), void *ctx) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || key.n > sizeof(key.bytes)) {
+    cudaGetLastError();
+    return false;
+  }
+  for (size_t q = 0; q < g_graphs.size(); q++) {
+    GraphEntry &e = g_graphs[q];
+    if (e.dev == dev && e.key.n == key.n && memcmp(e.key.bytes, key.bytes, key.n) == 0) {
+      if (cudaGraphLaunch(e.exec, g_stream.load()) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+      }
+      g_launches.fetch_add(e.kernels, std::memory_order_relaxed);
+      return true;
+    }
+  }
+  if (!g_capture[dev] && cudaStreamCreateWithFlags(&g_capture[dev], cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    g_capture[dev] = nullptr;
+    return false;
+  }
+  if (cudaStreamBeginCapture(g_capture[dev], cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const long long before = g_launches.load();
+  t_capture_stream = g_capture[dev];
+  body(ctx);
+  t_capture_stream = nullptr;
+  const long long kernels = g_launches.load() - before;
+  g_launches.fetch_sub(kernels, std::memory_order_relaxed);  // counted when replayed
+  cudaGraph_t graph = nullptr;
+  if (cudaStreamEndCapture(g_capture[dev], &graph) != cudaSuccess || !graph) {
+    cudaGetLastError();
+    if (graph) cudaGraphDestroy(graph);
+    return false;
+  }
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ie != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (g_graphs.size() >= kMaxGraphs) {
+    // the oldest entry goes; work it queued earlier keeps running (a graph
+    // exec destroyed while launched completes its launches)
+    cudaGraphExecDestroy(g_graphs.front().exec);
+    g_graphs.erase(g_graphs.begin());
+  }
+  g_graphs.push_back({dev, key, exec, kernels});
+  if (cudaGraphLaunch(exec, g_stream.load()) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  g_launches.fetch_add(kernels, std::memory_order_relaxed);
+  return true;
+}
 
 void set_error(int code, const char *fmt, ...) {
   g_err = code;
