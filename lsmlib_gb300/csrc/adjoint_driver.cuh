@@ -62,9 +62,10 @@ inline int pick_chunk(int n_march, long long threads_per_chunk, int per_sm) {
   return c;
 }
 
-// one reverse stage: x and z faces (writes out), then y faces (adds to out)
+// one reverse stage: x and z faces (writes out), then y faces (adds to out);
+// internal linkage, so the shared-memory limit is set on this unit's kernel
 template <class R, bool EXACT, int MODE>
-void launch_adj_stage(const AdjStageArgs<R> &a) {
+static void launch_adj_stage(const AdjStageArgs<R> &a) {
   const Layout &L = a.L;
   dim3 blk(32, kRows);
   if (L.nx <= kRowMax) {
