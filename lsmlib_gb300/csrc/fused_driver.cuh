@@ -87,16 +87,85 @@ __global__ void k_linear_bc(R *phi, Layout L, int axis, int kind) {
   }
 }
 
+// The three passes above leave each ghost cell with a composition of at most
+// three one-axis extrapolations of interior values: the x pass is final on
+// x-ghost cells of interior (y, z) rows, the y pass (which reads x-ghost
+// values at the y edge) on y-ghost cells of interior z planes, the z pass on
+// every z-ghost cell.  k_ghost_fill evaluates that composition directly, one
+// thread per ghost cell of the 3-layer shell, in one launch; every
+// extrapolation is the same arithmetic as k_linear_bc's, so the values are
+// identical to the three passes'.
+template <class R>
+__device__ __forceinline__ R extrap(R e, R n, int g, int kind) {
+  if (kind == LSMGPU_BC_COPY) return e;
+  const R s = (kind == LSMGPU_BC_SIGNED_LINEAR) ? copysign(R(1.0), e) * fabs(e - n) : e - n;
+  return e + s * R(g);
+}
+
+template <class R>
+struct GhostShell {
+  const R *phi;
+  Layout L;
+  int kind;
+  __device__ R at(int i, int j, int k) const { return phi[L.idx(i, j, k)]; }
+  __device__ R X(int i, int j, int k) const {  // j, k interior
+    if (i < 0) return extrap(at(0, j, k), at(1, j, k), -i, kind);
+    if (i >= L.nx) return extrap(at(L.nx - 1, j, k), at(L.nx - 2, j, k), i - (L.nx - 1), kind);
+    return at(i, j, k);
+  }
+  __device__ R Y(int i, int j, int k) const {  // k interior
+    if (j < 0) return extrap(X(i, 0, k), X(i, 1, k), -j, kind);
+    if (j >= L.ny) return extrap(X(i, L.ny - 1, k), X(i, L.ny - 2, k), j - (L.ny - 1), kind);
+    return X(i, j, k);
+  }
+  __device__ R Z(int i, int j, int k) const {
+    if (k < 0) return extrap(Y(i, j, 0), Y(i, j, 1), -k, kind);
+    if (k >= L.nz) return extrap(Y(i, j, L.nz - 1), Y(i, j, L.nz - 2), k - (L.nz - 1), kind);
+    return Y(i, j, k);
+  }
+};
+
+// ghost shell: blockIdx.z picks a face (z below / above over the full x, y
+// extent, y below / above over the full x extent and interior z, x below /
+// above over interior y, z); a thread takes one line through the face,
+// evaluates the edge value and its neighbour once and writes the 3 ghost
+// cells of the line.  The values depend only on interior cells, so the
+// threads' writes do not interfere.
+template <class R>
+__global__ void k_ghost_fill(R *phi, Layout L, int kind) {
+  const int a = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int b = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int face = (int)blockIdx.z, upper = face & 1;
+  const GhostShell<R> G{phi, L, kind};
+  R e, n;
+  if (face < 2) {
+    if (a >= L.nx + 6 || b >= L.ny + 6) return;
+    const int i = a - 3, j = b - 3, k0 = upper ? L.nz - 1 : 0, k1 = upper ? L.nz - 2 : 1;
+    e = G.Y(i, j, k0);
+    n = G.Y(i, j, k1);
+    for (int g = 1; g <= 3; g++) phi[L.idx(i, j, upper ? k0 + g : -g)] = extrap(e, n, g, kind);
+  } else if (face < 4) {
+    if (a >= L.nx + 6 || b >= L.nz) return;
+    const int i = a - 3, k = b, j0 = upper ? L.ny - 1 : 0, j1 = upper ? L.ny - 2 : 1;
+    e = G.X(i, j0, k);
+    n = G.X(i, j1, k);
+    for (int g = 1; g <= 3; g++) phi[L.idx(i, upper ? j0 + g : -g, k)] = extrap(e, n, g, kind);
+  } else {
+    if (a >= L.ny || b >= L.nz) return;
+    const int j = a, k = b, i0 = upper ? L.nx - 1 : 0, i1 = upper ? L.nx - 2 : 1;
+    e = G.at(i0, j, k);
+    n = G.at(i1, j, k);
+    for (int g = 1; g <= 3; g++) phi[L.idx(upper ? i0 + g : -g, j, k)] = extrap(e, n, g, kind);
+  }
+}
+
 template <class R>
 void launch_bc(R *buf, const Layout &L, int bc) {
   if (bc == LSMGPU_BC_PERIODIC) return;  // written by the stage kernel
-  const int n[3] = {L.nx, L.ny, L.nz};
-  for (int axis = 0; axis < 3; axis++) {
-    const int o1 = axis == 0 ? 1 : 0, o2 = axis == 2 ? 1 : 2;
-    dim3 blk(32, 8);
-    dim3 grd((unsigned)((n[o1] + 6 + 31) / 32), (unsigned)((n[o2] + 6 + 7) / 8));
-    LSMGPU_LAUNCH(k_linear_bc<R>, grd, blk, 0, buf, L, axis, bc);
-  }
+  const int wa = (L.nx + 6 > L.ny ? L.nx + 6 : L.ny), wb = (L.ny + 6 > L.nz ? L.ny + 6 : L.nz);
+  dim3 blk(32, 8);
+  dim3 grd((unsigned)((wa + 31) / 32), (unsigned)((wb + 7) / 8), 6);
+  LSMGPU_LAUNCH(k_ghost_fill<R>, grd, blk, 0, buf, L, bc);
 }
 
 // Launches one stage kernel; with prepare_only it only sets the kernel's
