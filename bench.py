@@ -811,6 +811,59 @@ def sub_geometry(stream, dev, n=512, reps=10):
 MEASURED_STAGE_TRAFFIC = 285.6e6
 
 
+# ---------------------------------------------------------------------------
+# one call of a hot-path workload on cuda:0, for profilers (--case)
+# ---------------------------------------------------------------------------
+def profile_case(a):
+    """One fused call on cuda:0 (no timing): `--case reinit|advect` runs
+    `--iters` WENO5 / TVD-RK3 iterations of the headline field at n^3 then the
+    mean curvature (kernels k_stage*); `adjoint` the objective gradient of
+    adjoint_case (checkpoint every 4; k_adj_xz_row, k_adj_y); `band`
+    `--iters` narrow-band steps of band_case (rebuild every 5, FP32);
+    `batched` `--iters` steps of n grids of batched_case; `geometry`
+    sub_geometry at n^3 with `--iters` calls per entry point."""
+    import torch
+    import lsmlib_gb300 as L
+    from lsmlib_gb300 import build as B
+    B.build()
+    L.set_stream(torch.cuda.current_stream().cuda_stream)
+    gb, fb = boxes(a.n)
+    dt = torch.float32 if a.precision == "f32" else torch.float64
+    if a.case == "adjoint":
+        phi0, vel, tgt, h, tstep = adjoint_case(a.n)
+        ghost = lambda v: torch.from_numpy(np.ascontiguousarray(np.pad(v, 3).T)).cuda().to(dt)
+        J, _, _ = L.advect_adjoint_weno5_tvdrk3(ghost(phi0), gb, fb, [ghost(v) for v in vel], gb, ghost(tgt), h,
+                                                tstep, a.iters, 1.5 * h, checkpoint_every=4, precision=a.precision)
+        info = "J %r" % J
+    elif a.case == "geometry":
+        r = sub_geometry(torch.cuda.current_stream(), "cuda", n=a.n, reps=a.iters)
+        info = str({k: v["ms_per_call"] for k, v in r.items() if isinstance(v, dict)})
+    elif a.case == "band":
+        phi, dx = band_case("cuda", a.n)
+        _, bands = L.band_flow_weno5_tvdrk3(phi, gb, fb, dx, a.iters, 5, 6 * dx, 3 * dx, a_n=1.0, b_n=0.1, cfl=0.5,
+                                            precision="f32")
+        info = "band cells %d" % int(bands[0])
+    elif a.case == "batched":
+        buf, offsets, dims, vel, spacing, tstep = batched_case("cuda", a.n)
+        L.advect_batch_weno5_tvdrk3(buf, offsets, dims, vel, spacing, tstep, a.iters)
+        info = "%d grids" % a.n
+    else:
+        phi64, dx = initial_phi(a.n)
+        phi = torch.from_numpy(np.ascontiguousarray(phi64.T)).cuda().to(dt)
+        kappa = torch.zeros_like(phi)
+        if a.case == "reinit":
+            L.reinit_weno5_tvdrk3(phi, gb, fb, dx, 0.5 * dx, a.iters, use_phi0_for_sgn=1, bc=a.bc,
+                                  precision=a.precision)
+        else:
+            L.advect_weno5_tvdrk3(phi, gb, fb, dx, dx / 3.5, a.iters, vel_const=(1.0, 0.5, 0.25), bc=a.bc,
+                                  precision=a.precision)
+        L.mean_curvature_o2(kappa, gb, phi, gb, fb, dx, precision=a.precision)
+        info = ""
+    torch.cuda.synchronize()
+    L.check()
+    print("ok", a.case, a.n, a.iters, a.precision, info, "launches", L.launch_count())
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -820,7 +873,15 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
     ap.add_argument("--no-extra", action="store_true", help="skip the other workloads")
+    ap.add_argument("--case", choices=["reinit", "advect", "adjoint", "band", "batched", "geometry"],
+                    help="run one call of that workload for a profiler instead of the benchmark")
+    ap.add_argument("--iters", type=int, default=1, help="iterations / steps / calls of --case")
+    ap.add_argument("--precision", choices=["f32", "f64"], default="f32", help="precision of --case")
+    ap.add_argument("--bc", type=int, default=2, help="boundary condition of --case reinit / advect")
     args = ap.parse_args()
+    if args.case:
+        profile_case(args)
+        return
     world, rank, local = dist_setup()
     if args.impl == "reference":
         reference_arm(args, world, rank)

@@ -55,6 +55,15 @@ int lsmgpu_synchronize(void);
 long long lsmgpu_launch_count(void);
 void lsmgpu_reset_launch_count(void);
 
+/* Number of CUDA graphs the fused steppers have captured since the process
+ * started.  A stepper call replays a cached graph when its buffers, sizes and
+ * parameters were seen before, and captures a new one otherwise. */
+long long lsmgpu_graph_capture_count(void);
+
+/* Device memory (bytes, all devices) the library's grow-only staging and
+ * temporary arena holds.  It grows with cudaMalloc and is never freed. */
+long long lsmgpu_arena_bytes(void);
+
 /* ---------------------------------------------------------------------------
  * Fused WENO5 / TVD-RK3 time steppers.
  *
@@ -228,7 +237,8 @@ int lsmgpu_reinit_vjp_weno5_tvdrk3_f32(const float *phi, const int *gb, const in
  *  - the velocity arrays must already be in device (or managed) memory;
  *  - the index box may hold at most 536,870,912 cells (65536 blocks of 8192
  *    cells); larger boxes return LSMGPU_ERR_CAPACITY and compute nothing;
- *  - dt may point to host or device memory (a host dt waits for the stream);
+ *  - dt may point to host, managed or device memory (a host or managed dt
+ *    waits for the stream; a device dt is written in stream order);
  *  - the first call on each device looks up the scratch address
  *    (cudaGetSymbolAddress); make that first call before any stream capture;
  *  - every call on a device shares the scratch and overwrites it, so calls

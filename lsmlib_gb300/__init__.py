@@ -43,6 +43,8 @@ def lib(path=None):
     handle.lsmgpu_set_stream.argtypes = [ctypes.c_void_p]
     handle.lsmgpu_get_stream.restype = ctypes.c_void_p
     handle.lsmgpu_launch_count.restype = ctypes.c_longlong
+    handle.lsmgpu_graph_capture_count.restype = ctypes.c_longlong
+    handle.lsmgpu_arena_bytes.restype = ctypes.c_longlong
     handle.lsmgpu_version.restype = ctypes.c_char_p
     if path is None:
         _lib = handle
@@ -69,6 +71,16 @@ def set_stream(stream_ptr, handle=None):
 
 def launch_count(handle=None):
     return int((handle or lib()).lsmgpu_launch_count())
+
+
+def graph_capture_count(handle=None):
+    """Graphs the fused steppers captured so far (a cache miss captures)."""
+    return int((handle or lib()).lsmgpu_graph_capture_count())
+
+
+def arena_bytes(handle=None):
+    """Device bytes held by the library's staging / temporary arena."""
+    return int((handle or lib()).lsmgpu_arena_bytes())
 
 
 _SCALAR_CT = {"real": ctypes.c_double, "double": ctypes.c_double, "int": ctypes.c_int,

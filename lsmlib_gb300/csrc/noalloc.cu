@@ -40,7 +40,11 @@ static std::mutex g_setup_lock;
 
 static double *scratch_for_current_device(int *err) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+  const cudaError_t ge = cudaGetDevice(&dev);
+  if (ge != cudaSuccess || dev < 0 || dev >= 64) {
+    if (ge != cudaSuccess) cudaGetLastError();
+    set_error(LSMGPU_ERR_CUDA, "lsmgpu_compute_stable_advection_dt_noalloc: %s",
+              ge != cudaSuccess ? cudaGetErrorString(ge) : "device index beyond the 64 this entry point tracks");
     *err = LSMGPU_ERR_CUDA;
     return nullptr;
   }
@@ -104,13 +108,18 @@ __global__ void __launch_bounds__(1024) k_finish(double *partial, int nblocks, R
   if (threadIdx.x == 0) partial[kMaxBlocks] = cfl / (s[0] + Consts<R>::tiny);
 }
 
-static bool device_resident(const void *p) {
+static cudaMemoryType memory_type(const void *p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return cudaMemoryTypeUnregistered;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  return a.type;
+}
+
+static bool device_resident(const void *p) {
+  const cudaMemoryType t = memory_type(p);
+  return t == cudaMemoryTypeDevice || t == cudaMemoryTypeManaged;
 }
 
 }  // namespace noalloc
@@ -168,7 +177,9 @@ extern "C" int lsmgpu_compute_stable_advection_dt_noalloc(
     return LSMGPU_ERR_CUDA;
   }
   e = cudaMemcpyAsync(dt, scratch + kMaxBlocks, sizeof(double), cudaMemcpyDefault, s);
-  if (e == cudaSuccess && !device_resident(dt)) e = cudaStreamSynchronize(s);
+  // only a dt in device memory is left to the stream: host and managed
+  // memory are read by host code, so the call waits for the copy
+  if (e == cudaSuccess && memory_type(dt) != cudaMemoryTypeDevice) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
     set_error(LSMGPU_ERR_CUDA, "%s: %s", name, cudaGetErrorString(e));
     return LSMGPU_ERR_CUDA;

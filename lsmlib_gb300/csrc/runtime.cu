@@ -23,6 +23,8 @@ thread_local int g_err = LSMGPU_OK;
 thread_local char g_msg[512] = "";
 std::atomic<cudaStream_t> g_stream{nullptr};
 std::atomic<long long> g_launches{0};
+std::atomic<long long> g_captures{0};     // graphs captured (cache misses)
+std::atomic<long long> g_arena_bytes{0};  // device bytes the arena holds
 
 // Device arena: a list of chunks per device, bump-allocated, reset at the
 // start of each call.  All users run in the library stream's order, so memory
@@ -86,6 +88,7 @@ bool graph_replay(const GraphKey &key, void (*body)(void *), void *ctx) {
     return false;
   }
   const long long before = g_launches.load();
+  g_captures.fetch_add(1, std::memory_order_relaxed);
   t_capture_stream = g_capture[dev];
   body(ctx);
   t_capture_stream = nullptr;
@@ -187,6 +190,7 @@ void *Call::arena_alloc(long long bytes) {
     return nullptr;
   }
   a.chunks.push_back({(char *)p, cap});
+  g_arena_bytes.fetch_add(cap, std::memory_order_relaxed);
   a.cur = (int)a.chunks.size() - 1;
   a.used = need;
   return p;
@@ -362,6 +366,8 @@ int lsmgpu_synchronize(void) {
 
 long long lsmgpu_launch_count(void) { return g_launches.load(); }
 void lsmgpu_reset_launch_count(void) { g_launches.store(0); }
+long long lsmgpu_graph_capture_count(void) { return g_captures.load(); }
+long long lsmgpu_arena_bytes(void) { return g_arena_bytes.load(); }
 
 const char *lsmgpu_version(void) { return "lsmgpu 0.1 (sm_103a)"; }
 

@@ -16,7 +16,7 @@ The argument lists come from the signature dump that oracle/f77ref.py writes
 when it translates the reference's Fortran (oracle/_ref/sigs.json, produced
 by `python -m oracle.build`), so every declaration has the reference
 routine's exact argument order; the C-header line cited beside each comes
-from the reference tree's own headers (searched under /root/reference/src).
+from the reference tree's own headers (searched under $LSMLIB_REFERENCE_TREE/src).
 
     python -m lsmlib_gb300.gen_abi
 """
@@ -25,7 +25,7 @@ import os
 import re
 import subprocess
 
-REF = "/root/reference"
+REF = os.environ.get("LSMLIB_REFERENCE_TREE", "/root/reference")
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 # symbol -> (header group, one-line description)

@@ -19,7 +19,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_TREE = "/root/reference"
+# LSMLIB source tree (read only); LSMLIB_REFERENCE_TREE overrides the default
+REFERENCE_TREE = os.environ.get("LSMLIB_REFERENCE_TREE", "/root/reference")
 
 # Hot-path Fortran sources of the reference, relative to its src/ directory.
 REF_SOURCES = [

@@ -128,3 +128,25 @@ def test_fused_advect_anisotropic_grid(precision, gpu_lib):
         assert H.same(want, got), (np.max(err), where)
     else:
         assert np.max(err[3:-3, 3:-3, 3:-3]) <= 1e-5, (np.max(err), where)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_identical_calls_replay_the_cached_graph(precision, gpu_lib):
+    """A second call with the same buffers, sizes and parameters replays the
+    graph captured by the first (no new capture) and gives the same result."""
+    import torch
+    phi = _phi(7)
+    dtype = torch.float64 if precision == "f64" else torch.float32
+    t0 = torch.from_numpy(np.ascontiguousarray(phi.T)).cuda().to(dtype)
+    a, b = t0.clone(), t0.clone()
+    L.reinit_weno5_tvdrk3(a, GB, FB, DX, 0.5 * DX, 3, use_phi0_for_sgn=1, bc=L.BC_SIGNED_LINEAR,
+                          precision=precision)
+    torch.cuda.synchronize()
+    before = L.graph_capture_count()
+    L.reinit_weno5_tvdrk3(b, GB, FB, DX, 0.5 * DX, 3, use_phi0_for_sgn=1, bc=L.BC_SIGNED_LINEAR,
+                          precision=precision)
+    torch.cuda.synchronize()
+    L.check()
+    assert L.graph_capture_count() == before
+    assert torch.equal(a, b)

@@ -8,7 +8,8 @@ file-scope device array that every call reuses, so these tests call it twice
 in a row with data whose maximum shrinks, which would expose a result left
 over from the previous call, and check both results against
 lsm3dcomputestableadvectiondt_ (the same maximum and formula, so the values
-must be equal).  This file is collected last on purpose.
+must be equal), and that the calls leave the library's device arena and the
+device's free memory unchanged.  This file is collected last on purpose.
 """
 import ctypes
 
@@ -73,6 +74,38 @@ def test_noalloc_dt_matches_existing_entry_point_on_two_calls(gpu_lib):
         assert got_dev == want and host.value == want, (call, got_dev, host.value, want)
         results.append(want)
     assert results[1] > results[0]  # the second call's smaller maximum was not masked
+
+
+def _arena_bytes(h):
+    fn = h.lsmgpu_arena_bytes
+    fn.restype = ctypes.c_longlong
+    return int(fn())
+
+
+@pytest.mark.gpu
+def test_noalloc_dt_allocates_nothing(gpu_lib):
+    """No arena growth and no change of the device's free memory across calls
+    (the first call of the process may load the library's module, which
+    places the fixed scratch array; free memory is compared after it)."""
+    import torch
+    fn = _noalloc(gpu_lib)
+    vel = _velocity(2.0, 5)
+    want = _existing(gpu_lib, vel, GB, IB)
+    torch.cuda.synchronize()
+    arena0 = _arena_bytes(gpu_lib)
+    host = ctypes.c_double(-1.0)
+    assert fn(*_args(ctypes.cast(ctypes.pointer(host), ctypes.c_void_p), vel, GB, IB)) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    torch0 = torch.cuda.memory_allocated()
+    for _ in range(3):
+        host.value = -1.0
+        assert fn(*_args(ctypes.cast(ctypes.pointer(host), ctypes.c_void_p), vel, GB, IB)) == 0
+        assert host.value == want
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert _arena_bytes(gpu_lib) == arena0
+    assert free1 == free0 and torch.cuda.memory_allocated() == torch0
 
 
 @pytest.mark.gpu
