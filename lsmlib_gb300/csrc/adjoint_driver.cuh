@@ -198,10 +198,9 @@ int run(const char *name, const Box &gb, const Box &fb, const Box &vb, const Adj
   }
   cudaMemcpyAsync(X, ck[0], (size_t)ne * sizeof(R), cudaMemcpyDeviceToDevice, s);
 
-  const long long ex = (long long)nx + fused::GX + 3, ey = (long long)ny + 2 * fused::GY,
-                  ez = (long long)nz + 2 * fused::GZ;
   auto tmap = [&](const R *p, CUtensorMap *m) {
-    return encode_tmap_3d(m, p, sizeof(R), ex, ey, ez, L.py, L.pz, fused::SX, fused::SY, fused::SZ);
+    return advect ? fused::encode_stage_tmap<R, fused::ADV_FIELD, EXACT>(m, p, L)
+                  : fused::encode_stage_tmap<R, fused::REINIT, EXACT>(m, p, L);
   };
   CUtensorMap tX, tT1, tT2;
   if (!tmap(X, &tX) || !tmap(T1, &tT1) || !tmap(T2, &tT2)) {

@@ -10,6 +10,7 @@
 #pragma once
 
 #include "fused_stage.cuh"
+#include "reinit_x2.cuh"
 #include "lsmgpu_common.cuh"
 #include "../../include/lsmgpu.h"
 
@@ -95,12 +96,6 @@ __global__ void k_linear_bc(R *phi, Layout L, int axis, int kind) {
 // thread per ghost cell of the 3-layer shell, in one launch; every
 // extrapolation is the same arithmetic as k_linear_bc's, so the values are
 // identical to the three passes'.
-template <class R>
-__device__ __forceinline__ R extrap(R e, R n, int g, int kind) {
-  if (kind == LSMGPU_BC_COPY) return e;
-  const R s = (kind == LSMGPU_BC_SIGNED_LINEAR) ? copysign(R(1.0), e) * fabs(e - n) : e - n;
-  return e + s * R(g);
-}
 
 template <class R>
 struct GhostShell {
@@ -168,19 +163,48 @@ void launch_bc(R *buf, const Layout &L, int bc) {
   LSMGPU_LAUNCH(k_ghost_fill<R>, grd, blk, 0, buf, L, bc);
 }
 
+// The FP32 reinitialization stage runs the window-sharing kernel of
+// reinit_x2.cuh (64 x 8 x RZ tiles); every other form runs k_stage /
+// k_stage_f32 (32 x 8 x TZ tiles).
+template <class R, int MODE, bool EXACT>
+constexpr bool uses_reinit_x2() {
+  return !EXACT && sizeof(R) == 4 && MODE == REINIT;
+}
+
+// Tensor map of a padded work buffer with the staged box of the stage kernel
+// launch_stage<R, MODE, EXACT> runs.
+template <class R, int MODE, bool EXACT>
+bool encode_stage_tmap(CUtensorMap *m, const R *p, const Layout &L) {
+  const long long ex = (long long)L.nx + GX + 3, ey = (long long)L.ny + 2 * GY, ez = (long long)L.nz + 2 * GZ;
+  if constexpr (uses_reinit_x2<R, MODE, EXACT>())
+    return encode_tmap_3d(m, p, sizeof(R), ex, ey, ez, L.py, L.pz, RSX, RSY, RSZ);
+  return encode_tmap_3d(m, p, sizeof(R), ex, ey, ez, L.py, L.pz, SX, SY, SZ);
+}
+
 // Launches one stage kernel; with prepare_only it only sets the kernel's
 // dynamic shared memory limit (done once, and before a launch is captured into
 // a graph).  The function has internal linkage: each translation unit that
 // launches a stage kernel has its own kernel instance, and its own copy of
 // this function and of the flag below, so the limit is set on the instance
-// the unit launches.
+// the unit launches.  `tm` must come from encode_stage_tmap<R, MODE, EXACT>.
 template <class R, int MODE, bool EXACT>
 static void launch_stage(const CUtensorMap &tm, const StageArgs<R> &a, bool prepare_only = false) {
   const Layout &L = a.L;
+  static bool attr_set = false;
+  if constexpr (uses_reinit_x2<R, MODE, EXACT>()) {
+    if (!attr_set) {
+      cudaFuncSetAttribute(k_reinit_x2<RZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kReinitX2Smem);
+      attr_set = true;
+    }
+    if (prepare_only) return;
+    dim3 grd((unsigned)((L.nx + RX - 1) / RX), (unsigned)((L.ny + RY - 1) / RY), (unsigned)((L.nz + RZ - 1) / RZ));
+    k_reinit_x2<RZ><<<grd, dim3(32, RY), kReinitX2Smem, stream()>>>(tm, a);
+    note_launch();
+    return;
+  }
   dim3 blk(TX, TY);
   dim3 grd((unsigned)((L.nx + TX - 1) / TX), (unsigned)((L.ny + TY - 1) / TY), (unsigned)((L.nz + TZ - 1) / TZ));
   const size_t smem = (size_t)SX * SY * SZ * sizeof(R);
-  static bool attr_set = false;
   if (!attr_set) {
     if constexpr (!EXACT && sizeof(R) == 4)
       cudaFuncSetAttribute(k_stage_f32<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -206,7 +230,7 @@ void add_stage_args(GraphKey &key, const StageArgs<R> &a) {
   key.add(a.out);
   for (int d = 0; d < 3; d++) { key.add(a.vconst[d]); key.add(a.inv[d]); }
   key.add(a.dt); key.add(a.dx_sq);
-  key.add(a.stage); key.add(a.use0); key.add(a.periodic);
+  key.add(a.stage); key.add(a.use0); key.add(a.periodic); key.add(a.ghost);
   key.add(a.err);
 }
 
@@ -252,10 +276,11 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, const R *vx
   int *err = call.temp<int>(1);
   if (!call.ok()) return lsmgpu_get_last_error(nullptr, 0);
 
+  // B and C need no initial values: a stage writes every interior cell of
+  // its output, and the ghost cells the next stage reads are either written
+  // by the stage (periodic images) or computed by the next stage's loader
   cudaStream_t s = stream();
   cudaMemsetAsync(err, 0, sizeof(int), s);
-  cudaMemsetAsync(B, 0, (size_t)ne * sizeof(R), s);
-  cudaMemsetAsync(C, 0, (size_t)ne * sizeof(R), s);
   {
     dim3 blk(32, 4, 2);
     dim3 grd((unsigned)((nx + 7 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));
@@ -267,10 +292,12 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, const R *vx
   if (P0) cudaMemcpyAsync(P0, A, (size_t)ne * sizeof(R), cudaMemcpyDeviceToDevice, s);
 
   CUtensorMap tA, tB, tC;
-  const long long ex = (long long)nx + GX + 3, ey = (long long)ny + 2 * GY, ez = (long long)nz + 2 * GZ;
-  if (!encode_tmap_3d(&tA, A, sizeof(R), ex, ey, ez, L.py, L.pz, SX, SY, SZ) ||
-      !encode_tmap_3d(&tB, B, sizeof(R), ex, ey, ez, L.py, L.pz, SX, SY, SZ) ||
-      !encode_tmap_3d(&tC, C, sizeof(R), ex, ey, ez, L.py, L.pz, SX, SY, SZ)) {
+  auto enc = [&](CUtensorMap *m, const R *p) {
+    if (rs.mode == REINIT) return encode_stage_tmap<R, REINIT, EXACT>(m, p, L);
+    if (rs.mode == ADV_CONST) return encode_stage_tmap<R, ADV_CONST, EXACT>(m, p, L);
+    return encode_stage_tmap<R, ADV_FIELD, EXACT>(m, p, L);
+  };
+  if (!enc(&tA, A) || !enc(&tB, B) || !enc(&tC, C)) {
     call.fail("tensor map encoding failed");
     return LSMGPU_ERR_CUDA;
   }
@@ -293,27 +320,33 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, const R *vx
   if (rs.mode == REINIT) launch_stage<R, REINIT, EXACT>(tA, a, true);
   else if (rs.mode == ADV_CONST) launch_stage<R, ADV_CONST, EXACT>(tA, a, true);
   else launch_stage<R, ADV_FIELD, EXACT>(tA, a, true);
-  // the n_steps x (3 stages + ghost fills) launches, replayed as one CUDA
-  // graph when the same buffers, sizes and parameters come again
+  // The n_steps x 3 stage launches, replayed as one CUDA graph when the same
+  // buffers, sizes and parameters come again.  With an extrapolation
+  // boundary condition LSMLIB's drivers fill the ghost cells after every
+  // stage; here each stage computes the face ghosts it reads from its input's
+  // interior cells while staging its tile (the same values), except the very
+  // first stage, which reads the caller's ghost cells as given, and one fill
+  // of the stored result follows the last stage.
+  const int ghost = a.periodic ? 0 : rs.bc;
   auto steps = [&]() {
     StageArgs<R> b = a;
     for (int step = 0; step < rs.n_steps; step++) {
       b.stage = 1; b.phi_n = A; b.out = B;
+      b.ghost = step == 0 ? 0 : ghost;
       if (rs.mode == REINIT) launch_stage<R, REINIT, EXACT>(tA, b);
       else if (rs.mode == ADV_CONST) launch_stage<R, ADV_CONST, EXACT>(tA, b);
       else launch_stage<R, ADV_FIELD, EXACT>(tA, b);
-      launch_bc(B, L, rs.bc);
       b.stage = 2; b.out = C;
+      b.ghost = ghost;
       if (rs.mode == REINIT) launch_stage<R, REINIT, EXACT>(tB, b);
       else if (rs.mode == ADV_CONST) launch_stage<R, ADV_CONST, EXACT>(tB, b);
       else launch_stage<R, ADV_FIELD, EXACT>(tB, b);
-      launch_bc(C, L, rs.bc);
       b.stage = 3; b.out = A;
       if (rs.mode == REINIT) launch_stage<R, REINIT, EXACT>(tC, b);
       else if (rs.mode == ADV_CONST) launch_stage<R, ADV_CONST, EXACT>(tC, b);
       else launch_stage<R, ADV_FIELD, EXACT>(tC, b);
-      launch_bc(A, L, rs.bc);
     }
+    launch_bc(A, L, rs.bc);
   };
   GraphKey key;
   key.add((int)sizeof(R));

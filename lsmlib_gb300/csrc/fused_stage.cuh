@@ -18,6 +18,8 @@
 // under- or overflow in single precision (see weno5_fast).
 #pragma once
 
+#include <type_traits>
+
 #include "lsmgpu_common.cuh"
 #include "stencil_math.cuh"
 #include "tma.cuh"
@@ -62,8 +64,67 @@ struct StageArgs {
   int stage;         // 1, 2 or 3
   int use0;          // reinitialization sign from phi0
   int periodic;      // write periodic ghost images of the result
+  int ghost;         // 0, or the LSMGPU_BC_* extrapolation whose face ghosts
+                     // the kernel computes in shared memory from the tile
   int *err;
 };
+
+// One-axis extrapolation of LSMLIB's ghost-cell routines
+// (boundary_conditions3d.f:46-462) at distance g from the edge value e, with
+// n the value next inside: linear (slope e - n), signed linear (slope
+// sign(e) |e - n|, :203-206) or copy (homogeneous Neumann).
+template <class R>
+__device__ __forceinline__ R extrap(R e, R n, int g, int kind) {
+  if (kind == LSMGPU_BC_COPY) return e;
+  const R s = (kind == LSMGPU_BC_SIGNED_LINEAR) ? copysign(R(1.0), e) * fabs(e - n) : e - n;
+  return e + s * R(g);
+}
+
+// The ghost cells a stage's stencils read (face ghosts: one coordinate in
+// the 3-cell layer, the other two interior) that lie in a staged tile,
+// computed from the tile's interior cells with LSMLIB's extrapolation
+// (boundary_conditions3d.f:46-462): identical values to a fill of the
+// stored array, whose faces are written x, then y, then z, because a face
+// ghost of an axis is written only by that axis' pass from interior cells.
+// (Edge and corner ghosts are read by no axis-aligned stencil.)  Tile cell
+// (a, b, c) holds interior cell (ox + a, oy + b, oz + c).
+template <class R>
+__device__ void fill_face_ghosts(R *tile, int sdx, int sdy, int sdz, int ox, int oy, int oz, const Layout &L,
+                                 int kind) {
+  const int nthr = blockDim.x * blockDim.y, tid = threadIdx.x + blockDim.x * threadIdx.y;
+  const int sxy = sdx * sdy;
+  // one face: ghost layers 1..3 of axis AX below (up = 0) or above (up = 1)
+  auto face = [&](auto ax_tag, int up) {
+    constexpr int AX = decltype(ax_tag)::value;
+    const int n0 = L.nx, n1 = L.ny, n2 = L.nz;
+    const int nax = AX == 0 ? n0 : (AX == 1 ? n1 : n2);
+    // ranges: ghost layers along AX, interior along the other two, clipped to the tile
+    int lo0 = AX == 0 ? (up ? n0 : -3) : 0, hi0 = AX == 0 ? (up ? n0 + 2 : -1) : n0 - 1;
+    int lo1 = AX == 1 ? (up ? n1 : -3) : 0, hi1 = AX == 1 ? (up ? n1 + 2 : -1) : n1 - 1;
+    int lo2 = AX == 2 ? (up ? n2 : -3) : 0, hi2 = AX == 2 ? (up ? n2 + 2 : -1) : n2 - 1;
+    lo0 = max(lo0, ox); hi0 = min(hi0, ox + sdx - 1);
+    lo1 = max(lo1, oy); hi1 = min(hi1, oy + sdy - 1);
+    lo2 = max(lo2, oz); hi2 = min(hi2, oz + sdz - 1);
+    if (lo0 > hi0 || lo1 > hi1 || lo2 > hi2) return;
+    const int e_at = up ? nax - 1 : 0, n_at = up ? nax - 2 : 1;
+    const int st = AX == 0 ? 1 : (AX == 1 ? sdx : sxy);
+    const int cx = hi0 - lo0 + 1, cy = hi1 - lo1 + 1;
+    const int cnt = cx * cy * (hi2 - lo2 + 1);
+    for (int q = tid; q < cnt; q += nthr) {
+      const int c0 = lo0 + q % cx, c1 = lo1 + (q / cx) % cy, c2 = lo2 + q / (cx * cy);
+      const int at = (c0 - ox) + (c1 - oy) * sdx + (c2 - oz) * sxy;
+      const int cax = AX == 0 ? c0 : (AX == 1 ? c1 : c2);
+      const int g = up ? cax - e_at : -cax;
+      tile[at] = extrap(tile[at + (e_at - cax) * st], tile[at + (n_at - cax) * st], g, kind);
+    }
+  };
+  face(std::integral_constant<int, 0>{}, 0);
+  face(std::integral_constant<int, 0>{}, 1);
+  face(std::integral_constant<int, 1>{}, 0);
+  face(std::integral_constant<int, 1>{}, 1);
+  face(std::integral_constant<int, 2>{}, 0);
+  face(std::integral_constant<int, 2>{}, 1);
+}
 
 // ---------------------------------------------------------------------------
 // FP32 arithmetic
@@ -152,6 +213,10 @@ __global__ void __launch_bounds__(TX * TY) k_stage(const __grid_constant__ CUten
     if (tid == 0) atomicExch(a.err, LSMGPU_ERR_TIMEOUT);
     mbar_wait(&bar, 0, kMaxPolls);  // let an in-flight copy land before exit
     return;
+  }
+  if (a.ghost) {
+    fill_face_ghosts<R>(tile, SX, SY, SZ, x0 - 4, y0 - 3, z0 - 3, a.L, a.ghost);
+    __syncthreads();
   }
 
   const Layout &L = a.L;
@@ -485,6 +550,10 @@ __global__ void __launch_bounds__(TX * TY) k_stage_f32(const __grid_constant__ C
     if (tid == 0) atomicExch(a.err, LSMGPU_ERR_TIMEOUT);
     mbar_wait(&bar, 0, kMaxPolls);
     return;
+  }
+  if (a.ghost) {
+    fill_face_ghosts<float>(tile, SX, SY, SZ, x0 - 4, y0 - 3, z0 - 3, a.L, a.ghost);
+    __syncthreads();
   }
   f32_tile<MODE, TZ>(tile, a, x0, y0, z0);
 }
