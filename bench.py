@@ -528,6 +528,19 @@ def _timed(fn, stream):
     return a.elapsed_time(b)
 
 
+def advection_case(n=128):
+    """Plain-method advection input on [-1, 1]^3: signed distance to a sphere
+    of radius 0.35 at (0.1, -0.05, 0) on the cell centres (ghosts included),
+    velocity (1, 0.5, 0.25), dt at CFL 0.5.  Returns (phi, vel, dt, dx)."""
+    dx = 2.0 / n
+    c = -1.0 + (np.arange(-GHOST, n + GHOST) + 0.5) * dx
+    X, Y, Z = np.meshgrid(c, c, c, indexing="ij")
+    phi = np.asfortranarray(np.sqrt((X - 0.1) ** 2 + (Y + 0.05) ** 2 + Z ** 2) - 0.35)
+    vel = (1.0, 0.5, 0.25)
+    dt = 0.5 * dx / sum(abs(v) for v in vel)
+    return phi, vel, dt, dx
+
+
 def sub_advection(stream, dev, n=128, steps=50):
     """Plain-method advection: 128^3 on [-1, 1]^3, periodic, signed distance
     to a sphere of radius 0.35 at (0.1, -0.05, 0), constant velocity
@@ -536,12 +549,7 @@ def sub_advection(stream, dev, n=128, steps=50):
     import torch
     import lsmlib_gb300 as L
     gb, fb = boxes(n)
-    dx = 2.0 / n
-    c = -1.0 + (np.arange(-GHOST, n + GHOST) + 0.5) * dx
-    X, Y, Z = np.meshgrid(c, c, c, indexing="ij")
-    phi = np.sqrt((X - 0.1) ** 2 + (Y + 0.05) ** 2 + Z ** 2) - 0.35
-    vel = (1.0, 0.5, 0.25)
-    dt = 0.5 * dx / sum(abs(v) for v in vel)
+    phi, vel, dt, dx = advection_case(n)
     out = {"workload": "advection-weno5-tvdrk3-128, sphere r=0.35, u=(1,0.5,0.25), CFL 0.5, 50 steps, periodic"}
     res = {}
     for prec, dtype in (("f64", torch.float64), ("f32", torch.float32)):
@@ -561,19 +569,21 @@ def sub_advection(stream, dev, n=128, steps=50):
     return out
 
 
-def band_case(dev, n=512, n_spheres=64, seed=7):
+def band_case(dev, n=512, n_spheres=64, seed=7, dtype=None):
     """Signed distance to the union of 64 spheres (centres U[-0.8, 0.8]^3,
-    radii U[0.03, 0.10], numpy seed 7) on the n^3 cell centres of [-1, 1]^3
-    with 3 ghost cells: a C-ordered FP32 CUDA tensor of the Fortran ghost-box
+    radii U[0.03, 0.10], numpy seed 7: centres drawn first, then radii) on
+    the n^3 cell centres of [-1, 1]^3 with 3 ghost cells: a C-ordered CUDA
+    tensor (FP32 unless `dtype` says otherwise) of the Fortran ghost-box
     array."""
     import torch
+    dtype = dtype or torch.float32
     rng = np.random.default_rng(seed)
     centres = rng.uniform(-0.8, 0.8, size=(n_spheres, 3))
     radii = rng.uniform(0.03, 0.10, size=n_spheres)
     dx = 2.0 / n
-    c = -1.0 + (torch.arange(-GHOST, n + GHOST, device=dev, dtype=torch.float32) + 0.5) * dx
+    c = -1.0 + (torch.arange(-GHOST, n + GHOST, device=dev, dtype=dtype) + 0.5) * dx
     z, y, x = c.view(-1, 1, 1), c.view(1, -1, 1), c.view(1, 1, -1)
-    phi = torch.full((n + 2 * GHOST,) * 3, 1e30, device=dev, dtype=torch.float32)
+    phi = torch.full((n + 2 * GHOST,) * 3, 1e30, device=dev, dtype=dtype)
     for (cx, cy, cz), r in zip(centres, radii):
         phi = torch.minimum(phi, torch.sqrt((x - float(cx)) ** 2 + (y - float(cy)) ** 2 + (z - float(cz)) ** 2)
                             - float(r))
@@ -602,19 +612,26 @@ def sub_narrow_band(stream, dev, n=512, steps=100, rebuild=5):
             "grid_cell_updates_per_s_equivalent": n ** 3 * steps / (ms / 1e3) / 1e9}
 
 
-def batched_case(dev, n_grids=4096, seed=11, lo=16, hi=96):
-    """4096 grids, sides U{16..96} per axis (numpy seed 11), each on [-1, 1]^3
-    with an ellipsoid level set (semi-axes U[0.2, 0.6], phi = (|x / a| - 1)
-    min(a)) and a constant velocity U[-1, 1]^3, dt at CFL 0.5.  Returns the
-    packed FP32 CUDA buffer (3 ghost cells per grid), offsets, dims,
-    velocities, spacings and dts."""
-    import torch
+def batched_params(n_grids=4096, seed=11, lo=16, hi=96):
+    """Per-grid parameters of the batched workload: sides U{16..96} per axis,
+    ellipsoid semi-axes U[0.2, 0.6], constant velocity U[-1, 1]^3 (numpy
+    seed 11, drawn in that order), spacing 2 / side, dt at CFL 0.5."""
     rng = np.random.default_rng(seed)
     dims = rng.integers(lo, hi + 1, size=(n_grids, 3))
     axes = rng.uniform(0.2, 0.6, size=(n_grids, 3))
     vel = rng.uniform(-1.0, 1.0, size=(n_grids, 3))
     spacing = 2.0 / dims
     dt = 0.5 / (np.abs(vel) / spacing).sum(axis=1)
+    return dims, axes, vel, spacing, dt
+
+
+def batched_case(dev, n_grids=4096, seed=11, lo=16, hi=96):
+    """4096 grids (batched_params), each on [-1, 1]^3 with an ellipsoid level
+    set (phi = (|x / a| - 1) min(a)) and a constant velocity.  Returns the
+    packed FP32 CUDA buffer (3 ghost cells per grid), offsets, dims,
+    velocities, spacings and dts."""
+    import torch
+    dims, axes, vel, spacing, dt = batched_params(n_grids, seed, lo, hi)
     sizes = np.prod(dims + 2 * GHOST, axis=1)
     offsets = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
     buf = torch.empty(int(sizes.sum()), device=dev, dtype=torch.float32)
