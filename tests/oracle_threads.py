@@ -4,8 +4,10 @@ k-slabs over threads, for the parity tests at the workloads' own sizes.
 Each LSMLIB routine of the sequence evaluates a cell-wise formula over its
 fill box, so calling it once per k-slab of the fill box (each slab with its
 own D1 scratch array) gives every cell exactly the arithmetic of one call
-over the whole box; ctypes releases the interpreter lock during a call, so
-the slabs run in parallel on the host cores.  The ghost fill after each
+over the whole box (lsm3dZeroOutLevelSetEqnRHS, which clears its whole
+ghost box, runs once per stage before the slabs); ctypes releases the
+interpreter lock during a call, so the slabs run in parallel on the host
+cores.  The ghost fill after each
 stage runs once over the whole array, as in oracle_runs.tvdrk3_run, whose
 results these runs reproduce bit for bit (tests/test_oracle_threads.py).
 """
@@ -119,7 +121,8 @@ class SlabRun:
         self._call("lsm3dupwindhjweno5_", s, {
             "phi": phi, "phi_x": self.g[0], "phi_y": self.g[1], "phi_z": self.g[2],
             "vel_x": vel[0], "vel_y": vel[1], "vel_z": vel[2]}, {"dx": dx, "dy": dy, "dz": dz}, d1=True)
-        self._call("lsm3dzerooutlevelseteqnrhs_", s, {"lse_rhs": self.rhs}, {})
+        # (lsm3dZeroOutLevelSetEqnRHS clears the whole ghost box, so run()
+        # calls it once per stage before the slabs start)
         self._call("lsm3daddadvectiontermtolserhs_", s, {
             "lse_rhs": self.rhs, "phi_x": self.g[0], "phi_y": self.g[1], "phi_z": self.g[2],
             "vel_x": vel[0], "vel_y": vel[1], "vel_z": vel[2]}, {})
@@ -150,12 +153,13 @@ class SlabRun:
                 self._call("lsm3dtvdrk3stage3_", s, {"u_next": un, "u_stage2": u2, "u_cur": phi,
                                                       "rhs": self.rhs}, {"dt": dt})
 
-            parallel(st1, n)
-            apply_bc(self.lib, u1, self.gb, self.fb, bc)
-            parallel(st2, n)
-            apply_bc(self.lib, u2, self.gb, self.fb, bc)
-            parallel(st3, n)
-            apply_bc(self.lib, un, self.gb, self.fb, bc)
+            for st, out in ((st1, u1), (st2, u2), (st3, un)):
+                if mode != "reinit":
+                    vals, _ = H.make_call("lsm3dzerooutlevelseteqnrhs_", self.gb, self.fb,
+                                          arrays={"lse_rhs": self.rhs})
+                    L.invoke(self.lib, "lsm3dzerooutlevelseteqnrhs_", vals)
+                parallel(st, n)
+                apply_bc(self.lib, out, self.gb, self.fb, bc)
             phi = un
         return phi
 

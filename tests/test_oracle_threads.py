@@ -42,6 +42,18 @@ def test_threaded_advection_matches_serial():
     assert H.same(want, got)
 
 
+def test_threaded_advection_matches_serial_at_64_on_many_threads():
+    # slabs racing for shared arrays show at this size (the zero-out of the
+    # right-hand side clears its whole ghost box)
+    import bench
+    gb, fb = bench.boxes(64)
+    phi, vel, dt, dx = bench.advection_case(64)
+    vf = [np.full(phi.shape, v, order="F") for v in vel]
+    want = O.tvdrk3_run(H.oracle(), "advect", phi, gb, fb, dx, dt, 1, L.BC_PERIODIC, vel=vf)
+    got = SlabRun(H.oracle(), gb, fb, threads=16).run("advect", phi, dx, dt, 1, L.BC_PERIODIC, vel=vf)
+    assert H.same(want, got)
+
+
 def test_threaded_curvature_matches_serial():
     from tests.test_fused_curvature import oracle_chain, GB as CGB, FB as CFB, DX as CDX, DY, DZ, _phi as cphi
     phi = cphi(1)
