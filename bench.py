@@ -254,6 +254,32 @@ class CpuReinit:
             self._stage(self.u2, self.un, 3, dt)
             self.phi, self.un = self.un, self.phi
 
+    def reset(self, phi):
+        self.phi[...] = phi
+        self.phi0[...] = phi
+
+    def _slab_curvature(self, s, kappa, mag):
+        lib, gb, fb = self.lib, self.gb, self.fb
+        k0, k1 = self.slabs[s]
+        F = [_ip(v) for v in (fb[0], fb[1], fb[2], fb[3], k0, k1)]
+        G = [_ip(v) for v in gb]
+        dx = _dp(self.dx)
+        g = self.pp
+        lib.lsm3dcentralgradorder2_(_arr(g[0]), _arr(g[1]), _arr(g[2]), *G, _arr(self.phi), *G, *F, dx, dx, dx)
+        lib.lsm3dgradientmagnitude_(_arr(g[0]), _arr(g[1]), _arr(g[2]), _arr(mag), *G, *F)
+        lib.lsm3dcomputemeancurvatureorder2_(_arr(kappa), *G, _arr(self.phi), *G, _arr(g[0]), _arr(g[1]),
+                                             _arr(g[2]), _arr(mag), *G, *F, dx, dx, dx)
+
+    def curvature(self, kappa, mag):
+        """LSMLIB's curvature pass on the current phi: second-order central
+        gradient, |grad phi|, mean curvature (per k-slab)."""
+        ths = [threading.Thread(target=self._slab_curvature, args=(s, kappa, mag))
+               for s in range(len(self.slabs))]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+
 
 def cpu_sample(n, iters, threads, warmup=0):
     """Time `iters` reinitialization iterations of the full n^3 workload on the
@@ -313,6 +339,11 @@ def headline_config(n, world):
 
 
 def reference_arm(args, world, rank):
+    """The reference's own kernels (LSMLIB's Fortran translated to C, or the C
+    oracle when the translation is absent) on the host: each step is the
+    whole workload of the GPU arm's step (the 20 reinitialization iterations
+    from the initial field, then the curvature pass), with every LSMLIB call
+    split into k-slabs over all host threads by this script."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
@@ -321,24 +352,30 @@ def reference_arm(args, world, rank):
     phi, dx = initial_phi(n)
     gb, fb = boxes(n)
     r = CpuReinit(lib, phi, gb, fb, dx, threads)
-    per_step = 1  # iterations of the 20 per step: a bounded sample of the workload
+    kappa = np.zeros_like(phi, order="F")
+    mag = np.zeros_like(phi, order="F")
+
+    def step():
+        r.reset(phi)
+        r.iterate(ITERS, 0.5 * dx)
+        r.curvature(kappa, mag)
+
     for _ in range(args.warmup):
-        r.iterate(per_step, 0.5 * dx)
+        step()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        r.iterate(per_step, 0.5 * dx)
+        step()
     sec = time.perf_counter() - t0
-    value = n ** 3 * per_step * args.steps / sec / 1e9
+    value = n ** 3 * ITERS * args.steps / sec / 1e9
+    sample = ("the whole workload per step (%d reinitialization iterations of the %d^3 field + the curvature "
+              "pass), LSMLIB's kernels called per k-slab over %d host threads by bench.py" % (ITERS, n, threads))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (analytic level set)",
-        "config": dict(headline_config(n, 1), sample="%d of the 20 iterations per step (the curvature pass "
-                                                      "is not timed)" % per_step),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-                         "sample": "%d reinitialization iteration(s) of the %d^3 workload per step, "
-                                   "k-slabs over %d host threads" % (per_step, n, threads)},
+        "config": dict(headline_config(n, 1), sample=sample),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -423,9 +460,10 @@ def gpu_arm(args, world, rank, local):
                 "frac": achieved / peak, "traffic": MEASURED_STAGE_TRAFFIC,
                 "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one stage-2 launch "
                                 "(algorithmic 268.4 MB for that stage; achieved uses the 3-stage mean, 14.67 B/cell)",
-                "kernel": "k_stage_f32<REINIT> (fused WENO5 + reinit RHS + TVD-RK3 stage, packed FP32x2)",
-                "note": "the kernel is bound by the FP32 FMA pipe, not by DRAM (ncu: sm__pipe_fma_cycles_active "
-                        "74%, DRAM traffic 1.06x algorithmic); see profiles/k_stage_reinit_f32_256.md",
+                "kernel": "k_reinit_x2 (fused WENO5 + reinit RHS + TVD-RK3 stage, windows shared between "
+                          "neighbouring cells, packed FP32x2)",
+                "note": "the kernel is bound by arithmetic issue, not by DRAM (fp32_pipe below); see "
+                        "profiles/k_reinit_x2_reinit_f32_256.md",
                 "stage_ms": stage_ms, "peak_source": peak_kind}
 
     # end to end through the C ABI with host (pinned) buffers
@@ -481,6 +519,25 @@ def gpu_arm(args, world, rank, local):
     fp64 = {"value": cells * ITERS / (ms64 / 1e3) / 1e9, "unit": UNIT, "ms_per_step": ms64,
             "fp32_speedup": ms64 / ms}
 
+    # arithmetic roofs, against the device's FMA rates measured by the
+    # library's probe kernels: the FP32 FMA pipe of the headline stage kernel
+    # (its FMA-pipe instructions per cell-stage from one ncu capture, times
+    # the live cell-stage rate, against the probe's FFMA2 instruction rate)
+    # and the FP64 pipe of the parity form (FP64 operations per cell-update
+    # from one ncu capture of a stage launch, times the live rate)
+    fp32_lane_ops, fp64_fmas = L.measure_fma_rates()
+    fp32_pipe = {"bound": "fp32 fma pipe", "unit": "FMA-pipe thread-instructions/s",
+                 "peak": fp32_lane_ops / 2.0, "peak_source": "measured (FFMA2 probe, lsmgpu_measure_fma_rates)",
+                 "instructions_per_cell_stage": MEASURED_FMA_PIPE_INSTR_PER_CELL_STAGE}
+    fp32_pipe["achieved"] = MEASURED_FMA_PIPE_INSTR_PER_CELL_STAGE * cells / (stage_ms / 1e3)
+    fp32_pipe["frac"] = fp32_pipe["achieved"] / fp32_pipe["peak"]
+    roofline["fp32_pipe"] = fp32_pipe
+    fp64["roofline"] = {"bound": "fp64 pipe", "unit": "FP64 operations/s", "peak": fp64_fmas,
+                        "peak_source": "measured (DFMA probe, lsmgpu_measure_fma_rates)",
+                        "fp64_ops_per_cell_update": MEASURED_FP64_OPS_PER_CELL_UPDATE}
+    fp64["roofline"]["achieved"] = MEASURED_FP64_OPS_PER_CELL_UPDATE * cells * ITERS / (ms64 / 1e3)
+    fp64["roofline"]["frac"] = fp64["roofline"]["achieved"] / fp64_fmas
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True,
@@ -500,11 +557,18 @@ def gpu_arm(args, world, rank, local):
             "dropin_192": sub_dropin(stream, dev),
         }
     if rank == 0 and world == 1 and not args.no_cpu:
+        # the reference's serial path (1 core), and the same kernels over
+        # k-slabs on every host core beside it
+        v, sec, kind = cpu_sample(n, 1, 1)
+        line["cpu_baseline"] = {"value": v / 1e9, "unit": UNIT, "cores": 1, "kind": kind,
+                                "sample": "1 reinitialization iteration of the %d^3 workload (%.1f s), serial, "
+                                          "as the reference runs" % (n, sec)}
         threads = os.cpu_count() or 1
         v, sec, kind = cpu_sample(n, 1, threads)
-        line["cpu_baseline"] = {"value": v / 1e9, "unit": UNIT, "cores": threads, "kind": kind,
-                                "sample": "1 reinitialization iteration of the %d^3 workload "
-                                          "(%.1f s), k-slabs over %d host threads" % (n, sec, threads)}
+        line["cpu_all_cores"] = {"value": v / 1e9, "unit": UNIT, "cores": threads, "kind": kind,
+                                 "sample": "1 reinitialization iteration of the %d^3 workload (%.1f s), the "
+                                           "reference's kernels called per k-slab over %d host threads by bench.py"
+                                           % (n, sec, threads)}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -826,6 +890,16 @@ def sub_geometry(stream, dev, n=512, reps=10):
 # k_stage_reinit_f32_256.md, packed FP32x2 kernel: 285.6 MB; the stage's
 # algorithmic bytes are 16 B/cell = 268.4 MB)
 MEASURED_STAGE_TRAFFIC = 285.6e6
+
+# FMA-pipe thread-instructions (a packed FFMA2 / FMUL2 / FADD2 counts once)
+# per cell of one headline stage launch (k_reinit_x2, ncu
+# sm__inst_executed_pipe_fma.sum x 32 / 256^3 cells), and FP64 pipe
+# operations (DFMA + DMUL + DADD thread-instructions, the IEEE division and
+# square-root sequences included) per cell-update of the FP64 parity form
+# (3 x one stage launch of k_stage<double, REINIT> at 128^3); both from the
+# captures summarised in profiles/k_reinit_x2_reinit_f32_256.md
+MEASURED_FMA_PIPE_INSTR_PER_CELL_STAGE = 115.3
+MEASURED_FP64_OPS_PER_CELL_UPDATE = 3 * 633.5
 
 
 # ---------------------------------------------------------------------------

@@ -401,6 +401,14 @@ int lsmgpu_count_nonfinite_f32(const float *field, const int *gb, const int *box
  * stays usable.  Returns LSMGPU_ERR_TIMEOUT (the expected outcome). */
 int lsmgpu_selftest_bounded_wait(unsigned int polls);
 
+/* Measures the device's sustained arithmetic rates with two fixed-length
+ * probe kernels: FP32 lane operations per second through packed FFMA2
+ * instructions (one FFMA2 = two lane operations) and FP64 fused
+ * multiply-adds per second.  These are the denominators of the FP32-pipe
+ * and FP64 rooflines the benchmark reports.  Synchronous; returns an
+ * LSMGPU_* status. */
+int lsmgpu_measure_fma_rates(double *fp32_lane_ops_per_s, double *fp64_ops_per_s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -78,6 +78,18 @@ def graph_capture_count(handle=None):
     return int((handle or lib()).lsmgpu_graph_capture_count())
 
 
+def measure_fma_rates(handle=None):
+    """(FP32 lane operations/s through packed FFMA2, FP64 FMAs/s) measured by
+    the library's fixed-length probe kernels on the current device."""
+    h = handle or lib()
+    a, b = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    h.lsmgpu_measure_fma_rates.restype = ctypes.c_int
+    rc = h.lsmgpu_measure_fma_rates(ctypes.byref(a), ctypes.byref(b))
+    if rc != 0:
+        raise RuntimeError("lsmgpu_measure_fma_rates failed: %s" % (last_error(h)[1],))
+    return a.value, b.value
+
+
 def arena_bytes(handle=None):
     """Device bytes held by the library's staging / temporary arena."""
     return int((handle or lib()).lsmgpu_arena_bytes())

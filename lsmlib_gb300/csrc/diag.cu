@@ -91,6 +91,43 @@ int count_nonfinite(const char *name, const T *field, const int *gb, const int *
   return lsmgpu_get_last_error(nullptr, 0);
 }
 
+// Arithmetic-rate probes: every thread runs eight independent chains of
+// fused multiply-adds (a = a * b + c with |b| < 1, so the values stay
+// bounded) for a fixed number of iterations; the grid fills every SM
+// several times over.  The result is the device's sustained rate of FP32
+// lane operations through packed FFMA2 instructions and of FP64 FMAs.
+constexpr int kProbeChains = 8;
+constexpr int kProbeThreads = 256;
+
+__global__ void __launch_bounds__(kProbeThreads) k_probe_ffma2(float *out, int iters, float b, float c) {
+  float2 acc[kProbeChains];
+#pragma unroll
+  for (int q = 0; q < kProbeChains; q++) acc[q] = make_float2(1e-3f * (threadIdx.x + q), 1e-3f * q);
+  const float2 b2 = make_float2(b, b), c2 = make_float2(c, c);
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int q = 0; q < kProbeChains; q++) acc[q] = __ffma2_rn(acc[q], b2, c2);
+  }
+  float r = 0.f;
+#pragma unroll
+  for (int q = 0; q < kProbeChains; q++) r += acc[q].x + acc[q].y;
+  if (r == -1.f) out[blockIdx.x] = r;  // never true; keeps the chains live
+}
+
+__global__ void __launch_bounds__(kProbeThreads) k_probe_dfma(double *out, int iters, double b, double c) {
+  double acc[kProbeChains];
+#pragma unroll
+  for (int q = 0; q < kProbeChains; q++) acc[q] = 1e-3 * (threadIdx.x + q);
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int q = 0; q < kProbeChains; q++) acc[q] = fma(acc[q], b, c);
+  }
+  double r = 0.0;
+#pragma unroll
+  for (int q = 0; q < kProbeChains; q++) r += acc[q];
+  if (r == -1.0) out[blockIdx.x] = r;
+}
+
 }  // namespace
 }  // namespace lsmgpu
 
@@ -124,6 +161,54 @@ int lsmgpu_selftest_bounded_wait(unsigned int polls) {
     set_error(h, "lsmgpu_selftest_bounded_wait: the device wait gave up after %u polls (as intended)", polls);
     return h;
   }
+  return LSMGPU_OK;
+}
+
+int lsmgpu_measure_fma_rates(double *fp32_lane_ops_per_s, double *fp64_ops_per_s) {
+  Call call("lsmgpu_measure_fma_rates");
+  if (!fp32_lane_ops_per_s || !fp64_ops_per_s) {
+    set_error(LSMGPU_ERR_ARGUMENT, "lsmgpu_measure_fma_rates: null argument");
+    return LSMGPU_ERR_ARGUMENT;
+  }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = 8 * (sms > 0 ? sms : 1);
+  void *sink = call.temp<double>(blocks);
+  if (!call.ok()) return lsmgpu_get_last_error(nullptr, 0);
+  cudaStream_t s = stream();
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  // best of three timed launches after one warm-up, per precision
+  auto timed = [&](bool f64, int iters) {
+    float best = 0.f;
+    for (int rep = 0; rep < 4; rep++) {
+      cudaEventRecord(e0, s);
+      if (f64) k_probe_dfma<<<blocks, kProbeThreads, 0, s>>>((double *)sink, iters, 0.5, 1.0);
+      else k_probe_ffma2<<<blocks, kProbeThreads, 0, s>>>((float *)sink, iters, 0.5f, 1.0f);
+      note_launch();
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+    }
+    return best;
+  };
+  const int it32 = 1 << 14, it64 = 1 << 9;
+  const float ms32 = timed(false, it32), ms64 = timed(true, it64);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  call.finish();
+  if (!cuda_ok(cudaGetLastError(), "lsmgpu_measure_fma_rates")) return lsmgpu_get_last_error(nullptr, 0);
+  if (!(ms32 > 0.f) || !(ms64 > 0.f)) {
+    set_error(LSMGPU_ERR_CUDA, "lsmgpu_measure_fma_rates: no timing");
+    return LSMGPU_ERR_CUDA;
+  }
+  const double threads = (double)blocks * kProbeThreads;
+  *fp32_lane_ops_per_s = threads * kProbeChains * 2.0 * it32 / (ms32 * 1e-3);
+  *fp64_ops_per_s = threads * kProbeChains * (double)it64 / (ms64 * 1e-3);
   return LSMGPU_OK;
 }
 
