@@ -177,7 +177,7 @@ template <class R, int MODE, bool EXACT>
 bool encode_stage_tmap(CUtensorMap *m, const R *p, const Layout &L) {
   const long long ex = (long long)L.nx + GX + 3, ey = (long long)L.ny + 2 * GY, ez = (long long)L.nz + 2 * GZ;
   if constexpr (uses_reinit_x2<R, MODE, EXACT>())
-    return encode_tmap_3d(m, p, sizeof(R), ex, ey, ez, L.py, L.pz, RSX, RSY, RSZ);
+    return encode_tmap_3d(m, p, sizeof(R), ex, ey, ez, L.py, L.pz, RSX, RSY, RZ + 6);
   return encode_tmap_3d(m, p, sizeof(R), ex, ey, ez, L.py, L.pz, SX, SY, SZ);
 }
 
@@ -193,12 +193,12 @@ static void launch_stage(const CUtensorMap &tm, const StageArgs<R> &a, bool prep
   static bool attr_set = false;
   if constexpr (uses_reinit_x2<R, MODE, EXACT>()) {
     if (!attr_set) {
-      cudaFuncSetAttribute(k_reinit_x2<RZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kReinitX2Smem);
+      cudaFuncSetAttribute(k_reinit_x2<RZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)reinit_x2_smem(RZ));
       attr_set = true;
     }
     if (prepare_only) return;
     dim3 grd((unsigned)((L.nx + RX - 1) / RX), (unsigned)((L.ny + RY - 1) / RY), (unsigned)((L.nz + RZ - 1) / RZ));
-    k_reinit_x2<RZ><<<grd, dim3(32, RY), kReinitX2Smem, stream()>>>(tm, a);
+    k_reinit_x2<RZ><<<grd, dim3(32, RY), reinit_x2_smem(RZ), stream()>>>(tm, a);
     note_launch();
     return;
   }

@@ -41,10 +41,15 @@
 namespace lsmgpu {
 namespace fused {
 
-constexpr int RX = 64, RY = 8, RZ = 16;                  // cells of a tile
-constexpr int RSX = RX + 8, RSY = RY + 6, RSZ = RZ + 6;  // staged tile
-constexpr size_t kReinitX2Smem = (size_t)RSX * RSY * RSZ * sizeof(float);
-static_assert(RZ % 2 == 0 && RZ % RY == 0, "the prologues pack plane pairs and cover RZ planes by rows");
+constexpr int RX = 64, RY = 8;    // cells of a tile in x and y
+constexpr int RSX = RX + 8, RSY = RY + 6;  // staged tile in x and y
+constexpr int RZ = 8;             // planes of a tile (the depth the steppers launch)
+// staged tile of a TILE_Z-plane tile: 72 x 14 x (TILE_Z + 6) floats
+constexpr size_t reinit_x2_smem(int tile_z) { return (size_t)RSX * RSY * (tile_z + 6) * sizeof(float); }
+// CTAs per SM the kernel is built for: three 8-plane tiles fit the SM's
+// shared memory (67 KB each with the static arrays) and registers (80 per
+// thread); a 16-plane tile needs 100 KB, so two.
+constexpr int reinit_x2_ctas(int tile_z) { return tile_z <= 8 ? 3 : 2; }
 
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return fma2(b, sp(-1.f), a); }
 __device__ __forceinline__ float rcp_approx(float x) {
@@ -94,18 +99,16 @@ __device__ __forceinline__ Tri tri_forms(float2 d0, float2 d1, float2 d2) {
 }
 
 // Weight products of a window from its three indicator forms (x4) and the
-// maximum squared difference m: q_k = (4 S_k + 4 eps) 2^-e with 2^e <= 4 eps
-// < 2^(e+1), eps = 1e-6 m + 1e-36 (LSMLIB's, spatial_derivatives3d.f.in:1296
-// in units of the unscaled differences); only ratios of the q_k enter the
-// weights.  1 <= q_k < 7e7, so the squared products stay below 2e31.
+// maximum squared difference m: q_k = 4 S_k / (4 eps) + 1 = (S_k + eps) / eps,
+// eps = 1e-6 m + 1e-36 (LSMLIB's, spatial_derivatives3d.f.in:1296, in units
+// of the unscaled differences); only ratios of the q_k enter the weights.
+// 1 <= q_k < 4e7, so the squared products stay below 3e30.
 struct WQ {
   float2 q23, q13, q12;  // (q2 q3)^2, (q1 q3)^2, (q1 q2)^2
 };
 __device__ __forceinline__ WQ window_q(float2 s1, float2 s2, float2 s3, float2 m) {
-  const float2 e4 = fma2(sp(4e-6f), m, sp(4e-36f));
-  const float2 s = pow2_recip2(e4);
-  const float2 e = mul2(e4, s);
-  const float2 q1 = fma2(s1, s, e), q2 = fma2(s2, s, e), q3 = fma2(s3, s, e);
+  const float2 s = rcp2(fma2(sp(4e-6f), m, sp(4e-36f)));  // 1 / (4 eps), finite: 4 eps >= 4e-36
+  const float2 q1 = fma2(s1, s, sp(1.f)), q2 = fma2(s2, s, sp(1.f)), q3 = fma2(s3, s, sp(1.f));
   const float2 a = mul2(q2, q3), b = mul2(q1, q3), c = mul2(q1, q2);
   return {mul2(a, a), mul2(b, b), mul2(c, c)};
 }
@@ -166,8 +169,11 @@ __device__ __forceinline__ void write_periodic_images(float *out, const Layout &
 // (a template so that each translation unit including this header has its
 // own instance, as with the other stage kernels)
 template <int TILE_Z = RZ>
-__global__ void __launch_bounds__(256, 2) k_reinit_x2(const __grid_constant__ CUtensorMap tm, StageArgs<float> a) {
-  static_assert(TILE_Z == RZ, "one tile depth");
+__global__ void __launch_bounds__(256, reinit_x2_ctas(TILE_Z))
+    k_reinit_x2(const __grid_constant__ CUtensorMap tm, StageArgs<float> a) {
+  static_assert(TILE_Z % 2 == 0 && TILE_Z % RY == 0, "the prologues pack plane pairs and cover the planes by rows");
+  constexpr int RZ = TILE_Z, RSZ = TILE_Z + 6;
+  constexpr size_t kReinitX2Smem = reinit_x2_smem(TILE_Z);
   extern __shared__ __align__(128) unsigned char smem_raw[];
   float *tile = reinterpret_cast<float *>(smem_raw);
   __shared__ __align__(8) uint64_t bar;
@@ -393,15 +399,14 @@ __global__ void __launch_bounds__(256, 2) k_reinit_x2(const __grid_constant__ CU
     const float2 pc = pc_src ? pc_ld : u0;
     float2 n2 = sp(0.f);
     {
-      // Godunov: pc > 0: max(-g+, g-, 0); else max(g+, -g-, 0)
-      const bool px = pc.x > 0.f, py = pc.y > 0.f;
+      // Godunov: pc > 0: max(-g+, g-, 0); else max(g+, -g-, 0), i.e.
+      // max(-s g+, s g-, 0) with s = sign of pc
+      const float2 sg = make_float2(pc.x > 0.f ? 1.f : -1.f, pc.y > 0.f ? 1.f : -1.f);
       const float2 g[3][2] = {{gpx, gmx}, {gpy, gmy}, {gpz, gmz_cur}};
 #pragma unroll
       for (int d = 0; d < 3; d++) {
-        const float2 gp = g[d][0], gm = g[d][1];
-        const float sx_ = px ? max3f(-gp.x, gm.x, 0.f) : max3f(gp.x, -gm.x, 0.f);
-        const float sy_ = py ? max3f(-gp.y, gm.y, 0.f) : max3f(gp.y, -gm.y, 0.f);
-        const float2 st = make_float2(sx_, sy_);
+        const float2 ap = mul2(g[d][0], sg), am = mul2(g[d][1], sg);
+        const float2 st = make_float2(max3f(-ap.x, am.x, 0.f), max3f(-ap.y, am.y, 0.f));
         n2 = fma2(mul2(st, iv2[d]), st, n2);
       }
     }
