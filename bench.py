@@ -898,7 +898,7 @@ MEASURED_STAGE_TRAFFIC = 285.6e6
 # square-root sequences included) per cell-update of the FP64 parity form
 # (3 x one stage launch of k_stage<double, REINIT> at 128^3); both from the
 # captures summarised in profiles/k_reinit_x2_reinit_f32_256.md
-MEASURED_FMA_PIPE_INSTR_PER_CELL_STAGE = 115.3
+MEASURED_FMA_PIPE_INSTR_PER_CELL_STAGE = 130.2
 MEASURED_FP64_OPS_PER_CELL_UPDATE = 3 * 633.5
 
 
