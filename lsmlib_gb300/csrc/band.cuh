@@ -79,7 +79,11 @@ __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_count(F f, long long n, int
     for (int q = 0; q < SCAN_ITEMS; q++) {
       const long long e = base + 32LL * q;
       const int b = (e < n) ? f.flags(e) : 0;
-      c0 += __popc(__ballot_sync(0xffffffffu, b & 1));
+      const unsigned m0 = __ballot_sync(0xffffffffu, b & 1);
+      // the round's 32 elements are consecutive: its ballot is their bit mask
+      if constexpr (F::kStoreBallots)
+        if (lane == 0 && e - lane < n) f.store_ballot((e - lane) >> 5, m0);
+      c0 += __popc(m0);
       c1 += __popc(__ballot_sync(0xffffffffu, b & 2));
       c2 += __popc(__ballot_sync(0xffffffffu, b & 4));
     }
@@ -261,10 +265,16 @@ struct Level0T {
   // (the largest float below width) and (double)a >= width_inner <=>
   // a >= inner_ge (the smallest float not below width_inner)
   float width_lt, inner_ge;
-  U8 *mark_lin = nullptr;   // when set (nb box == phi's box): level-0 marks written by the count pass
+  // when set (nb box == phi's box): the count pass writes every cell's
+  // classification bits into its mark byte (1 level 0, 2 outer minus, 4 outer
+  // plus); the emit pass (Level0Marks) reads them back instead of phi and
+  // leaves the final marks (1 in level 0, 0 elsewhere)
+  U8 *mark_lin = nullptr;
   static constexpr bool kPrefetch = true;
+  static constexpr bool kStoreBallots = false;
+  __device__ void store_ballot(long long, unsigned) const {}
   __device__ void counted(long long e, int bits) const {
-    if (mark_lin) mark_lin[e] = (bits & 1) ? 1 : 0;
+    if (mark_lin) mark_lin[e] = (U8)bits;
   }
   typedef T V;
   __device__ T load(long long e) const { return phi.p[e]; }
@@ -319,6 +329,27 @@ struct Level0T {
 
 typedef Level0T<R> Level0;
 
+// emit pass of a fused-marks level-0 build: the classification comes from the
+// mark bytes the count pass wrote (a quarter of phi's bytes for FP32, an
+// eighth for FP64); each listed cell's byte becomes its final mark 1
+template <class T>
+struct Level0Marks {
+  Level0T<T> z;
+  U8 *marks;
+  static constexpr bool kPrefetch = true;
+  static constexpr bool kStoreBallots = false;
+  typedef U8 V;
+  __device__ U8 load(long long e) const { return marks[e]; }
+  __device__ int classify(U8 raw, long long) const { return raw; }
+  __device__ int flags(long long e) const { return marks[e]; }
+  __device__ void counted(long long, int) const {}
+  __device__ void store_ballot(long long, unsigned) const {}
+  __device__ void emit(long long e, int bits, long long r0, long long r1, long long r2) const {
+    z.emit(e, bits, r0, r1, r2);
+    marks[e] = 1;
+  }
+};
+
 // every cell of phi's ghost box gets its level-0 mark (1 in the band, 0 out);
 // threads along x and y, each walking kMarkZ planes
 constexpr int kMarkZ = 16;
@@ -367,6 +398,13 @@ struct Bfs {
   }
   __device__ long long cidx(int a, int b, int c) const { return nb.off(a, b, c); }
   static constexpr bool kPrefetch = false;  // dependent gathers; the one-pass form keeps registers low
+  // the count pass stores each round's winner ballot (one bit per candidate)
+  // when `wbits` is set, for BfsWinners' emit pass
+  static constexpr bool kStoreBallots = true;
+  unsigned *wbits = nullptr;
+  __device__ void store_ballot(long long word, unsigned mask) const {
+    if (wbits) wbits[word] = mask;
+  }
   typedef int V;
   __device__ int load(long long) const { return 0; }
   __device__ int classify(int, long long t) const { return flags(t); }
@@ -390,6 +428,22 @@ struct Bfs {
     nb.p[o] = mark;
     claim[o] = kUnclaimed;
   }
+};
+
+// emit pass of a breadth-first level from the winner bits of its count pass:
+// only winners gather their parent and touch the grid
+struct BfsWinners {
+  Bfs f;
+  const unsigned *wbits;
+  static constexpr bool kPrefetch = false;
+  static constexpr bool kStoreBallots = false;
+  typedef int V;
+  __device__ int load(long long) const { return 0; }
+  __device__ int classify(int, long long t) const { return flags(t); }
+  __device__ void counted(long long, int) const {}
+  __device__ void store_ballot(long long, unsigned) const {}
+  __device__ int flags(long long t) const { return (int)((wbits[t >> 5] >> (t & 31)) & 1u); }
+  __device__ void emit(long long t, int b, long long r0, long long r1, long long r2) const { f.emit(t, b, r0, r1, r2); }
 };
 
 __global__ void k_bfs_claim(Bfs f, long long n) {
@@ -428,6 +482,8 @@ bool bfs_levels(Call &call, View<U8> nb, const Box &nbb, int *ix, int *iy, int *
       Bfs f{nb, nbb, claim, ix, iy, iz, nlo, lo[lv - 1], (int)count, (U8)(lv + 1)};
       const long long n = 6 * np;
       const unsigned g = (unsigned)((n + 255) / 256);
+      f.wbits = call.temp<unsigned>((n + SCAN_TILE - 1) / SCAN_TILE * (SCAN_TILE / 32));
+      if (!call.ok()) return false;
       LSMGPU_LAUNCH(k_bfs_claim, g, 256, 0, f, n);
       // the compaction writes list entries count .. count+added-1; the
       // counts are checked against the capacity before anything is written
@@ -438,7 +494,7 @@ bool bfs_levels(Call &call, View<U8> nb, const Box &nbb, int *ix, int *iy, int *
         set_error(LSMGPU_ERR_CAPACITY, "narrow band lists exceed nhi_index");
         return false;
       }
-      cw.emit(f);
+      cw.emit(BfsWinners{f, f.wbits});
       added = tot[0];
     }
     if (added > 0) {
@@ -543,12 +599,15 @@ bool band_build(Call &call, const T *phi, const Box &gb, U8 *nbd, const Box &nbb
               tot[1] + tot[2]);
     return false;
   }
-  if (!fused)
+  if (fused) {
+    c0.emit(Level0Marks<T>{z, nbd});
+  } else {
     LSMGPU_LAUNCH(k_mark0<T>,
                   dim3((unsigned)((gb.n(0) + 31) / 32), (unsigned)((gb.n(1) + 7) / 8),
                        (unsigned)((gb.n(2) + kMarkZ - 1) / kMarkZ)),
                   dim3(32, 8), 0, z);
-  c0.emit(z);
+    c0.emit(z);
+  }
   lo.assign(level + 1, -1);
   hi.assign(level + 1, -1);
   lo[0] = nlo;
