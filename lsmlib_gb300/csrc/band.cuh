@@ -71,6 +71,7 @@ __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_count(F f, long long n, int
       const long long e = base + 32LL * q;
       const int b = (e < n) ? f.classify(v[q], e) : 0;
       if (e < n) f.counted(e, b);
+      if (__ballot_sync(0xffffffffu, b) == 0) continue;  // most rounds of a sparse band hold nothing
       c0 += __popc(__ballot_sync(0xffffffffu, b & 1));
       c1 += __popc(__ballot_sync(0xffffffffu, b & 2));
       c2 += __popc(__ballot_sync(0xffffffffu, b & 4));
@@ -101,30 +102,44 @@ __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_count(F f, long long n, int
   }
 }
 
-// exclusive scan of the per-block counts (one block; serial chunks per
-// thread, then a shared-memory scan of the chunk totals); totals[r] at the end
-__global__ void k_scan_blocks(int *counts, int nblocks, long long *offsets, long long *totals) {
-  __shared__ long long chunk[3][1024];
-  const int t = threadIdx.x, nt = blockDim.x;
+// exclusive scan of the per-block counts (one block of 1024 threads: serial
+// chunks per thread, then a warp-shuffle scan of the chunk totals);
+// totals[r] at the end
+__device__ __forceinline__ long long warp_incl_scan(long long v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long u = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += u;
+  }
+  return v;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_blocks(int *counts, int nblocks, long long *offsets,
+                                                       long long *totals) {
+  __shared__ long long wsum[3][32];
+  const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, w = t >> 5;
   const int per = (nblocks + nt - 1) / nt;
   const int b0 = t * per, b1 = min(nblocks, b0 + per);
   long long loc[3] = {0, 0, 0};
   for (int b = b0; b < b1; b++)
     for (int r = 0; r < 3; r++) loc[r] += counts[3 * b + r];
-  for (int r = 0; r < 3; r++) chunk[r][t] = loc[r];
-  __syncthreads();
-  if (t == 0) {
-    long long acc[3] = {0, 0, 0};
-    for (int u = 0; u < nt; u++)
-      for (int r = 0; r < 3; r++) {
-        const long long v = chunk[r][u];
-        chunk[r][u] = acc[r];
-        acc[r] += v;
-      }
-    for (int r = 0; r < 3; r++) totals[r] = acc[r];
+  long long incl[3];
+  for (int r = 0; r < 3; r++) {
+    incl[r] = warp_incl_scan(loc[r], lane);
+    if (lane == 31) wsum[r][w] = incl[r];
   }
   __syncthreads();
-  long long run[3] = {chunk[0][t], chunk[1][t], chunk[2][t]};
+  if (w == 0) {
+    for (int r = 0; r < 3; r++) {
+      const long long v = lane < nt / 32 ? wsum[r][lane] : 0;
+      const long long x = warp_incl_scan(v, lane);
+      wsum[r][lane] = x - v;  // exclusive prefix of the warp totals
+      if (lane == 31) totals[r] = x;
+    }
+  }
+  __syncthreads();
+  long long run[3];
+  for (int r = 0; r < 3; r++) run[r] = wsum[r][w] + incl[r] - loc[r];
   for (int b = b0; b < b1; b++)
     for (int r = 0; r < 3; r++) {
       offsets[3 * b + r] = run[r];
@@ -152,6 +167,7 @@ __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_emit(F f, long long n, cons
     for (int q = 0; q < SCAN_ITEMS; q++) {
       const long long e = base + 32LL * q;
       bits[q] = (e < n) ? f.classify(v[q], e) : 0;
+      if (__ballot_sync(0xffffffffu, bits[q]) == 0) continue;
 #pragma unroll
       for (int r = 0; r < 3; r++) c[r] += __popc(__ballot_sync(0xffffffffu, (bits[q] >> r) & 1));
     }
@@ -179,6 +195,7 @@ __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_emit(F f, long long n, cons
     int b;
     if constexpr (F::kPrefetch) b = bits[q];
     else b = (e < n) ? f.flags(e) : 0;
+    if (__ballot_sync(0xffffffffu, b) == 0) continue;
     const unsigned m0 = __ballot_sync(0xffffffffu, b & 1);
     const unsigned m1 = __ballot_sync(0xffffffffu, b & 2);
     const unsigned m2 = __ballot_sync(0xffffffffu, b & 4);
