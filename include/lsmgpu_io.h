@@ -61,6 +61,31 @@ typedef struct LsmgpuGrid {
   double beta, gamma;
 } LsmgpuGrid;
 
+/* Grid construction (src/utils/lsm_grid.c:36-321, 789-1036), so a program
+ * written against LSMLIB's lsm_grid.h needs no LSMLIB object for its index
+ * spaces.  `accuracy` is LSMLIB's LSMLIB_SPATIAL_DERIVATIVE_ACCURACY_TYPE:
+ * 0 LOW (ENO1, 2 ghost cells), 1 MEDIUM (ENO2, 3), 2 HIGH (ENO3, 5),
+ * 3 VERY_HIGH (WENO5, 4).  Structures come from calloc (release with
+ * destroyGrid or free).  A dimension other than 2 or 3 is reported on
+ * stderr and replaced by 2, as LSMLIB does. */
+LsmgpuGrid *allocateGrid(void);                                                   /* lsm_grid.c:36  */
+LsmgpuGrid *createGridSetDx(int num_dims, double dx, double *x_lo, double *x_hi, int accuracy); /* :51 */
+LsmgpuGrid *createGridSetDxDyDz(int num_dims, double dx, double dy, double dz, double *x_lo, double *x_hi,
+                                int accuracy);                                    /* lsm_grid.c:117 */
+LsmgpuGrid *createGridSetGridDims(int num_dims, int *grid_dims, double *x_lo, double *x_hi,
+                                  int accuracy);                                  /* lsm_grid.c:189 */
+LsmgpuGrid *copyGrid(LsmgpuGrid *grid);                                           /* lsm_grid.c:253 */
+void destroyGrid(LsmgpuGrid *grid);                                               /* lsm_grid.c:317 */
+/* Index spaces (ghost box from 0, fill box, D1/D2/D3 fill boxes) for the
+ * scheme's stencil reach; setIndexSpaceLimits also sets the narrow-band
+ * level count, the marks and the widths beta, gamma (lsm_grid.c:987-1036). */
+void setIndexSpaceLimitsCentral(LsmgpuGrid *grid);                                /* lsm_grid.c:789 */
+void setIndexSpaceLimitsENO1(LsmgpuGrid *grid);                                   /* lsm_grid.c:832 */
+void setIndexSpaceLimitsENO2(LsmgpuGrid *grid);                                   /* lsm_grid.c:874 */
+void setIndexSpaceLimitsENO3(LsmgpuGrid *grid);                                   /* lsm_grid.c:918 */
+void setIndexSpaceLimitsWENO5(LsmgpuGrid *grid);                                  /* lsm_grid.c:962 */
+void setIndexSpaceLimits(int accuracy, LsmgpuGrid *grid);                         /* lsm_grid.c:987 */
+
 /* Writes `grid` in the binary Grid format.  Replaces writeGridToBinaryFile
  * (src/utils/lsm_grid.c:614; C declaration src/utils/lsm_grid.h:313). */
 void writeGridToBinaryFile(LsmgpuGrid *grid, char *file_name, int zip_status);

@@ -264,6 +264,162 @@ void writeGridToBinaryFile(LsmgpuGrid *grid, char *file_name, int zip_status) {
   rezip(what, file_name, zip_status);
 }
 
+// ---- Grid construction -------------------------------------------------
+// Ghost cells per accuracy level: LOW (ENO1) 2, MEDIUM (ENO2) 3, HIGH (ENO3)
+// 5, VERY_HIGH (WENO5) 4 (lsm_grid.c:47).
+static int grid_ghost_cells(int accuracy) {
+  static const int g[4] = {2, 3, 5, 4};
+  return (accuracy >= 0 && accuracy < 4) ? g[accuracy] : g[1];
+}
+
+LsmgpuGrid *allocateGrid(void) { return (LsmgpuGrid *)calloc(1, sizeof(LsmgpuGrid)); }
+
+void destroyGrid(LsmgpuGrid *grid) { free(grid); }
+
+LsmgpuGrid *copyGrid(LsmgpuGrid *grid) {
+  LsmgpuGrid *g = allocateGrid();
+  if (g && grid) *g = *grid;
+  return g;
+}
+
+static int grid_dims_of(int num_dims, const char *what) {
+  if (num_dims == 2 || num_dims == 3) return num_dims;
+  fprintf(stderr, "\n%s: invalid number of dimensions (%d), set to 2.\n", what, num_dims);
+  set_error(LSMGPU_ERR_ARGUMENT, "%s: invalid number of dimensions (%d), set to 2", what, num_dims);
+  return 2;
+}
+
+// ghost-box extents from the interior ones; the third axis of a 2D grid is
+// one cell with zero extent and spacing (lsm_grid.c:90-108)
+static void grid_finish(LsmgpuGrid *g, int accuracy) {
+  const int ng = grid_ghost_cells(accuracy);
+  g->num_gridpts = 1;
+  for (int i = 0; i < g->num_dims; i++) {
+    g->grid_dims_ghostbox[i] = g->grid_dims[i] + 2 * ng;
+    g->x_lo_ghostbox[i] = g->x_lo[i] - ng * g->dx[i];
+    g->x_hi_ghostbox[i] = g->x_hi[i] + ng * g->dx[i];
+    g->num_gridpts *= g->grid_dims_ghostbox[i];
+  }
+  if (g->num_dims == 2) {
+    g->x_lo[2] = 0;
+    g->x_hi[2] = 0;
+    g->x_lo_ghostbox[2] = 0;
+    g->x_hi_ghostbox[2] = 0;
+    g->grid_dims[2] = 1;
+    g->grid_dims_ghostbox[2] = 1;
+    g->dx[2] = 0;
+  }
+  setIndexSpaceLimits(accuracy, g);
+}
+
+// spacing given: the cell count is the nearest integer to the extent over
+// the spacing, and x_hi moves to x_lo + cells * spacing (lsm_grid.c:82-88)
+static LsmgpuGrid *grid_from_spacing(int num_dims, const double sp[3], const double *x_lo, const double *x_hi,
+                                     int accuracy, const char *what) {
+  LsmgpuGrid *g = allocateGrid();
+  if (!g) return nullptr;
+  g->num_dims = grid_dims_of(num_dims, what);
+  for (int i = 0; i < 3; i++) g->dx[i] = sp[i];
+  for (int i = 0; i < g->num_dims; i++) {
+    g->grid_dims[i] = (int)rint((x_hi[i] - x_lo[i]) / g->dx[i]);
+    g->x_lo[i] = x_lo[i];
+    g->x_hi[i] = x_lo[i] + g->grid_dims[i] * g->dx[i];
+  }
+  grid_finish(g, accuracy);
+  return g;
+}
+
+LsmgpuGrid *createGridSetDx(int num_dims, double dx, double *x_lo, double *x_hi, int accuracy) {
+  clear_error();
+  const double sp[3] = {dx, dx, num_dims == 3 ? dx : 0.0};
+  LsmgpuGrid *g = grid_from_spacing(num_dims, sp, x_lo, x_hi, accuracy, "createGridSetDx");
+  if (g && g->num_dims == 3) g->dx[2] = dx;
+  return g;
+}
+
+LsmgpuGrid *createGridSetDxDyDz(int num_dims, double dx, double dy, double dz, double *x_lo, double *x_hi,
+                                int accuracy) {
+  clear_error();
+  const double sp[3] = {dx, dy, dz};
+  return grid_from_spacing(num_dims, sp, x_lo, x_hi, accuracy, "createGridSetDxDyDz");
+}
+
+// cell counts given: the spacing is the extent over the count (lsm_grid.c:216)
+LsmgpuGrid *createGridSetGridDims(int num_dims, int *grid_dims, double *x_lo, double *x_hi, int accuracy) {
+  clear_error();
+  LsmgpuGrid *g = allocateGrid();
+  if (!g) return nullptr;
+  g->num_dims = grid_dims_of(num_dims, "createGridSetGridDims");
+  for (int i = 0; i < g->num_dims; i++) {
+    g->grid_dims[i] = grid_dims[i];
+    g->x_hi[i] = x_hi[i];
+    g->x_lo[i] = x_lo[i];
+    g->dx[i] = (g->x_hi[i] - g->x_lo[i]) / g->grid_dims[i];
+  }
+  grid_finish(g, accuracy);
+  return g;
+}
+
+// ghost box from 0; the D1 / D2 / D3 fill boxes lose 1 / 2 / 3 cells per
+// side (lsm_grid.c:789-812)
+void setIndexSpaceLimitsCentral(LsmgpuGrid *g) {
+  int *gb[3][2] = {{&g->ilo_gb, &g->ihi_gb}, {&g->jlo_gb, &g->jhi_gb}, {&g->klo_gb, &g->khi_gb}};
+  int *d1[3][2] = {{&g->ilo_D1_fb, &g->ihi_D1_fb}, {&g->jlo_D1_fb, &g->jhi_D1_fb}, {&g->klo_D1_fb, &g->khi_D1_fb}};
+  int *d2[3][2] = {{&g->ilo_D2_fb, &g->ihi_D2_fb}, {&g->jlo_D2_fb, &g->jhi_D2_fb}, {&g->klo_D2_fb, &g->khi_D2_fb}};
+  int *d3[3][2] = {{&g->ilo_D3_fb, &g->ihi_D3_fb}, {&g->jlo_D3_fb, &g->jhi_D3_fb}, {&g->klo_D3_fb, &g->khi_D3_fb}};
+  for (int a = 0; a < 3; a++) {
+    const int top = g->grid_dims_ghostbox[a] - 1;
+    *gb[a][0] = 0; *gb[a][1] = top;
+    *d1[a][0] = 1; *d1[a][1] = top - 1;
+    *d2[a][0] = 2; *d2[a][1] = top - 2;
+    *d3[a][0] = 3; *d3[a][1] = top - 3;
+  }
+}
+
+// fill box = the cells where both the plus and the minus derivative are
+// defined: minus from D_lo + lo_shift, plus up to D_hi - hi_shift
+static void fill_box_from(LsmgpuGrid *g, int order, int lo_shift, int hi_shift) {
+  setIndexSpaceLimitsCentral(g);
+  const int lo[3] = {order == 1 ? g->ilo_D1_fb : order == 2 ? g->ilo_D2_fb : g->ilo_D3_fb,
+                     order == 1 ? g->jlo_D1_fb : order == 2 ? g->jlo_D2_fb : g->jlo_D3_fb,
+                     order == 1 ? g->klo_D1_fb : order == 2 ? g->klo_D2_fb : g->klo_D3_fb};
+  const int hi[3] = {order == 1 ? g->ihi_D1_fb : order == 2 ? g->ihi_D2_fb : g->ihi_D3_fb,
+                     order == 1 ? g->jhi_D1_fb : order == 2 ? g->jhi_D2_fb : g->jhi_D3_fb,
+                     order == 1 ? g->khi_D1_fb : order == 2 ? g->khi_D2_fb : g->khi_D3_fb};
+  g->ilo_fb = lo[0] + lo_shift; g->ihi_fb = hi[0] - hi_shift;
+  g->jlo_fb = lo[1] + lo_shift; g->jhi_fb = hi[1] - hi_shift;
+  g->klo_fb = lo[2] + lo_shift; g->khi_fb = hi[2] - hi_shift;
+}
+
+void setIndexSpaceLimitsENO1(LsmgpuGrid *g) { fill_box_from(g, 1, 0, 1); }   // lsm_grid.c:832-865
+void setIndexSpaceLimitsENO2(LsmgpuGrid *g) { fill_box_from(g, 2, 1, 1); }   // :874-909
+void setIndexSpaceLimitsENO3(LsmgpuGrid *g) { fill_box_from(g, 3, 1, 2); }   // :918-953
+void setIndexSpaceLimitsWENO5(LsmgpuGrid *g) { fill_box_from(g, 1, 2, 3); }  // :962-985
+
+// marks 120 (ghost box), 119, 118, 117 (D1-D3), 120 - levels (fill box);
+// beta / gamma 3 / 6 cells above MEDIUM accuracy, else 2 / 4 (:987-1036)
+void setIndexSpaceLimits(int accuracy, LsmgpuGrid *g) {
+  g->mark_gb = 120;
+  g->mark_D1 = (unsigned char)(g->mark_gb - 1);
+  g->mark_D2 = (unsigned char)(g->mark_gb - 2);
+  g->mark_D3 = (unsigned char)(g->mark_gb - 3);
+  g->num_nb_levels = grid_ghost_cells(accuracy);
+  g->mark_fb = (unsigned char)(g->mark_gb - g->num_nb_levels);
+  if (accuracy > 1) {
+    g->beta = 3 * g->dx[0];
+    g->gamma = 6 * g->dx[0];
+  } else {
+    g->beta = 2 * g->dx[0];
+    g->gamma = 4 * g->dx[0];
+  }
+  switch (accuracy) {
+    case 0: setIndexSpaceLimitsENO1(g); break;
+    case 2: setIndexSpaceLimitsENO3(g); break;
+    case 3: setIndexSpaceLimitsWENO5(g); break;
+    default: setIndexSpaceLimitsENO2(g);
+  }
+}
+
 LsmgpuGrid *readGridFromBinaryFile(char *file_name) {
   const char *what = "readGridFromBinaryFile";
   clear_error();
