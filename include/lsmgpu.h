@@ -15,7 +15,8 @@
  *    device, computed, and copied back before the call returns, which is the
  *    synchronous behaviour LSMLIB's serial routines have.
  *  - Scratch arrays of the LSMLIB interface (D1, D2, D3 of the dense
- *    derivative routines) are accepted and not written.
+ *    derivative routines) are accepted and not written, unless the exact
+ *    side-effect mode is on (lsmgpu_set_exact_side_effects below).
  *
  * Errors: LSMLIB's routines return nothing and do not check their input.  Here
  * each call validates its index boxes (the fill box plus the stencil's reach
@@ -54,6 +55,19 @@ int lsmgpu_synchronize(void);
  * since lsmgpu_reset_launch_count). */
 long long lsmgpu_launch_count(void);
 void lsmgpu_reset_launch_count(void);
+
+/* Exact side-effect mode.  LSMLIB's dense HJ ENO1/2/3 and WENO5 routines
+ * (plus/minus and upwind) leave their scratch arrays D1, D2, D3 holding the
+ * last undivided differences they formed (the z direction's, 1e10 outside
+ * their fill range; src/toolbox/lsm_spatial_derivatives3d.f.in:49-176 and
+ * the lsm3dComputeDn calls of each routine).  By default these routines do
+ * not write the scratch arrays (nothing of LSMLIB reads them back); with the
+ * mode on they replay LSMLIB's lsm3dComputeDn calls after the derivative, so
+ * a driver that reads D1 / D2 / D3 sees LSMLIB's values.  The mode starts as
+ * the environment variable LSMGPU_EXACT_SIDE_EFFECTS says (unset or 0: off).
+ * Process-wide. */
+void lsmgpu_set_exact_side_effects(int on);
+int lsmgpu_get_exact_side_effects(void);
 
 /* Number of CUDA graphs the fused steppers have captured since the process
  * started.  A stepper call replays a cached graph when its buffers, sizes and

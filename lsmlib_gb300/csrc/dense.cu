@@ -438,6 +438,40 @@ void curv_variant(const char *name, R *kappa, const Box &kb, const R *phi, const
   call.finish();
 }
 
+extern "C" void lsm3dcomputedn_(R *Dn, const int *, const int *, const int *, const int *, const int *,
+                                const int *, const R *Dn_minus_one, const int *, const int *, const int *,
+                                const int *, const int *, const int *, const int *ilo_fb, const int *ihi_fb,
+                                const int *jlo_fb, const int *jhi_fb, const int *klo_fb, const int *khi_fb,
+                                const int *n, const int *dir);
+
+// Exact side-effect mode: the lsm3dComputeDn calls a derivative routine of
+// LSMLIB makes, in its order (per direction x, y, z: D1 from phi, then D2 from
+// D1, D3 from D2, over the fill box grown along that direction by `grow`;
+// spatial_derivatives3d.f.in:281-341 ENO1, :487-635 ENO2, :795-1066 ENO3,
+// :1266-1511 WENO5, and the same in the upwind routines), so the scratch
+// arrays end as LSMLIB leaves them.  Runs after the derivative call (each
+// replayed call is an entry point of its own) and only if it succeeded; a 2D
+// or 1D routine running on the 3D one replays its own directions only.
+static void replay_scratch(int scheme, const R *phi, const Box &fphi, R *const D[3], const Box db[3],
+                           const Box &fb) {
+  if (!exact_side_effects() || lsmgpu_get_last_error(nullptr, 0) != LSMGPU_OK) return;
+  const int orders = scheme == ENO2 ? 2 : (scheme == ENO3 ? 3 : 1);
+  const int grow[3] = {scheme == ENO1 ? 0 : (scheme == ENO2 ? 1 : 2), scheme == ENO2 ? 1 : 2, 1};
+  for (int ax = 0; ax < g_lift_dims; ax++)
+    for (int n = 1; n <= orders; n++) {
+      Box cb = fb;
+      cb.lo[ax] -= grow[n - 1];
+      cb.hi[ax] += grow[n - 1];
+      const Box &ob = db[n - 1], &sb = n == 1 ? fphi : db[n - 2];
+      const R *src = n == 1 ? phi : D[n - 2];
+      const int dir = ax + 1;
+      lsm3dcomputedn_(D[n - 1], &ob.lo[0], &ob.hi[0], &ob.lo[1], &ob.hi[1], &ob.lo[2], &ob.hi[2], src, &sb.lo[0],
+                      &sb.hi[0], &sb.lo[1], &sb.hi[1], &sb.lo[2], &sb.hi[2], &cb.lo[0], &cb.hi[0], &cb.lo[1],
+                      &cb.hi[1], &cb.lo[2], &cb.hi[2], &n, &dir);
+      if (lsmgpu_get_last_error(nullptr, 0) != LSMGPU_OK) return;
+    }
+}
+
 extern "C" {
 
 #define PM_PARAMS                                                                        \
@@ -449,18 +483,38 @@ extern "C" {
 void lsm3dhjeno1_(PM_PARAMS, SCR(D1), FBARGS, DXP) {
   hj_pm<ENO1>("lsm3dhjeno1_", phi_x_plus, phi_y_plus, phi_z_plus, BOXOF(p), phi_x_minus, phi_y_minus,
               phi_z_minus, BOXOF(m), phi, BOXOF(f), FBOX, *dx, *dy, *dz);
+  {
+    R *const D[3] = {D1, nullptr, nullptr};
+    const Box db[3] = {BOXOF(D1), Box{}, Box{}};
+    replay_scratch(ENO1, phi, BOXOF(f), D, db, FBOX);
+  }
 }
 void lsm3dhjeno2_(PM_PARAMS, SCR(D1), SCR(D2), FBARGS, DXP) {
   hj_pm<ENO2>("lsm3dhjeno2_", phi_x_plus, phi_y_plus, phi_z_plus, BOXOF(p), phi_x_minus, phi_y_minus,
               phi_z_minus, BOXOF(m), phi, BOXOF(f), FBOX, *dx, *dy, *dz);
+  {
+    R *const D[3] = {D1, D2, nullptr};
+    const Box db[3] = {BOXOF(D1), BOXOF(D2), Box{}};
+    replay_scratch(ENO2, phi, BOXOF(f), D, db, FBOX);
+  }
 }
 void lsm3dhjeno3_(PM_PARAMS, SCR(D1), SCR(D2), SCR(D3), FBARGS, DXP) {
   hj_pm<ENO3>("lsm3dhjeno3_", phi_x_plus, phi_y_plus, phi_z_plus, BOXOF(p), phi_x_minus, phi_y_minus,
               phi_z_minus, BOXOF(m), phi, BOXOF(f), FBOX, *dx, *dy, *dz);
+  {
+    R *const D[3] = {D1, D2, D3};
+    const Box db[3] = {BOXOF(D1), BOXOF(D2), BOXOF(D3)};
+    replay_scratch(ENO3, phi, BOXOF(f), D, db, FBOX);
+  }
 }
 void lsm3dhjweno5_(PM_PARAMS, SCR(D1), FBARGS, DXP) {
   hj_pm<WENO5>("lsm3dhjweno5_", phi_x_plus, phi_y_plus, phi_z_plus, BOXOF(p), phi_x_minus,
                phi_y_minus, phi_z_minus, BOXOF(m), phi, BOXOF(f), FBOX, *dx, *dy, *dz);
+  {
+    R *const D[3] = {D1, nullptr, nullptr};
+    const Box db[3] = {BOXOF(D1), Box{}, Box{}};
+    replay_scratch(WENO5, phi, BOXOF(f), D, db, FBOX);
+  }
 }
 
 #define UP_PARAMS                                                                     \
@@ -470,18 +524,38 @@ void lsm3dhjweno5_(PM_PARAMS, SCR(D1), FBARGS, DXP) {
 void lsm3dupwindhjeno1_(UP_PARAMS, SCR(D1), FBARGS, DXP) {
   hj_upwind<ENO1>("lsm3dupwindhjeno1_", phi_x, phi_y, phi_z, BOXOF(g), phi, BOXOF(f), vel_x, vel_y,
                   vel_z, BOXOF(v), FBOX, *dx, *dy, *dz);
+  {
+    R *const D[3] = {D1, nullptr, nullptr};
+    const Box db[3] = {BOXOF(D1), Box{}, Box{}};
+    replay_scratch(ENO1, phi, BOXOF(f), D, db, FBOX);
+  }
 }
 void lsm3dupwindhjeno2_(UP_PARAMS, SCR(D1), SCR(D2), FBARGS, DXP) {
   hj_upwind<ENO2>("lsm3dupwindhjeno2_", phi_x, phi_y, phi_z, BOXOF(g), phi, BOXOF(f), vel_x, vel_y,
                   vel_z, BOXOF(v), FBOX, *dx, *dy, *dz);
+  {
+    R *const D[3] = {D1, D2, nullptr};
+    const Box db[3] = {BOXOF(D1), BOXOF(D2), Box{}};
+    replay_scratch(ENO2, phi, BOXOF(f), D, db, FBOX);
+  }
 }
 void lsm3dupwindhjeno3_(UP_PARAMS, SCR(D1), SCR(D2), SCR(D3), FBARGS, DXP) {
   hj_upwind<ENO3>("lsm3dupwindhjeno3_", phi_x, phi_y, phi_z, BOXOF(g), phi, BOXOF(f), vel_x, vel_y,
                   vel_z, BOXOF(v), FBOX, *dx, *dy, *dz);
+  {
+    R *const D[3] = {D1, D2, D3};
+    const Box db[3] = {BOXOF(D1), BOXOF(D2), BOXOF(D3)};
+    replay_scratch(ENO3, phi, BOXOF(f), D, db, FBOX);
+  }
 }
 void lsm3dupwindhjweno5_(UP_PARAMS, SCR(D1), FBARGS, DXP) {
   hj_upwind<WENO5>("lsm3dupwindhjweno5_", phi_x, phi_y, phi_z, BOXOF(g), phi, BOXOF(f), vel_x, vel_y,
                    vel_z, BOXOF(v), FBOX, *dx, *dy, *dz);
+  {
+    R *const D[3] = {D1, nullptr, nullptr};
+    const Box db[3] = {BOXOF(D1), Box{}, Box{}};
+    replay_scratch(WENO5, phi, BOXOF(f), D, db, FBOX);
+  }
 }
 
 static void central(const char *name, int order, R *px, R *py, R *pz, const Box &gb, const R *phi,

@@ -159,6 +159,10 @@ template <class F>
 bool graph_replay(const GraphKey &key, F &body) {
   return graph_replay(key, [](void *c) { (*static_cast<F *>(c))(); }, &body);
 }
+// LSMLIB's scratch side effects requested (lsmgpu_set_exact_side_effects or
+// LSMGPU_EXACT_SIDE_EFFECTS=1): the dense derivative routines then also leave
+// D1 / D2 / D3 as LSMLIB's do
+bool exact_side_effects();
 void set_error(int code, const char *fmt, ...);
 void clear_error();
 bool cuda_ok(cudaError_t e, const char *what);  // records and returns false on error

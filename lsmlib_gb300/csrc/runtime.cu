@@ -2,6 +2,7 @@
 // stream, launch counting, a grow-only device arena for staged host arrays and
 // temporaries, and the per-call staging context.
 #include <stdarg.h>
+#include <stdlib.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -41,6 +42,21 @@ Arena g_arena[64];
 }  // namespace
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// exact side-effect mode: -1 until first asked, then the environment's
+// LSMGPU_EXACT_SIDE_EFFECTS (unset or "0": off) unless set through the API
+std::atomic<int> g_side_effects{-1};
+bool exact_side_effects() {
+  int v = g_side_effects.load();
+  if (v < 0) {
+    const char *e = getenv("LSMGPU_EXACT_SIDE_EFFECTS");
+    v = (e && e[0] && !(e[0] == '0' && e[1] == 0)) ? 1 : 0;
+    int expect = -1;
+    g_side_effects.compare_exchange_strong(expect, v);
+    v = g_side_effects.load();
+  }
+  return v == 1;
+}
 
 namespace {
 thread_local cudaStream_t t_capture_stream = nullptr;  // set while a graph is captured
@@ -367,6 +383,9 @@ int lsmgpu_synchronize(void) {
 long long lsmgpu_launch_count(void) { return g_launches.load(); }
 void lsmgpu_reset_launch_count(void) { g_launches.store(0); }
 long long lsmgpu_graph_capture_count(void) { return g_captures.load(); }
+
+void lsmgpu_set_exact_side_effects(int on) { g_side_effects.store(on ? 1 : 0); }
+int lsmgpu_get_exact_side_effects(void) { return exact_side_effects() ? 1 : 0; }
 long long lsmgpu_arena_bytes(void) { return g_arena_bytes.load(); }
 
 const char *lsmgpu_version(void) { return "lsmgpu 0.1 (sm_103a)"; }
