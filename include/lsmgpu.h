@@ -69,6 +69,15 @@ void lsmgpu_reset_launch_count(void);
 void lsmgpu_set_exact_side_effects(int on);
 int lsmgpu_get_exact_side_effects(void);
 
+/* Bounds-check build (python -m lsmlib_gb300.build --bounds-check, which
+ * writes lsmlib_gb300/liblsmgpu_bc.so): every array access of the drop-in
+ * kernels is checked against the array's box; an out-of-range one is
+ * counted, the first one's (i, j, k) kept, and the array's first element used
+ * instead of memory outside it.  lsmgpu_bounds_check_read waits for the
+ * library stream, returns the count and first index of the current device
+ * and clears them.  In the regular library it returns LSMGPU_ERR_ARGUMENT. */
+int lsmgpu_bounds_check_read(long long *count, int *first);
+
 /* Number of CUDA graphs the fused steppers have captured since the process
  * started.  A stepper call replays a cached graph when its buffers, sizes and
  * parameters were seen before, and captures a new one otherwise. */

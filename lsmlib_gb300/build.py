@@ -18,6 +18,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblsmgpu.so")
+# the bounds-check build (LSMGPU_BOUNDS_CHECK): its own objects and library
+BUILD_BC = os.path.join(HERE, "_build_bc")
+libBC = os.path.join(HERE, "liblsmgpu_bc.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Host code computes some per-call constants (e.g. the cut-off's (gamma -
@@ -39,8 +42,8 @@ def nvcc():
     raise RuntimeError("nvcc not found: the lsmgpu CUDA library cannot be built")
 
 
-def _compile(src, extra):
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+def _compile(src, extra, build_dir=BUILD):
+    obj = os.path.join(build_dir, os.path.basename(src) + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) >= _newest_input(src):
         return obj, ""
     flags = list(COMMON)
@@ -62,27 +65,30 @@ def _newest_input(src):
     return t
 
 
-def build(verbose=False, extra=None):
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose=False, extra=None, bounds_check=False):
+    """Compile and link liblsmgpu.so (or, with bounds_check, the
+    bounds-checked liblsmgpu_bc.so); returns the library's path."""
+    build_dir, lib = (BUILD_BC, libBC) if bounds_check else (BUILD, LIB)
+    os.makedirs(build_dir, exist_ok=True)
     srcs = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
-    extra = list(extra or [])
+    extra = list(extra or []) + (["-DLSMGPU_BOUNDS_CHECK"] if bounds_check else [])
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
-        results = list(ex.map(lambda s: _compile(s, extra), srcs))
+        results = list(ex.map(lambda s: _compile(s, extra, build_dir), srcs))
     objs = [o for o, _ in results]
     if verbose:
         for _, log in results:
             if log.strip():
                 print(log)
     newest = max(os.path.getmtime(o) for o in objs)
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
-        tmp = LIB + ".tmp"
+    if not os.path.exists(lib) or os.path.getmtime(lib) < newest:
+        tmp = lib + ".tmp"
         cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-ldl"]
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), p.stdout + p.stderr))
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv))
+    print(build(verbose="-v" in sys.argv, bounds_check="--bounds-check" in sys.argv))

@@ -85,16 +85,46 @@ inline Box mkbox(const int *ilo, const int *ihi, const int *jlo, const int *jhi,
   return b;
 }
 
-// A device view of one column-major array.
+#ifdef LSMGPU_BOUNDS_CHECK
+// Bounds-check build: the device status word of the current device (count of
+// out-of-range accesses, then the first one's i, j, k), allocated once.
+int *bounds_word();
+__device__ __forceinline__ void bounds_fail(int *w, int i, int j, int k) {
+  if (!w) return;
+  if (atomicAdd(&w[0], 1) == 0) {
+    w[1] = i;
+    w[2] = j;
+    w[3] = k;
+  }
+}
+#endif
+
+// A device view of one column-major array.  In a build with
+// LSMGPU_BOUNDS_CHECK defined every access checks the index against the
+// array's box (along the axes with a stride: a 2D / 1D call's missing axes
+// have none), records an out-of-range one in the status word
+// (lsmgpu_bounds_check_read) and uses the array's first element instead.
 template <class T>
 struct View {
   T *p;
   int lo0, lo1, lo2;
   long long s1, s2;
+#ifdef LSMGPU_BOUNDS_CHECK
+  int hi0 = 0x7fffffff, hi1 = 0x7fffffff, hi2 = 0x7fffffff;
+  int *oob = nullptr;
+#endif
   __device__ __forceinline__ long long off(int i, int j, int k) const {
     return (long long)(i - lo0) + s1 * (long long)(j - lo1) + s2 * (long long)(k - lo2);
   }
-  __device__ __forceinline__ T &operator()(int i, int j, int k) const { return p[off(i, j, k)]; }
+  __device__ __forceinline__ T &operator()(int i, int j, int k) const {
+#ifdef LSMGPU_BOUNDS_CHECK
+    if (i < lo0 || i > hi0 || (s1 != 0 && (j < lo1 || j > hi1)) || (s2 != 0 && (k < lo2 || k > hi2))) {
+      bounds_fail(oob, i, j, k);
+      return p[0];
+    }
+#endif
+    return p[off(i, j, k)];
+  }
   __device__ __forceinline__ long long stride(int d) const { return d == 0 ? 1 : (d == 1 ? s1 : s2); }
 };
 
@@ -105,6 +135,10 @@ inline View<T> view(T *p, const Box &b) {
   v.lo0 = b.lo[0]; v.lo1 = b.lo[1]; v.lo2 = b.lo[2];
   v.s1 = g_lift_dims < 2 ? 0 : b.n(0);
   v.s2 = g_lift_dims < 3 ? 0 : b.n(0) * b.n(1);
+#ifdef LSMGPU_BOUNDS_CHECK
+  v.hi0 = b.hi[0]; v.hi1 = b.hi[1]; v.hi2 = b.hi[2];
+  v.oob = bounds_word();
+#endif
   return v;
 }
 

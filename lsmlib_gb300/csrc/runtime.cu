@@ -43,6 +43,30 @@ Arena g_arena[64];
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+#ifdef LSMGPU_BOUNDS_CHECK
+namespace {
+int *g_oob_word[64] = {};
+std::mutex g_oob_lock;
+}  // namespace
+int *bounds_word() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> guard(g_oob_lock);
+  if (!g_oob_word[dev]) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, 4 * sizeof(int)) != cudaSuccess || cudaMemset(p, 0, 4 * sizeof(int)) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    g_oob_word[dev] = (int *)p;
+  }
+  return g_oob_word[dev];
+}
+#endif
+
 // exact side-effect mode: -1 until first asked, then the environment's
 // LSMGPU_EXACT_SIDE_EFFECTS (unset or "0": off) unless set through the API
 std::atomic<int> g_side_effects{-1};
@@ -383,6 +407,29 @@ int lsmgpu_synchronize(void) {
 long long lsmgpu_launch_count(void) { return g_launches.load(); }
 void lsmgpu_reset_launch_count(void) { g_launches.store(0); }
 long long lsmgpu_graph_capture_count(void) { return g_captures.load(); }
+
+int lsmgpu_bounds_check_read(long long *count, int *first) {
+#ifdef LSMGPU_BOUNDS_CHECK
+  clear_error();
+  int h[4] = {0, 0, 0, 0};
+  int *w = bounds_word();
+  if (!w) return lsmgpu_get_last_error(nullptr, 0);
+  std::lock_guard<std::mutex> guard(g_lock);
+  if (!cuda_ok(cudaStreamSynchronize(g_stream.load()), "lsmgpu_bounds_check_read") ||
+      !cuda_ok(cudaMemcpy(h, w, sizeof(h), cudaMemcpyDeviceToHost), "lsmgpu_bounds_check_read") ||
+      !cuda_ok(cudaMemset(w, 0, sizeof(h)), "lsmgpu_bounds_check_read"))
+    return g_err;
+  if (count) *count = h[0];
+  if (first)
+    for (int q = 0; q < 3; q++) first[q] = h[1 + q];
+  return LSMGPU_OK;
+#else
+  (void)count;
+  (void)first;
+  set_error(LSMGPU_ERR_ARGUMENT, "lsmgpu_bounds_check_read: this library was built without LSMGPU_BOUNDS_CHECK");
+  return LSMGPU_ERR_ARGUMENT;
+#endif
+}
 
 void lsmgpu_set_exact_side_effects(int on) { g_side_effects.store(on ? 1 : 0); }
 int lsmgpu_get_exact_side_effects(void) { return exact_side_effects() ? 1 : 0; }
