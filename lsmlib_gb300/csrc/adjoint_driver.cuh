@@ -12,7 +12,10 @@
 
 #include <vector>
 
+#include <type_traits>
+
 #include "adjoint.cuh"
+#include "adjoint_x2.cuh"
 #include "fused_driver.cuh"
 
 namespace lsmgpu {
@@ -62,12 +65,58 @@ inline int pick_chunk(int n_march, long long threads_per_chunk, int per_sm) {
   return c;
 }
 
+// march length per CTA for kernels whose every CTA marches a chunk of n_march
+// cells (plus 6 warm-up cells) and `items` CTAs cover one chunk: the length
+// that minimises waves x (chunk + 6), with `slots` CTAs resident at once
+// (a partly filled last wave costs a whole one); the longest such chunk
+inline int pick_chunk_waves(int n_march, long long items, long long slots) {
+  int best = n_march;
+  long long best_cost = -1;
+  for (int c = n_march; c >= 8; c--) {
+    const long long n = ((long long)n_march + c - 1) / c;
+    const long long waves = (items * n + slots - 1) / slots;
+    const long long cost = waves * (c + 6);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = c;
+    }
+  }
+  return best;
+}
+
+// the FP32 reverse stages run the two-line kernels of adjoint_x2.cuh where
+// the x rows fit one CTA
+template <class R, bool EXACT>
+constexpr bool adj_x2_kernels() {
+  return std::is_same<R, float>::value && !EXACT;
+}
+inline bool adj_x2_fits(const Layout &L) { return L.nx <= kRowMax && L.elems() < (1LL << 31); }
+
 // one reverse stage: x and z faces (writes out), then y faces (adds to out);
 // internal linkage, so the shared-memory limit is set on this unit's kernel
 template <class R, bool EXACT, int MODE>
 static void launch_adj_stage(const AdjStageArgs<R> &a) {
   const Layout &L = a.L;
   dim3 blk(32, kRows);
+  if constexpr (adj_x2_kernels<R, EXACT>()) {
+    if (adj_x2_fits(L)) {
+      const int w = (L.nx + 31) / 32;
+      static bool attr = false;
+      if (!attr) {
+        cudaFuncSetAttribute(k_adj_xz_x2<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)adj_xz_x2_smem(kRowMax));
+        attr = true;
+      }
+      dim3 g1((unsigned)((L.ny + 1) / 2), (unsigned)((L.nz + a.zchunk - 1) / a.zchunk));
+      k_adj_xz_x2<MODE><<<g1, dim3(32, w), adj_xz_x2_smem(L.nx), stream()>>>(a);
+      note_launch();
+      dim3 g2((unsigned)((L.nx + 31) / 32), (unsigned)((L.nz + 2 * kYRows - 1) / (2 * kYRows)),
+              (unsigned)((L.ny + a.ychunk - 1) / a.ychunk));
+      k_adj_y_x2<MODE><<<g2, dim3(32, kYRows), 0, stream()>>>(a);
+      note_launch();
+      return;
+    }
+  }
   if (L.nx <= kRowMax) {
     // one CTA per x row
     const int w = (L.nx + 31) / 32;
@@ -300,9 +349,34 @@ int run(const char *name, const Box &gb, const Box &fb, const Box &vb, const Adj
     aa.inv[0] = fa.inv[0]; aa.inv[1] = fa.inv[1]; aa.inv[2] = fa.inv[2];
     // thread targets per SM measured best at 192^3 (more chunks than resident
     // threads: latency hiding outweighs the extra warm-up cells)
-    aa.zchunk = pick_chunk(nz, nx <= kRowMax ? 32LL * ((nx + 31) / 32) * ny : 32LL * ((nx + kSeg - 1) / kSeg) * ny,
-                           LSMGPU_ADJ_Z_THREADS);
-    aa.ychunk = pick_chunk(ny, (long long)nx * nz, LSMGPU_ADJ_Y_THREADS);
+    if (adj_x2_kernels<R, EXACT>() && adj_x2_fits(L)) {
+      // two lines per thread; chunks from the resident CTAs of each kernel
+      int sms = 152, dev = 0, occ_xz = 1, occ_y = 1;
+      if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if constexpr (adj_x2_kernels<R, EXACT>()) {
+        const int w = (nx + 31) / 32;
+        const int mode = advect ? ADJ_ADV : ADJ_LIN;
+        auto occ = [&](auto kern, int threads, size_t smem) {
+          int v = 0;
+          cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj_xz_x2_smem(kRowMax));
+          if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, threads, smem) != cudaSuccess || v < 1) {
+            cudaGetLastError();
+            v = 1;
+          }
+          return v;
+        };
+        occ_xz = mode == ADJ_ADV ? occ(k_adj_xz_x2<ADJ_ADV>, 32 * w, adj_xz_x2_smem(nx))
+                                 : occ(k_adj_xz_x2<ADJ_LIN>, 32 * w, adj_xz_x2_smem(nx));
+        occ_y = mode == ADJ_ADV ? occ(k_adj_y_x2<ADJ_ADV>, 32 * kYRows, 0) : occ(k_adj_y_x2<ADJ_LIN>, 32 * kYRows, 0);
+      }
+      aa.zchunk = pick_chunk_waves(nz, (ny + 1) / 2, (long long)occ_xz * sms);
+      aa.ychunk = pick_chunk_waves(ny, (long long)((nx + 31) / 32) * ((nz + 2 * kYRows - 1) / (2 * kYRows)),
+                                   (long long)occ_y * sms);
+    } else {
+      aa.zchunk = pick_chunk(nz, nx <= kRowMax ? 32LL * ((nx + 31) / 32) * ny : 32LL * ((nx + kSeg - 1) / kSeg) * ny,
+                             LSMGPU_ADJ_Z_THREADS);
+      aa.ychunk = pick_chunk(ny, (long long)nx * nz, LSMGPU_ADJ_Y_THREADS);
+    }
     const dim3 cgrid((unsigned)((nx + 31) / 32), (unsigned)((ny + 7) / 8), (unsigned)nz), cblk(32, 8);
     // one reverse stage at forward state `st`
     auto rstage = [&]() {
