@@ -909,7 +909,7 @@ def profile_case(a):
     """One fused call on cuda:0 (no timing): `--case reinit|advect` runs
     `--iters` WENO5 / TVD-RK3 iterations of the headline field at n^3 then the
     mean curvature (kernels k_stage*); `adjoint` the objective gradient of
-    adjoint_case (checkpoint every 4; k_adj_xz_row, k_adj_y); `band`
+    adjoint_case (checkpoint every 4; k_adj_x_x2, k_adj_march_x2); `band`
     `--iters` narrow-band steps of band_case (rebuild every 5, FP32);
     `batched` `--iters` steps of n grids of batched_case; `geometry`
     sub_geometry at n^3 with `--iters` calls per entry point."""

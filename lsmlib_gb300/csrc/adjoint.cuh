@@ -303,6 +303,7 @@ struct AdjStageArgs {
   R dt;
   R inv[3];
   int zchunk;         // planes per warp along z (k_adj_xz)
+  int xchunk;         // planes per CTA of the x-face kernel of the two-line path
   int ychunk;         // rows per thread along y (k_adj_y)
 };
 

@@ -66,16 +66,16 @@ inline int pick_chunk(int n_march, long long threads_per_chunk, int per_sm) {
 }
 
 // march length per CTA for kernels whose every CTA marches a chunk of n_march
-// cells (plus 6 warm-up cells) and `items` CTAs cover one chunk: the length
-// that minimises waves x (chunk + 6), with `slots` CTAs resident at once
-// (a partly filled last wave costs a whole one); the longest such chunk
-inline int pick_chunk_waves(int n_march, long long items, long long slots) {
+// cells (plus `warm` warm-up cells) and `items` CTAs cover one chunk: the
+// length that minimises waves x (chunk + warm), with `slots` CTAs resident at
+// once (a partly filled last wave costs a whole one); the longest such chunk
+inline int pick_chunk_waves(int n_march, long long items, long long slots, int warm) {
   int best = n_march;
   long long best_cost = -1;
   for (int c = n_march; c >= 8; c--) {
     const long long n = ((long long)n_march + c - 1) / c;
     const long long waves = (items * n + slots - 1) / slots;
-    const long long cost = waves * (c + 6);
+    const long long cost = waves * (c + warm);
     if (best_cost < 0 || cost < best_cost) {
       best_cost = cost;
       best = c;
@@ -103,16 +103,20 @@ static void launch_adj_stage(const AdjStageArgs<R> &a) {
       const int w = (L.nx + 31) / 32;
       static bool attr = false;
       if (!attr) {
-        cudaFuncSetAttribute(k_adj_xz_x2<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)adj_xz_x2_smem(kRowMax));
+        cudaFuncSetAttribute(k_adj_x_x2<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)adj_x_x2_smem(kRowMax));
         attr = true;
       }
-      dim3 g1((unsigned)((L.ny + 1) / 2), (unsigned)((L.nz + a.zchunk - 1) / a.zchunk));
-      k_adj_xz_x2<MODE><<<g1, dim3(32, w), adj_xz_x2_smem(L.nx), stream()>>>(a);
+      dim3 g1((unsigned)((L.ny + 1) / 2), (unsigned)((L.nz + a.xchunk - 1) / a.xchunk));
+      k_adj_x_x2<MODE><<<g1, dim3(32, w), adj_x_x2_smem(L.nx), stream()>>>(a);
       note_launch();
-      dim3 g2((unsigned)((L.nx + 31) / 32), (unsigned)((L.nz + 2 * kYRows - 1) / (2 * kYRows)),
+      dim3 g2((unsigned)((L.nx + 31) / 32), (unsigned)((L.ny + 2 * kMarchRows - 1) / (2 * kMarchRows)),
+              (unsigned)((L.nz + a.zchunk - 1) / a.zchunk));
+      k_adj_march_x2<MODE, 2><<<g2, dim3(32, kMarchRows), 0, stream()>>>(a);
+      note_launch();
+      dim3 g3((unsigned)((L.nx + 31) / 32), (unsigned)((L.nz + 2 * kMarchRows - 1) / (2 * kMarchRows)),
               (unsigned)((L.ny + a.ychunk - 1) / a.ychunk));
-      k_adj_y_x2<MODE><<<g2, dim3(32, kYRows), 0, stream()>>>(a);
+      k_adj_march_x2<MODE, 1><<<g3, dim3(32, kMarchRows), 0, stream()>>>(a);
       note_launch();
       return;
     }
@@ -351,27 +355,31 @@ int run(const char *name, const Box &gb, const Box &fb, const Box &vb, const Adj
     // threads: latency hiding outweighs the extra warm-up cells)
     if (adj_x2_kernels<R, EXACT>() && adj_x2_fits(L)) {
       // two lines per thread; chunks from the resident CTAs of each kernel
-      int sms = 152, dev = 0, occ_xz = 1, occ_y = 1;
+      int sms = 152, dev = 0, occ_x = 1, occ_m = 1;
       if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       if constexpr (adj_x2_kernels<R, EXACT>()) {
         const int w = (nx + 31) / 32;
-        const int mode = advect ? ADJ_ADV : ADJ_LIN;
         auto occ = [&](auto kern, int threads, size_t smem) {
           int v = 0;
-          cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj_xz_x2_smem(kRowMax));
+          if (smem) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj_x_x2_smem(kRowMax));
           if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, threads, smem) != cudaSuccess || v < 1) {
             cudaGetLastError();
             v = 1;
           }
           return v;
         };
-        occ_xz = mode == ADJ_ADV ? occ(k_adj_xz_x2<ADJ_ADV>, 32 * w, adj_xz_x2_smem(nx))
-                                 : occ(k_adj_xz_x2<ADJ_LIN>, 32 * w, adj_xz_x2_smem(nx));
-        occ_y = mode == ADJ_ADV ? occ(k_adj_y_x2<ADJ_ADV>, 32 * kYRows, 0) : occ(k_adj_y_x2<ADJ_LIN>, 32 * kYRows, 0);
+        occ_x = advect ? occ(k_adj_x_x2<ADJ_ADV>, 32 * w, adj_x_x2_smem(nx))
+                       : occ(k_adj_x_x2<ADJ_LIN>, 32 * w, adj_x_x2_smem(nx));
+        occ_m = advect ? occ(k_adj_march_x2<ADJ_ADV, 1>, 32 * kMarchRows, 0)
+                       : occ(k_adj_march_x2<ADJ_LIN, 1>, 32 * kMarchRows, 0);
       }
-      aa.zchunk = pick_chunk_waves(nz, (ny + 1) / 2, (long long)occ_xz * sms);
-      aa.ychunk = pick_chunk_waves(ny, (long long)((nx + 31) / 32) * ((nz + 2 * kYRows - 1) / (2 * kYRows)),
-                                   (long long)occ_y * sms);
+      const long long cols = (nx + 31) / 32;
+      // the x kernel carries nothing between planes: short chunks keep its
+      // resident CTAs full to the end
+      aa.xchunk = nz < 8 ? nz : 8;
+      (void)occ_x;
+      aa.zchunk = pick_chunk_waves(nz, cols * ((ny + 2 * kMarchRows - 1) / (2 * kMarchRows)), (long long)occ_m * sms, 6);
+      aa.ychunk = pick_chunk_waves(ny, cols * ((nz + 2 * kMarchRows - 1) / (2 * kMarchRows)), (long long)occ_m * sms, 6);
     } else {
       aa.zchunk = pick_chunk(nz, nx <= kRowMax ? 32LL * ((nx + 31) / 32) * ny : 32LL * ((nx + kSeg - 1) / kSeg) * ny,
                              LSMGPU_ADJ_Z_THREADS);

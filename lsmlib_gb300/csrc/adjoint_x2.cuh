@@ -3,15 +3,15 @@
 //
 // The arithmetic is that of k_adj_xz_row / k_adj_y in adjoint.cuh (same
 // slots, same face sums) evaluated for two independent lines per thread,
-// one in each lane of a float2:
-//   k_adj_xz_x2: a CTA owns two x rows (j, j+1) and marches along z; lane x
-//     of the pair is row j, lane y row j+1.  The x stencils come from a ring
-//     of the last eight planes of both rows in shared memory (each thread
-//     stores the column value it loads for the z march, scaled by 1/dx, with
-//     periodic copies at the row ends), and the x slots are exchanged through
-//     shared memory as in the scalar row kernel: one barrier per plane.
-//   k_adj_y_x2: a thread owns the columns (i, k) and (i, k+1) and marches
-//     along y.
+// one in each lane of a float2.  Three launches per reverse stage:
+//   k_adj_x_x2: a CTA owns two x rows (j, j+1) and a chunk of planes; per
+//     plane the rows' values are staged in shared memory (scaled by 1/dx,
+//     with periodic copies at the row ends) and the x slots exchanged there;
+//     writes out = mu + A_x (+ P, Q terms).  No state is carried between
+//     planes, so the kernel needs few registers and no warm-up planes.
+//   k_adj_march_x2<AX>: a thread owns two lines along y (AX = 1, the lines
+//     at z = k, k+1) or z (AX = 2, at y = j, j+1) and marches them with a
+//     register window and a face-sum ring; adds A_AX to out.
 // The slot evaluation (lin_slots_x2) is the FP32 epsilon-scaled WENO5
 // derivative of lin_slots_f32 written for packed lanes: per lane only the
 // stencil orientation, the epsilon maximum and its argument are selected.
@@ -43,13 +43,21 @@ using fused::sub2;
 // with s = 1 / (4 eps); the adjoint weight yb is folded in before the
 // indicator derivatives (bh_k = yb beta_k / 2).  eps = 1e-6 max v^2 + 1e-36;
 // its derivative goes to the last index of the maximum, as in the FP64 form.
+// ORIENT: 0 = per lane (mx, my), 1 = both lanes minus, 2 = both lanes plus.
+template <int ORIENT>
 __device__ __forceinline__ float2 lin_slots_x2(const float2 D[6], float2 yb, bool mx, bool my, float2 G[6]) {
   const float c13 = 1.f / 3.f, c76 = 7.f / 6.f, c116 = 11.f / 6.f, c16 = 1.f / 6.f, c56 = 5.f / 6.f;
   const float c133 = 13.f / 3.f;
+  // the minus-side value a or the plus-side value b of each lane
+  auto pick = [&](float2 a, float2 b) {
+    if constexpr (ORIENT == 1) return a;
+    else if constexpr (ORIENT == 2) return b;
+    else return make_float2(mx ? a.x : b.x, my ? a.y : b.y);
+  };
   float2 v[5], sq[5];
 #pragma unroll
   for (int q = 0; q < 5; q++) {
-    v[q] = make_float2(mx ? D[q].x : D[5 - q].x, my ? D[q].y : D[5 - q].y);
+    v[q] = pick(D[q], D[5 - q]);
     sq[q] = mul2(v[q], v[q]);
   }
   const float2 m = make_float2(max3f(max3f(sq[0].x, sq[1].x, sq[2].x), sq[3].x, sq[4].x),
@@ -111,9 +119,19 @@ __device__ __forceinline__ float2 lin_slots_x2(const float2 D[6], float2 yb, boo
 #pragma unroll
   for (int k = 0; k < 6; k++) {
     const float2 lo = k < 5 ? g[k] : sp(0.f), hi = k > 0 ? g[5 - k] : sp(0.f);
-    G[k] = make_float2(mx ? lo.x : hi.x, my ? lo.y : hi.y);
+    G[k] = pick(lo, hi);
   }
   return W;
+}
+
+// lin_slots_x2 with the orientation resolved per warp where all its lanes
+// take the same side (the common case: the upwind side follows the sign of a
+// smooth coefficient field), per lane otherwise
+__device__ __forceinline__ float2 lin_slots_x2_any(const float2 D[6], float2 yb, bool mx, bool my, float2 G[6]) {
+  const unsigned act = __activemask();
+  if (!__any_sync(act, !(mx && my))) return lin_slots_x2<1>(D, yb, mx, my, G);
+  if (!__any_sync(act, mx || my)) return lin_slots_x2<2>(D, yb, mx, my, G);
+  return lin_slots_x2<0>(D, yb, mx, my, G);
 }
 
 // Coefficients of one cell on two lines along axis d: the adjoint weight
@@ -141,20 +159,26 @@ __device__ __forceinline__ Coef2<MODE> load_coef2(const AdjStageArgs<float> &a, 
 
 // Slots of the cells of two lines along axis d; returns the velocity adjoint
 // dt mu (-W) of each (advection; zero where the term is off).
-template <int MODE>
+// WARP_SIDES: resolve the stencil side per warp where possible
+// (lin_slots_x2_any); otherwise per lane
+template <int MODE, bool WARP_SIDES>
 __device__ __forceinline__ float2 coef_slots_x2(const float2 D[6], const Coef2<MODE> &cf, int d, float2 mu,
                                                 float2 dt_inv, float dt, float2 G[6]) {
+  auto slots = [&](float2 yb, bool mx, bool my) {
+    if constexpr (WARP_SIDES) return lin_slots_x2_any(D, yb, mx, my, G);
+    else return lin_slots_x2<0>(D, yb, mx, my, G);
+  };
   if constexpr (MODE == ADJ_ADV) {
     const bool onx = !(fabsf(cf.k.x) < 1e-11f), ony = !(fabsf(cf.k.y) < 1e-11f);
     const float2 kap = make_float2(onx ? -cf.k.x : 0.f, ony ? -cf.k.y : 0.f);
     const float2 yb = mul2(mul2(dt_inv, mu), kap);
-    const float2 W = lin_slots_x2(D, yb, cf.k.x > 0.f, cf.k.y > 0.f, G);
+    const float2 W = slots(yb, cf.k.x > 0.f, cf.k.y > 0.f);
     const float2 gv = mul2(mul2(sp(-dt), mu), W);
     return make_float2(onx ? gv.x : 0.f, ony ? gv.y : 0.f);
   } else {
     const unsigned bx = (cf.sx >> (2 * d)) & 3u, by = (cf.sy >> (2 * d)) & 3u;
     const float2 kap = make_float2(bx ? cf.k.x : 0.f, by ? cf.k.y : 0.f);
-    lin_slots_x2(D, mul2(mul2(dt_inv, mu), kap), bx == 2u, by == 2u, G);
+    slots(mul2(mul2(dt_inv, mu), kap), bx == 2u, by == 2u);
     return sp(0.f);
   }
 }
@@ -193,181 +217,156 @@ __device__ __forceinline__ Cursor cursor_next(Cursor c, int n, unsigned pitch) {
   return c;
 }
 
-// shared memory of k_adj_xz_x2: an 8-plane ring of both rows' s / dx and two
-// buffers of the six x slots, each row of nx + 6 float2 (3 periodic copies
-// per end)
-__host__ __device__ constexpr size_t adj_xz_x2_smem(int nx) { return (size_t)(8 + 2 * 6) * (nx + 6) * sizeof(float2); }
-
-// register cap of k_adj_xz_x2: 112 per thread keeps three 192-thread CTAs
-// (a 192-cell row) resident per SM without spills
-#ifndef LSMGPU_ADJ_XZ_X2_NREG
-#define LSMGPU_ADJ_XZ_X2_NREG 112
+// shared memory of k_adj_x_x2: two buffers of both rows' s / dx and two of
+// the six x slots, each row of nx + 6 float2 (3 periodic copies per end)
+__host__ __device__ constexpr size_t adj_x_x2_smem(int nx) { return (size_t)(2 + 2 * 6) * (nx + 6) * sizeof(float2); }
+#ifndef LSMGPU_ADJ_X_X2_NREG
+#define LSMGPU_ADJ_X_X2_NREG 80
 #endif
-#define LSMGPU_ADJ_XZ_X2_BOUNDS __maxnreg__(LSMGPU_ADJ_XZ_X2_NREG)
 
+// x faces of a chunk of planes of two x rows (j, j+1): per plane each thread
+// stages its column value (times 1/dx) with periodic copies at the row ends,
+// evaluates its cell's x slots from the staged row and exchanges them; one
+// barrier per plane (the staging of plane k+1 and the slots of plane k share
+// it).  Writes out = mu + A_x (+ P, Q terms).
 template <int MODE>
-__global__ void LSMGPU_ADJ_XZ_X2_BOUNDS k_adj_xz_x2(AdjStageArgs<float> a) {
-  extern __shared__ __align__(16) unsigned char xz2_smem[];
+__global__ void __maxnreg__(LSMGPU_ADJ_X_X2_NREG) k_adj_x_x2(AdjStageArgs<float> a) {
+  extern __shared__ __align__(16) unsigned char x2_smem[];
   const Layout &L = a.L;
   const int nx = L.nx, nz = L.nz;
   const int hp = nx + 6;
-  float2 *ring = reinterpret_cast<float2 *>(xz2_smem);  // [8][hp]
-  float2 *gbuf = ring + 8 * hp;                        // [2][6][hp]
+  float2 *sbuf = reinterpret_cast<float2 *>(x2_smem);  // [2][hp]
+  float2 *gbuf = sbuf + 2 * hp;                        // [2][6][hp]
   const int x = threadIdx.y * 32 + threadIdx.x;
   const bool own = x < nx;
   const int xc = own ? x : nx - 1;  // idle lanes shadow the last cell
   const int j0 = 2 * blockIdx.x;
   const int j1 = j0 + 1 < L.ny ? j0 + 1 : j0;  // odd ny: the last CTA's second row repeats the first
   const bool two = j1 != j0;
-  const int z0 = blockIdx.y * a.zchunk;
-  const int zend = min(z0 + a.zchunk, nz);
+  const int z0 = blockIdx.y * a.xchunk;
+  if (z0 >= nz) return;  // whole CTA, before any barrier
+  const int zend = min(z0 + a.xchunk, nz);
   const float dt = a.dt;
-  const float2 msc = sp(a.mscale), ix = sp(a.inv[0]), iz = sp(a.inv[2]);
-  const float2 dtix = sp(a.dt * a.inv[0]), dtiz = sp(a.dt * a.inv[2]);
+  const float2 msc = sp(a.mscale), ix = sp(a.inv[0]), dtix = sp(a.dt * a.inv[0]);
   const unsigned pz = (unsigned)L.pz;
   const unsigned col0 = (unsigned)(fused::GX + xc) + (unsigned)L.py * (unsigned)(j0 + fused::GY);
   const unsigned col1 = (unsigned)(fused::GX + xc) + (unsigned)L.py * (unsigned)(j1 + fused::GY);
-  // shared-memory positions this thread writes: its cell and a periodic copy
   const int p_main = xc + 3;
   const int p_copy = xc < 3 ? nx + 3 + xc : (xc >= nx - 3 ? xc - (nx - 3) : -1);
-  const bool wr = own;
   auto ld2 = [&](const float *p, unsigned o) { return make_float2(p[col0 + o], p[col1 + o]); };
-
-  float2 dw[6], mring[4], F[6], last, prevV = sp(0.f);
-  {
-    float2 w[6];
-#pragma unroll
-    for (int q = 0; q < 6; q++) {
-      w[q] = ld2(a.s, cursor_at(z0 - 6 + q, nz, pz, fused::GZ).off);
-      F[q] = sp(0.f);
+  auto stage_s = [&](float2 *row, float2 v) {
+    if (own) {
+      const float2 sv = mul2(v, ix);
+      row[p_main] = sv;
+      if (p_copy >= 0) row[p_copy] = sv;
     }
-    dw[0] = sp(0.f);
-#pragma unroll
-    for (int f = 0; f < 5; f++) dw[f + 1] = mul2(sub2(w[f + 1], w[f]), iz);
-    last = w[5];
-  }
-#pragma unroll
-  for (int q = 0; q < 4; q++) mring[q] = sp(0.f);
-  // cursors: plane kk of the march, its lead plane kk + 4, the output plane kk - 3
-  Cursor ck = cursor_at(z0 - 3, nz, pz, fused::GZ);
-  Cursor cl = cursor_at(z0 + 1, nz, pz, fused::GZ);
-  Cursor co = cursor_at(z0, nz, pz, fused::GZ);
-  float2 cs = ld2(a.s, co.off);  // plane z0 = kk + 3 of the first step
-  float2 cm = ld2(a.M, ck.off);
-  Coef2<MODE> cv = load_coef2<MODE>(a, 2, col0 + ck.off, col1 + ck.off);
-  // x coefficient of the next output plane, loaded one plane ahead
-  Coef2<MODE> cx = load_coef2<MODE>(a, 0, col0 + co.off, col1 + co.off);
-  int b = 0;
-  for (int kk = z0 - 3; kk < zend + 3; kk++) {
-    const int k = kk - 3;
-    const bool xs = k >= z0;  // an output plane (uniform over the CTA)
-    const unsigned ok = co.off;
-    // the x accumulator and the P / Q terms of plane k are loaded before the
-    // z slot evaluation, which hides their latency
-    const bool gxw = MODE == ADJ_ADV && a.gvel[0] && own && xs;
+  };
+
+  unsigned ok = pz * (unsigned)(z0 + fused::GZ);
+  stage_s(sbuf, ld2(a.s, ok));
+  // the next plane's values are loaded one plane ahead
+  float2 sn = sp(0.f), mn = ld2(a.M, ok);
+  Coef2<MODE> cn = load_coef2<MODE>(a, 0, col0 + ok, col1 + ok);
+  if (z0 + 1 < zend) sn = ld2(a.s, ok + pz);
+  __syncthreads();
+  for (int k = z0; k < zend; k++) {
+    const int b = k & 1;
+    const float2 mu = mul2(msc, mn);
+    const Coef2<MODE> ux = cn;
+    const float2 s_next = sn;
+    const unsigned okn = ok + pz;
+    const bool more = k + 1 < zend;
+    if (more) {
+      mn = ld2(a.M, okn);
+      cn = load_coef2<MODE>(a, 0, col0 + okn, col1 + okn);
+      if (k + 2 < zend) sn = ld2(a.s, okn + pz);
+    }
+    const bool gxw = MODE == ADJ_ADV && a.gvel[0] && own;
     float2 gx_old = sp(0.f), pq = sp(0.f);
     if (gxw) gx_old = ld2(a.gvel[0], ok);
-    if (own && xs) {
+    if (own) {
       if (a.P) pq = mul2(sp(a.pscale), ld2(a.P, ok));
       if (a.Q) pq = fma2(sp(a.qscale), ld2(a.Q, ok), pq);
     }
-    // plane kk + 3 of both rows, scaled by 1/dx, for the x stencils of plane kk + 3
-    if (wr && kk + 3 < zend) {
-      const float2 sv = mul2(cs, ix);
-      float2 *rp = ring + ((kk + 3) & 7) * hp;
-      rp[p_main] = sv;
-      if (p_copy >= 0) rp[p_copy] = sv;
-    }
-#pragma unroll
-    for (int f = 0; f < 5; f++) dw[f] = dw[f + 1];
-    dw[5] = mul2(sub2(cs, last), iz);
-    last = cs;
-#pragma unroll
-    for (int q = 0; q < 3; q++) mring[q] = mring[q + 1];
-    mring[3] = mul2(msc, cm);
-    const Coef2<MODE> uz = cv;
-    const unsigned okk = ck.off;
-    ck = cursor_next(ck, nz, pz);
-    if (kk + 1 < zend + 3) {
-      cs = ld2(a.s, cl.off);
-      cm = ld2(a.M, ck.off);
-      cv = load_coef2<MODE>(a, 2, col0 + ck.off, col1 + ck.off);
-    }
-    cl = cursor_next(cl, nz, pz);
-    const bool gzw = MODE == ADJ_ADV && a.gvel[2] && own && kk >= z0 && kk < zend;
-    float2 gz_old = sp(0.f);
-    if (gzw) gz_old = ld2(a.gvel[2], okk);
-    float2 G[6];
-    const float2 gz = coef_slots_x2<MODE>(dw, uz, 2, mring[3], dtiz, dt, G);
-    if (gzw) {
-      a.gvel[2][col0 + okk] = gz_old.x + gz.x;
-      if (two) a.gvel[2][col1 + okk] = gz_old.y + gz.y;
-    }
-    const float2 Az = ring_step2(F, prevV, G);
-    if (!xs) continue;
-    if (k == z0) __syncthreads();  // the ring's first planes were written without a barrier since
-
-    // x slots of plane k from the ring
-    const float2 *rw = ring + (k & 7) * hp + xc;
     float2 D[6];
     {
+      const float2 *rw = sbuf + b * hp + xc;
       float2 w7[7];
 #pragma unroll
       for (int q = 0; q < 7; q++) w7[q] = rw[q];
 #pragma unroll
       for (int f = 0; f < 6; f++) D[f] = sub2(w7[f + 1], w7[f]);
     }
-    const Coef2<MODE> ux = cx;
-    co = cursor_next(co, nz, pz);
-    if (k + 1 < zend) cx = load_coef2<MODE>(a, 0, col0 + co.off, col1 + co.off);
-    const float2 gx = coef_slots_x2<MODE>(D, ux, 0, mring[0], dtix, dt, G);
+    float2 G[6];
+    const float2 gx = coef_slots_x2<MODE, true>(D, ux, 0, mu, dtix, dt, G);
     if (gxw) {
       a.gvel[0][col0 + ok] = gx_old.x + gx.x;
       if (two) a.gvel[0][col1 + ok] = gx_old.y + gx.y;
     }
     float2 *bb = gbuf + b * 6 * hp;
-    if (wr) {
+    if (own) {
 #pragma unroll
       for (int m = 0; m < 6; m++) {
         bb[m * hp + p_main] = G[m];
         if (p_copy >= 0) bb[m * hp + p_copy] = G[m];
       }
     }
+    if (more) stage_s(sbuf + (b ^ 1) * hp, s_next);
     __syncthreads();
     // A(x) = Vbar(x) - Vbar(x+1) = sum_m G_m(x + 2 - m) - G_m(x + 3 - m)
     float2 Ax = sp(0.f);
 #pragma unroll
     for (int m = 0; m < 6; m++) Ax = add2(Ax, sub2(bb[m * hp + xc + 5 - m], bb[m * hp + xc + 6 - m]));
-    b ^= 1;
-    if (!own) continue;
-    const float2 o = add2(add2(mring[0], add2(Ax, Az)), pq);
-    a.out[col0 + ok] = o.x;
-    if (two) a.out[col1 + ok] = o.y;
+    if (own) {
+      const float2 o = add2(add2(mu, Ax), pq);
+      a.out[col0 + ok] = o.x;
+      if (two) a.out[col1 + ok] = o.y;
+    }
+    ok = okn;
   }
 }
 
-// CTAs of 32 x kYRows threads (column pairs), kYCtas resident per SM
-constexpr int kYRows = 4;
-#ifndef LSMGPU_ADJ_Y_X2_CTAS
-#define LSMGPU_ADJ_Y_X2_CTAS 5
+// CTAs of 32 x kMarchRows threads (line pairs), LSMGPU_ADJ_MARCH_X2_CTAS
+// resident per SM
+constexpr int kMarchRows = 4;
+#ifndef LSMGPU_ADJ_MARCH_X2_CTAS
+#define LSMGPU_ADJ_MARCH_X2_CTAS 4
+#endif
+// per-warp stencil sides in the march kernels (with per-lane sides only, the
+// kernels fit 96 registers, five CTAs per SM; measured at 192^3, the per-warp
+// sides at four CTAs are faster)
+#ifndef LSMGPU_ADJ_MARCH_WARP_SIDES
+#define LSMGPU_ADJ_MARCH_WARP_SIDES 1
+#endif
+// lead values and coefficients loaded this many cells ahead (1 or 2)
+#ifndef LSMGPU_ADJ_MARCH_PREFETCH
+#define LSMGPU_ADJ_MARCH_PREFETCH 1
 #endif
 
-template <int MODE>
-__global__ void __launch_bounds__(32 * kYRows, LSMGPU_ADJ_Y_X2_CTAS) k_adj_y_x2(AdjStageArgs<float> a) {
+// Faces along axis AX (1: y, 2: z) of a chunk of the march: a thread owns two
+// lines along AX at (i, the pair 2p, 2p+1 of the remaining axis) and marches
+// them with the window / face-ring scheme of k_adj_y; adds dt A_AX to out.
+template <int MODE, int AX>
+__global__ void __launch_bounds__(32 * kMarchRows, LSMGPU_ADJ_MARCH_X2_CTAS) k_adj_march_x2(AdjStageArgs<float> a) {
+  static_assert(AX == 1 || AX == 2, "march along y or z");
   const Layout &L = a.L;
   const int i = blockIdx.x * 32 + threadIdx.x;
-  const int k0 = 2 * (blockIdx.y * kYRows + threadIdx.y);
-  if (i >= L.nx || k0 >= L.nz) return;
-  const int k1 = k0 + 1 < L.nz ? k0 + 1 : k0;  // odd nz: the last pair's second column repeats the first
-  const bool two = k1 != k0;
-  const int y0 = blockIdx.z * a.ychunk;
-  const int yend = min(y0 + a.ychunk, L.ny);
-  const int ny = L.ny;
+  const int n_pair = AX == 1 ? L.nz : L.ny;  // the axis the pairs run along
+  const int q0 = 2 * (blockIdx.y * kMarchRows + threadIdx.y);
+  if (i >= L.nx || q0 >= n_pair) return;
+  const int q1 = q0 + 1 < n_pair ? q0 + 1 : q0;  // odd count: the last pair's second line repeats the first
+  const bool two = q1 != q0;
+  const int n = AX == 1 ? L.ny : L.nz;         // march length
+  const int g = AX == 1 ? fused::GY : fused::GZ;
+  const unsigned pm = (unsigned)(AX == 1 ? L.py : L.pz);       // march pitch
+  const unsigned pq_ = (unsigned)(AX == 1 ? L.pz : L.py);      // pair pitch
+  const int gq = AX == 1 ? fused::GZ : fused::GY;
+  const int y0 = blockIdx.z * (AX == 1 ? a.ychunk : a.zchunk);
+  const int yend = min(y0 + (AX == 1 ? a.ychunk : a.zchunk), n);
   const float dt = a.dt;
-  const float2 msc = sp(a.mscale), iy = sp(a.inv[1]), dtiy = sp(a.dt * a.inv[1]);
-  const unsigned py = (unsigned)L.py;
-  const unsigned b0 = (unsigned)(i + fused::GX) + (unsigned)L.pz * (unsigned)(k0 + fused::GZ);
-  const unsigned b1 = (unsigned)(i + fused::GX) + (unsigned)L.pz * (unsigned)(k1 + fused::GZ);
+  const float2 msc = sp(a.mscale), iy = sp(a.inv[AX]), dtiy = sp(a.dt * a.inv[AX]);
+  const unsigned b0 = (unsigned)(i + fused::GX) + pq_ * (unsigned)(q0 + gq);
+  const unsigned b1 = (unsigned)(i + fused::GX) + pq_ * (unsigned)(q1 + gq);
   auto ld2 = [&](const float *p, unsigned o) { return make_float2(p[b0 + o], p[b1 + o]); };
 
   float2 dw[6], mring[4], F[6], last, prevV = sp(0.f);
@@ -375,7 +374,7 @@ __global__ void __launch_bounds__(32 * kYRows, LSMGPU_ADJ_Y_X2_CTAS) k_adj_y_x2(
     float2 w[6];
 #pragma unroll
     for (int q = 0; q < 6; q++) {
-      w[q] = ld2(a.s, cursor_at(y0 - 6 + q, ny, py, fused::GY).off);
+      w[q] = ld2(a.s, cursor_at(y0 - 6 + q, n, pm, g).off);
       F[q] = sp(0.f);
     }
     dw[0] = sp(0.f);
@@ -385,44 +384,65 @@ __global__ void __launch_bounds__(32 * kYRows, LSMGPU_ADJ_Y_X2_CTAS) k_adj_y_x2(
   }
 #pragma unroll
   for (int q = 0; q < 4; q++) mring[q] = sp(0.f);
-  // cursors: row jj of the march, its lead row jj + 4, the output row jj - 3
-  Cursor cj = cursor_at(y0 - 3, ny, py, fused::GY);
-  Cursor cl = cursor_at(y0 + 1, ny, py, fused::GY);
-  Cursor co = cursor_at(y0, ny, py, fused::GY);
-  float2 cs = ld2(a.s, co.off);  // row y0 = jj + 3 of the first step
-  float2 cm = ld2(a.M, cj.off);
-  Coef2<MODE> cv = load_coef2<MODE>(a, 1, b0 + cj.off, b1 + cj.off);
+  // cursors: cell jj of the march, the cell jj + P whose values are loaded
+  // (P = LSMGPU_ADJ_MARCH_PREFETCH cells ahead) and its lead cell jj + P + 3,
+  // the output cell jj - 3
+  constexpr int P = LSMGPU_ADJ_MARCH_PREFETCH;
+  static_assert(P == 1 || P == 2, "prefetch distance 1 or 2");
+  Cursor cj = cursor_at(y0 - 3, n, pm, g);
+  Cursor cp = cursor_at(y0 - 3 + P, n, pm, g);
+  Cursor cl = cursor_at(y0 + P, n, pm, g);
+  Cursor co = cursor_at(y0, n, pm, g);
+  // [0]: the values of the next step, [1]: of the step after (P = 2)
+  float2 cs[P], cm[P];
+  Coef2<MODE> cv[P];
+  cs[0] = ld2(a.s, co.off);  // cell y0 = jj + 3 of the first step
+  cm[0] = ld2(a.M, cj.off);
+  cv[0] = load_coef2<MODE>(a, AX, b0 + cj.off, b1 + cj.off);
+  if constexpr (P == 2) {
+    const unsigned o1 = cursor_next(cj, n, pm).off;
+    cs[1] = ld2(a.s, cursor_next(co, n, pm).off);
+    cm[1] = ld2(a.M, o1);
+    cv[1] = load_coef2<MODE>(a, AX, b0 + o1, b1 + o1);
+  }
   for (int jj = y0 - 3; jj < yend + 3; jj++) {
 #pragma unroll
     for (int f = 0; f < 5; f++) dw[f] = dw[f + 1];
-    dw[5] = mul2(sub2(cs, last), iy);
-    last = cs;
+    dw[5] = mul2(sub2(cs[0], last), iy);
+    last = cs[0];
 #pragma unroll
     for (int q = 0; q < 3; q++) mring[q] = mring[q + 1];
-    mring[3] = mul2(msc, cm);
-    const Coef2<MODE> uy = cv;
+    mring[3] = mul2(msc, cm[0]);
+    const Coef2<MODE> uy = cv[0];
     const unsigned ojj = cj.off;
-    cj = cursor_next(cj, ny, py);
-    if (jj + 1 < yend + 3) {
-      cs = ld2(a.s, cl.off);
-      cm = ld2(a.M, cj.off);
-      cv = load_coef2<MODE>(a, 1, b0 + cj.off, b1 + cj.off);
+    cj = cursor_next(cj, n, pm);
+#pragma unroll
+    for (int q = 0; q + 1 < P; q++) {
+      cs[q] = cs[q + 1];
+      cm[q] = cm[q + 1];
+      cv[q] = cv[q + 1];
     }
-    cl = cursor_next(cl, ny, py);
+    if (jj + P < yend + 3) {
+      cs[P - 1] = ld2(a.s, cl.off);
+      cm[P - 1] = ld2(a.M, cp.off);
+      cv[P - 1] = load_coef2<MODE>(a, AX, b0 + cp.off, b1 + cp.off);
+    }
+    cp = cursor_next(cp, n, pm);
+    cl = cursor_next(cl, n, pm);
     // the accumulators' old values are loaded before the slot evaluation so
     // their latency overlaps it (out, gvel and the state arrays are distinct)
-    const bool gw = MODE == ADJ_ADV && a.gvel[1] && jj >= y0 && jj < yend;
+    const bool gw = MODE == ADJ_ADV && a.gvel[AX] && jj >= y0 && jj < yend;
     const bool ow = jj - 3 >= y0;
     const unsigned otg = co.off;
-    if (ow) co = cursor_next(co, ny, py);
+    if (ow) co = cursor_next(co, n, pm);
     float2 g_old = sp(0.f), o_old = sp(0.f);
-    if (gw) g_old = ld2(a.gvel[1], ojj);
+    if (gw) g_old = ld2(a.gvel[AX], ojj);
     if (ow) o_old = ld2(a.out, otg);
     float2 G[6];
-    const float2 gy = coef_slots_x2<MODE>(dw, uy, 1, mring[3], dtiy, dt, G);
+    const float2 gy = coef_slots_x2<MODE, LSMGPU_ADJ_MARCH_WARP_SIDES != 0>(dw, uy, AX, mring[3], dtiy, dt, G);
     if (gw) {
-      a.gvel[1][b0 + ojj] = g_old.x + gy.x;
-      if (two) a.gvel[1][b1 + ojj] = g_old.y + gy.y;
+      a.gvel[AX][b0 + ojj] = g_old.x + gy.x;
+      if (two) a.gvel[AX][b1 + ojj] = g_old.y + gy.y;
     }
     const float2 Ay = ring_step2(F, prevV, G);
     if (!ow) continue;

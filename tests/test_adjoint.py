@@ -200,8 +200,12 @@ def test_adjoint_checkpoint_spacing_changes_nothing(precision, gpu_lib):
 
 
 @pytest.mark.gpu
-def test_adjoint_f32_against_fp64_oracle(gpu_lib):
-    dims = (24, 20, 18)
+@pytest.mark.parametrize("dims", [(24, 20, 18), (37, 19, 21), (33, 7, 13), (264, 7, 9)])
+def test_adjoint_f32_against_fp64_oracle(dims, gpu_lib):
+    """Odd ny / nz: the last line pair of the two-line FP32 kernels has one
+    line; nx not a multiple of 32: idle lanes; nz not a multiple of the x
+    kernel's 8-plane chunks; nx = 264: rows longer than one CTA takes (the
+    scalar kernels)."""
     phi, vel, tgt, sp, dt = adjoint_case(dims)
     eps = 1.5 * sp[0]
     Jw, _, gw, gvw = oracle_adjoint(phi, vel, tgt, sp, dt, 6, eps)
@@ -443,8 +447,8 @@ def test_reinit_vjp_f64_matches_oracle(dims, steps, ckpt, gpu_lib):
 
 
 @pytest.mark.gpu
-def test_reinit_vjp_f32_against_fp64_oracle(gpu_lib):
-    dims = (24, 20, 18)
+@pytest.mark.parametrize("dims", [(24, 20, 18), (35, 17, 11)])
+def test_reinit_vjp_f32_against_fp64_oracle(dims, gpu_lib):
     phi, sp, dtau = reinit_case(dims)
     rng = np.random.default_rng(22)
     gout = np.asfortranarray(rng.standard_normal(dims))
