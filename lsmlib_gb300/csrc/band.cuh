@@ -80,11 +80,7 @@ __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_count(F f, long long n, int
     for (int q = 0; q < SCAN_ITEMS; q++) {
       const long long e = base + 32LL * q;
       const int b = (e < n) ? f.flags(e) : 0;
-      const unsigned m0 = __ballot_sync(0xffffffffu, b & 1);
-      // the round's 32 elements are consecutive: its ballot is their bit mask
-      if constexpr (F::kStoreBallots)
-        if (lane == 0 && e - lane < n) f.store_ballot((e - lane) >> 5, m0);
-      c0 += __popc(m0);
+      c0 += __popc(__ballot_sync(0xffffffffu, b & 1));
       c1 += __popc(__ballot_sync(0xffffffffu, b & 2));
       c2 += __popc(__ballot_sync(0xffffffffu, b & 4));
     }
@@ -288,8 +284,6 @@ struct Level0T {
   // leaves the final marks (1 in level 0, 0 elsewhere)
   U8 *mark_lin = nullptr;
   static constexpr bool kPrefetch = true;
-  static constexpr bool kStoreBallots = false;
-  __device__ void store_ballot(long long, unsigned) const {}
   __device__ void counted(long long e, int bits) const {
     if (mark_lin) mark_lin[e] = (U8)bits;
   }
@@ -354,16 +348,42 @@ struct Level0Marks {
   Level0T<T> z;
   U8 *marks;
   static constexpr bool kPrefetch = true;
-  static constexpr bool kStoreBallots = false;
   typedef U8 V;
   __device__ U8 load(long long e) const { return marks[e]; }
   __device__ int classify(U8 raw, long long) const { return raw; }
   __device__ int flags(long long e) const { return marks[e]; }
   __device__ void counted(long long, int) const {}
-  __device__ void store_ballot(long long, unsigned) const {}
   __device__ void emit(long long e, int bits, long long r0, long long r1, long long r2) const {
     z.emit(e, bits, r0, r1, r2);
     marks[e] = 1;
+  }
+};
+
+// Level-0 pass of a rebuild inside the narrow-band flow over the previous
+// level-0 list (ox, oy, oz) instead of the grid: between rebuilds the flow
+// writes phi only at level-0 cells, so a cell outside the previous level 0
+// still has |phi| >= width and the new level 0 (and its outer layer) is the
+// ordered sub-sequence of the previous level-0 list whose cells pass the test
+// (the previous list is in the reference's sweep order).  The caller clears
+// the previous band's marks first; each listed cell gets mark 1.
+template <class T>
+struct Level0List {
+  Level0T<T> z;
+  const int *ox, *oy, *oz;
+  static constexpr bool kPrefetch = true;
+  typedef T V;
+  __device__ T load(long long e) const { return z.phi.p[z.phi.off(ox[e], oy[e], oz[e])]; }
+  __device__ int classify(T raw, long long) const { return z.classify(raw, 0); }
+  __device__ int flags(long long e) const { return classify(load(e), e); }
+  __device__ void counted(long long, int) const {}
+  __device__ void emit(long long e, int bits, long long r0, long long r1, long long r2) const {
+    const int i = ox[e], j = oy[e], k = oz[e];
+    z.ix[r0] = i;
+    z.iy[r0] = j;
+    z.iz[r0] = k;
+    if (bits & 2) z.outer[r1] = z.nlo + (int)r0;
+    if (bits & 4) z.outer[(z.nhi_outer - z.nlo_outer) - r2] = z.nlo + (int)r0;
+    z.nb(i, j, k) = 1;
   }
 };
 
@@ -398,78 +418,135 @@ struct Bfs {
   int plo;                // first parent entry of this level
   int count0;             // first free entry
   U8 mark;
-  __device__ bool nbr(long long t, int &a, int &b, int &c) const {
-    const long long m = plo + t / 6;
-    const int q = (int)(t % 6);
-    const long long e = m - nlo;
-    a = ix[e]; b = iy[e]; c = iz[e];
-    switch (q) {
-      case 0: if (!(a < nbb.hi[0])) return false; a += 1; break;
-      case 1: if (!(a > nbb.lo[0])) return false; a -= 1; break;
-      case 2: if (!(b < nbb.hi[1])) return false; b += 1; break;
-      case 3: if (!(b > nbb.lo[1])) return false; b -= 1; break;
-      case 4: if (!(c < nbb.hi[2])) return false; c += 1; break;
-      default: if (!(c > nbb.lo[2])) return false; c -= 1; break;
-    }
-    return true;
-  }
   __device__ long long cidx(int a, int b, int c) const { return nb.off(a, b, c); }
-  static constexpr bool kPrefetch = false;  // dependent gathers; the one-pass form keeps registers low
-  // the count pass stores each round's winner ballot (one bit per candidate)
-  // when `wbits` is set, for BfsWinners' emit pass
-  static constexpr bool kStoreBallots = true;
-  unsigned *wbits = nullptr;
-  __device__ void store_ballot(long long word, unsigned mask) const {
-    if (wbits) wbits[word] = mask;
-  }
-  typedef int V;
-  __device__ int load(long long) const { return 0; }
-  __device__ int classify(int, long long t) const { return flags(t); }
-  __device__ void counted(long long, int) const {}
-  __device__ int flags(long long t) const {
-    int a, b, c;
-    if (!nbr(t, a, b, c)) return 0;
-    const long long o = cidx(a, b, c);
-    return (nb.p[o] == 0 && claim[o] == (int)t) ? 1 : 0;
-  }
-  // lists the winner, marks its cell with the level and releases the claim
-  // (a cell has exactly one winner, so only this call changes that cell)
-  __device__ void emit(long long t, int, long long r0, long long, long long) const {
-    int a, b, c;
-    nbr(t, a, b, c);
-    const long long pos = (long long)count0 - nlo + r0;
-    ix[pos] = a;
-    iy[pos] = b;
-    iz[pos] = c;
-    const long long o = cidx(a, b, c);
-    nb.p[o] = mark;
-    claim[o] = kUnclaimed;
-  }
 };
 
-// emit pass of a breadth-first level from the winner bits of its count pass:
-// only winners gather their parent and touch the grid
-struct BfsWinners {
-  Bfs f;
-  const unsigned *wbits;
-  static constexpr bool kPrefetch = false;
-  static constexpr bool kStoreBallots = false;
-  typedef int V;
-  __device__ int load(long long) const { return 0; }
-  __device__ int classify(int, long long t) const { return flags(t); }
-  __device__ void counted(long long, int) const {}
-  __device__ void store_ballot(long long, unsigned) const {}
-  __device__ int flags(long long t) const { return (int)((wbits[t >> 5] >> (t & 31)) & 1u); }
-  __device__ void emit(long long t, int b, long long r0, long long r1, long long r2) const { f.emit(t, b, r0, r1, r2); }
-};
+// A level runs with one thread per parent and its six candidates
+// t = 6 p + d (parent p of the level, direction d): the claim (atomicMin of
+// t), then an ordered compaction of the winners in t order whose count pass
+// stores each parent's winner bits (one byte) and whose emit pass ranks a
+// parent's winners by a warp scan of the bit counts, lists them, marks their
+// cells with the level and releases the claims.
+constexpr int BFS_ITEMS = 8;                         // parents per thread
+constexpr long long BFS_TILE = (long long)SCAN_BLOCK * BFS_ITEMS;
 
-__global__ void k_bfs_claim(Bfs f, long long n) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  int a, b, c;
-  if (!f.nbr(t, a, b, c)) return;
-  const long long o = f.cidx(a, b, c);
-  if (f.nb.p[o] == 0) atomicMin(&f.claim[o], (int)t);
+__device__ __forceinline__ bool bfs_nbr6(const Bfs &f, int a, int b, int c, int d, int &x, int &y, int &z) {
+  x = a; y = b; z = c;
+  switch (d) {
+    case 0: if (!(a < f.nbb.hi[0])) return false; x = a + 1; break;
+    case 1: if (!(a > f.nbb.lo[0])) return false; x = a - 1; break;
+    case 2: if (!(b < f.nbb.hi[1])) return false; y = b + 1; break;
+    case 3: if (!(b > f.nbb.lo[1])) return false; y = b - 1; break;
+    case 4: if (!(c < f.nbb.hi[2])) return false; z = c + 1; break;
+    default: if (!(c > f.nbb.lo[2])) return false; z = c - 1; break;
+  }
+  return true;
+}
+
+__global__ void k_bfs_claim6(Bfs f, long long np) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const long long e = f.plo + p - f.nlo;
+  const int a = f.ix[e], b = f.iy[e], c = f.iz[e];
+#pragma unroll
+  for (int d = 0; d < 6; d++) {
+    int x, y, z;
+    if (!bfs_nbr6(f, a, b, c, d, x, y, z)) continue;
+    const long long o = f.cidx(x, y, z);
+    if (f.nb.p[o] == 0) atomicMin(&f.claim[o], (int)(6 * p + d));
+  }
+}
+
+// winner bits of parent p (bit d: candidate 6 p + d won its cell)
+__device__ __forceinline__ unsigned bfs_winners6(const Bfs &f, long long p) {
+  const long long e = f.plo + p - f.nlo;
+  const int a = f.ix[e], b = f.iy[e], c = f.iz[e];
+  unsigned m = 0;
+#pragma unroll
+  for (int d = 0; d < 6; d++) {
+    int x, y, z;
+    if (!bfs_nbr6(f, a, b, c, d, x, y, z)) continue;
+    const long long o = f.cidx(x, y, z);
+    if (f.nb.p[o] == 0 && f.claim[o] == (int)(6 * p + d)) m |= 1u << d;
+  }
+  return m;
+}
+
+__global__ void __launch_bounds__(SCAN_BLOCK) k_bfs_count6(Bfs f, long long np, int *counts, U8 *wm) {
+  __shared__ int s[SCAN_WARPS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long base = (long long)blockIdx.x * BFS_TILE + (long long)w * 32 * BFS_ITEMS + lane;
+  int cnt = 0;
+#pragma unroll
+  for (int q = 0; q < BFS_ITEMS; q++) {
+    const long long p = base + 32LL * q;
+    if (p < np) {
+      const unsigned m = bfs_winners6(f, p);
+      wm[p] = (U8)m;
+      cnt += __popc(m);
+    }
+  }
+  cnt = __reduce_add_sync(0xffffffffu, (unsigned)cnt);
+  if (lane == 0) s[w] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int u = 0; u < SCAN_WARPS; u++) t += s[u];
+    counts[3 * blockIdx.x] = t;
+    counts[3 * blockIdx.x + 1] = 0;
+    counts[3 * blockIdx.x + 2] = 0;
+  }
+}
+
+__global__ void __launch_bounds__(SCAN_BLOCK) k_bfs_emit6(Bfs f, long long np, const long long *offsets,
+                                                          const int *counts, const U8 *wm) {
+  if (counts[3 * blockIdx.x] == 0) return;
+  __shared__ int s[SCAN_WARPS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long base = (long long)blockIdx.x * BFS_TILE + (long long)w * 32 * BFS_ITEMS + lane;
+  unsigned m[BFS_ITEMS];
+  int cnt = 0;
+#pragma unroll
+  for (int q = 0; q < BFS_ITEMS; q++) {
+    const long long p = base + 32LL * q;
+    m[q] = p < np ? wm[p] : 0u;
+    cnt += __popc(m[q]);
+  }
+  cnt = __reduce_add_sync(0xffffffffu, (unsigned)cnt);
+  if (lane == 0) s[w] = cnt;
+  __syncthreads();
+  long long run = offsets[3 * blockIdx.x];
+  for (int u = 0; u < w; u++) run += s[u];
+#pragma unroll
+  for (int q = 0; q < BFS_ITEMS; q++) {
+    const int c = __popc(m[q]);
+    int incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (m[q]) {
+      const long long p = base + 32LL * q;
+      const long long e = f.plo + p - f.nlo;
+      const int a = f.ix[e], b = f.iy[e], cc = f.iz[e];
+      long long pos = (long long)f.count0 - f.nlo + run + incl - c;
+      for (int d = 0; d < 6; d++) {
+        if (!((m[q] >> d) & 1u)) continue;
+        int x, y, z;
+        bfs_nbr6(f, a, b, cc, d, x, y, z);
+        f.ix[pos] = x;
+        f.iy[pos] = y;
+        f.iz[pos] = z;
+        const long long o = f.cidx(x, y, z);
+        f.nb.p[o] = f.mark;
+        f.claim[o] = kUnclaimed;
+        pos++;
+      }
+    }
+    run += total;
+  }
 }
 
 // claim array over the nb box, every entry kUnclaimed; bfs_levels leaves it so
@@ -497,21 +574,27 @@ bool bfs_levels(Call &call, View<U8> nb, const Box &nbb, int *ix, int *iy, int *
         return false;
       }
       Bfs f{nb, nbb, claim, ix, iy, iz, nlo, lo[lv - 1], (int)count, (U8)(lv + 1)};
-      const long long n = 6 * np;
-      const unsigned g = (unsigned)((n + 255) / 256);
-      f.wbits = call.temp<unsigned>((n + SCAN_TILE - 1) / SCAN_TILE * (SCAN_TILE / 32));
+      // one thread per parent (its six candidates in t order)
+      const long long nbk = (np + BFS_TILE - 1) / BFS_TILE;
+      U8 *wm = call.temp<U8>(np);
+      int *counts = call.temp<int>(3 * nbk);
+      long long *offs = call.temp<long long>(3 * nbk), *totd = call.temp<long long>(3);
       if (!call.ok()) return false;
-      LSMGPU_LAUNCH(k_bfs_claim, g, 256, 0, f, n);
-      // the compaction writes list entries count .. count+added-1; the
-      // counts are checked against the capacity before anything is written
+      LSMGPU_LAUNCH(k_bfs_claim6, (unsigned)((np + 255) / 256), 256, 0, f, np);
+      LSMGPU_LAUNCH(k_bfs_count6, (unsigned)nbk, SCAN_BLOCK, 0, f, np, counts, wm);
+      LSMGPU_LAUNCH(k_scan_blocks, 1, 1024, 0, counts, (int)nbk, offs, totd);
+      // the emit writes list entries count .. count+added-1; the total is
+      // checked against the capacity before anything is written
       long long tot[3];
-      Compaction cw;
-      if (!cw.count(call, f, n, tot)) return false;
+      if (!cuda_ok(cudaMemcpyAsync(tot, totd, 3 * sizeof(long long), cudaMemcpyDeviceToHost, stream()),
+                   "cudaMemcpyAsync(totals)") ||
+          !cuda_ok(cudaStreamSynchronize(stream()), "cudaStreamSynchronize"))
+        return false;
       if (count + tot[0] - 1 > nhi) {
         set_error(LSMGPU_ERR_CAPACITY, "narrow band lists exceed nhi_index");
         return false;
       }
-      cw.emit(BfsWinners{f, f.wbits});
+      LSMGPU_LAUNCH(k_bfs_emit6, (unsigned)nbk, SCAN_BLOCK, 0, f, np, offs, counts, wm);
       added = tot[0];
     }
     if (added > 0) {
@@ -577,12 +660,20 @@ struct BandForm {
 // outer-list bounds {plus lo, plus hi, minus lo, minus hi}, *nwrite (when
 // set) the number of levels the reference writes.  Returns false after
 // recording an error (capacity or CUDA).
+// prev (optional, level-0 selection |phi| < width only): the previous
+// level-0 list {ox, oy, oz, count} of a rebuild inside the narrow-band flow
+// (Level0List); the caller has cleared that band's marks
+struct PrevLevel0 {
+  const int *ox = nullptr, *oy = nullptr, *oz = nullptr;
+  long long n = 0;
+};
+
 template <class T>
 bool band_build(Call &call, const T *phi, const Box &gb, U8 *nbd, const Box &nbb, int *ix, int *iy, int *iz,
                 int nlo, int nhi, int *outer, int nlo_outer, int nhi_outer, double width, double width_inner,
                 int level, std::vector<int> &lo, std::vector<int> &hi, int ob[4], long long *level0_count,
                 int *claim, bool fuse_marks = false, const BandForm<T> &form = BandForm<T>(),
-                int *nwrite = nullptr) {
+                int *nwrite = nullptr, const PrevLevel0 *prev = nullptr) {
   const long long cap = (long long)nhi - nlo + 1;
   const long long ocap = (long long)nhi_outer - nlo_outer + 1;
   Level0T<T> z;
@@ -607,16 +698,23 @@ bool band_build(Call &call, const T *phi, const Box &gb, U8 *nbd, const Box &nbb
   // marks are then written before the capacity check
   const bool fused = fuse_marks && nbb.lo[0] == gb.lo[0] && nbb.hi[0] == gb.hi[0] && nbb.lo[1] == gb.lo[1] &&
                      nbb.hi[1] == gb.hi[1] && nbb.lo[2] == gb.lo[2] && nbb.hi[2] == gb.hi[2];
-  if (fused) z.mark_lin = nbd;
+  const bool from_list = prev && prev->ox && form.l0_mode == 0;
+  if (fused && !from_list) z.mark_lin = nbd;
   Compaction c0;
-  if (!c0.count(call, z, n, tot)) return false;
+  if (from_list) {
+    if (!c0.count(call, Level0List<T>{z, prev->ox, prev->oy, prev->oz}, prev->n, tot)) return false;
+  } else if (!c0.count(call, z, n, tot)) {
+    return false;
+  }
   z.mark_lin = nullptr;
   if (tot[0] > cap || tot[1] + tot[2] > ocap) {
     set_error(LSMGPU_ERR_CAPACITY, "narrow band (%lld cells) or outer layer (%lld) exceeds the index arrays", tot[0],
               tot[1] + tot[2]);
     return false;
   }
-  if (fused) {
+  if (from_list) {
+    c0.emit(Level0List<T>{z, prev->ox, prev->oy, prev->oz});
+  } else if (fused) {
     c0.emit(Level0Marks<T>{z, nbd});
   } else {
     LSMGPU_LAUNCH(k_mark0<T>,

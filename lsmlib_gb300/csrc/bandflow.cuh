@@ -279,6 +279,21 @@ static __global__ void k_band_stage_x2(BandArgs<float> a) {
   if (two) a.out.p[o1] = rk_update<float>(a.stage, n1v, us1, dt, cutoff<float>(r.y, us1, a.beta, a.gamma));
 }
 
+// clears the marks of the listed cells (the previous band, before a rebuild)
+// and copies the level-0 entries (the first n0) to ox, oy, oz
+static __global__ void k_band_retire(U8 *nb, View<const U8> v, const int *ix, const int *iy, const int *iz, int n,
+                                     int n0, int *ox, int *oy, int *oz) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= n) return;
+  const int i = ix[l], j = iy[l], k = iz[l];
+  nb[v.off(i, j, k)] = 0;
+  if (l < n0) {
+    ox[l] = i;
+    oy[l] = j;
+    oz[l] = k;
+  }
+}
+
 // phi -> u1, u2 at the listed cells
 template <class R>
 __global__ void k_copy_band(const R *phi, R *u1, R *u2, View<const R> v, const int *ix, const int *iy, const int *iz,
@@ -315,23 +330,51 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
   std::vector<int> lo, hi;
   int ob[4];
   int n0 = 0, nrebuild = 0;
+  // the previous level-0 list of a rebuild (the first build scans the grid)
+  int *ox = nullptr, *oy = nullptr, *oz = nullptr;
   for (int step = 0; step < n_steps; step++) {
     if (step % rebuild_every == 0) {
       long long c0 = 0;
+      PrevLevel0 prev;
+      if (nrebuild > 0) {
+        // phi changed only at level-0 cells since the last build: the new
+        // band's level 0 is drawn from the old one (Level0List); the old
+        // band's marks are cleared so the breadth-first levels start clean
+        int nlist = 0;
+        for (int lv = 0; lv <= level; lv++)
+          if (hi[lv] + 1 > nlist) nlist = hi[lv] + 1;
+        if (nlist > 0)
+          LSMGPU_LAUNCH(k_band_retire, (unsigned)((nlist + 255) / 256), 256, 0, nb, view((const U8 *)nb, gb), ix, iy,
+                        iz, nlist, n0, ox, oy, oz);
+        prev.ox = ox;
+        prev.oy = oy;
+        prev.oz = oz;
+        prev.n = n0;
+      }
       if (!band_build<R>(call, phi, gb, nb, gb, ix, iy, iz, 0, (int)(n - 1), outer, 0, (int)(n - 1), (double)gamma,
-                         (double)beta, level, lo, hi, ob, &c0, claim, true))
+                         (double)beta, level, lo, hi, ob, &c0, claim, true, BandForm<R>(), nullptr,
+                         nrebuild > 0 ? &prev : nullptr))
         return lsmgpu_get_last_error(nullptr, 0);
+      if (nrebuild == 0 && c0 > 0) {
+        // later level-0 lists are sub-sequences of this one
+        ox = call.temp<int>(c0);
+        oy = call.temp<int>(c0);
+        oz = call.temp<int>(c0);
+        if (!call.ok()) return lsmgpu_get_last_error(nullptr, 0);
+      }
       n0 = (int)c0;
       if (band_log) band_log[nrebuild] = c0;
       nrebuild++;
       // stage fields hold phi^n on band levels 1..3 (every cell a level-0
-      // stencil reads); level-0 cells are overwritten by each stage
+      // stencil reads besides level 0); level-0 cells are written by each
+      // stage before any stage reads them, so only levels 1..3 are copied
       int nlist = 0;
       for (int lv = 0; lv <= level; lv++)
         if (hi[lv] + 1 > nlist) nlist = hi[lv] + 1;
-      if (n0 > 0 && nlist > 0)
-        LSMGPU_LAUNCH(k_copy_band<R>, (unsigned)((nlist + 255) / 256), 256, 0, (const R *)phi, u1, u2,
-                      view((const R *)phi, gb), ix, iy, iz, nlist);
+      const int first = n0;  // levels 1..3 follow level 0 in the lists
+      if (n0 > 0 && nlist > first)
+        LSMGPU_LAUNCH(k_copy_band<R>, (unsigned)((nlist - first + 255) / 256), 256, 0, (const R *)phi, u1, u2,
+                      view((const R *)phi, gb), ix + first, iy + first, iz + first, nlist - first);
     }
     if (n0 == 0) continue;
     BandArgs<R> a{};

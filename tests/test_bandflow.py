@@ -65,6 +65,25 @@ def test_band_flow_f64_bit_exact(device, gpu_lib):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("n_steps,rebuild_every,gamma", [(12, 2, 2.5 * DX), (13, 1, 3 * DX)])
+def test_band_flow_f64_many_rebuilds_bit_exact(n_steps, rebuild_every, gamma, gpu_lib):
+    """Rebuilds after the first draw the new level 0 from the previous one
+    (the flow changes phi only there); many rebuilds on a moving front, every
+    level-0 count, dt and the final phi equal to the oracle's (which rebuilds
+    over the whole grid each time)."""
+    phi = spheres_phi(seed=9, count=4)
+    args = dict(ARGS, n_steps=n_steps, rebuild_every=rebuild_every, gamma=gamma, beta=gamma / 2)
+    want, want_dt, bands = O.band_run(H.oracle(), phi, GB, FB, DX, n_steps, rebuild_every, args["gamma"],
+                                      args["beta"], args["a_n"], args["b_n"], args["cfl"])
+    got = phi.copy(order="F")
+    dts, counts = L.band_flow_weno5_tvdrk3(got, GB, FB, DX, n_steps, rebuild_every, args["gamma"], args["beta"],
+                                           args["a_n"], args["b_n"], args["cfl"], "f64")
+    assert [int(b[5][0] + 1) for b in bands] == list(counts)
+    assert np.array_equal(np.asarray(want_dt), dts)
+    assert H.same(want, got), np.max(np.abs(want - got))
+
+
+@pytest.mark.gpu
 def test_band_flow_f32_within_tolerance(gpu_lib):
     phi = spheres_phi()
     want, want_dt, bands = oracle_result(phi)
