@@ -7,9 +7,13 @@
 // launch per grid; each CTA double-buffers its tiles in shared memory with
 // TMA loads from per-grid tensor maps kept in global memory.  The n_steps x 3
 // stage launches of a call are captured once into a CUDA graph and replayed.
-// The tile depth TZ and the CTAs per SM come from a small autotuner that
-// times the candidates on the batch at hand and keeps the choice per batch
-// shape for the life of the process.
+// Each grid gets the tile shape (32 x 8 or 16 x 16 cells of a plane) that
+// pads its x rows least: the 256 threads of a CTA cover one tile plane, and
+// lanes past the row's end idle through the whole tile.  A table of
+// (grid, tile position) per global tile index, built on the host, replaces
+// any search or division in the kernel.  The tile depth TZ and the CTAs per
+// SM come from a small autotuner that times the candidates on the batch at
+// hand and keeps the choice per batch shape for the life of the process.
 //
 // For comparison the same batch can run as a loop of single-grid launches
 // (one stage kernel per grid per stage), which is what calling the
@@ -43,26 +47,32 @@ struct GridDesc {
   float vconst[3], inv[3], dt;
   int tile_base;  // first global tile index of this grid
   int ntx, nty, ntz;
+  int wide;       // 1: 32 x 8 tiles, 0: 16 x 16 tiles
 };
 
-__device__ __forceinline__ int find_grid(const GridDesc *g, int n, int t) {
-  int lo = 0, hi = n - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (g[mid].tile_base <= t) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
+// tile shapes: (32 x 8) and (16 x 16) cells per plane, 8 halo columns and 6
+// halo rows; the shared-memory buffer holds the larger staged plane
+constexpr int kWideSX = 32 + 8, kWideSY = 8 + 6, kNarrowSX = 16 + 8, kNarrowSY = 16 + 6;
+constexpr int kPlaneMax = kWideSX * kWideSY > kNarrowSX * kNarrowSY ? kWideSX * kWideSY : kNarrowSX * kNarrowSY;
+
+// one global tile: its grid and position (tiles per axis < 2^16 per grid)
+struct TileRef {
+  int g;
+  unsigned short bx, by;
+  unsigned short bz, pad;
+};
 
 template <int TZ_>
 __global__ void __launch_bounds__(TX * TY) k_batch_stage(const GridDesc *__restrict__ gd,
-                                                        const CUtensorMap *__restrict__ tmaps, int ngrids,
-                                                        int ntiles, int stage, float *A, float *B, float *C,
-                                                        int *counter, int *err, int periodic) {
+                                                        const CUtensorMap *__restrict__ tmaps,
+                                                        const TileRef *__restrict__ tiles_ref, int ntiles, int stage,
+                                                        float *A, float *B, float *C, int *counter, int *err,
+                                                        int periodic) {
   constexpr int SZ_ = TZ_ + 6;
-  constexpr uint32_t kTileBytes = (uint32_t)(SX * SY * SZ_ * sizeof(float));
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  float *tiles[2] = {reinterpret_cast<float *>(smem_raw), reinterpret_cast<float *>(smem_raw) + SX * SY * SZ_};
+  // buffer b at tiles + b * kPlaneMax * SZ_ (no indexed pointer array: that
+  // would live in local memory)
+  float *const tiles = reinterpret_cast<float *>(smem_raw);
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ int s_tile[2];
   const int tid = threadIdx.x + TX * threadIdx.y;
@@ -70,15 +80,16 @@ __global__ void __launch_bounds__(TX * TY) k_batch_stage(const GridDesc *__restr
   float *outb = stage == 1 ? B : (stage == 2 ? C : A);
 
   auto issue = [&](int t, int b) {
-    const int g = find_grid(gd, ngrids, t);
-    const GridDesc &G = gd[g];
-    const int lt = t - G.tile_base;
-    const int bx = lt % G.ntx, by = (lt / G.ntx) % G.nty, bz = lt / (G.ntx * G.nty);
-    const CUtensorMap *m = tmaps + 3 * g + in_buf;
+    const TileRef r = tiles_ref[t];
+    const int wide = gd[r.g].wide;
+    const int tw = wide ? 32 : 16, th = wide ? 8 : 16;
+    const CUtensorMap *m = tmaps + 3 * r.g + in_buf;
+    const uint32_t bytes = (uint32_t)((wide ? kWideSX * kWideSY : kNarrowSX * kNarrowSY) * SZ_ * sizeof(float));
     // the maps live in global memory and are rewritten between calls
     asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"((uint64_t)m) : "memory");
-    mbar_arrive_expect_tx(&bars[b], kTileBytes);
-    tma_load_3d(tiles[b], m, bx * TX + GX - 4, by * TY + GY - 3, bz * TZ_ + GZ - 3, &bars[b]);
+    mbar_arrive_expect_tx(&bars[b], bytes);
+    tma_load_3d(tiles + b * kPlaneMax * SZ_, m, r.bx * tw + GX - 4, r.by * th + GY - 3, r.bz * TZ_ + GZ - 3,
+                &bars[b]);
   };
 
   if (tid == 0) {
@@ -89,7 +100,7 @@ __global__ void __launch_bounds__(TX * TY) k_batch_stage(const GridDesc *__restr
   }
   __syncthreads();
   int cur = 0;
-  uint32_t phase[2] = {0, 0};
+  uint32_t phase = 0;  // bit b: the parity buffer b waits for next
   int t = s_tile[0];
   if (tid == 0 && t < ntiles) issue(t, 0);
   while (t < ntiles) {
@@ -97,17 +108,16 @@ __global__ void __launch_bounds__(TX * TY) k_batch_stage(const GridDesc *__restr
     __syncthreads();  // next index visible; buffer cur^1 no longer read
     const int tn = s_tile[cur ^ 1];
     if (tid == 0 && tn < ntiles) issue(tn, cur ^ 1);
-    if (!mbar_wait(&bars[cur], phase[cur], fused::kMaxPolls)) {
+    if (!mbar_wait(&bars[cur], (phase >> cur) & 1u, fused::kMaxPolls)) {
       if (tid == 0) atomicExch(err, LSMGPU_ERR_TIMEOUT);
-      mbar_wait(&bars[cur], phase[cur], fused::kMaxPolls);
-      if (tn < ntiles) mbar_wait(&bars[cur ^ 1], phase[cur ^ 1], fused::kMaxPolls);
+      mbar_wait(&bars[cur], (phase >> cur) & 1u, fused::kMaxPolls);
+      if (tn < ntiles) mbar_wait(&bars[cur ^ 1], (phase >> (cur ^ 1)) & 1u, fused::kMaxPolls);
       return;
     }
-    phase[cur] ^= 1;
-    const int g = find_grid(gd, ngrids, t);
-    const GridDesc &G = gd[g];
-    const int lt = t - G.tile_base;
-    const int bx = lt % G.ntx, by = (lt / G.ntx) % G.nty, bz = lt / (G.ntx * G.nty);
+    phase ^= 1u << cur;
+    const float *tile = tiles + cur * kPlaneMax * SZ_;
+    const TileRef r = tiles_ref[t];
+    const GridDesc &G = gd[r.g];
     StageArgs<float> a;
     a.L = G.L;
     a.phi_n = A + G.off;
@@ -124,7 +134,10 @@ __global__ void __launch_bounds__(TX * TY) k_batch_stage(const GridDesc *__restr
     a.use0 = 0;
     a.periodic = periodic;
     a.err = err;
-    fused::f32_tile<fused::ADV_CONST, TZ_>(tiles[cur], a, bx * TX, by * TY, bz * TZ_);
+    if (G.wide)
+      fused::f32_tile<fused::ADV_CONST, TZ_, 32, 8>(tile, a, r.bx * 32, r.by * 8, r.bz * TZ_, tid & 31, tid >> 5);
+    else
+      fused::f32_tile<fused::ADV_CONST, TZ_, 16, 16>(tile, a, r.bx * 16, r.by * 16, r.bz * TZ_, tid & 15, tid >> 4);
     cur ^= 1;
     t = tn;
   }
@@ -159,18 +172,19 @@ struct Batch {
 };
 
 template <int TZ_>
-void launch_batch_stage(const GridDesc *gd, const CUtensorMap *tm, const Batch &b, int stage, float *A, float *B,
-                        float *C, int *counter, int *err, int periodic, int blocks, cudaStream_t s) {
+void launch_batch_stage(const GridDesc *gd, const CUtensorMap *tm, const TileRef *tr, const Batch &b, int stage,
+                        float *A, float *B, float *C, int *counter, int *err, int periodic, int blocks,
+                        cudaStream_t s) {
   // the shared-memory attribute is set by max_blocks_per_sm() before any launch
-  const size_t smem = 2 * (size_t)SX * SY * (TZ_ + 6) * sizeof(float);
-  k_batch_stage<TZ_><<<blocks, dim3(TX, TY), smem, s>>>(gd, tm, b.n, b.ntiles, stage, A, B, C, counter, err,
+  const size_t smem = 2 * (size_t)kPlaneMax * (TZ_ + 6) * sizeof(float);
+  k_batch_stage<TZ_><<<blocks, dim3(TX, TY), smem, s>>>(gd, tm, tr, b.ntiles, stage, A, B, C, counter, err,
                                                         periodic);
   note_launch();
 }
 
 int max_blocks_per_sm(int tz) {
   int v = 1;
-  const size_t smem = 2 * (size_t)SX * SY * (tz + 6) * sizeof(float);
+  const size_t smem = 2 * (size_t)kPlaneMax * (tz + 6) * sizeof(float);
   if (tz == 4) {
     cudaFuncSetAttribute(k_batch_stage<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_batch_stage<4>, TX * TY, smem);
@@ -226,7 +240,9 @@ extern "C" int lsmgpu_advect_batch_weno5_tvdrk3_f32(float *phi, const long long 
   if (!call.ok()) return lsmgpu_get_last_error(nullptr, 0);
   cudaStream_t s = stream();
 
-  auto build_desc = [&](int tz) {
+  std::vector<TileRef> tref;
+  // force_wide: every grid on 32 x 8 tiles (the single-grid kernel's maps)
+  auto build_desc = [&](int tz, bool force_wide = false) {
     long long off = 0;
     int tiles = 0;
     for (int g = 0; g < n_grids; g++) {
@@ -239,18 +255,41 @@ extern "C" int lsmgpu_advect_batch_weno5_tvdrk3_f32(float *phi, const long long 
         G.inv[d] = 1.0f / spacing[3 * g + d];
       }
       G.dt = dt[g];
-      G.ntx = (G.L.nx + TX - 1) / TX;
-      G.nty = (G.L.ny + TY - 1) / TY;
+      // the shape that pads the x rows less (16-wide on a tie is no better)
+      G.wide = (force_wide || (G.L.nx + 31) / 32 * 32 <= (G.L.nx + 15) / 16 * 16) ? 1 : 0;
+      const int tw = G.wide ? 32 : 16, th = G.wide ? 8 : 16;
+      G.ntx = (G.L.nx + tw - 1) / tw;
+      G.nty = (G.L.ny + th - 1) / th;
       G.ntz = (G.L.nz + tz - 1) / tz;
       G.tile_base = tiles;
       tiles += G.ntx * G.nty * G.ntz;
     }
     b.total = off;
     b.ntiles = tiles;
+    tref.resize((size_t)tiles);
+    for (int g = 0; g < n_grids; g++) {
+      const GridDesc &G = b.desc[g];
+      int t = G.tile_base;
+      for (int bz = 0; bz < G.ntz; bz++)
+        for (int by = 0; by < G.nty; by++)
+          for (int bx = 0; bx < G.ntx; bx++)
+            tref[(size_t)t++] = TileRef{g, (unsigned short)bx, (unsigned short)by, (unsigned short)bz, 0};
+    }
   };
   build_desc(8);
+  // the tile table is sized for the smallest tile depth the autotuner tries
+  long long max_tiles = 0;
+  for (int g = 0; g < n_grids; g++) {
+    const int nx = dims[3 * g], ny = dims[3 * g + 1], nz = dims[3 * g + 2];
+    max_tiles += (long long)((nx + 15) / 16) * ((ny + 7) / 8) * ((nz + 3) / 4);
+  }
+  if (max_tiles > 0x7fffffffLL) {
+    set_error(LSMGPU_ERR_CAPACITY, "%s: more than 2^31 tiles", name);
+    return LSMGPU_ERR_CAPACITY;
+  }
   float *A = call.temp<float>(b.total), *B = call.temp<float>(b.total), *C = call.temp<float>(b.total);
   GridDesc *gd = call.temp<GridDesc>(n_grids);
+  TileRef *trd = call.temp<TileRef>(max_tiles);
   CUtensorMap *tm = (CUtensorMap *)call.temp<unsigned char>((long long)sizeof(CUtensorMap) * 3 * n_grids);
   int *counters = call.temp<int>(3 * (long long)std::max(n_steps, 1) + 64);
   int *err = call.temp<int>(1);
@@ -267,7 +306,8 @@ extern "C" int lsmgpu_advect_batch_weno5_tvdrk3_f32(float *phi, const long long 
       const Layout &L = b.desc[g].L;
       for (int q = 0; q < 3; q++)
         if (!encode_tmap_3d(&tmh[3 * g + q], bufs[q] + b.desc[g].off, 4, (long long)L.nx + GX + 3,
-                            (long long)L.ny + 2 * GY, (long long)L.nz + 2 * GZ, L.py, L.pz, SX, SY, tz + 6))
+                            (long long)L.ny + 2 * GY, (long long)L.nz + 2 * GZ, L.py, L.pz,
+                            b.desc[g].wide ? kWideSX : kNarrowSX, b.desc[g].wide ? kWideSY : kNarrowSY, tz + 6))
           return false;
     }
     return cudaMemcpyAsync(tm, tmh.data(), sizeof(CUtensorMap) * tmh.size(), cudaMemcpyHostToDevice, s) ==
@@ -275,6 +315,7 @@ extern "C" int lsmgpu_advect_batch_weno5_tvdrk3_f32(float *phi, const long long 
   };
   auto upload_desc = [&]() {
     cudaMemcpyAsync(gd, b.desc.data(), sizeof(GridDesc) * n_grids, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(trd, tref.data(), sizeof(TileRef) * tref.size(), cudaMemcpyHostToDevice, s);
   };
   upload_desc();
   {
@@ -287,13 +328,14 @@ extern "C" int lsmgpu_advect_batch_weno5_tvdrk3_f32(float *phi, const long long 
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
 
   auto run_stage = [&](int tz, int stage, int *counter, int blocks) {
-    if (tz == 4) launch_batch_stage<4>(gd, tm, b, stage, A, B, C, counter, err, 1, blocks, s);
-    else if (tz == 16) launch_batch_stage<16>(gd, tm, b, stage, A, B, C, counter, err, 1, blocks, s);
-    else launch_batch_stage<8>(gd, tm, b, stage, A, B, C, counter, err, 1, blocks, s);
+    if (tz == 4) launch_batch_stage<4>(gd, tm, trd, b, stage, A, B, C, counter, err, 1, blocks, s);
+    else if (tz == 16) launch_batch_stage<16>(gd, tm, trd, b, stage, A, B, C, counter, err, 1, blocks, s);
+    else launch_batch_stage<8>(gd, tm, trd, b, stage, A, B, C, counter, err, 1, blocks, s);
   };
 
   if (want_loop) {
     // comparison mode: one single-grid stage launch per grid per stage
+    build_desc(8, true);
     if (!encode_all(8)) { call.fail("tensor map encoding failed"); return LSMGPU_ERR_CUDA; }
     const size_t smem = (size_t)SX * SY * fused::SZ * sizeof(float);
     cudaFuncSetAttribute(fused::k_stage_f32<fused::ADV_CONST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -380,9 +422,9 @@ extern "C" int lsmgpu_advect_batch_weno5_tvdrk3_f32(float *phi, const long long 
       for (int step = 0; step < n_steps; step++)
         for (int stage = 1; stage <= 3; stage++) {
           int *ctr = counters + 3 * step + stage - 1;
-          if (tz == 4) launch_batch_stage<4>(gd, tm, b, stage, A, B, C, ctr, err, 1, blocks, cs);
-          else if (tz == 16) launch_batch_stage<16>(gd, tm, b, stage, A, B, C, ctr, err, 1, blocks, cs);
-          else launch_batch_stage<8>(gd, tm, b, stage, A, B, C, ctr, err, 1, blocks, cs);
+          if (tz == 4) launch_batch_stage<4>(gd, tm, trd, b, stage, A, B, C, ctr, err, 1, blocks, cs);
+          else if (tz == 16) launch_batch_stage<16>(gd, tm, trd, b, stage, A, B, C, ctr, err, 1, blocks, cs);
+          else launch_batch_stage<8>(gd, tm, trd, b, stage, A, B, C, ctr, err, 1, blocks, cs);
         }
       cudaError_t ce = cudaStreamEndCapture(cs, &graph);
       if (ce != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {

@@ -425,24 +425,26 @@ __device__ __forceinline__ void weno5_pm_x2(const float2 D[6], float2 &gp, float
   gp = combine(q1p, q2p, q3p, P1p, B, A);
 }
 
-// Computes one 32 x 8 x TZ_ tile whose haloed input (40 x 14 x (TZ_ + 6)) is
-// in `tile`; shared by the single-grid kernel and the batched persistent
-// kernel (which picks TZ_ with its autotuner).
-template <int MODE, int TZ_ = TZ>
-__device__ __forceinline__ void f32_tile(const float *tile, const StageArgs<float> &a, int x0, int y0, int z0) {
-  const int tx = threadIdx.x, ty = threadIdx.y;
+// Computes one TX_ x TY_ x TZ_ tile whose haloed input ((TX_ + 8) x (TY_ + 6)
+// x (TZ_ + 6)) is in `tile`, the calling thread at (tx, ty) of the tile;
+// shared by the single-grid kernel (32 x 8 tiles) and the batched persistent
+// kernel (32 x 8 or 16 x 16 tiles per grid, TZ_ from its autotuner).
+template <int MODE, int TZ_ = TZ, int TX_ = TX, int TY_ = TY>
+__device__ __forceinline__ void f32_tile(const float *tile, const StageArgs<float> &a, int x0, int y0, int z0,
+                                         int tx, int ty) {
+  constexpr int SX_ = TX_ + 8, SY_ = TY_ + 6;
   const Layout &L = a.L;
   const int i = x0 + tx, j = y0 + ty;
   if (i >= L.nx || j >= L.ny) return;
   const int sx = tx + 4, sy = ty + 3;
   const int kmax = min(TZ_, L.nz - z0);
-  const int st[3] = {1, SX, SX * SY};
+  const int st[3] = {1, SX_, SX_ * SY_};
   const float2 inv[3] = {sp(a.inv[0]), sp(a.inv[1]), sp(a.inv[2])};
 
   for (int tz = 0; tz < kmax; tz += 2) {
     const bool two = tz + 1 < kmax;  // the second lane is a real cell
-    const float *c0 = tile + ((tz + 3) * SY + sy) * SX + sx;
-    const float *c1 = two ? c0 + SX * SY : c0;
+    const float *c0 = tile + ((tz + 3) * SY_ + sy) * SX_ + sx;
+    const float *c1 = two ? c0 + SX_ * SY_ : c0;
     const int k0 = z0 + tz, k1 = two ? k0 + 1 : k0;
     const long long cell0 = L.idx(i, j, k0), cell1 = L.idx(i, j, k1);
     float2 rhs;
@@ -483,17 +485,26 @@ __device__ __forceinline__ void f32_tile(const float *tile, const StageArgs<floa
         for (int q = -3; q <= 3; q++) a7[q + 3] = mul2(make_float2(c0[q * st[d]], c1[q * st[d]]), inv[d]);
 #pragma unroll
         for (int f = 0; f < 6; f++) D[f] = fma2(sp(-1.f), a7[f], a7[f + 1]);
-        const bool b0 = vel0[d] > 0.f, b1 = vel1[d] > 0.f;
-        float2 v[5];
+        if constexpr (MODE == ADV_CONST) {
+          // one velocity for the whole grid: the side and the zero cut are
+          // uniform, so the stencil is chosen by a (non-divergent) branch
+          const float u = a.vconst[d];
+          if (fabsf(u) < 1e-11f) continue;
+          const float2 g = u > 0.f ? weno5_x2(D[0], D[1], D[2], D[3], D[4]) : weno5_x2(D[5], D[4], D[3], D[2], D[1]);
+          dot = fma2(sp(u), g, dot);
+        } else {
+          const bool b0 = vel0[d] > 0.f, b1 = vel1[d] > 0.f;
+          float2 v[5];
 #pragma unroll
-        for (int q = 0; q < 5; q++) {
-          v[q].x = b0 ? D[q].x : D[5 - q].x;
-          v[q].y = b1 ? D[q].y : D[5 - q].y;
+          for (int q = 0; q < 5; q++) {
+            v[q].x = b0 ? D[q].x : D[5 - q].x;
+            v[q].y = b1 ? D[q].y : D[5 - q].y;
+          }
+          float2 g = weno5_x2(v[0], v[1], v[2], v[3], v[4]);
+          if (fabsf(vel0[d]) < 1e-11f) g.x = 0.f;
+          if (fabsf(vel1[d]) < 1e-11f) g.y = 0.f;
+          dot = fma2(make_float2(vel0[d], vel1[d]), g, dot);
         }
-        float2 g = weno5_x2(v[0], v[1], v[2], v[3], v[4]);
-        if (fabsf(vel0[d]) < 1e-11f) g.x = 0.f;
-        if (fabsf(vel1[d]) < 1e-11f) g.y = 0.f;
-        dot = fma2(make_float2(vel0[d], vel1[d]), g, dot);
       }
       rhs = make_float2(-dot.x, -dot.y);
     }
@@ -511,18 +522,24 @@ __device__ __forceinline__ void f32_tile(const float *tile, const StageArgs<floa
     for (int lane = 0; lane < (two ? 2 : 1); lane++) {
       const int k = lane ? k1 : k0;
       const float val = lane ? u.y : u.x;
-      a.out[L.idx(i, j, k)] = val;
+      const long long c = L.idx(i, j, k);
+      a.out[c] = val;
       if (a.periodic) {
-        int oi[2] = {0, 0}, oj[2] = {0, 0}, ok_[2] = {0, 0};
-        int ni = 1, nj = 1, nk = 1;
-        if (i < 3) oi[ni++] = L.nx; else if (i >= L.nx - 3) oi[ni++] = -L.nx;
-        if (j < 3) oj[nj++] = L.ny; else if (j >= L.ny - 3) oj[nj++] = -L.ny;
-        if (k < 3) ok_[nk++] = L.nz; else if (k >= L.nz - 3) ok_[nk++] = -L.nz;
-        if (ni + nj + nk > 3)
-          for (int p = 0; p < ni; p++)
-            for (int q = 0; q < nj; q++)
-              for (int r = 0; r < nk; r++)
-                if (p | q | r) a.out[L.idx(i + oi[p], j + oj[q], k + ok_[r])] = val;
+        // the cell's periodic images in the ghost layers (up to 7: each
+        // combination of the axes along which it lies within 3 of a face)
+        const int oi = i < 3 ? L.nx : (i >= L.nx - 3 ? -L.nx : 0);
+        const int oj = j < 3 ? L.ny : (j >= L.ny - 3 ? -L.ny : 0);
+        const int ok = k < 3 ? L.nz : (k >= L.nz - 3 ? -L.nz : 0);
+        if (oi | oj | ok) {
+          const long long sx = oi, sy = L.py * oj, sz = L.pz * ok;
+          if (oi) a.out[c + sx] = val;
+          if (oj) a.out[c + sy] = val;
+          if (ok) a.out[c + sz] = val;
+          if (oi && oj) a.out[c + sx + sy] = val;
+          if (oi && ok) a.out[c + sx + sz] = val;
+          if (oj && ok) a.out[c + sy + sz] = val;
+          if (oi && oj && ok) a.out[c + sx + sy + sz] = val;
+        }
       }
     }
   }
@@ -555,7 +572,7 @@ __global__ void __launch_bounds__(TX * TY) k_stage_f32(const __grid_constant__ C
     fill_face_ghosts<float>(tile, SX, SY, SZ, x0 - 4, y0 - 3, z0 - 3, a.L, a.ghost);
     __syncthreads();
   }
-  f32_tile<MODE, TZ>(tile, a, x0, y0, z0);
+  f32_tile<MODE, TZ>(tile, a, x0, y0, z0, tx, ty);
 }
 
 }  // namespace fused
