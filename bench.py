@@ -433,9 +433,10 @@ def gpu_arm(args, world, rank, local):
     value = world * cells * ITERS / (ms / 1e3) / 1e9
 
     # roofline of the dominant kernel (the fused reinitialization stage):
-    # stage-only time from the difference of two runs, periodic boundaries
-    # (no ghost-fill launches), so the difference is 3*(n_b - n_a) stage
-    # launches exactly
+    # stage-only time from the difference of two runs with the workload's
+    # boundary condition (each stage computes its face ghosts; one ghost fill
+    # follows the last stage of a call), so the difference is 3*(n_b - n_a)
+    # stage launches exactly
     def stage_time(iters, reps=3):
         best = None
         for _ in range(reps):
@@ -443,8 +444,7 @@ def gpu_arm(args, world, rank, local):
             torch.cuda.synchronize()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            L.reinit_weno5_tvdrk3(phi, gb, fb, dx, dtau, iters, use_phi0_for_sgn=1, bc=L.BC_PERIODIC,
-                                  precision="f32")
+            L.reinit_weno5_tvdrk3(phi, gb, fb, dx, dtau, iters, use_phi0_for_sgn=1, bc=bc, precision="f32")
             b.record(stream)
             torch.cuda.synchronize()
             t = a.elapsed_time(b)

@@ -88,10 +88,16 @@ __device__ __forceinline__ R extrap(R e, R n, int g, int kind) {
 // ghost of an axis is written only by that axis' pass from interior cells.
 // (Edge and corner ghosts are read by no axis-aligned stencil.)  Tile cell
 // (a, b, c) holds interior cell (ox + a, oy + b, oz + c).
+// The faces write disjoint cells and read only interior ones, so they are
+// filled in any order; a tile inside the domain on every axis has none (one
+// uniform test).  Threads cover each face plane in 2D (x along threadIdx.x,
+// the other axis along threadIdx.y) and walk the ghost layers, so no index
+// is decomposed by division.  Not inlined, so the stage kernels' register
+// allocation does not depend on it.
 template <class R>
-__device__ void fill_face_ghosts(R *tile, int sdx, int sdy, int sdz, int ox, int oy, int oz, const Layout &L,
+__device__ __noinline__ void fill_face_ghosts(R *tile, int sdx, int sdy, int sdz, int ox, int oy, int oz, const Layout &L,
                                  int kind) {
-  const int nthr = blockDim.x * blockDim.y, tid = threadIdx.x + blockDim.x * threadIdx.y;
+  if (ox >= 0 && ox + sdx <= L.nx && oy >= 0 && oy + sdy <= L.ny && oz >= 0 && oz + sdz <= L.nz) return;
   const int sxy = sdx * sdy;
   // one face: ghost layers 1..3 of axis AX below (up = 0) or above (up = 1)
   auto face = [&](auto ax_tag, int up) {
@@ -108,15 +114,21 @@ __device__ void fill_face_ghosts(R *tile, int sdx, int sdy, int sdz, int ox, int
     if (lo0 > hi0 || lo1 > hi1 || lo2 > hi2) return;
     const int e_at = up ? nax - 1 : 0, n_at = up ? nax - 2 : 1;
     const int st = AX == 0 ? 1 : (AX == 1 ? sdx : sxy);
-    const int cx = hi0 - lo0 + 1, cy = hi1 - lo1 + 1;
-    const int cnt = cx * cy * (hi2 - lo2 + 1);
-    for (int q = tid; q < cnt; q += nthr) {
-      const int c0 = lo0 + q % cx, c1 = lo1 + (q / cx) % cy, c2 = lo2 + q / (cx * cy);
-      const int at = (c0 - ox) + (c1 - oy) * sdx + (c2 - oz) * sxy;
-      const int cax = AX == 0 ? c0 : (AX == 1 ? c1 : c2);
-      const int g = up ? cax - e_at : -cax;
-      tile[at] = extrap(tile[at + (e_at - cax) * st], tile[at + (n_at - cax) * st], g, kind);
-    }
+    // plane axes: (1, 2) for an x face, (0, 2) for y, (0, 1) for z
+    constexpr int PA = AX == 0 ? 1 : 0, PB = AX == 2 ? 1 : 2;
+    const int loA = PA == 0 ? lo0 : lo1, hiA = PA == 0 ? hi0 : hi1;
+    const int loB = PB == 1 ? lo1 : lo2, hiB = PB == 1 ? hi1 : hi2;
+    const int loG = AX == 0 ? lo0 : (AX == 1 ? lo1 : lo2), hiG = AX == 0 ? hi0 : (AX == 1 ? hi1 : hi2);
+    for (int pa = loA + (int)threadIdx.x; pa <= hiA; pa += blockDim.x)
+      for (int pb = loB + (int)threadIdx.y; pb <= hiB; pb += blockDim.y)
+        for (int g = loG; g <= hiG; g++) {
+          const int c0 = AX == 0 ? g : pa;
+          const int c1 = AX == 1 ? g : (PA == 1 ? pa : pb);
+          const int c2 = AX == 2 ? g : pb;
+          const int at = (c0 - ox) + (c1 - oy) * sdx + (c2 - oz) * sxy;
+          const int d = up ? g - e_at : -g;
+          tile[at] = extrap(tile[at + (e_at - g) * st], tile[at + (n_at - g) * st], d, kind);
+        }
   };
   face(std::integral_constant<int, 0>{}, 0);
   face(std::integral_constant<int, 0>{}, 1);
