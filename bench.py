@@ -886,10 +886,10 @@ def sub_geometry(stream, dev, n=512, reps=10):
 
 
 # DRAM bytes (read + write) of one fused FP32 reinitialization stage launch
-# at 256^3, from one ncu capture of a stage-2 launch (profiles/
-# k_stage_reinit_f32_256.md, packed FP32x2 kernel: 285.6 MB; the stage's
+# at 256^3, from one ncu capture of a stage-2 launch of k_reinit_x2
+# (profiles/k_reinit_x2_reinit_f32_256.md: 233.1 + 51.5 MB; the stage's
 # algorithmic bytes are 16 B/cell = 268.4 MB)
-MEASURED_STAGE_TRAFFIC = 285.6e6
+MEASURED_STAGE_TRAFFIC = 284.6e6
 
 # FMA-pipe thread-instructions (a packed FFMA2 / FMUL2 / FADD2 counts once)
 # per cell of one headline stage launch (k_reinit_x2, ncu
@@ -898,7 +898,7 @@ MEASURED_STAGE_TRAFFIC = 285.6e6
 # square-root sequences included) per cell-update of the FP64 parity form
 # (3 x one stage launch of k_stage<double, REINIT> at 128^3); both from the
 # captures summarised in profiles/k_reinit_x2_reinit_f32_256.md
-MEASURED_FMA_PIPE_INSTR_PER_CELL_STAGE = 130.2
+MEASURED_FMA_PIPE_INSTR_PER_CELL_STAGE = 119.9
 MEASURED_FP64_OPS_PER_CELL_UPDATE = 3 * 633.5
 
 
