@@ -30,6 +30,7 @@ struct BandArgs {
   View<const R> phin;     // phi^n (stages 2, 3)
   View<R> out;            // stage output
   const int *ix, *iy, *iz;
+  const int *off0;        // padded offset of each level-0 entry (written at each rebuild)
   int n0;                 // level-0 entries (list elements 0..n0-1)
   R dx, a_n, b_n, beta, gamma, cfl;
   R *rhs;                 // per level-0 entry (stage 1)
@@ -226,8 +227,8 @@ template <class R>
 __global__ void k_band_update1(BandArgs<R> a) {
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= a.n0) return;
-  const int i = a.ix[l], j = a.iy[l], k = a.iz[l];
-  a.out(i, j, k) = rk_update<R>(1, a.src(i, j, k), a.src(i, j, k), *a.dt, a.rhs[l]);
+  const long long o = a.off0[l];
+  a.out.p[o] = rk_update<R>(1, a.src.p[o], a.src.p[o], *a.dt, a.rhs[l]);
 }
 
 // stages 2 and 3: RHS, cut-off and update in one pass
@@ -244,13 +245,23 @@ __global__ void k_band_stage(BandArgs<R> a) {
 
 // FP32 forms of k_band_rhs and k_band_stage on pairs of consecutive list
 // entries (the second of an odd tail repeats the first and is not written)
+// offsets of the entry pair l0, l0 + 1 (the second repeats the first at an
+// odd tail); off0 has an even number of elements, so the pair load is in bounds
+static __device__ __forceinline__ void pair_offsets(const BandArgs<float> &a, int l0, bool two, long long &o0,
+                                                    long long &o1) {
+  const int2 p = *reinterpret_cast<const int2 *>(a.off0 + l0);
+  o0 = p.x;
+  o1 = two ? p.y : p.x;
+}
+
 static __global__ void k_band_rhs_x2(BandArgs<float> a) {
   const int l0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
   double h = -1.0e308;
   if (l0 < a.n0) {
     const bool two = l0 + 1 < a.n0;
     const int l1 = two ? l0 + 1 : l0;
-    const long long o0 = a.src.off(a.ix[l0], a.iy[l0], a.iz[l0]), o1 = a.src.off(a.ix[l1], a.iy[l1], a.iz[l1]);
+    long long o0, o1;
+    pair_offsets(a, l0, two, o0, o1);
     float2 hd;
     const float2 r = cell_rhs_x2(a, o0, o1, hd);
     h = (double)hd.x;
@@ -268,8 +279,8 @@ static __global__ void k_band_stage_x2(BandArgs<float> a) {
   const int l0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
   if (l0 >= a.n0) return;
   const bool two = l0 + 1 < a.n0;
-  const int l1 = two ? l0 + 1 : l0;
-  const long long o0 = a.src.off(a.ix[l0], a.iy[l0], a.iz[l0]), o1 = a.src.off(a.ix[l1], a.iy[l1], a.iz[l1]);
+  long long o0, o1;
+  pair_offsets(a, l0, two, o0, o1);
   float2 hd;
   const float2 r = cell_rhs_x2(a, o0, o1, hd);
   const float dt = *a.dt;
@@ -277,6 +288,15 @@ static __global__ void k_band_stage_x2(BandArgs<float> a) {
   const float n0v = a.phin.p[o0], n1v = a.phin.p[o1];
   a.out.p[o0] = rk_update<float>(a.stage, n0v, us0, dt, cutoff<float>(r.x, us0, a.beta, a.gamma));
   if (two) a.out.p[o1] = rk_update<float>(a.stage, n1v, us1, dt, cutoff<float>(r.y, us1, a.beta, a.gamma));
+}
+
+// the padded offset of each level-0 entry, for the stage kernels (one 4-byte
+// read per entry instead of three coordinates)
+template <class R>
+__global__ void k_band_offsets(View<const R> v, const int *ix, const int *iy, const int *iz, int n, int *off) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= n) return;
+  off[l] = (int)v.off(ix[l], iy[l], iz[l]);
 }
 
 // clears the marks of the listed cells (the previous band, before a rebuild)
@@ -312,6 +332,7 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
   Call call(name);
   if (!gb.contains(fb, 0, 0, 0)) call.fail("fill box outside the ghost box");
   if (rebuild_every <= 0) call.fail("rebuild_every must be positive");
+  if (gb.size() >= (1LL << 31)) call.fail("ghost box of 2^31 cells or more");
   if (!call.ok()) return LSMGPU_ERR_BOUNDS;
   if (n_steps <= 0) return LSMGPU_OK;
   const long long n = gb.size();
@@ -320,6 +341,7 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
   U8 *nb = call.temp<U8>(n);
   int *ix = call.temp<int>(n), *iy = call.temp<int>(n), *iz = call.temp<int>(n), *outer = call.temp<int>(n);
   R *rhs = call.temp<R>(n);
+  int *off0 = call.temp<int>(n + 1);  // n + 1: the pair loads read an even count
   R *dt = call.temp<R>(1);
   unsigned long long *key = call.temp<unsigned long long>(1);
   double *dtl = dt_log ? call.temp<double>(n_steps) : nullptr;
@@ -371,6 +393,9 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
       int nlist = 0;
       for (int lv = 0; lv <= level; lv++)
         if (hi[lv] + 1 > nlist) nlist = hi[lv] + 1;
+      if (n0 > 0)
+        LSMGPU_LAUNCH(k_band_offsets<R>, (unsigned)((n0 + 255) / 256), 256, 0, view((const R *)phi, gb), ix, iy, iz,
+                      n0, off0);
       const int first = n0;  // levels 1..3 follow level 0 in the lists
       if (n0 > 0 && nlist > first)
         LSMGPU_LAUNCH(k_copy_band<R>, (unsigned)((nlist - first + 255) / 256), 256, 0, (const R *)phi, u1, u2,
@@ -379,6 +404,7 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
     if (n0 == 0) continue;
     BandArgs<R> a{};
     a.ix = ix; a.iy = iy; a.iz = iz;
+    a.off0 = off0;
     a.n0 = n0;
     a.dx = dx; a.a_n = a_n; a.b_n = b_n; a.beta = beta; a.gamma = gamma; a.cfl = cfl;
     a.rhs = rhs;
