@@ -469,24 +469,28 @@ def gpu_arm(args, world, rank, local):
     # end to end through the C ABI with host (pinned) buffers
     host_phi = torch.from_numpy(np.ascontiguousarray(phi64.T).astype(np.float32)).pin_memory()
     host_kappa = torch.zeros_like(host_phi).pin_memory()
-    e2e_steps = max(1, min(args.steps, 3))
-    # reinitialization works in place: each step gets its own pinned copy of
-    # the input, made before the timed region
-    host_inputs = [host_phi.clone().pin_memory() for _ in range(e2e_steps + 1)]
+    e2e_steps = max(1, min(args.steps, 10))
+    # reinitialization works in place: the pinned input is restored from the
+    # pristine host copy before each step, outside the step's timed interval
+    host_work = host_phi.clone().pin_memory()
 
-    def e2e_step(q):
-        wk = host_inputs[q].numpy()
+    def e2e_step():
+        wk = host_work.numpy()
         L.reinit_weno5_tvdrk3(wk.ctypes.data, gb, fb, dx, dtau, ITERS, use_phi0_for_sgn=1, bc=bc,
                               precision="f32")
         L.mean_curvature_o2(host_kappa.numpy().ctypes.data, gb, wk.ctypes.data, gb, fb, dx,
                             precision="f32")
 
-    e2e_step(e2e_steps)
+    host_work.copy_(host_phi)
+    e2e_step()
     barrier(world)
-    t0 = time.perf_counter()
+    e2e_total = 0.0
     for q in range(e2e_steps):
-        e2e_step(q)
-    e2e_sec = (time.perf_counter() - t0) / e2e_steps
+        host_work.copy_(host_phi)
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_total += time.perf_counter() - t0
+    e2e_sec = e2e_total / e2e_steps
     e2e_sec = max_over_ranks(e2e_sec, world, dev)
     arr_bytes = host_phi.numel() * 4
     e2e = {"value": world * cells * ITERS / e2e_sec / 1e9, "unit": UNIT,

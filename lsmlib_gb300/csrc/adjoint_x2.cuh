@@ -161,9 +161,22 @@ __device__ __forceinline__ Coef2<MODE> load_coef2(const AdjStageArgs<float> &a, 
 // dt mu (-W) of each (advection; zero where the term is off).
 // WARP_SIDES: resolve the stencil side per warp where possible
 // (lin_slots_x2_any); otherwise per lane
+// live: some cell of the warp has a nonzero adjoint weight mu (warp_live).
+// Where mu is zero in every cell of the warp (the adjoint field spreads from
+// the objective's support by the stencil reach per stage) every slot and
+// velocity adjoint is exactly zero and the evaluation is skipped.
+__device__ __forceinline__ bool warp_live(float2 mu) {
+  return __any_sync(__activemask(), mu.x != 0.f || mu.y != 0.f);
+}
+
 template <int MODE, bool WARP_SIDES>
 __device__ __forceinline__ float2 coef_slots_x2(const float2 D[6], const Coef2<MODE> &cf, int d, float2 mu,
-                                                float2 dt_inv, float dt, float2 G[6]) {
+                                                float2 dt_inv, float dt, float2 G[6], bool live) {
+  if (!live) {
+#pragma unroll
+    for (int m = 0; m < 6; m++) G[m] = sp(0.f);
+    return sp(0.f);
+  }
   auto slots = [&](float2 yb, bool mx, bool my) {
     if constexpr (WARP_SIDES) return lin_slots_x2_any(D, yb, mx, my, G);
     else return lin_slots_x2<0>(D, yb, mx, my, G);
@@ -281,7 +294,8 @@ __global__ void __maxnreg__(LSMGPU_ADJ_X_X2_NREG) k_adj_x_x2(AdjStageArgs<float>
       cn = load_coef2<MODE>(a, 0, col0 + okn, col1 + okn);
       if (k + 2 < zend) sn = ld2(a.s, okn + pz);
     }
-    const bool gxw = MODE == ADJ_ADV && a.gvel[0] && own;
+    const bool live = warp_live(mu);
+    const bool gxw = MODE == ADJ_ADV && a.gvel[0] && own && live;
     float2 gx_old = sp(0.f), pq = sp(0.f);
     if (gxw) gx_old = ld2(a.gvel[0], ok);
     if (own) {
@@ -298,7 +312,7 @@ __global__ void __maxnreg__(LSMGPU_ADJ_X_X2_NREG) k_adj_x_x2(AdjStageArgs<float>
       for (int f = 0; f < 6; f++) D[f] = sub2(w7[f + 1], w7[f]);
     }
     float2 G[6];
-    const float2 gx = coef_slots_x2<MODE, true>(D, ux, 0, mu, dtix, dt, G);
+    const float2 gx = coef_slots_x2<MODE, true>(D, ux, 0, mu, dtix, dt, G, live);
     if (gxw) {
       a.gvel[0][col0 + ok] = gx_old.x + gx.x;
       if (two) a.gvel[0][col1 + ok] = gx_old.y + gx.y;
@@ -370,6 +384,7 @@ __global__ void __launch_bounds__(32 * kMarchRows, LSMGPU_ADJ_MARCH_X2_CTAS) k_a
   auto ld2 = [&](const float *p, unsigned o) { return make_float2(p[b0 + o], p[b1 + o]); };
 
   float2 dw[6], mring[4], F[6], last, prevV = sp(0.f);
+  int quiet = 0;
   {
     float2 w[6];
 #pragma unroll
@@ -429,23 +444,29 @@ __global__ void __launch_bounds__(32 * kMarchRows, LSMGPU_ADJ_MARCH_X2_CTAS) k_a
     }
     cp = cursor_next(cp, n, pm);
     cl = cursor_next(cl, n, pm);
+    // warp-uniform: some cell has a nonzero weight; quiet counts the steps
+    // since one had (after 7 the face ring holds only zeros and A_AX = 0)
+    const bool live = warp_live(mring[3]);
+    quiet = live ? 0 : quiet + 1;
     // the accumulators' old values are loaded before the slot evaluation so
     // their latency overlaps it (out, gvel and the state arrays are distinct)
-    const bool gw = MODE == ADJ_ADV && a.gvel[AX] && jj >= y0 && jj < yend;
+    const bool gw = MODE == ADJ_ADV && a.gvel[AX] && jj >= y0 && jj < yend && live;
     const bool ow = jj - 3 >= y0;
+    const bool orw = ow && quiet < 7;
     const unsigned otg = co.off;
     if (ow) co = cursor_next(co, n, pm);
     float2 g_old = sp(0.f), o_old = sp(0.f);
     if (gw) g_old = ld2(a.gvel[AX], ojj);
-    if (ow) o_old = ld2(a.out, otg);
+    if (orw) o_old = ld2(a.out, otg);
     float2 G[6];
-    const float2 gy = coef_slots_x2<MODE, LSMGPU_ADJ_MARCH_WARP_SIDES != 0>(dw, uy, AX, mring[3], dtiy, dt, G);
+    const float2 gy =
+        coef_slots_x2<MODE, LSMGPU_ADJ_MARCH_WARP_SIDES != 0>(dw, uy, AX, mring[3], dtiy, dt, G, live);
     if (gw) {
       a.gvel[AX][b0 + ojj] = g_old.x + gy.x;
       if (two) a.gvel[AX][b1 + ojj] = g_old.y + gy.y;
     }
     const float2 Ay = ring_step2(F, prevV, G);
-    if (!ow) continue;
+    if (!orw) continue;
     a.out[b0 + otg] = o_old.x + Ay.x;
     if (two) a.out[b1 + otg] = o_old.y + Ay.y;
   }

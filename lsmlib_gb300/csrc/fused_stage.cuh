@@ -130,12 +130,13 @@ __device__ __noinline__ void fill_face_ghosts(R *tile, int sdx, int sdy, int sdz
           tile[at] = extrap(tile[at + (e_at - g) * st], tile[at + (n_at - g) * st], d, kind);
         }
   };
-  face(std::integral_constant<int, 0>{}, 0);
-  face(std::integral_constant<int, 0>{}, 1);
-  face(std::integral_constant<int, 1>{}, 0);
-  face(std::integral_constant<int, 1>{}, 1);
-  face(std::integral_constant<int, 2>{}, 0);
-  face(std::integral_constant<int, 2>{}, 1);
+  // only the faces the tile crosses
+  if (ox < 0) face(std::integral_constant<int, 0>{}, 0);
+  if (ox + sdx > L.nx) face(std::integral_constant<int, 0>{}, 1);
+  if (oy < 0) face(std::integral_constant<int, 1>{}, 0);
+  if (oy + sdy > L.ny) face(std::integral_constant<int, 1>{}, 1);
+  if (oz < 0) face(std::integral_constant<int, 2>{}, 0);
+  if (oz + sdz > L.nz) face(std::integral_constant<int, 2>{}, 1);
 }
 
 // ---------------------------------------------------------------------------
