@@ -558,14 +558,17 @@ __device__ __forceinline__ void f32_tile(const float *tile, const StageArgs<floa
   }
 }
 
-template <int MODE>
+// 32 x 8 x TZ_ tiles; the steppers launch TZ_ = 8, or 4 where 4-plane tiles
+// fill the machine's waves better (fused_driver.cuh, stage_tz_f32)
+template <int MODE, int TZ_ = TZ>
 __global__ void __launch_bounds__(TX * TY) k_stage_f32(const __grid_constant__ CUtensorMap tm, StageArgs<float> a) {
+  constexpr int SZ_ = TZ_ + 6;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   float *tile = reinterpret_cast<float *>(smem_raw);
   __shared__ __align__(8) uint64_t bar;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int tid = tx + TX * ty;
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ_;
   if (tid == 0) {
     prefetch_tmap(&tm);
     mbar_init(&bar, 1);
@@ -573,7 +576,7 @@ __global__ void __launch_bounds__(TX * TY) k_stage_f32(const __grid_constant__ C
   }
   __syncthreads();
   if (tid == 0) {
-    mbar_arrive_expect_tx(&bar, (uint32_t)(SX * SY * SZ * sizeof(float)));
+    mbar_arrive_expect_tx(&bar, (uint32_t)(SX * SY * SZ_ * sizeof(float)));
     tma_load_3d(tile, &tm, x0 + GX - 4, y0 + GY - 3, z0 + GZ - 3, &bar);
   }
   if (!mbar_wait(&bar, 0, kMaxPolls)) {
@@ -582,10 +585,10 @@ __global__ void __launch_bounds__(TX * TY) k_stage_f32(const __grid_constant__ C
     return;
   }
   if (a.ghost) {
-    fill_face_ghosts<float>(tile, SX, SY, SZ, x0 - 4, y0 - 3, z0 - 3, a.L, a.ghost);
+    fill_face_ghosts<float>(tile, SX, SY, SZ_, x0 - 4, y0 - 3, z0 - 3, a.L, a.ghost);
     __syncthreads();
   }
-  f32_tile<MODE, TZ>(tile, a, x0, y0, z0, tx, ty);
+  f32_tile<MODE, TZ_>(tile, a, x0, y0, z0, tx, ty);
 }
 
 }  // namespace fused
