@@ -172,10 +172,11 @@ constexpr bool uses_reinit_x2() {
 }
 
 // Tile depth of the FP32 k_stage_f32 launches of a grid: 8, or 4 where the
-// 4-plane tiles fill whole waves of resident CTAs better (a partly filled
-// last wave costs a whole one; five CTAs per SM at either depth).  Measured
-// at 128^3: 1024 8-plane tiles are 1.35 waves on 152 SMs, 2048 4-plane
-// tiles 2.7.
+// 4-plane tiles fill whole waves of resident CTAs at least 10% better (a
+// partly filled last wave costs a whole one; five CTAs per SM at either
+// depth; a grid of less than one wave gets twice the CTAs).  At 128^3, 1024
+// 8-plane tiles are 1.35 waves on 152 SMs, 2048 4-plane tiles 2.7; at 192^3
+// and 256^3 both depths fill their waves equally and 8 is kept.
 inline int stage_tz_f32(const Layout &L) {
   static int sms = 0;
   if (sms == 0) {
@@ -192,7 +193,7 @@ inline int stage_tz_f32(const Layout &L) {
     const long long waves = (tiles + slots - 1) / slots;
     return (double)L.nz / ((double)waves * slots * tz / (double)cols);  // used fraction of the wave slots
   };
-  return eff(4) > eff(8) + 0.05 ? 4 : 8;
+  return eff(4) > 1.1 * eff(8) ? 4 : 8;
 }
 
 // Tensor map of a padded work buffer with the staged box of the stage kernel

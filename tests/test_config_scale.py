@@ -63,6 +63,41 @@ def test_config1_advection_128_fp64_bit_exact(gpu_lib):
     got = _host(t)
     L.check()
     assert H.same(want, got), np.max(np.abs(want - got))
+    # the FP32 form (4-plane tiles at this size) against the same oracle run:
+    # within 1e-5 within 3 dx of the interface, 5e-5 elsewhere
+    t32 = _dev(phi, torch.float32)
+    L.advect_weno5_tvdrk3(t32, gb, fb, dx, dt, steps, vel_const=vel, precision="f32")
+    got32 = _host(t32).astype(np.float64)
+    L.check()
+    inner = (slice(3, -3),) * 3
+    err = np.abs(got32 - want)[inner]
+    near = np.abs(want[inner]) <= 3 * dx
+    assert np.max(err[near]) <= 1e-5, np.max(err[near])
+    assert np.max(err) <= 5e-5, np.max(err)
+
+
+@pytest.mark.gpu
+def test_advection_f32_192_eight_plane_tiles(gpu_lib):
+    """192^3 (the adjoint workload's size, where the FP32 advection stage runs
+    8-plane tiles), velocity field of the adjoint workload, 4 steps, periodic:
+    within 1e-5 of the FP64 oracle within 3 dx of the interface, 5e-5 elsewhere."""
+    import torch
+    n, steps = 192, 4
+    gb, fb = bench.boxes(n)
+    phi, vel, tgt, dx, dt = bench.adjoint_case(n)
+    pad = lambda a: np.asfortranarray(np.pad(a, 3, mode="wrap"))
+    P, V = pad(phi), [pad(v) for v in vel]
+    want = SlabRun(H.oracle(), gb, fb).run("advect", P, dx, dt, steps, L.BC_PERIODIC, vel=V)
+    t = _dev(P, torch.float32)
+    vt = [_dev(v, torch.float32) for v in V]
+    L.advect_weno5_tvdrk3(t, gb, fb, dx, dt, steps, vel=vt, vel_gb=gb, precision="f32")
+    got = _host(t).astype(np.float64)
+    L.check()
+    inner = (slice(3, -3),) * 3
+    err = np.abs(got - want)[inner]
+    near = np.abs(want[inner]) <= 3 * dx
+    assert np.max(err[near]) <= 1e-5, np.max(err[near])
+    assert np.max(err) <= 5e-5, np.max(err)
 
 
 # ---------------------------------------------------------------------------

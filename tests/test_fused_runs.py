@@ -131,6 +131,33 @@ def test_fused_advect_anisotropic_grid(precision, gpu_lib):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("bc", [L.BC_PERIODIC, L.BC_SIGNED_LINEAR])
+@pytest.mark.parametrize("vel", [(1.0, 0.5, 0.25), (-0.6, 0.8, -0.3)])
+def test_fused_advect_f32_four_plane_tiles(bc, vel, gpu_lib):
+    """64^3 with 13 planes: the FP32 advection stage runs 4-plane tiles there
+    (they fill the waves of resident CTAs better than 8-plane ones), the last
+    one ragged; constant velocities of either sign (the per-grid stencil
+    side), periodic and extrapolated ghosts (the in-tile face ghosts)."""
+    n, nz = 64, 13
+    fb = (0, n - 1, 0, n - 1, 0, nz - 1)
+    gb = (-3, n + 2, -3, n + 2, -3, nz + 2)
+    sp = (2.0 / n, 2.0 / n, 2.0 / nz)
+    c = [-1.0 + (np.arange(-3, m + 3) + 0.5) * 2.0 / m for m in (n, n, nz)]
+    X, Y, Z = np.meshgrid(*c, indexing="ij")
+    phi = np.asfortranarray(np.sqrt((X - 0.1) ** 2 + (Y + 0.05) ** 2 + Z ** 2) - 0.45)
+    dt = 0.5 / sum(abs(v) / s for v, s in zip(vel, sp))
+    v = [np.full(phi.shape, x, order="F") for x in vel]
+    steps = 3
+    want = O.tvdrk3_run(H.oracle(), "advect", phi, gb, fb, sp, dt, steps, bc, vel=v)
+    got = np.asfortranarray(phi.astype(np.float32))
+    L.advect_weno5_tvdrk3(got, gb, fb, sp[0], dt, steps, vel_const=vel, bc=bc, precision="f32",
+                          dy=sp[1], dz=sp[2])
+    L.check()
+    err = np.abs(got.astype(np.float64) - want)[3:-3, 3:-3, 3:-3]
+    assert np.max(err) <= 1e-5, np.max(err)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["f64", "f32"])
 def test_identical_calls_replay_the_cached_graph(precision, gpu_lib):
     """A second call with the same buffers, sizes and parameters replays the
