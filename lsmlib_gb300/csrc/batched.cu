@@ -228,6 +228,11 @@ extern "C" int lsmgpu_advect_batch_weno5_tvdrk3_f32(float *phi, const long long 
       set_error(LSMGPU_ERR_BOUNDS, "%s: grid %d is smaller than 6 cells on an axis", name, g);
       return LSMGPU_ERR_BOUNDS;
     }
+    // tile positions are 16-bit (16-cell tiles at the finest)
+    if (nx > 65535 * 16 || ny > 65535 * 8 || nz > 65535 * 4) {
+      set_error(LSMGPU_ERR_BOUNDS, "%s: grid %d has more than 65535 tiles along an axis", name, g);
+      return LSMGPU_ERR_BOUNDS;
+    }
     uoff[g] = offsets[g];
     user_total = std::max(user_total, offsets[g] + (long long)(nx + 6) * (ny + 6) * (nz + 6));
   }
