@@ -276,7 +276,7 @@ __global__ void __maxnreg__(LSMGPU_ADJ_X_X2_NREG) k_adj_x_x2(AdjStageArgs<float>
   };
 
   unsigned ok = pz * (unsigned)(z0 + fused::GZ);
-  stage_s(sbuf, ld2(a.s, ok));
+  stage_s(sbuf + (z0 & 1) * hp, ld2(a.s, ok));  // plane k is read from buffer k & 1
   // the next plane's values are loaded one plane ahead
   float2 sn = sp(0.f), mn = ld2(a.M, ok);
   Coef2<MODE> cn = load_coef2<MODE>(a, 0, col0 + ok, col1 + ok);
