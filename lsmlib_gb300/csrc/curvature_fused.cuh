@@ -56,6 +56,90 @@ __global__ void k_mean_curvature(CurvArgs<R> a) {
   a.kappa(i, j, k) = out;
 }
 
+inline bool pinned_host(const void *p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
+// Pinned host phi and kappa: the transfers overlap the kernel and each other.
+// The fill box is cut into z slabs; phi's planes go to the device on copy
+// stream 0 in order (each plane once: phi's planes are contiguous in its
+// column-major layout), the kernel of a slab runs on the library stream once
+// its planes and their one-plane halo are there, and the slab's kappa goes
+// back on copy stream 1.  Returns false (nothing queued) when the streams or
+// events are not available, so the caller stages the arrays whole instead.
+template <class R>
+bool run_pipelined(Call &call, CurvArgs<R> a, R *kappa, const Box &kb, const R *phi, const Box &pb,
+                   const Box &fb) {
+  constexpr int kSlabs = 8;
+  cudaStream_t s = stream(), cin = copy_stream(0), cout = copy_stream(1);
+  if (!cin || !cout || fb.n(2) < 2 * kSlabs) return false;
+  R *phid = call.temp<R>(pb.size());
+  R *kapd = call.temp<R>(kb.size());
+  if (!call.ok()) return false;
+  cudaEvent_t ev[2 * kSlabs + 2];
+  int made = 0;
+  for (; made < 2 * kSlabs + 2; made++)
+    if (cudaEventCreateWithFlags(&ev[made], cudaEventDisableTiming) != cudaSuccess) break;
+  bool ok = made == 2 * kSlabs + 2;
+  if (ok) {
+    // the copy streams start after the work already queued on the library stream
+    ok = cuda_ok(cudaEventRecord(ev[2 * kSlabs], s), "cudaEventRecord") &&
+         cuda_ok(cudaStreamWaitEvent(cin, ev[2 * kSlabs], 0), "cudaStreamWaitEvent") &&
+         cuda_ok(cudaStreamWaitEvent(cout, ev[2 * kSlabs], 0), "cudaStreamWaitEvent");
+  }
+  a.phi = view((const R *)phid, pb);
+  a.kappa = view(kapd, kb);
+  const long long plane = pb.n(0) * pb.n(1);
+  const long long nz = fb.n(2);
+  int copied = pb.lo[2] - 1;  // last phi plane on the device
+  for (int q = 0; q < kSlabs && ok; q++) {
+    Box sb = fb;
+    sb.lo[2] = fb.lo[2] + (int)(nz * q / kSlabs);
+    sb.hi[2] = fb.lo[2] + (int)(nz * (q + 1) / kSlabs) - 1;
+    const int need = sb.hi[2] + 1 < pb.hi[2] ? sb.hi[2] + 1 : pb.hi[2];
+    if (need > copied) {
+      const long long z0 = copied + 1 - pb.lo[2], n = (long long)(need - copied) * plane;
+      ok = cuda_ok(cudaMemcpyAsync(phid + z0 * plane, phi + z0 * plane, (size_t)n * sizeof(R), cudaMemcpyHostToDevice,
+                                   cin), "cudaMemcpyAsync(H2D slab)");
+      copied = need;
+    }
+    ok = ok && cuda_ok(cudaEventRecord(ev[q], cin), "cudaEventRecord") &&
+         cuda_ok(cudaStreamWaitEvent(s, ev[q], 0), "cudaStreamWaitEvent");
+    if (!ok) break;
+    a.fb = sb;
+    Grid3 g = cover(sb);
+    LSMGPU_LAUNCH(k_mean_curvature<R>, g.grid, g.block, 0, a);
+    ok = cuda_ok(cudaEventRecord(ev[kSlabs + q], s), "cudaEventRecord") &&
+         cuda_ok(cudaStreamWaitEvent(cout, ev[kSlabs + q], 0), "cudaStreamWaitEvent");
+    if (!ok) break;
+    // the slab's kappa rows: one 3D copy out of kappa's ghost-box layout
+    cudaMemcpy3DParms m = {};
+    const size_t pitch = (size_t)kb.n(0) * sizeof(R);
+    m.srcPtr = make_cudaPitchedPtr(kapd, pitch, pitch, (size_t)kb.n(1));
+    m.dstPtr = make_cudaPitchedPtr(kappa, pitch, pitch, (size_t)kb.n(1));
+    m.srcPos = m.dstPos = make_cudaPos((size_t)(sb.lo[0] - kb.lo[0]) * sizeof(R), (size_t)(sb.lo[1] - kb.lo[1]),
+                                       (size_t)(sb.lo[2] - kb.lo[2]));
+    m.extent = make_cudaExtent((size_t)sb.n(0) * sizeof(R), (size_t)sb.n(1), (size_t)sb.n(2));
+    m.kind = cudaMemcpyDeviceToHost;
+    ok = cuda_ok(cudaMemcpy3DAsync(&m, cout), "cudaMemcpy3DAsync(D2H slab)");
+  }
+  // the library stream (and so the caller) waits for every copy; the call
+  // returns once they are done, as a staged call does
+  const bool joined = made == 2 * kSlabs + 2 && cuda_ok(cudaEventRecord(ev[2 * kSlabs + 1], cout), "cudaEventRecord") &&
+                      cuda_ok(cudaStreamWaitEvent(s, ev[2 * kSlabs + 1], 0), "cudaStreamWaitEvent") &&
+                      cuda_ok(cudaEventRecord(ev[2 * kSlabs], cin), "cudaEventRecord") &&
+                      cuda_ok(cudaStreamWaitEvent(s, ev[2 * kSlabs], 0), "cudaStreamWaitEvent");
+  const bool synced = cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  for (int e = 0; e < made; e++) cudaEventDestroy(ev[e]);
+  if (!(ok && joined && synced)) call.fail("pipelined transfer failed");
+  return true;
+}
+
 template <class R>
 int run(const char *name, R *kappa, const Box &kb, const R *phi, const Box &pb, R *mag, const Box &fb,
         R dx, R dy, R dz) {
@@ -64,16 +148,24 @@ int run(const char *name, R *kappa, const Box &kb, const R *phi, const Box &pb, 
   if (!kb.contains(fb, 0, 0, 0)) call.fail("kappa ghost box does not cover the fill box");
   if (!call.ok()) return LSMGPU_ERR_BOUNDS;
   if (fb.empty()) return LSMGPU_OK;
+  if (!phi || !kappa) {
+    call.fail("null array pointer");
+    return LSMGPU_ERR_ARGUMENT;
+  }
   CurvArgs<R> a{};
+  a.gx = R(0.5) / dx; a.gy = R(0.5) / dy; a.gz = R(0.5) / dz;
+  a.fxx = R(1.0) / dx / dx; a.fyy = R(1.0) / dy / dy; a.fzz = R(1.0) / dz / dz;
+  a.fxy = R(0.25) / dx / dy; a.fxz = R(0.25) / dx / dz; a.fyz = R(0.25) / dy / dz;
+  if (!mag && pinned_host(phi) && pinned_host(kappa) && run_pipelined<R>(call, a, kappa, kb, phi, pb, fb)) {
+    call.finish();
+    return lsmgpu_get_last_error(nullptr, 0);
+  }
   a.phi = view((const R *)call.in(phi, pb.size()), pb);
   // kappa and |grad phi| are written on every fill-box cell and nowhere else
   a.kappa = view(call.out_region(kappa, kb, fb), kb);
   a.mag = mag ? view(call.out_region(mag, kb, fb), kb) : View<R>{};
   if (!call.ok()) return lsmgpu_get_last_error(nullptr, 0);
   a.fb = fb;
-  a.gx = R(0.5) / dx; a.gy = R(0.5) / dy; a.gz = R(0.5) / dz;
-  a.fxx = R(1.0) / dx / dx; a.fyy = R(1.0) / dy / dy; a.fzz = R(1.0) / dz / dz;
-  a.fxy = R(0.25) / dx / dy; a.fxz = R(0.25) / dx / dz; a.fyz = R(0.25) / dy / dz;
   Grid3 g = cover(fb);
   LSMGPU_LAUNCH(k_mean_curvature<R>, g.grid, g.block, 0, a);
   call.finish();

@@ -166,6 +166,7 @@ inline Grid3 cover(const Box &fb, int bx = 32, int by = 4, int bz = 2) {
 // runtime (runtime.cu)
 // ---------------------------------------------------------------------------
 cudaStream_t stream();                      // library stream (lsmgpu_set_stream)
+cudaStream_t copy_stream(int which);        // library copy streams 0 and 1 (nullptr if unavailable)
 void note_launch();                         // counts kernels for lsmgpu_launch_count()
 
 // Replays `body`'s stream work as a CUDA graph on the library stream.  The

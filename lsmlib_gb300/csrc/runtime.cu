@@ -99,6 +99,23 @@ cudaStream_t g_capture[64] = {};
 
 cudaStream_t stream() { return t_capture_stream ? t_capture_stream : g_stream.load(); }
 
+// Two library-owned streams per device for host transfers that overlap the
+// library stream's work (created on first use; used inside a Call, with the
+// library lock held).
+cudaStream_t copy_stream(int which) {
+  static cudaStream_t streams[64][2] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || which < 0 || which > 1) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (!streams[dev][which] && cudaStreamCreateWithFlags(&streams[dev][which], cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    streams[dev][which] = nullptr;
+  }
+  return streams[dev][which];
+}
+
 // Called with the library lock held (inside a Call), so the cache and the
 // capture stream are not shared with another thread meanwhile.
 bool graph_replay(const GraphKey &key, void (*body)(void *), void *ctx) {

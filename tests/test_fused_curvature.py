@@ -83,3 +83,31 @@ def test_fused_curvature_f32_within_tolerance(gpu_lib):
                         dy=DY, dz=DZ)
     err = np.max(np.abs(kap[FBS].astype(np.float64) - want_k[FBS]))
     assert err <= 1e-4 * np.max(np.abs(want_k[FBS])), err
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_fused_curvature_pinned_host_pipelined(precision, gpu_lib):
+    """Pinned host phi and kappa without |grad phi|: the slab-pipelined
+    transfers (37 fill-box planes cut into 8 uneven slabs).  Equal bit for bit
+    to the call on device arrays; kappa outside the fill box keeps the
+    caller's values."""
+    import torch
+    gb = (-3, 21, -2, 17, -4, 40)
+    fb = (0, 18, 0, 15, -2, 34)
+    real = np.float64 if precision == "f64" else np.float32
+    phi = H.sphere_phi(gb, DX, center=(0.9, 0.8, 1.5), r=0.8, lo=0.0)
+    phi = np.asfortranarray((phi * (1.0 + 0.2 * np.random.default_rng(5).random(phi.shape))).astype(real))
+    pattern = np.asfortranarray(np.random.default_rng(6).standard_normal(phi.shape).astype(real))
+    host = lambda a: torch.from_numpy(np.ascontiguousarray(a.T)).pin_memory()
+    hp, hk = host(phi), host(pattern)
+    L.mean_curvature_o2(hk, gb, hp, gb, fb, DX, precision=precision, dy=DY, dz=DZ)
+    dp, dk = hp.cuda(), host(pattern).cuda()
+    L.mean_curvature_o2(dk, gb, dp, gb, fb, DX, precision=precision, dy=DY, dz=DZ)
+    torch.cuda.synchronize()
+    got, want = hk.numpy().T, dk.cpu().numpy().T
+    assert H.same(got, want)
+    fbs = tuple(slice(fb[2 * d] - gb[2 * d], fb[2 * d + 1] - gb[2 * d] + 1) for d in range(3))
+    outside = np.ones(got.shape, bool)
+    outside[fbs] = False
+    assert H.same(got[outside], pattern[outside])
