@@ -237,17 +237,17 @@ int run(const char *name, const Box &gb, const Box &fb, const Box &vb, const Adj
 
   cudaStream_t s = stream();
   cudaMemsetAsync(err, 0, sizeof(int), s);
-  dim3 pblk(32, 4, 2);
-  dim3 pgrd((unsigned)((nx + 7 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));
+  const dim3 pblk = fused::pack_block(), pgrd = fused::pack_grid(nx, ny, nz, fused::GX);
   LSMGPU_LAUNCH(fused::k_pack<R>, pgrd, pblk, 0, ck[0], L, view(phi_d, gb), gb, fb.lo[0], fb.lo[1], fb.lo[2]);
   if (objective)
     LSMGPU_LAUNCH(fused::k_pack<R>, pgrd, pblk, 0, TG, L, view(tgt_d, gb), gb, fb.lo[0], fb.lo[1], fb.lo[2]);
   for (int d = 0; d < 3 && advect; d++)
     LSMGPU_LAUNCH(fused::k_pack<R>, pgrd, pblk, 0, V[d], L, view(vel_d[d], vb), vb, fb.lo[0], fb.lo[1], fb.lo[2]);
   {
+    const dim3 fblk(32, 4, 2);
     dim3 gf((unsigned)((nx + 6 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));
     // the initial state is the periodic extension of the fill-box values
-    LSMGPU_LAUNCH(k_fill_periodic<R>, gf, pblk, 0, ck[0], L);
+    LSMGPU_LAUNCH(k_fill_periodic<R>, gf, fblk, 0, ck[0], L);
   }
   cudaMemcpyAsync(X, ck[0], (size_t)ne * sizeof(R), cudaMemcpyDeviceToDevice, s);
 
@@ -322,8 +322,7 @@ int run(const char *name, const Box &gb, const Box &fb, const Box &vb, const Adj
     }
   }
   if (phi_out_d) {
-    dim3 blk(32, 4, 2);
-    dim3 grd((unsigned)((nx + 6 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));
+    const dim3 blk = fused::pack_block(), grd = fused::pack_grid(nx, ny, nz, 3);
     LSMGPU_LAUNCH(fused::k_unpack<R>, grd, blk, 0, view(phi_out_d, gb), gb, X, L, fb.lo[0], fb.lo[1], fb.lo[2]);
   }
   if (objective) {

@@ -20,30 +20,56 @@ namespace fused {
 // copy between the caller's ghost-box array and the padded layout over the
 // region the layout holds (interior plus GX/3 ghost cells), clipped to the
 // caller's box; cells of the layout outside the caller's box are zeroed
+// Copies between a caller's array over its ghost box and the padded work
+// layout: threads along x and y, each walking kPackZ planes with all its
+// loads issued before its stores (one element in flight per thread leaves
+// the copy far below the memory's rate).
+constexpr int kPackZ = 8;
+
 template <class R>
 __global__ void k_pack(R *dst, Layout L, View<const R> src, Box gb, int ilo, int jlo, int klo) {
   const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x) - GX;
   const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y) - GY;
-  const int k = (int)(blockIdx.z * blockDim.z + threadIdx.z) - GZ;
-  if (i > L.nx + 2 || j > L.ny + 2 || k > L.nz + 2) return;
-  const int gi = i + ilo, gj = j + jlo, gk = k + klo;
-  R v = R(0);
-  if (gi >= gb.lo[0] && gi <= gb.hi[0] && gj >= gb.lo[1] && gj <= gb.hi[1] && gk >= gb.lo[2] &&
-      gk <= gb.hi[2])
-    v = src(gi, gj, gk);
-  dst[L.idx(i, j, k)] = v;
+  const int k0 = (int)(blockIdx.z * kPackZ) - GZ;
+  if (i > L.nx + 2 || j > L.ny + 2) return;
+  const int gi = i + ilo, gj = j + jlo;
+  const bool in_xy = gi >= gb.lo[0] && gi <= gb.hi[0] && gj >= gb.lo[1] && gj <= gb.hi[1];
+  R v[kPackZ];
+#pragma unroll
+  for (int q = 0; q < kPackZ; q++) {
+    const int gk = k0 + q + klo;
+    v[q] = (in_xy && gk >= gb.lo[2] && gk <= gb.hi[2]) ? src(gi, gj, gk) : R(0);
+  }
+#pragma unroll
+  for (int q = 0; q < kPackZ; q++)
+    if (k0 + q <= L.nz + 2) dst[L.idx(i, j, k0 + q)] = v[q];
 }
 
 template <class R>
 __global__ void k_unpack(View<R> dst, Box gb, const R *src, Layout L, int ilo, int jlo, int klo) {
   const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x) - 3;
   const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y) - 3;
-  const int k = (int)(blockIdx.z * blockDim.z + threadIdx.z) - 3;
-  if (i > L.nx + 2 || j > L.ny + 2 || k > L.nz + 2) return;
-  const int gi = i + ilo, gj = j + jlo, gk = k + klo;
-  if (gi >= gb.lo[0] && gi <= gb.hi[0] && gj >= gb.lo[1] && gj <= gb.hi[1] && gk >= gb.lo[2] &&
-      gk <= gb.hi[2])
-    dst(gi, gj, gk) = src[L.idx(i, j, k)];
+  const int k0 = (int)(blockIdx.z * kPackZ) - 3;
+  if (i > L.nx + 2 || j > L.ny + 2) return;
+  const int gi = i + ilo, gj = j + jlo;
+  if (!(gi >= gb.lo[0] && gi <= gb.hi[0] && gj >= gb.lo[1] && gj <= gb.hi[1])) return;
+  R v[kPackZ];
+#pragma unroll
+  for (int q = 0; q < kPackZ; q++)
+    if (k0 + q <= L.nz + 2) v[q] = src[L.idx(i, j, k0 + q)];
+#pragma unroll
+  for (int q = 0; q < kPackZ; q++) {
+    const int gk = k0 + q + klo;
+    if (k0 + q <= L.nz + 2 && gk >= gb.lo[2] && gk <= gb.hi[2]) dst(gi, gj, gk) = v[q];
+  }
+}
+
+// launch geometry of k_pack / k_unpack over the padded box (x from -GX, y
+// and z from -3) or the ghost box (from -3)
+inline dim3 pack_block() { return dim3(32, 8, 1); }
+inline dim3 pack_grid(int nx, int ny, int nz, int x_ghosts_below) {
+  return dim3((unsigned)((nx + x_ghosts_below + 3 + 31) / 32), (unsigned)((ny + 6 + 7) / 8),
+              (unsigned)((nz + 6 + kPackZ - 1) / kPackZ));
 }
 
 // Extrapolation into the 3 ghost layers along one axis: linear
@@ -319,8 +345,7 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, const R *vx
   cudaStream_t s = stream();
   cudaMemsetAsync(err, 0, sizeof(int), s);
   {
-    dim3 blk(32, 4, 2);
-    dim3 grd((unsigned)((nx + 7 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));
+    const dim3 blk = pack_block(), grd = pack_grid(nx, ny, nz, GX);
     LSMGPU_LAUNCH(k_pack<R>, grd, blk, 0, A, L, view((const R *)phi_d, gb), gb, fb.lo[0], fb.lo[1], fb.lo[2]);
     if (rs.mode == ADV_FIELD)
       for (int d = 0; d < 3; d++)
@@ -397,8 +422,7 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, const R *vx
   add_stage_args(key, a);
   if (!graph_replay(key, steps)) steps();
   {
-    dim3 blk(32, 4, 2);
-    dim3 grd((unsigned)((nx + 6 + 31) / 32), (unsigned)((ny + 6 + 3) / 4), (unsigned)((nz + 6 + 1) / 2));
+    const dim3 blk = pack_block(), grd = pack_grid(nx, ny, nz, 3);
     LSMGPU_LAUNCH(k_unpack<R>, grd, blk, 0, view(phi_d, gb), gb, A, L, fb.lo[0], fb.lo[1], fb.lo[2]);
   }
   int herr = 0;
