@@ -26,8 +26,10 @@ namespace fused {
 // the copy far below the memory's rate).
 constexpr int kPackZ = 8;
 
+// dst2 (optional) receives the same values (the phi0 copy of the
+// reinitialization's sign form)
 template <class R>
-__global__ void k_pack(R *dst, Layout L, View<const R> src, Box gb, int ilo, int jlo, int klo) {
+__global__ void k_pack(R *dst, Layout L, View<const R> src, Box gb, int ilo, int jlo, int klo, R *dst2 = nullptr) {
   const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x) - GX;
   const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y) - GY;
   const int k0 = (int)(blockIdx.z * kPackZ) - GZ;
@@ -42,7 +44,11 @@ __global__ void k_pack(R *dst, Layout L, View<const R> src, Box gb, int ilo, int
   }
 #pragma unroll
   for (int q = 0; q < kPackZ; q++)
-    if (k0 + q <= L.nz + 2) dst[L.idx(i, j, k0 + q)] = v[q];
+    if (k0 + q <= L.nz + 2) {
+      const long long c = L.idx(i, j, k0 + q);
+      dst[c] = v[q];
+      if (dst2) dst2[c] = v[q];
+    }
 }
 
 template <class R>
@@ -346,12 +352,13 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, const R *vx
   cudaMemsetAsync(err, 0, sizeof(int), s);
   {
     const dim3 blk = pack_block(), grd = pack_grid(nx, ny, nz, GX);
-    LSMGPU_LAUNCH(k_pack<R>, grd, blk, 0, A, L, view((const R *)phi_d, gb), gb, fb.lo[0], fb.lo[1], fb.lo[2]);
+    // the phi0 copy of the sign form (read at interior cells only) is
+    // written by the same pass
+    LSMGPU_LAUNCH(k_pack<R>, grd, blk, 0, A, L, view((const R *)phi_d, gb), gb, fb.lo[0], fb.lo[1], fb.lo[2], P0);
     if (rs.mode == ADV_FIELD)
       for (int d = 0; d < 3; d++)
         LSMGPU_LAUNCH(k_pack<R>, grd, blk, 0, V[d], L, view(vel_d[d], vb), vb, fb.lo[0], fb.lo[1], fb.lo[2]);
   }
-  if (P0) cudaMemcpyAsync(P0, A, (size_t)ne * sizeof(R), cudaMemcpyDeviceToDevice, s);
 
   CUtensorMap tA, tB, tC;
   auto enc = [&](CUtensorMap *m, const R *p) {
