@@ -210,13 +210,16 @@ constexpr bool uses_reinit_x2() {
 // 8-plane tiles are 1.35 waves on 152 SMs, 2048 4-plane tiles 2.7; at 192^3
 // and 256^3 both depths fill their waves equally and 8 is kept.
 inline int stage_tz_f32(const Layout &L) {
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0, v = 152;
-    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
-      sms = v;
-    else
-      sms = 152;
+  static int sms_of[64] = {};  // SM count per device, read once
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) {
+    if (sms_of[dev] == 0) {
+      int v = 0;
+      sms_of[dev] = cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0 ? v : 152;
+    }
+    sms = sms_of[dev];
+  } else {
+    cudaGetLastError();
   }
   const long long slots = 5LL * sms;
   const long long cols = (long long)((L.nx + TX - 1) / TX) * ((L.ny + TY - 1) / TY);
