@@ -254,25 +254,43 @@ static __device__ __forceinline__ void pair_offsets(const BandArgs<float> &a, in
   o1 = two ? p.y : p.x;
 }
 
+// Stage 1 of the FP32 form stores, per entry pair p, the float4
+// (src[l0], src[l1], rhs[l0], rhs[l1]) at a.rhs + 4p, so that the update
+// after the dt reduction reads one contiguous record instead of gathering src.
+// The dt maximum is taken in FP32 (a maximum is exact in either precision;
+// the one conversion to FP64 per warp gives the same key) to keep the slow
+// FP64 pipe out of the kernel.
 static __global__ void k_band_rhs_x2(BandArgs<float> a) {
-  const int l0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-  double h = -1.0e308;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int l0 = 2 * p;
+  float h = -INFINITY;
   if (l0 < a.n0) {
     const bool two = l0 + 1 < a.n0;
-    const int l1 = two ? l0 + 1 : l0;
     long long o0, o1;
     pair_offsets(a, l0, two, o0, o1);
     float2 hd;
     const float2 r = cell_rhs_x2(a, o0, o1, hd);
-    h = (double)hd.x;
-    a.rhs[l0] = cutoff<float>(r.x, a.src.p[o0], a.beta, a.gamma);
-    if (two) {
-      h = fmax(h, (double)hd.y);
-      a.rhs[l1] = cutoff<float>(r.y, a.src.p[o1], a.beta, a.gamma);
-    }
+    h = two ? fmaxf(hd.x, hd.y) : hd.x;
+    const float s0 = a.src.p[o0], s1 = a.src.p[o1];
+    reinterpret_cast<float4 *>(a.rhs)[p] =
+        make_float4(s0, s1, cutoff<float>(r.x, s0, a.beta, a.gamma), cutoff<float>(r.y, s1, a.beta, a.gamma));
   }
-  for (int o = 16; o > 0; o >>= 1) h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(a.key, okey(h));
+  for (int o = 16; o > 0; o >>= 1) h = fmaxf(h, __shfl_xor_sync(0xffffffffu, h, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(a.key, okey((double)h));
+}
+
+// stage 1, pass 2 of the FP32 form: one entry pair per thread from its record
+static __global__ void k_band_update1_x2(BandArgs<float> a) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int l0 = 2 * p;
+  if (l0 >= a.n0) return;
+  const bool two = l0 + 1 < a.n0;
+  long long o0, o1;
+  pair_offsets(a, l0, two, o0, o1);
+  const float4 v = reinterpret_cast<const float4 *>(a.rhs)[p];
+  const float dt = *a.dt;
+  a.out.p[o0] = rk_update<float>(1, v.x, v.x, dt, v.z);
+  if (two) a.out.p[o1] = rk_update<float>(1, v.y, v.y, dt, v.w);
 }
 
 static __global__ void k_band_stage_x2(BandArgs<float> a) {
@@ -340,7 +358,8 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
   R *u1 = call.temp<R>(n), *u2 = call.temp<R>(n);
   U8 *nb = call.temp<U8>(n);
   int *ix = call.temp<int>(n), *iy = call.temp<int>(n), *iz = call.temp<int>(n), *outer = call.temp<int>(n);
-  R *rhs = call.temp<R>(n);
+  constexpr bool packed = !EXACT && sizeof(R) == 4;
+  R *rhs = nullptr;  // per level-0 entry; sized at the first build
   int *off0 = call.temp<int>(n + 1);  // n + 1: the pair loads read an even count
   R *dt = call.temp<R>(1);
   unsigned long long *key = call.temp<unsigned long long>(1);
@@ -382,6 +401,8 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
         ox = call.temp<int>(c0);
         oy = call.temp<int>(c0);
         oz = call.temp<int>(c0);
+        // the FP32 form keeps a 4-value record per entry pair
+        rhs = call.temp<R>(packed ? 2 * c0 + 4 : c0);
         if (!call.ok()) return lsmgpu_get_last_error(nullptr, 0);
       }
       n0 = (int)c0;
@@ -412,7 +433,6 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
     a.key = key;
     const unsigned blocks = (unsigned)((n0 + 127) / 128);
     const unsigned blocks2 = (unsigned)((n0 + 255) / 256);  // pairs of entries
-    constexpr bool packed = !EXACT && sizeof(R) == 4;
     // stage 1
     a.src = view((const R *)phi, gb);
     a.phin = a.src;
@@ -422,7 +442,8 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
     if constexpr (packed) LSMGPU_LAUNCH(k_band_rhs_x2, blocks2, 128, 0, a);
     else LSMGPU_LAUNCH((k_band_rhs<R, EXACT>), blocks, 128, 0, a);
     LSMGPU_LAUNCH(k_band_dt<R>, 1, 1, 0, key, dt, cfl, dtl ? dtl + step : nullptr);
-    LSMGPU_LAUNCH(k_band_update1<R>, blocks, 128, 0, a);
+    if constexpr (packed) LSMGPU_LAUNCH(k_band_update1_x2, blocks2, 128, 0, a);
+    else LSMGPU_LAUNCH(k_band_update1<R>, blocks, 128, 0, a);
     // stage 2
     a.src = view((const R *)u1, gb);
     a.out = view(u2, gb);
