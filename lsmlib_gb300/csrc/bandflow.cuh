@@ -33,6 +33,9 @@ struct BandArgs {
   const int *off0;        // padded offset of each level-0 entry (written at each rebuild)
   int n0;                 // level-0 entries (list elements 0..n0-1)
   R dx, a_n, b_n, beta, gamma, cfl;
+  // per-call constants of the stencils, divided on the host in R exactly as
+  // the per-cell expressions would: 0.5/dx, 1/dx/dx, 0.25/dx/dx, 1/dx
+  R f_half, f_xx, f_xy, inv_dx;
   R *rhs;                 // per level-0 entry (stage 1)
   const R *dt;            // device scalar
   unsigned long long *key;
@@ -85,8 +88,7 @@ __device__ __forceinline__ R weno_local(R v1, R v2, R v3, R v4, R v5) {
 // (spatial_derivatives3d_local.f.in:825-839, :1251-1272; curvature3d_local.f.in)
 template <class R>
 __device__ __forceinline__ R cell_vn(const BandArgs<R> &a, const R *c, const long long s[3]) {
-  const R dx = a.dx;
-  const R f = R(0.5) / dx;
+  const R f = a.f_half;
   const R g0 = (c[s[0]] - c[-s[0]]) * f, g1 = (c[s[1]] - c[-s[1]]) * f, g2 = (c[s[2]] - c[-s[2]]) * f;
   const R tol = Consts<double>::zero_tol;
   R x2 = g0 * g0, y2 = g1 * g1, z2 = g2 * g2;
@@ -95,7 +97,7 @@ __device__ __forceinline__ R cell_vn(const BandArgs<R> &a, const R *c, const lon
   if (z2 < tol) z2 = R(0);
   const R t = sqrt(x2 + y2 + z2);
   const R mag = (t < tol) ? R(0) : t;
-  const R fxx = R(1.0) / dx / dx, fxy = R(0.25) / dx / dx;
+  const R fxx = a.f_xx, fxy = a.f_xy;
   const R xx = (c[s[0]] - R(2.0) * c[0] + c[-s[0]]) * fxx;
   const R yy = (c[s[1]] - R(2.0) * c[0] + c[-s[1]]) * fxx;
   const R zz = (c[s[2]] - R(2.0) * c[0] + c[-s[2]]) * fxx;
@@ -116,7 +118,7 @@ __device__ __forceinline__ R godunov_rhs(const BandArgs<R> &a, R vn, const R gp[
   const R sq = godunov_normal_sq<R>(vn > R(0), gp, gm);
   R rhs = R(0);
   if (fabs(vn) >= tol) rhs = rhs - vn * sqrt(sq);
-  const R dx = a.dx, inv = R(1.0) / dx;
+  const R dx = a.dx, inv = a.inv_dx;
   const R mx2 = dx * dx;
   const R cx = rmax(fabs(gp[0]), fabs(gm[0])), cy = rmax(fabs(gp[1]), fabs(gm[1])), cz = rmax(fabs(gp[2]), fabs(gm[2]));
   const R ng = sqrt(cx * cx + cy * cy + cz * cz + mx2);
@@ -131,7 +133,7 @@ __device__ __forceinline__ R cell_rhs(const BandArgs<R> &a, int i, int j, int k,
   const long long s[3] = {1, a.src.s1, a.src.s2};
   const R vn = cell_vn<R>(a, c, s);
   // HJ WENO5 plus/minus from the band values of src
-  const R inv = R(1.0) / a.dx;
+  const R inv = a.inv_dx;
   R gp[3], gm[3];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
@@ -151,7 +153,7 @@ static __device__ __forceinline__ float2 cell_rhs_x2(const BandArgs<float> &a, l
   const float *c0 = a.src.p + o0, *c1 = a.src.p + o1;
   const long long s[3] = {1, a.src.s1, a.src.s2};
   const float vn0 = cell_vn<float>(a, c0, s), vn1 = cell_vn<float>(a, c1, s);
-  const float2 inv = fused::sp(1.0f / a.dx);
+  const float2 inv = fused::sp(a.inv_dx);
   float gp0[3], gm0[3], gp1[3], gm1[3];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
@@ -428,6 +430,10 @@ int run(const char *name, R *phi_user, const Box &gb, const Box &fb, R dx, R a_n
     a.off0 = off0;
     a.n0 = n0;
     a.dx = dx; a.a_n = a_n; a.b_n = b_n; a.beta = beta; a.gamma = gamma; a.cfl = cfl;
+    a.f_half = R(0.5) / dx;
+    a.f_xx = R(1.0) / dx / dx;
+    a.f_xy = R(0.25) / dx / dx;
+    a.inv_dx = R(1.0) / dx;
     a.rhs = rhs;
     a.dt = dt;
     a.key = key;
