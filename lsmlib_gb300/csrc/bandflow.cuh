@@ -51,6 +51,14 @@ __device__ __forceinline__ double okey_inv(unsigned long long k) {
   return __longlong_as_double((long long)u);
 }
 
+// running maximum of the dt keys: the key only grows, so a warp whose key
+// does not exceed the value it reads cannot raise it and skips the atomic
+// (a stale read only costs an atomic); keeps tens of thousands of warps from
+// queueing on one address
+__device__ __forceinline__ void raise_key(unsigned long long *key, unsigned long long k) {
+  if (k > __ldcg(key)) atomicMax(key, k);
+}
+
 // WENO5 with the local routines' epsilon floor (spatial_derivatives2d_local.f.in:892)
 template <class R, bool EXACT>
 __device__ __forceinline__ R weno_local(R v1, R v2, R v3, R v4, R v5) {
@@ -212,7 +220,7 @@ __global__ void k_band_rhs(BandArgs<R> a) {
     a.rhs[l] = cutoff<R>(r, a.src(i, j, k), a.beta, a.gamma);
   }
   for (int o = 16; o > 0; o >>= 1) h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(a.key, okey(h));
+  if ((threadIdx.x & 31) == 0) raise_key(a.key, okey(h));
 }
 
 template <class R>
@@ -278,7 +286,7 @@ static __global__ void k_band_rhs_x2(BandArgs<float> a) {
         make_float4(s0, s1, cutoff<float>(r.x, s0, a.beta, a.gamma), cutoff<float>(r.y, s1, a.beta, a.gamma));
   }
   for (int o = 16; o > 0; o >>= 1) h = fmaxf(h, __shfl_xor_sync(0xffffffffu, h, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(a.key, okey((double)h));
+  if ((threadIdx.x & 31) == 0) raise_key(a.key, okey((double)h));
 }
 
 // stage 1, pass 2 of the FP32 form: one entry pair per thread from its record
