@@ -154,13 +154,55 @@ __device__ __forceinline__ R cell_rhs(const BandArgs<R> &a, int i, int j, int k,
   return godunov_rhs<R>(a, vn, gp, gm, h_over_dx);
 }
 
+// cell_vn on two cells in packed FP32x2: the central gradient, the second
+// differences and the curvature numerator (summed as
+// xx (y^2 + z^2) + yy (x^2 + z^2) + zz (x^2 + y^2) - 2 (xy x y + xz x z + yz y z))
+// run on the pair; the zero_tol clamps, |grad phi| and the division per cell
+static __device__ __forceinline__ float2 cell_vn_x2(const BandArgs<float> &a, const float *c0, const float *c1,
+                                                    const long long s[3]) {
+  using fused::add2;
+  using fused::fma2;
+  using fused::mul2;
+  using fused::sp;
+  const auto at = [&](long long o) { return make_float2(c0[o], c1[o]); };
+  const auto sub = [](float2 x, float2 y) { return fma2(y, sp(-1.f), x); };
+  const float2 cc = at(0);
+  const float2 xp = at(s[0]), xm = at(-s[0]), yp = at(s[1]), ym = at(-s[1]), zp = at(s[2]), zm = at(-s[2]);
+  const float2 f = sp(a.f_half);
+  const float2 gx = mul2(sub(xp, xm), f), gy = mul2(sub(yp, ym), f), gz = mul2(sub(zp, zm), f);
+  const float tol = Consts<double>::zero_tol;
+  const float2 sx = mul2(gx, gx), sy = mul2(gy, gy), sz = mul2(gz, gz);
+  // |grad phi| with each square below zero_tol dropped
+  const float2 q = add2(add2(make_float2(sx.x < tol ? 0.f : sx.x, sx.y < tol ? 0.f : sx.y),
+                             make_float2(sy.x < tol ? 0.f : sy.x, sy.y < tol ? 0.f : sy.y)),
+                        make_float2(sz.x < tol ? 0.f : sz.x, sz.y < tol ? 0.f : sz.y));
+  float m0 = sqrtf(q.x), m1 = sqrtf(q.y);
+  m0 = (m0 < tol) ? 0.f : m0;
+  m1 = (m1 < tol) ? 0.f : m1;
+  const float2 fxx = sp(a.f_xx), fxy = sp(a.f_xy), m2 = sp(-2.f);
+  const float2 xx = mul2(add2(fma2(m2, cc, xp), xm), fxx);
+  const float2 yy = mul2(add2(fma2(m2, cc, yp), ym), fxx);
+  const float2 zz = mul2(add2(fma2(m2, cc, zp), zm), fxx);
+  const float2 xy = mul2(add2(sub(sub(at(s[0] + s[1]), at(s[0] - s[1])), at(-s[0] + s[1])), at(-s[0] - s[1])), fxy);
+  const float2 xz = mul2(add2(sub(sub(at(s[0] + s[2]), at(s[0] - s[2])), at(-s[0] + s[2])), at(-s[0] - s[2])), fxy);
+  const float2 yz = mul2(add2(sub(sub(at(s[1] + s[2]), at(s[1] - s[2])), at(-s[1] + s[2])), at(-s[1] - s[2])), fxy);
+  const float2 diag = fma2(xx, add2(sy, sz), fma2(yy, add2(sx, sz), mul2(zz, add2(sx, sy))));
+  const float2 cross = fma2(mul2(xy, gx), gy, fma2(mul2(xz, gx), gz, mul2(mul2(yz, gy), gz)));
+  const float2 num = fma2(m2, cross, diag);
+  const float d0 = m0 * m0 * m0, d1 = m1 * m1 * m1;
+  const float k0 = (d0 < tol) ? 0.f : num.x / d0, k1 = (d1 < tol) ? 0.f : num.y / d1;
+  return make_float2(a.a_n - a.b_n * k0, a.a_n - a.b_n * k1);
+}
+
 // FP32 RHS of two level-0 cells (padded offsets o0, o1): the six WENO5
-// reconstructions run on the pair in Blackwell's packed FP32x2 arithmetic,
-// both sides of an axis together; curvature and the Godunov term per cell
+// reconstructions and the curvature run on the pair in Blackwell's packed
+// FP32x2 arithmetic (WENO5: both sides of an axis together); the Godunov term
+// per cell
 static __device__ __forceinline__ float2 cell_rhs_x2(const BandArgs<float> &a, long long o0, long long o1, float2 &hd) {
   const float *c0 = a.src.p + o0, *c1 = a.src.p + o1;
   const long long s[3] = {1, a.src.s1, a.src.s2};
-  const float vn0 = cell_vn<float>(a, c0, s), vn1 = cell_vn<float>(a, c1, s);
+  const float2 vn = cell_vn_x2(a, c0, c1, s);
+  const float vn0 = vn.x, vn1 = vn.y;
   const float2 inv = fused::sp(a.inv_dx);
   float gp0[3], gm0[3], gp1[3], gm1[3];
 #pragma unroll
@@ -270,7 +312,7 @@ static __device__ __forceinline__ void pair_offsets(const BandArgs<float> &a, in
 // The dt maximum is taken in FP32 (a maximum is exact in either precision;
 // the one conversion to FP64 per warp gives the same key) to keep the slow
 // FP64 pipe out of the kernel.
-static __global__ void k_band_rhs_x2(BandArgs<float> a) {
+static __global__ void __launch_bounds__(128, 8) k_band_rhs_x2(BandArgs<float> a) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const int l0 = 2 * p;
   float h = -INFINITY;
