@@ -36,7 +36,8 @@ struct BandArgs {
   // per-call constants of the stencils, divided on the host in R exactly as
   // the per-cell expressions would: 0.5/dx, 1/dx/dx, 0.25/dx/dx, 1/dx
   R f_half, f_xx, f_xy, inv_dx;
-  R *rhs;                 // per level-0 entry (stage 1)
+  R *rhs;                 // stage 1: the RHS per level-0 entry (FP32 form: a
+                          // (src, src, rhs, rhs) record per entry pair)
   const R *dt;            // device scalar
   unsigned long long *key;
   int stage;
